@@ -1,0 +1,262 @@
+"""hcore-gb300: HCORE's tile low-rank kernels on one GB300 GPU.
+
+The product is the C-ABI library ``libhcore_gb300.so`` (include/hcore_d.h,
+include/hcore_s.h, include/hcore_gb300.h).  This package is its Python host
+side: it loads the library with ctypes and mirrors the reference's operator
+interface so tests and benchmarks read like the reference's own:
+
+* :func:`hcore_dgemm` / :func:`hcore_sgemm` — one update with the signature
+  and semantics of HCORE_dgemm / HCORE_sgemm (src/compute/hcore_dgemm.c:703),
+  on numpy arrays, through the drop-in C entry points;
+* :class:`Batch` — many independent updates in one plan (device tensors),
+  executed by the batched GPU kernels and capturable in a CUDA graph;
+* :func:`dense_batched` — HCORE_dsyrk / HCORE_dgemmcd tile updates.
+
+There is no CPU fallback: importing works without a GPU, but every call into
+the library needs the compiled extension and a CUDA device, and raises
+otherwise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import LIB as _LIB_PATH
+
+__all__ = ["lib", "LrTask", "DenseTask", "Batch", "hcore_dgemm", "hcore_sgemm", "hcore_dgemm_fast",
+           "dense_batched", "HcoreError", "STATUS", "FlopCounter"]
+
+F64, F32 = 0, 1
+FAST_RULES = 0x1
+STATUS = {0: "ok", 1: "zero rank", 2: "rank sum > 2*maxrk", 3: "rank sum > ld_newV",
+          4: "new rank > maxrk", 5: "new rank > storage maxrank", 6: "Jacobi did not converge",
+          7: "bad shape"}
+
+
+class HcoreError(RuntimeError):
+    pass
+
+
+class LrTask(C.Structure):
+    """Mirror of hcore_lr_task (include/hcore_gb300.h)."""
+
+    _fields_ = [("M", C.c_int), ("a", C.c_int), ("b", C.c_int), ("c", C.c_int), ("rk", C.c_int),
+                ("maxrk", C.c_int), ("ld_newv", C.c_int), ("storage_maxrank", C.c_int),
+                ("alpha", C.c_double), ("beta", C.c_double), ("acc", C.c_double),
+                ("AU", C.c_void_p), ("AV", C.c_void_p), ("lda", C.c_int),
+                ("BU", C.c_void_p), ("BV", C.c_void_p), ("ldb", C.c_int),
+                ("Bdense", C.c_void_p),
+                ("CU", C.c_void_p), ("CV", C.c_void_p), ("ldc", C.c_int),
+                ("CUo", C.c_void_p), ("CVo", C.c_void_p), ("ldco", C.c_int)]
+
+
+class DenseTask(C.Structure):
+    """Mirror of hcore_dense_task (include/hcore_gb300.h)."""
+
+    _fields_ = [("kind", C.c_int), ("M", C.c_int), ("a", C.c_int), ("b", C.c_int),
+                ("alpha", C.c_double), ("Au", C.c_void_p), ("Av", C.c_void_p), ("lda", C.c_int),
+                ("Bu", C.c_void_p), ("Bv", C.c_void_p), ("ldb", C.c_int), ("CD", C.c_void_p),
+                ("ldcd", C.c_int)]
+
+
+class FlopCounter(C.Structure):
+    """Mirror of flop_counter (include/flop_util_structs.h)."""
+
+    _fields_ = [("__pad1", C.c_ulong), ("__pad2", C.c_ulong), ("copy", C.c_ulong),
+                ("flop", C.c_ulong), ("tid", C.c_int), ("potrf", C.c_ulong),
+                ("trsm", C.c_ulong), ("syrk", C.c_ulong), ("update", C.c_ulong)] + [
+        (n, C.c_ulong) for n in (
+            "geqrfu", "geqrfv", "geqrfv_gemm", "gesvd", "gesvd_gemm", "gesvd_lasetu",
+            "gesvd_lasetv", "gesvd_lacpyu", "gesvd_lacpyv", "gesvd_dscal", "ormqru",
+            "ormqru_laset", "ormqru_lacpy", "ormqrv", "ormqrv_laset", "ormqrv_lacpy",
+            "omatcopy")] + [("numthreads", C.c_int), ("__pad3", C.c_ulong),
+                            ("__pad4", C.c_ulong)]
+
+
+_lib = None
+_dp, _fp, _ip = C.POINTER(C.c_double), C.POINTER(C.c_float), C.POINTER(C.c_int)
+
+
+def lib_path() -> str:
+    return _LIB_PATH
+
+
+def lib() -> C.CDLL:
+    """Load libhcore_gb300.so (built by hcore_gb300/build.py); raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise HcoreError(f"{_LIB_PATH} is missing: run `python -m hcore_gb300.build` first")
+    L = C.CDLL(_LIB_PATH)
+    vp = C.c_void_p
+    L.hcore_gpu_plan_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.POINTER(LrTask), C.c_uint]
+    L.hcore_gpu_plan_execute.argtypes = [vp, vp]
+    L.hcore_gpu_plan_results.argtypes = [vp, _ip, _ip, vp]
+    L.hcore_gpu_plan_sigma.argtypes = [vp, C.c_int, _dp, _ip, vp]
+    L.hcore_gpu_plan_destroy.argtypes = [vp]
+    L.hcore_gpu_plan_device_ranks.argtypes = [vp]
+    L.hcore_gpu_plan_device_ranks.restype = vp
+    L.hcore_gpu_plan_device_status.argtypes = [vp]
+    L.hcore_gpu_plan_device_status.restype = vp
+    L.hcore_gpu_plan_workspace_bytes.argtypes = [vp]
+    L.hcore_gpu_plan_workspace_bytes.restype = C.c_size_t
+    L.hcore_gpu_dgemm_batched.argtypes = [C.c_int, C.POINTER(LrTask), _ip, _ip, vp]
+    L.hcore_gpu_sgemm_batched.argtypes = [C.c_int, C.POINTER(LrTask), _ip, _ip, vp]
+    L.hcore_gpu_dense_batched.argtypes = [C.c_int, C.POINTER(DenseTask), vp]
+    L.hcore_gpu_last_error.restype = C.c_char_p
+    L.hcore_gpu_thread_stream.restype = vp
+    for name, rp, real in (("HCORE_dgemm", _dp, C.c_double), ("HCORE_sgemm", _fp, C.c_float)):
+        f = getattr(L, name)
+        f.restype = None
+        f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, real, rp, rp, rp, C.c_int, rp, rp, rp,
+                      C.c_int, real, rp, rp, rp, C.c_int, C.c_int, C.c_int, real, rp,
+                      C.POINTER(FlopCounter)]
+    L.HCORE_dgemm_fast.restype = None
+    L.HCORE_dgemm_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp,
+                                   C.c_int, _dp, _dp, _dp, C.c_int, C.c_double, _dp, _dp, _dp,
+                                   C.c_int, C.c_int, C.c_int, C.c_double, _dp]
+    L.HCORE_dsyrk.restype = None
+    L.HCORE_dsyrk.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, C.c_int, _dp,
+                              C.c_int, C.c_double, _dp, C.c_int, _dp, C.POINTER(FlopCounter)]
+    L.HCORE_dgemmcd.restype = None
+    L.HCORE_dgemmcd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_int, C.c_int,
+                                _dp, _dp, C.c_int, C.c_int, C.c_double, _dp, C.c_int, C.c_int, _dp,
+                                C.POINTER(FlopCounter)]
+    for name, rp, real in (("HCORE_dgemm_dense", _dp, C.c_double),
+                           ("HCORE_sgemm_dense", _fp, C.c_float)):
+        f = getattr(L, name)
+        f.restype = None
+        f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, real, rp, C.c_int, rp, C.c_int,
+                      real, rp, C.c_int]
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return lib().hcore_gpu_last_error().decode()
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0 and rc != -4:
+        raise HcoreError(f"{what} failed ({rc}): {last_error()}")
+
+
+def _fortran(a, dtype):
+    return np.asfortranarray(np.asarray(a, dtype=dtype))
+
+
+def _lr_update(name, M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, rk, maxrk, acc, dtype,
+               fast=False):
+    """Call the drop-in entry point on host arrays; returns (rank, CU, CV, flops)."""
+    L = lib()
+    rp = _fp if dtype == np.float32 else _dp
+    AU, AV, BU, BV = (_fortran(x, dtype) for x in (AU, AV, BU, BV))
+    ldc = CU.shape[0]
+    ncol = max(a + c, c, 1)
+    CUo = np.zeros((ldc, ncol), dtype=dtype, order="F")
+    CVo = np.zeros((ldc, ncol), dtype=dtype, order="F")
+    CUo[:, :c] = CU[:, :c]
+    CVo[:, :c] = CV[:, :c]
+    ra, rb, rc = (np.array([v], dtype=dtype) for v in (a, b, c))
+    p = lambda x: x.ctypes.data_as(rp)  # noqa: E731
+    if fast:
+        L.HCORE_dgemm_fast(111, 112, M, M, alpha, p(AU), p(AV), p(ra), AU.shape[0], p(BU), p(BV),
+                           p(rb), BV.shape[0], beta, p(CUo), p(CVo), p(rc), ldc, rk, maxrk, acc,
+                           None)
+        fl = None
+    else:
+        fc = FlopCounter()
+        getattr(L, name)(111, 112, M, M, alpha, p(AU), p(AV), p(ra), AU.shape[0], p(BU), p(BV),
+                         p(rb), BV.shape[0], beta, p(CUo), p(CVo), p(rc), ldc, rk, maxrk, acc,
+                         None, C.byref(fc))
+        fl = fc.update
+    r = int(rc[0])
+    return r, CUo[:, :r].copy(order="F"), CVo[:, :r].copy(order="F"), fl
+
+
+def hcore_dgemm(M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, *, rk=0, maxrk, acc):
+    """HCORE_dgemm on host arrays (drop-in path). Returns (rank, CU, CV, flops)."""
+    return _lr_update("HCORE_dgemm", M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, rk, maxrk,
+                      acc, np.float64)
+
+
+def hcore_sgemm(M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, *, rk=0, maxrk, acc):
+    """HCORE_sgemm on host arrays (drop-in path). Returns (rank, CU, CV, flops)."""
+    return _lr_update("HCORE_sgemm", M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, rk, maxrk,
+                      acc, np.float32)
+
+
+def hcore_dgemm_fast(M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, *, rk=0, maxrk, acc):
+    """HCORE_dgemm_fast on host arrays. Returns (rank, CU, CV, None)."""
+    return _lr_update("HCORE_dgemm_fast", M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, rk,
+                      maxrk, acc, np.float64, fast=True)
+
+
+class Batch:
+    """A plan over many independent low-rank updates (device pointers).
+
+    ``tasks`` is a sequence of :class:`LrTask` whose pointers are device (or
+    pinned host) addresses, e.g. ``tensor.data_ptr()`` of column-major torch
+    tensors.  The plan allocates its workspace once; :meth:`execute` only
+    launches kernels (no allocation, no host synchronisation) and may be
+    captured in a CUDA graph.
+    """
+
+    def __init__(self, tasks, precision=F64, flags=0):
+        L = lib()
+        self.n = len(tasks)
+        self._tasks = (LrTask * max(self.n, 1))(*tasks)
+        self._plan = C.c_void_p()
+        _check(L.hcore_gpu_plan_create(C.byref(self._plan), precision, self.n, self._tasks, flags),
+               "hcore_gpu_plan_create")
+
+    def execute(self, stream=None):
+        _check(lib().hcore_gpu_plan_execute(self._plan, stream or None), "hcore_gpu_plan_execute")
+
+    def results(self, stream=None):
+        ranks = np.zeros(max(self.n, 1), dtype=np.int32)
+        status = np.zeros(max(self.n, 1), dtype=np.int32)
+        _check(lib().hcore_gpu_plan_results(self._plan, ranks.ctypes.data_as(_ip),
+                                            status.ctypes.data_as(_ip), stream or None),
+               "hcore_gpu_plan_results")
+        return ranks[:self.n], status[:self.n]
+
+    def sigma(self, i, stream=None):
+        k = C.c_int(0)
+        lib().hcore_gpu_plan_sigma(self._plan, i, None, C.byref(k), stream or None)
+        out = np.zeros(max(k.value, 1))
+        _check(lib().hcore_gpu_plan_sigma(self._plan, i, out.ctypes.data_as(_dp), C.byref(k),
+                                          stream or None), "hcore_gpu_plan_sigma")
+        return out[:k.value]
+
+    @property
+    def device_ranks_ptr(self) -> int:
+        return lib().hcore_gpu_plan_device_ranks(self._plan)
+
+    @property
+    def device_status_ptr(self) -> int:
+        return lib().hcore_gpu_plan_device_status(self._plan)
+
+    @property
+    def workspace_bytes(self) -> int:
+        return int(lib().hcore_gpu_plan_workspace_bytes(self._plan))
+
+    def close(self):
+        if self._plan:
+            lib().hcore_gpu_plan_destroy(self._plan)
+            self._plan = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def dense_batched(tasks, stream=None):
+    """Run HCORE_dsyrk / HCORE_dgemmcd tasks (device pointers) in one batch."""
+    arr = (DenseTask * max(len(tasks), 1))(*tasks)
+    _check(lib().hcore_gpu_dense_batched(len(tasks), arr, stream or None), "hcore_gpu_dense_batched")

@@ -1,0 +1,878 @@
+// hcore-gb300 — the reference's C entry points (include/hcore_d.h,
+// include/hcore_s.h) on the GPU, plus the batched dense-C API.
+//
+// Each drop-in call validates its arguments exactly where the reference
+// would exit(-1), stages pageable host buffers into a per-thread device
+// arena (device and pinned pointers are used in place), runs the same
+// kernels as the batched path with a batch of one on the calling thread's own
+// stream, copies the results back and updates the caller's flop counter with
+// the reference's model.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "hc_host.h"
+#include "hcore_d.h"
+#include "hcore_s.h"
+
+// ---- the reference's globals -------------------------------------------------
+extern "C" {
+int use_trmm = 0;           // hcore_dgemm.c:37 (no effect: T = R_A R_B^T either way)
+int gemm_print_index = 0;   // hcore_dgemm.c:41
+int gemm_print_mat = 0;     // hcore_dgemm.c:42
+int hc_nelm_limit = 512;    // hcore_dgemm.c:43
+int sgemm_use_trmm = 0;     // hcore_sgemm.c:37
+int sgemm_print_index = 0;  // hcore_sgemm.c:41
+int sgemm_print_mat = 0;    // hcore_sgemm.c:42
+int shc_nelm_limit = 512;   // hcore_sgemm.c:43
+int syrk_print_index = 0;   // hcore_dsyrk.c:21
+int gemmcd_print_index = 0; // hcore_dgemmcd.c:24
+int gemmcd_print_mat = 0;   // hcore_dgemmcd.c:25
+int gemmcd_use_scratch = 0; // hcore_dgemmcd.c:26
+// defined by the caller, as in the reference (hcore_dgemm.c:38); weak so that
+// a caller without it still links and reads 0
+extern int use_scratch __attribute__((weak));
+}
+
+namespace hc {
+
+static int scratch_mode() { return &use_scratch ? use_scratch : 0; }
+
+void fatal(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vfprintf(stderr, fmt, ap);
+    va_end(ap);
+    fflush(stderr);
+    exit(-1);
+}
+
+ThreadCtx::~ThreadCtx() {
+    // the runtime may already be shut down at thread/process exit: ignore errors
+    if (dev) cudaFree(dev);
+    if (pin) cudaFreeHost(pin);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+cudaError_t ThreadCtx::init() {
+    if (stream) return cudaSuccess;
+    return cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+}
+
+void *ThreadCtx::dev_ensure(size_t bytes) {
+    if (bytes <= dev_bytes) return dev;
+    if (dev) {
+        cudaStreamSynchronize(stream);
+        cudaFree(dev);
+    }
+    dev = nullptr;
+    dev_bytes = 0;
+    size_t want = std::max(bytes, (size_t)1 << 20);
+    if (cudaMalloc(&dev, want) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    dev_bytes = want;
+    return dev;
+}
+
+void *ThreadCtx::pin_ensure(size_t bytes) {
+    if (bytes <= pin_bytes) return pin;
+    if (pin) {
+        cudaStreamSynchronize(stream);
+        cudaFreeHost(pin);
+    }
+    pin = nullptr;
+    pin_bytes = 0;
+    size_t want = std::max(bytes, (size_t)1 << 16);
+    if (cudaMallocHost(&pin, want) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    pin_bytes = want;
+    return pin;
+}
+
+ThreadCtx &thread_ctx() {
+    static thread_local ThreadCtx ctx;
+    if (ctx.init() != cudaSuccess) fatal("hcore-gb300: cannot create a CUDA stream\n");
+    return ctx;
+}
+
+unsigned long flop_counts(char op, unsigned long a, unsigned long b, unsigned long c,
+                          unsigned long d) {
+    unsigned long res = 0;
+    if (op == 'q') {  // geqrf, m >= n; single-precision division as in flop_counts.c:7
+        const unsigned long m = a, n = b;
+        res = 2 * m * n * n - (unsigned long)((float)(2 * n * n * n) / 3.0f) + 2 * m * n +
+              (unsigned long)((float)(17 * n) / 3.0f);
+    } else if (op == 'm') {
+        res = a * b * c * 2;
+    } else if (op == 's') {
+        res = 22 * a * a * a;
+    } else if (op == 'o') {
+        const unsigned long m = a, n = b, k = c;
+        if (d == 1) res = 4 * n * m * k - 2 * n * k * k + 3 * n * k;
+        else if (d == 2) res = 4 * n * m * k - 2 * m * k * k + 2 * m * k + n * k - k * k / 2 + k / 2;
+    }
+    return res;
+}
+
+// flops of phase 1 (QR, factor products, SVD, scaling) of one update
+static unsigned long phase1_flops(int M, int a, int b, int c, int r, bool dense_b) {
+    const unsigned long k = (unsigned long)(a + c);
+    unsigned long f = flop_counts('q', M, k, 0, 0);
+    if (dense_b) f += flop_counts('m', M, a, M, 0);
+    else f += flop_counts('m', a, b, M, 0) + flop_counts('m', M, a, b, 0);
+    f += flop_counts('q', M, k, 0, 0) + flop_counts('s', k, 0, 0, 0) + (unsigned long)r * k;
+    return f;
+}
+static unsigned long phase2_flops(int M, int k, int r) {
+    return flop_counts('o', M, r, k, 1) + flop_counts('o', r, M, k, 2);
+}
+unsigned long update_flops(int M, int a, int b, int c, int r, bool dense_b) {
+    return phase1_flops(M, a, b, c, r, dense_b) + phase2_flops(M, a + c, r);
+}
+
+static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+// pinned staging of a single call: descriptor at 0, rank/status at kPinRankOff
+constexpr size_t kPinRankOff = 512, kPinBytes = 1024;
+static_assert(sizeof(Desc) <= kPinRankOff, "descriptor larger than its pinned slot");
+
+// ---- one update through the batched kernels --------------------------------
+template <typename T>
+struct Single {
+    ThreadCtx &tc;
+    hcore_lr_task t;
+    Desc d{};
+    WsLayout L{};
+    int k = 0;
+    char *arena = nullptr;
+    T *ws = nullptr;
+    Desc *d_desc = nullptr;
+    int *d_rs = nullptr;  // rank, status
+    T *stCU = nullptr, *stCV = nullptr;
+    bool out_staged = false;
+
+    explicit Single(const hcore_lr_task &task) : tc(thread_ctx()), t(task) {}
+
+    // copy a host (ld x ncol) block to a packed device block with ld = rows
+    void h2d(T *dst, const void *src, int rows, int ncol, int ld) {
+        if (ncol <= 0) return;
+        cudaMemcpy2DAsync(dst, rows * sizeof(T), src, (size_t)ld * sizeof(T), rows * sizeof(T),
+                          ncol, cudaMemcpyHostToDevice, tc.stream);
+    }
+
+    // Validate, stage and upload; returns the task status (0 = runnable) or
+    // -1 on a CUDA failure.  `ws_from_host` leaves the workspace for the
+    // caller to fill (split API, second half).
+    int prepare(unsigned flags) {
+        const int st = fill_desc(t, flags, false, d, k);
+        if (st) return st;
+        const int M = t.M, a = t.a, b = t.b, c = t.c;
+        L = ws_layout(M, a, b, k);
+        const bool dense_b = t.Bdense != nullptr;
+        bool dev_in = true;
+        for (const void *p : {a ? t.AU : nullptr, a ? t.AV : nullptr,
+                              dense_b ? t.Bdense : (b ? t.BU : nullptr),
+                              dense_b ? nullptr : (b ? t.BV : nullptr), c ? t.CU : nullptr,
+                              c ? t.CV : nullptr})
+            if (p && !is_device_memory(p)) dev_in = false;
+        const bool dev_out = is_device_memory(t.CUo) && is_device_memory(t.CVo);
+        size_t in_elems = dev_in ? 0
+                                 : (size_t)M * (2 * a + 2 * c) +
+                                       (dense_b ? (size_t)M * M : (size_t)2 * M * b);
+        size_t out_elems = dev_out ? 0 : (size_t)2 * M * k;
+        const size_t b_in = al256(in_elems * sizeof(T)), b_out = al256(out_elems * sizeof(T));
+        const size_t b_ws = al256((size_t)L.total * sizeof(T));
+        const size_t total = b_in + b_out + b_ws + al256(sizeof(Desc)) + 256;
+        arena = (char *)tc.dev_ensure(total);
+        Desc *pin = (Desc *)tc.pin_ensure(kPinBytes);
+        if (!arena || !pin) return -1;
+        T *in = (T *)arena;
+        stCU = (T *)(arena + b_in);
+        stCV = stCU + (size_t)M * k;
+        ws = (T *)(arena + b_in + b_out);
+        d_desc = (Desc *)(arena + b_in + b_out + b_ws);
+        d_rs = (int *)((char *)d_desc + al256(sizeof(Desc)));
+        if (!dev_in) {
+            T *p = in;
+            if (a) {
+                h2d(p, t.AU, M, a, t.lda); d.AU = p; p += (size_t)M * a;
+                h2d(p, t.AV, M, a, t.lda); d.AV = p; p += (size_t)M * a;
+                d.lda = M;
+            }
+            if (dense_b) {
+                if (a) { h2d(p, t.Bdense, M, M, t.ldb); d.Bd = p; p += (size_t)M * M; d.ldb = M; }
+            } else if (b) {
+                h2d(p, t.BU, M, b, t.ldb); d.BU = p; p += (size_t)M * b;
+                h2d(p, t.BV, M, b, t.ldb); d.BV = p; p += (size_t)M * b;
+                d.ldb = M;
+            }
+            if (c) {
+                h2d(p, t.CU, M, c, t.ldc); d.CU = p; p += (size_t)M * c;
+                h2d(p, t.CV, M, c, t.ldc); d.CV = p; p += (size_t)M * c;
+                d.ldc = M;
+            }
+        }
+        out_staged = !dev_out;
+        if (out_staged) {
+            d.CUo = stCU;
+            d.CVo = stCV;
+            d.ldco = M;
+        }
+        d.ws = 0;
+        d.idx = 0;
+        d.status0 = 0;
+        *pin = d;
+        cudaMemcpyAsync(d_desc, pin, sizeof(Desc), cudaMemcpyHostToDevice, tc.stream);
+        return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    }
+
+    // run phases, fetch rank and status
+    int run(unsigned phases, int *rank, int *status) {
+        cudaError_t e = launch_recompress<T>(d_desc, 1, ws, d_rs, d_rs + 1, t.M, k, tc.stream, phases);
+        int *pin = (int *)((char *)tc.pin_ensure(kPinBytes) + kPinRankOff);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(pin, d_rs, 2 * sizeof(int), cudaMemcpyDeviceToHost, tc.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(tc.stream);
+        if (e != cudaSuccess) return -1;
+        *rank = pin[0];
+        *status = pin[1];
+        return 0;
+    }
+
+    // copy r result columns back to the caller's CU/CV when they were staged
+    int fetch(int r) {
+        if (out_staged && r > 0) {
+            cudaMemcpy2DAsync(t.CUo, (size_t)t.ldco * sizeof(T), stCU, t.M * sizeof(T),
+                              t.M * sizeof(T), r, cudaMemcpyDeviceToHost, tc.stream);
+            cudaMemcpy2DAsync(t.CVo, (size_t)t.ldco * sizeof(T), stCV, t.M * sizeof(T),
+                              t.M * sizeof(T), r, cudaMemcpyDeviceToHost, tc.stream);
+        }
+        return cudaStreamSynchronize(tc.stream) == cudaSuccess ? 0 : -1;
+    }
+};
+
+static void cuda_fatal(const char *where) {
+    fatal("%s: CUDA error: %s\n", where, cudaGetErrorString(cudaGetLastError()));
+}
+
+// HCORE_dgemm / HCORE_sgemm / HCORE_dgemm_fast share this body.
+template <typename T>
+static void lr_update(const char *fn, int M, T alpha, T *AU, T *AV, T *Ark, int LDA, T *BU,
+                      T *BV, T *Brk, int LDB, T beta, T *CU, T *CV, T *Crk, int LDC, int rk,
+                      int maxrk, T acc, flop_counter *flops, bool fast) {
+    const int a = (int)Ark[0], b = (int)Brk[0], c = (int)Crk[0];
+    if (!fast && (a == 0 || b == 0 || c == 0))  // hcore_dgemm.c:743-746
+        fatal("%s: _Ark=%d _Brk=%d _Crk=%d. These rank values should not be zero.\n", fn, a, b, c);
+    if (!fast && a + c > 2 * maxrk)  // __qra, hcore_dgemm.c:91-95
+        fatal("%s: Sum of ranks (%d) is too big! _Ark:%d _Crk:%d maxrank:%d (x2: %d)\n", fn,
+              a + c, a, c, maxrk, 2 * maxrk);
+    if (!fast && maxrk < a + c)  // ld_newV = maxrk, hcore_dgemm.c:924-927
+        fatal("%s: Increase maxrank. %d is not enough ld_newV:%d CU_ncols:%d\n", fn, maxrk,
+              maxrk, a + c);
+    hcore_lr_task t{};
+    t.M = M; t.a = a; t.b = b; t.c = c; t.rk = rk; t.maxrk = maxrk; t.ld_newv = maxrk;
+    t.alpha = alpha; t.beta = beta; t.acc = acc;
+    t.AU = AU; t.AV = AV; t.lda = LDA; t.BU = BU; t.BV = BV; t.ldb = LDB;
+    t.CU = CU; t.CV = CV; t.ldc = LDC; t.CUo = CU; t.CVo = CV; t.ldco = LDC;
+    Single<T> s(t);
+    int st = s.prepare(fast ? HCORE_GPU_FAST_RULES : 0);
+    if (st < 0) cuda_fatal(fn);
+    if (st) fatal("%s: invalid update (status %d): M=%d ranks %d,%d,%d maxrk=%d\n", fn, st, M, a,
+                  b, c, maxrk);
+    int r = 0;
+    if (s.run(kPhaseAll, &r, &st)) cuda_fatal(fn);
+    if (st == HCORE_GPU_S_RANK_MAX)  // hcore_dgemm.c:465-468
+        fatal("%s: Rank after truncation is too big! finalrank:%d maxrank:%d\n", fn, r, maxrk);
+    if (st) fatal("%s: recompression failed (status %d)\n", fn, st);
+    if (s.fetch(r)) cuda_fatal(fn);
+    Crk[0] = (T)r;
+    if (flops) flops->update += update_flops(M, a, b, c, r, false);
+}
+
+// ---- split API (hcore_dgemm.c:1022-1699) -----------------------------------
+// The first half runs stack/QR/SVD on the GPU and returns the intermediate
+// state in host buffers laid out as the reference leaves them: _CU/_CV (the
+// clones) hold the two QR factorizations (M x CU_ncols, ld M), qrtauA/B the
+// reflector scalars, newU (ld nb) the left singular vectors and newV
+// (ld 2*maxrk) the rows S V^T.  The second half uploads that state and
+// rebuilds the factors into _CU_save/_CV_save.
+template <typename T>
+static void split_first_half(const char *fn, int M, T alpha, T *AU, T *AV, int *Ark, int LDA,
+                             T *BU, T *BV, int *Brk, T *Bdense, int LDB, T beta, T *CU, T *CV,
+                             int *Crk, int LDC, int rk, int storage_maxrank, int maxrk, T acc,
+                             T *work, flop_counter *flops, T **_p_work_new, T **_p__CU,
+                             T **_p__CV, int *_p_CU_ncols, int *_p_new_UVrk, T **_p_newU,
+                             int *_p_ld_newU, T **_p_qrtauA, int *_p_CV_ncols, T **_p_newV,
+                             int *_p_ld_newV, T **_p_qrtauB, int *_p_use_CUV_clone,
+                             T **_p_CUclone, int *_p_ld_CUclone, T **_p__CU_save, T **_p_CVclone,
+                             int *_p_ld_CVclone, T **_p__CV_save) {
+    const int a = Ark[0], b = Brk ? Brk[0] : 0, c = Crk[0];
+    const bool dense_b = Bdense != nullptr;
+    if (dense_b && (a == 0 || c == 0))  // hcore_dgemm.c:1077-1080
+        fatal("%s: _Ark=%d _Crk=%d. These rank values should not be zero.\n", fn, a, c);
+    if (a + c > 2 * maxrk)
+        fatal("%s: Sum of ranks (%d) is too big! _Ark:%d _Crk:%d maxrank:%d (x2: %d)\n", fn,
+              a + c, a, c, maxrk, 2 * maxrk);
+    if (a + c == 0)  // hcore_dgemm.c:1462-1465
+        fatal("%s: CU_ncols=0 CV_ncols=0. These values should not be zero.\n", fn);
+    const int k = a + c;
+    const int ld_newU = M, ld_newV = 2 * maxrk;  // :1479-1480
+    if (ld_newV < k)
+        fatal("%s: Increase computation maxrank. %d is not enough ld_newV:%d CU_ncols:%d\n", fn,
+              maxrk, ld_newV, k);
+    hcore_lr_task t{};
+    t.M = M; t.a = a; t.b = b; t.c = c; t.rk = rk; t.maxrk = maxrk; t.ld_newv = ld_newV;
+    t.alpha = alpha; t.beta = beta; t.acc = acc;
+    t.AU = AU; t.AV = AV; t.lda = LDA; t.BU = BU; t.BV = BV; t.ldb = LDB; t.Bdense = Bdense;
+    t.CU = CU; t.CV = CV; t.ldc = LDC; t.CUo = CU; t.CVo = CV; t.ldco = LDC;
+    Single<T> s(t);
+    int st = s.prepare(0);
+    if (st < 0) cuda_fatal(fn);
+    if (st) fatal("%s: invalid update (status %d)\n", fn, st);
+    int r = 0;
+    if (s.run(kPhaseStack | kPhaseQR | kPhaseSVD, &r, &st)) cuda_fatal(fn);
+    if (st == HCORE_GPU_S_RANK_MAX)
+        fatal("%s: Rank after truncation is too big! finalrank:%d maxrank:%d\n", fn, r, maxrk);
+    if (st) fatal("%s: recompression failed (status %d)\n", fn, st);
+
+    // host buffers in the reference's layout (:1395-1450, :1474-1495)
+    T *CUclone, *CVclone, *tauA, *tauB, *newU, *newV;
+    const size_t clone_n = (size_t)M * 2 * maxrk;
+    if (scratch_mode()) {
+        CUclone = work; work += clone_n;
+        CVclone = work; work += clone_n;
+        tauA = work;
+        tauB = work + M;
+        newU = work + 2 * M + (size_t)maxrk * maxrk;
+        newV = newU + (size_t)ld_newU * 2 * maxrk;
+    } else {
+        CUclone = (T *)malloc(clone_n * sizeof(T));
+        CVclone = (T *)malloc(clone_n * sizeof(T));
+        tauA = (T *)malloc((size_t)M * sizeof(T));
+        tauB = (T *)malloc((size_t)M * sizeof(T));
+        newU = (T *)malloc((size_t)ld_newU * 2 * maxrk * sizeof(T));
+        newV = (T *)malloc((size_t)M * ld_newV * sizeof(T));
+    }
+    cudaStream_t st_ = s.tc.stream;
+    const WsLayout &L = s.L;
+    cudaMemcpyAsync(CUclone, s.ws + L.UA, (size_t)M * k * sizeof(T), cudaMemcpyDeviceToHost, st_);
+    cudaMemcpyAsync(CVclone, s.ws + L.VB, (size_t)M * k * sizeof(T), cudaMemcpyDeviceToHost, st_);
+    cudaMemcpyAsync(tauA, s.ws + L.tauA, k * sizeof(T), cudaMemcpyDeviceToHost, st_);
+    cudaMemcpyAsync(tauB, s.ws + L.tauB, k * sizeof(T), cudaMemcpyDeviceToHost, st_);
+    std::vector<T> Uo((size_t)k * (r > 0 ? r : 1)), Vo((size_t)k * (r > 0 ? r : 1));
+    if (r > 0) {
+        cudaMemcpyAsync(Uo.data(), s.ws + L.Uo, (size_t)k * r * sizeof(T), cudaMemcpyDeviceToHost, st_);
+        cudaMemcpyAsync(Vo.data(), s.ws + L.Vo, (size_t)k * r * sizeof(T), cudaMemcpyDeviceToHost, st_);
+    }
+    if (cudaStreamSynchronize(st_) != cudaSuccess) cuda_fatal(fn);
+    for (int j = 0; j < r; ++j)
+        for (int i = 0; i < k; ++i) {
+            newU[(size_t)j * ld_newU + i] = Uo[(size_t)j * k + i];  // U(:, j)
+            newV[(size_t)i * ld_newV + j] = Vo[(size_t)j * k + i];  // (S V^T)(j, i)
+        }
+    if (flops) flops->update += phase1_flops(M, a, b, c, r, dense_b);
+    *_p_work_new = work;
+    *_p__CU = CUclone;
+    *_p__CV = CVclone;
+    *_p_CU_ncols = k;
+    *_p_new_UVrk = r;
+    *_p_newU = newU;
+    *_p_ld_newU = ld_newU;
+    *_p_qrtauA = tauA;
+    *_p_CV_ncols = k;
+    *_p_newV = newV;
+    *_p_ld_newV = ld_newV;
+    *_p_qrtauB = tauB;
+    *_p_use_CUV_clone = 1;
+    *_p_CUclone = CUclone;
+    *_p_ld_CUclone = M;
+    *_p__CU_save = CU;
+    *_p_CVclone = CVclone;
+    *_p_ld_CVclone = M;
+    *_p__CV_save = CV;
+}
+
+template <typename T>
+static void split_second_half(const char *fn, int M, int *Crk, int LDC, int storage_maxrank,
+                              flop_counter *flops, T *_CU, T *_CV, int CU_ncols, int new_UVrk,
+                              T *newU, int ld_newU, T *qrtauA, int CV_ncols, T *newV,
+                              int ld_newV, T *qrtauB, int use_CUV_clone, T *CUclone, T *_CU_save,
+                              T *CVclone, T *_CV_save) {
+    if (new_UVrk > storage_maxrank)  // hcore_dgemm.c:1648-1651
+        fatal("%s: Increase storage maxrank %d. Observed rank for U and V is %d\n", fn,
+              storage_maxrank, new_UVrk);
+    const int k = CU_ncols, r = new_UVrk;
+    if (CV_ncols != k || k > M) fatal("%s: inconsistent factor widths %d/%d\n", fn, CU_ncols, CV_ncols);
+    // a task whose first three phases are replaced by the uploaded state
+    hcore_lr_task t{};
+    t.M = M; t.a = k; t.b = 0; t.c = 0; t.rk = r > 0 ? r : 1; t.maxrk = k; t.ld_newv = k;
+    t.alpha = 1; t.beta = 1; t.acc = 0;
+    t.AU = _CU; t.AV = _CU; t.lda = M;
+    t.CUo = _CU_save; t.CVo = _CV_save; t.ldco = LDC;
+    Single<T> s(t);
+    int st = s.prepare(0);
+    if (st < 0) cuda_fatal(fn);
+    if (st) fatal("%s: invalid state (status %d)\n", fn, st);
+    if (r > 0) {
+        cudaStream_t st_ = s.tc.stream;
+        const WsLayout &L = s.L;
+        std::vector<T> Uo((size_t)k * r), Vo((size_t)k * r);
+        for (int j = 0; j < r; ++j)
+            for (int i = 0; i < k; ++i) {
+                Uo[(size_t)j * k + i] = newU[(size_t)j * ld_newU + i];
+                Vo[(size_t)j * k + i] = newV[(size_t)i * ld_newV + j];
+            }
+        cudaMemcpyAsync(s.ws + L.UA, _CU, (size_t)M * k * sizeof(T), cudaMemcpyHostToDevice, st_);
+        cudaMemcpyAsync(s.ws + L.VB, _CV, (size_t)M * k * sizeof(T), cudaMemcpyHostToDevice, st_);
+        cudaMemcpyAsync(s.ws + L.tauA, qrtauA, k * sizeof(T), cudaMemcpyHostToDevice, st_);
+        cudaMemcpyAsync(s.ws + L.tauB, qrtauB, k * sizeof(T), cudaMemcpyHostToDevice, st_);
+        cudaMemcpyAsync(s.ws + L.Uo, Uo.data(), (size_t)k * r * sizeof(T), cudaMemcpyHostToDevice, st_);
+        cudaMemcpyAsync(s.ws + L.Vo, Vo.data(), (size_t)k * r * sizeof(T), cudaMemcpyHostToDevice, st_);
+        const int rs[2] = {r, 0};
+        // the descriptor upload still reads the start of the pinned buffer;
+        // the rank slot lives past it
+        int *pin = (int *)((char *)s.tc.pin_ensure(kPinBytes) + kPinRankOff + 64);
+        pin[0] = rs[0];
+        pin[1] = rs[1];
+        cudaMemcpyAsync(s.d_rs, pin, 2 * sizeof(int), cudaMemcpyHostToDevice, st_);
+        int rr = 0, sst = 0;
+        if (s.run(kPhaseApply, &rr, &sst)) cuda_fatal(fn);
+        if (s.fetch(r)) cuda_fatal(fn);
+    }
+    if (use_CUV_clone == 1 && !scratch_mode()) {
+        free(CUclone);
+        free(CVclone);
+    }
+    if (!scratch_mode()) {
+        free(qrtauA);
+        free(qrtauB);
+        free(newU);
+        free(newV);
+    }
+    Crk[0] = r;
+    if (flops) flops->update += phase2_flops(M, k, r);
+}
+
+// ---- dense updates -----------------------------------------------------------
+struct DenseRun {
+    ThreadCtx &tc;
+    DenseRun() : tc(thread_ctx()) {}
+};
+
+// Run a list of dense tasks (device-accessible pointers) on stream s.
+static int run_dense(int n, const hcore_dense_task *tasks, cudaStream_t s, bool sync) {
+    if (n <= 0) return HCORE_GPU_OK;
+    // group tasks by output tile, keeping list order inside each group
+    std::map<const double *, int> gid;
+    std::vector<std::vector<int>> groups;
+    int maxM = 1;
+    std::vector<DenseWork> work(n);
+    long long ws = 0;
+    for (int i = 0; i < n; ++i) {
+        const hcore_dense_task &t = tasks[i];
+        if ((t.kind != 0 && t.kind != 1) || t.M < 1 || t.a < 0 || t.b < 0 || !t.CD ||
+            t.ldcd < t.M) {
+            set_error("hcore_gpu_dense_batched: invalid task %d", i);
+            return HCORE_GPU_EINVAL;
+        }
+        auto it = gid.find(t.CD);
+        if (it == gid.end()) {
+            gid[t.CD] = (int)groups.size();
+            groups.push_back({i});
+        } else {
+            if (tasks[groups[it->second][0]].M != t.M) {
+                set_error("hcore_gpu_dense_batched: tasks on one tile disagree on M");
+                return HCORE_GPU_EINVAL;
+            }
+            groups[it->second].push_back(i);
+        }
+        maxM = std::max(maxM, t.M);
+        DenseWork &w = work[i];
+        w.ws = ws;
+        const long long sq = t.kind == 0 ? (long long)t.a * t.a : (long long)t.a * t.b;
+        const int kk = t.kind == 0 ? t.a : std::min(t.a, t.b);
+        ws += ((sq + (long long)t.M * kk + 31) / 32) * 32;
+        w.syrk = t.kind == 0;
+        w.kk = kk;
+        w.coef = t.kind == 0 ? t.alpha : -1.0;
+    }
+    std::vector<int> gstart(groups.size() + 1, 0), gtasks;
+    for (size_t g = 0; g < groups.size(); ++g) {
+        gstart[g + 1] = gstart[g] + (int)groups[g].size();
+        for (int i : groups[g]) gtasks.push_back(i);
+    }
+    ThreadCtx &tc = thread_ctx();
+    const size_t b_tasks = al256(n * sizeof(hcore_dense_task)), b_work = al256(n * sizeof(DenseWork));
+    const size_t b_gs = al256(gstart.size() * sizeof(int)), b_gt = al256(gtasks.size() * sizeof(int));
+    const size_t b_ws = al256((size_t)ws * sizeof(double));
+    char *arena = (char *)tc.dev_ensure(b_tasks + b_work + b_gs + b_gt + b_ws);
+    char *pin = (char *)tc.pin_ensure(b_tasks + b_work + b_gs + b_gt);
+    if (!arena || !pin) {
+        set_error("hcore_gpu_dense_batched: out of memory");
+        return HCORE_GPU_ENOMEM;
+    }
+    double *d_ws = (double *)(arena + b_tasks + b_work + b_gs + b_gt);
+    for (int i = 0; i < n; ++i) {
+        const hcore_dense_task &t = tasks[i];
+        DenseWork &w = work[i];
+        const long long sq = t.kind == 0 ? (long long)t.a * t.a : (long long)t.a * t.b;
+        const double *computed = d_ws + w.ws + sq;
+        if (t.kind == 0) {
+            w.P = computed; w.ldp = t.M; w.Q = t.Au; w.ldq = t.lda;
+        } else if (t.a > t.b) {
+            w.P = computed; w.ldp = t.M; w.Q = t.Bu; w.ldq = t.M;
+        } else {
+            w.P = t.Au; w.ldp = t.M; w.Q = computed; w.ldq = t.M;
+        }
+    }
+    // the previous call on this stream may still read the pinned buffer
+    cudaStreamSynchronize(s);
+    memcpy(pin, tasks, n * sizeof(hcore_dense_task));
+    memcpy(pin + b_tasks, work.data(), n * sizeof(DenseWork));
+    memcpy(pin + b_tasks + b_work, gstart.data(), gstart.size() * sizeof(int));
+    memcpy(pin + b_tasks + b_work + b_gs, gtasks.data(), gtasks.size() * sizeof(int));
+    cudaMemcpyAsync(arena, pin, b_tasks + b_work + b_gs + b_gt, cudaMemcpyHostToDevice, s);
+    const hcore_dense_task *d_tasks = (const hcore_dense_task *)arena;
+    const DenseWork *d_work = (const DenseWork *)(arena + b_tasks);
+    cudaError_t e = launch_dense_prep(d_tasks, d_work, n, d_ws, s);
+    if (e == cudaSuccess)
+        e = launch_dense_tiles(d_tasks, d_work, (const int *)(arena + b_tasks + b_work),
+                               (const int *)(arena + b_tasks + b_work + b_gs), (int)groups.size(),
+                               maxM, s);
+    if (e == cudaSuccess && sync) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_error("hcore_gpu_dense_batched: %s", cudaGetErrorString(e));
+        return HCORE_GPU_ECUDA;
+    }
+    return HCORE_GPU_OK;
+}
+
+// stage one dense host block (rows x cols, ld) into dst (ld rows)
+static void stage(double *dst, const double *src, int rows, int cols, int ld, cudaStream_t s) {
+    if (cols > 0 && rows > 0)
+        cudaMemcpy2DAsync(dst, rows * sizeof(double), src, (size_t)ld * sizeof(double),
+                          rows * sizeof(double), cols, cudaMemcpyHostToDevice, s);
+}
+
+}  // namespace hc
+
+using namespace hc;
+
+extern "C" {
+
+void HCORE_dgemm(HCORE_enum transA, int transB, int M, int N, double alpha, double *AU,
+                 double *AV, double *Ark, int LDA, double *BU, double *BV, double *Brk, int LDB,
+                 double beta, double *CU, double *CV, double *Crk, int LDC, int rk, int maxrk,
+                 double acc, double *work, flop_counter *flops) {
+    (void)transA; (void)transB; (void)N; (void)work;
+    lr_update<double>("HCORE_dgemm", M, alpha, AU, AV, Ark, LDA, BU, BV, Brk, LDB, beta, CU, CV,
+                      Crk, LDC, rk, maxrk, acc, flops, false);
+}
+
+void HCORE_sgemm(HCORE_enum transA, HCORE_enum transB, int M, int N, float alpha, float *AU,
+                 float *AV, float *Ark, int LDA, float *BU, float *BV, float *Brk, int LDB,
+                 float beta, float *CU, float *CV, float *Crk, int LDC, int rk, int maxrk,
+                 float acc, float *work, flop_counter *flops) {
+    (void)transA; (void)transB; (void)N; (void)work;
+    lr_update<float>("HCORE_sgemm", M, alpha, AU, AV, Ark, LDA, BU, BV, Brk, LDB, beta, CU, CV,
+                     Crk, LDC, rk, maxrk, acc, flops, false);
+}
+
+void HCORE_dgemm_fast(HCORE_enum transA, int transB, int M, int N, double alpha, double *AU,
+                      double *AV, double *Ark, int LDA, double *BU, double *BV, double *Brk,
+                      int LDB, double beta, double *CU, double *CV, double *Crk, int LDC, int rk,
+                      int maxrk, double acc, double *work) {
+    (void)transA; (void)transB; (void)N; (void)work;
+    lr_update<double>("HCORE_dgemm_fast", M, alpha, AU, AV, Ark, LDA, BU, BV, Brk, LDB, beta, CU,
+                      CV, Crk, LDC, rk, maxrk, acc, nullptr, true);
+}
+
+void HCORE_dgemm_qr_svd(int transA, int transB, int M, int N, double alpha, double *AU,
+                        double *AV, int *Ark, int LDA, double *BU, double *BV, int *Brk, int LDB,
+                        double beta, double *CU, double *CV, int *Crk, int LDC, int rk,
+                        int storage_maxrank, int maxrk, double acc, double *work,
+                        flop_counter *flops, double **_p_work_new, double **_p__CU,
+                        double **_p__CV, int *_p_CU_ncols, int *_p_new_UVrk, double **_p_newU,
+                        int *_p_ld_newU, double **_p_qrtauA, int *_p_CV_ncols, double **_p_newV,
+                        int *_p_ld_newV, double **_p_qrtauB, int *_p_use_CUV_clone,
+                        double **_p_CUclone, int *_p_ld_CUclone, double **_p__CU_save,
+                        double **_p_CVclone, int *_p_ld_CVclone, double **_p__CV_save) {
+    (void)transA; (void)transB; (void)N;
+    split_first_half<double>("HCORE_dgemm_qr_svd", M, alpha, AU, AV, Ark, LDA, BU, BV, Brk,
+                             nullptr, LDB, beta, CU, CV, Crk, LDC, rk, storage_maxrank, maxrk,
+                             acc, work, flops, _p_work_new, _p__CU, _p__CV, _p_CU_ncols,
+                             _p_new_UVrk, _p_newU, _p_ld_newU, _p_qrtauA, _p_CV_ncols, _p_newV,
+                             _p_ld_newV, _p_qrtauB, _p_use_CUV_clone, _p_CUclone, _p_ld_CUclone,
+                             _p__CU_save, _p_CVclone, _p_ld_CVclone, _p__CV_save);
+}
+
+void HCORE_dgemm_qr_svd_b_dense(int transA, int transB, int M, int N, double alpha, double *AU,
+                                double *AV, int *Ark, int LDA, double *B, int LDB, double beta,
+                                double *CU, double *CV, int *Crk, int LDC, int rk,
+                                int storage_maxrank, int maxrk, double acc, double *work,
+                                flop_counter *flops, double **_p_work_new, double **_p__CU,
+                                double **_p__CV, int *_p_CU_ncols, int *_p_new_UVrk,
+                                double **_p_newU, int *_p_ld_newU, double **_p_qrtauA,
+                                int *_p_CV_ncols, double **_p_newV, int *_p_ld_newV,
+                                double **_p_qrtauB, int *_p_use_CUV_clone, double **_p_CUclone,
+                                int *_p_ld_CUclone, double **_p__CU_save, double **_p_CVclone,
+                                int *_p_ld_CVclone, double **_p__CV_save) {
+    (void)transA; (void)transB; (void)N;
+    split_first_half<double>("HCORE_dgemm_qr_svd_b_dense", M, alpha, AU, AV, Ark, LDA, nullptr,
+                             nullptr, nullptr, B, LDB, beta, CU, CV, Crk, LDC, rk,
+                             storage_maxrank, maxrk, acc, work, flops, _p_work_new, _p__CU,
+                             _p__CV, _p_CU_ncols, _p_new_UVrk, _p_newU, _p_ld_newU, _p_qrtauA,
+                             _p_CV_ncols, _p_newV, _p_ld_newV, _p_qrtauB, _p_use_CUV_clone,
+                             _p_CUclone, _p_ld_CUclone, _p__CU_save, _p_CVclone, _p_ld_CVclone,
+                             _p__CV_save);
+}
+
+void HCORE_dgemm_ormqr(int transA, int transB, int M, int N, double alpha, double *AU,
+                       double *AV, int *Ark, int LDA, double beta, double *CU, double *CV,
+                       int *Crk, int LDC, int rk, int storage_maxrank, int maxrk, double acc,
+                       double *work, flop_counter *flops, double *_CU, double *_CV,
+                       int CU_ncols, int new_UVrk, double *newU, int ld_newU, double *qrtauA,
+                       int CV_ncols, double *newV, int ld_newV, double *qrtauB,
+                       int use_CUV_clone, double *CUclone, int ld_CUclone, double *_CU_save,
+                       double *CVclone, int ld_CVclone, double *_CV_save) {
+    (void)transA; (void)transB; (void)N; (void)alpha; (void)AU; (void)AV; (void)Ark; (void)LDA;
+    (void)beta; (void)CU; (void)CV; (void)rk; (void)maxrk; (void)acc; (void)work;
+    (void)ld_CUclone; (void)ld_CVclone;
+    split_second_half<double>("HCORE_dgemm_ormqr", M, Crk, LDC, storage_maxrank, flops, _CU, _CV,
+                              CU_ncols, new_UVrk, newU, ld_newU, qrtauA, CV_ncols, newV, ld_newV,
+                              qrtauB, use_CUV_clone, CUclone, _CU_save, CVclone, _CV_save);
+}
+
+void HCORE_sgemm_qr_svd(int transA, int transB, int M, int N, float alpha, float *AU, float *AV,
+                        int *Ark, int LDA, float *BU, float *BV, int *Brk, int LDB, float beta,
+                        float *CU, float *CV, int *Crk, int LDC, int rk, int storage_maxrank,
+                        int maxrk, float acc, float *work, flop_counter *flops,
+                        float **_p_work_new, float **_p__CU, float **_p__CV, int *_p_CU_ncols,
+                        int *_p_new_UVrk, float **_p_newU, int *_p_ld_newU, float **_p_qrtauA,
+                        int *_p_CV_ncols, float **_p_newV, int *_p_ld_newV, float **_p_qrtauB,
+                        int *_p_use_CUV_clone, float **_p_CUclone, int *_p_ld_CUclone,
+                        float **_p__CU_save, float **_p_CVclone, int *_p_ld_CVclone,
+                        float **_p__CV_save) {
+    (void)transA; (void)transB; (void)N;
+    split_first_half<float>("HCORE_sgemm_qr_svd", M, alpha, AU, AV, Ark, LDA, BU, BV, Brk,
+                            nullptr, LDB, beta, CU, CV, Crk, LDC, rk, storage_maxrank, maxrk, acc,
+                            work, flops, _p_work_new, _p__CU, _p__CV, _p_CU_ncols, _p_new_UVrk,
+                            _p_newU, _p_ld_newU, _p_qrtauA, _p_CV_ncols, _p_newV, _p_ld_newV,
+                            _p_qrtauB, _p_use_CUV_clone, _p_CUclone, _p_ld_CUclone, _p__CU_save,
+                            _p_CVclone, _p_ld_CVclone, _p__CV_save);
+}
+
+void HCORE_sgemm_qr_svd_b_dense(int transA, int transB, int M, int N, float alpha, float *AU,
+                                float *AV, int *Ark, int LDA, float *B, int LDB, float beta,
+                                float *CU, float *CV, int *Crk, int LDC, int rk,
+                                int storage_maxrank, int maxrk, float acc, float *work,
+                                flop_counter *flops, float **_p_work_new, float **_p__CU,
+                                float **_p__CV, int *_p_CU_ncols, int *_p_new_UVrk,
+                                float **_p_newU, int *_p_ld_newU, float **_p_qrtauA,
+                                int *_p_CV_ncols, float **_p_newV, int *_p_ld_newV,
+                                float **_p_qrtauB, int *_p_use_CUV_clone, float **_p_CUclone,
+                                int *_p_ld_CUclone, float **_p__CU_save, float **_p_CVclone,
+                                int *_p_ld_CVclone, float **_p__CV_save) {
+    (void)transA; (void)transB; (void)N;
+    split_first_half<float>("HCORE_sgemm_qr_svd_b_dense", M, alpha, AU, AV, Ark, LDA, nullptr,
+                            nullptr, nullptr, B, LDB, beta, CU, CV, Crk, LDC, rk, storage_maxrank,
+                            maxrk, acc, work, flops, _p_work_new, _p__CU, _p__CV, _p_CU_ncols,
+                            _p_new_UVrk, _p_newU, _p_ld_newU, _p_qrtauA, _p_CV_ncols, _p_newV,
+                            _p_ld_newV, _p_qrtauB, _p_use_CUV_clone, _p_CUclone, _p_ld_CUclone,
+                            _p__CU_save, _p_CVclone, _p_ld_CVclone, _p__CV_save);
+}
+
+void HCORE_sgemm_ormqr(int transA, int transB, int M, int N, float alpha, float *AU, float *AV,
+                       int *Ark, int LDA, float beta, float *CU, float *CV, int *Crk, int LDC,
+                       int rk, int storage_maxrank, int maxrk, float acc, float *work,
+                       flop_counter *flops, float *_CU, float *_CV, int CU_ncols, int new_UVrk,
+                       float *newU, int ld_newU, float *qrtauA, int CV_ncols, float *newV,
+                       int ld_newV, float *qrtauB, int use_CUV_clone, float *CUclone,
+                       int ld_CUclone, float *_CU_save, float *CVclone, int ld_CVclone,
+                       float *_CV_save) {
+    (void)transA; (void)transB; (void)N; (void)alpha; (void)AU; (void)AV; (void)Ark; (void)LDA;
+    (void)beta; (void)CU; (void)CV; (void)rk; (void)maxrk; (void)acc; (void)work;
+    (void)ld_CUclone; (void)ld_CVclone;
+    split_second_half<float>("HCORE_sgemm_ormqr", M, Crk, LDC, storage_maxrank, flops, _CU, _CV,
+                             CU_ncols, new_UVrk, newU, ld_newU, qrtauA, CV_ncols, newV, ld_newV,
+                             qrtauB, use_CUV_clone, CUclone, _CU_save, CVclone, _CV_save);
+}
+
+void HCORE_dsyrk(HCORE_enum uplo, HCORE_enum trans, int M, int K, double alpha, const double *AU,
+                 int LDAU, const double *AV, int LDAV, double beta, double *CD, int LDCD,
+                 double *work, flop_counter *flops) {
+    (void)uplo; (void)trans; (void)LDAV; (void)beta; (void)work;
+    ThreadCtx &tc = thread_ctx();
+    const int N = LDAU;  // hcore_dsyrk.c:57: AV has LDAU rows, every factor ld is LDAU
+    hcore_dense_task t{};
+    t.kind = 0; t.M = M; t.a = K; t.alpha = alpha;
+    const bool dev = is_device_memory(AU) && is_device_memory(AV) && is_device_memory(CD);
+    double *stage_cd = nullptr;
+    if (dev) {
+        t.Au = AU; t.Av = AV; t.lda = LDAU; t.CD = CD; t.ldcd = LDCD;
+    } else {
+        const size_t nf = (size_t)N * K, nc = (size_t)M * M;
+        // the dense runner uses the thread arena itself; stage into a separate buffer
+        static thread_local double *buf = nullptr;
+        static thread_local size_t buf_n = 0;
+        if (buf_n < 2 * nf + nc) {
+            if (buf) cudaFree(buf);
+            buf = nullptr;
+            buf_n = 0;
+            if (cudaMalloc(&buf, (2 * nf + nc) * sizeof(double)) != cudaSuccess) cuda_fatal("HCORE_dsyrk");
+            buf_n = 2 * nf + nc;
+        }
+        stage(buf, AU, N, K, LDAU, tc.stream);
+        stage(buf + nf, AV, N, K, LDAU, tc.stream);
+        stage(buf + 2 * nf, CD, M, M, LDCD, tc.stream);
+        t.Au = buf; t.Av = buf + nf; t.lda = N; t.CD = buf + 2 * nf; t.ldcd = M;
+        stage_cd = buf + 2 * nf;
+    }
+    if (run_dense(1, &t, tc.stream, true)) fatal("HCORE_dsyrk: %s\n", last_error());
+    if (stage_cd) {
+        cudaMemcpy2DAsync(CD, (size_t)LDCD * sizeof(double), stage_cd, M * sizeof(double),
+                          M * sizeof(double), M, cudaMemcpyDeviceToHost, tc.stream);
+        if (cudaStreamSynchronize(tc.stream) != cudaSuccess) cuda_fatal("HCORE_dsyrk");
+    }
+    if (flops)  // hcore_dsyrk.c:104-188
+        flops->syrk += flop_counts('m', K, K, N, 0) + flop_counts('m', M, K, K, 0) +
+                       flop_counts('m', M, M, K, 0);
+}
+
+void HCORE_dgemmcd(HCORE_enum transA, HCORE_enum transB, int M, double alpha, double *Au,
+                   double *Av, int Arank, int LDA, double *Bu, double *Bv, int Brank, int LDB,
+                   double beta, double *CD, int LDC, int maxrank, double *work,
+                   flop_counter *flops) {
+    (void)transA; (void)transB; (void)alpha; (void)LDA; (void)LDB; (void)beta; (void)LDC;
+    (void)maxrank; (void)work; (void)flops;  // the reference counts no flops here
+    ThreadCtx &tc = thread_ctx();
+    hcore_dense_task t{};
+    t.kind = 1; t.M = M; t.a = Arank; t.b = Brank; t.alpha = -1.0;
+    const bool dev = is_device_memory(Au) && is_device_memory(Av) && is_device_memory(Bu) &&
+                     is_device_memory(Bv) && is_device_memory(CD);
+    double *stage_cd = nullptr;
+    if (dev) {
+        t.Au = Au; t.Av = Av; t.Bu = Bu; t.Bv = Bv; t.lda = M; t.ldb = M; t.CD = CD; t.ldcd = M;
+    } else {
+        const size_t na = (size_t)M * Arank, nb = (size_t)M * Brank, nc = (size_t)M * M;
+        static thread_local double *buf = nullptr;
+        static thread_local size_t buf_n = 0;
+        const size_t need = 2 * na + 2 * nb + nc;
+        if (buf_n < need) {
+            if (buf) cudaFree(buf);
+            buf = nullptr;
+            buf_n = 0;
+            if (cudaMalloc(&buf, need * sizeof(double)) != cudaSuccess) cuda_fatal("HCORE_dgemmcd");
+            buf_n = need;
+        }
+        // every leading dimension is M (hcore_dgemmcd.c:66-99)
+        stage(buf, Au, M, Arank, M, tc.stream);
+        stage(buf + na, Av, M, Arank, M, tc.stream);
+        stage(buf + 2 * na, Bu, M, Brank, M, tc.stream);
+        stage(buf + 2 * na + nb, Bv, M, Brank, M, tc.stream);
+        stage(buf + 2 * na + 2 * nb, CD, M, M, M, tc.stream);
+        t.Au = buf; t.Av = buf + na; t.Bu = buf + 2 * na; t.Bv = buf + 2 * na + nb;
+        t.lda = M; t.ldb = M; t.CD = buf + 2 * na + 2 * nb; t.ldcd = M;
+        stage_cd = t.CD;
+    }
+    if (run_dense(1, &t, tc.stream, true)) fatal("HCORE_dgemmcd: %s\n", last_error());
+    if (stage_cd) {
+        cudaMemcpyAsync(CD, stage_cd, (size_t)M * M * sizeof(double), cudaMemcpyDeviceToHost, tc.stream);
+        if (cudaStreamSynchronize(tc.stream) != cudaSuccess) cuda_fatal("HCORE_dgemmcd");
+    }
+}
+
+}  // extern "C"
+
+template <typename T>
+static void dense_gemm(const char *fn, int transA, int transB, int M, int N, int K, T alpha,
+                       const T *A, int LDA, const T *B, int LDB, T beta, T *C, int LDC) {
+    ThreadCtx &tc = thread_ctx();
+    const int ta = transA == HCORE_Trans || transA == HCORE_ConjTrans;
+    const int tb = transB == HCORE_Trans || transB == HCORE_ConjTrans;
+    const int ar = ta ? K : M, ac = ta ? M : K, br = tb ? N : K, bc = tb ? K : N;
+    const bool dev = is_device_memory(A) && is_device_memory(B) && is_device_memory(C);
+    if (dev) {
+        if (launch_gemm_dense<T>(ta, tb, M, N, K, alpha, A, LDA, B, LDB, beta, C, LDC, tc.stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(tc.stream) != cudaSuccess)
+            cuda_fatal(fn);
+        return;
+    }
+    const size_t na = (size_t)ar * ac, nb = (size_t)br * bc, nc = (size_t)M * N;
+    T *buf = (T *)tc.dev_ensure((na + nb + nc) * sizeof(T) + 256);
+    if (!buf) cuda_fatal(fn);
+    T *dA = buf, *dB = buf + na, *dC = buf + na + nb;
+    auto h2d = [&](T *dst, const T *src, int rows, int cols, int ld) {
+        if (rows > 0 && cols > 0)
+            cudaMemcpy2DAsync(dst, rows * sizeof(T), src, (size_t)ld * sizeof(T), rows * sizeof(T),
+                              cols, cudaMemcpyHostToDevice, tc.stream);
+    };
+    h2d(dA, A, ar, ac, LDA);
+    h2d(dB, B, br, bc, LDB);
+    h2d(dC, C, M, N, LDC);
+    if (launch_gemm_dense<T>(ta, tb, M, N, K, alpha, dA, ar, dB, br, beta, dC, M, tc.stream) !=
+        cudaSuccess)
+        cuda_fatal(fn);
+    if (M > 0 && N > 0)
+        cudaMemcpy2DAsync(C, (size_t)LDC * sizeof(T), dC, M * sizeof(T), M * sizeof(T), N,
+                          cudaMemcpyDeviceToHost, tc.stream);
+    if (cudaStreamSynchronize(tc.stream) != cudaSuccess) cuda_fatal(fn);
+}
+
+extern "C" {
+
+void HCORE_dgemm_dense(HCORE_enum transA, int transB, int M, int N, int K, double alpha,
+                       const double *A, int LDA, const double *B, int LDB, double beta,
+                       double *C, int LDC) {
+    dense_gemm<double>("HCORE_dgemm_dense", transA, transB, M, N, K, alpha, A, LDA, B, LDB, beta,
+                       C, LDC);
+}
+
+void HCORE_sgemm_dense(HCORE_enum transA, int transB, int M, int N, int K, float alpha,
+                       const float *A, int LDA, const float *B, int LDB, float beta, float *C,
+                       int LDC) {
+    dense_gemm<float>("HCORE_sgemm_dense", transA, transB, M, N, K, alpha, A, LDA, B, LDB, beta,
+                      C, LDC);
+}
+
+int hcore_gpu_dense_batched(int n, const hcore_dense_task *tasks, void *stream) {
+    if (n < 0 || (n > 0 && !tasks)) {
+        set_error("hcore_gpu_dense_batched: invalid argument");
+        return HCORE_GPU_EINVAL;
+    }
+    // translate pinned host pointers to their device aliases
+    std::vector<hcore_dense_task> tt(tasks, tasks + n);
+    for (auto &t : tt) {
+        t.Au = (const double *)device_alias(t.Au);
+        t.Av = (const double *)device_alias(t.Av);
+        if (t.kind == 1) {
+            t.Bu = (const double *)device_alias(t.Bu);
+            t.Bv = (const double *)device_alias(t.Bv);
+            if (!t.Bu || !t.Bv) {
+                set_error("hcore_gpu_dense_batched: B factors are not device-accessible");
+                return HCORE_GPU_EINVAL;
+            }
+        }
+        t.CD = (double *)device_alias(t.CD);
+        if (!t.Au || !t.Av || !t.CD) {
+            set_error("hcore_gpu_dense_batched: pointers must be device or pinned memory");
+            return HCORE_GPU_EINVAL;
+        }
+    }
+    return run_dense(n, tt.data(), (cudaStream_t)stream, true);
+}
+
+void *hcore_gpu_thread_stream(void) { return (void *)thread_ctx().stream; }
+
+}  // extern "C"

@@ -1,0 +1,93 @@
+// hcore-gb300 internal definitions shared by the kernels and the host API.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hcore_gb300.h"
+
+namespace hc {
+
+// Per-update descriptor as the kernels see it (device resident, one per task).
+// All pointers are device-accessible (device memory, or pinned host memory
+// through its device alias).  Offsets are in elements of the plan's scalar.
+struct Desc {
+    const void *AU, *AV, *BU, *BV, *Bd, *CU, *CV;
+    void *CUo, *CVo;
+    long long ws;        // start of this update's workspace
+    double alpha, beta, acc;
+    int lda, ldb, ldc, ldco;
+    int M, a, b, c, k;
+    int rk;              // fixed output rank (0: by acc)
+    int max_rank;        // largest accepted new rank (reference: maxrk)
+    int storage_rank;    // second limit (split API storage_maxrank), INT_MAX if none
+    int rank_start;      // rank search starts here (1, or 2 for the fast rules)
+    int status0;         // non-zero: rejected on the host, skip
+    int idx;             // task index (rank/status slots)
+    int pad_;
+};
+
+// Workspace layout of one update (element offsets from Desc::ws), k = a + c:
+//   UA  M*k   stacked [beta CU | alpha AU], then its QR (R on top, reflectors below)
+//   VB  M*k   stacked [CV | G], then its QR
+//   tauA k, tauB k, sig k
+//   F   a*b   AV^T BV
+//   W   k*k   Jacobi working matrix (used when it does not fit shared memory)
+//   V   k*k   Jacobi right vectors (same)
+//   Uo  k*k   U_r (k x r, ld k)
+//   Vo  k*k   V_r S_r (k x r, ld k)
+struct WsLayout {
+    long long UA, VB, tauA, tauB, sig, F, W, V, Uo, Vo, total;
+};
+
+__host__ __device__ inline long long hc_align32(long long x) { return (x + 31) & ~31LL; }
+
+__host__ __device__ inline WsLayout ws_layout(int M, int a, int b, int k) {
+    WsLayout L;
+    long long o = 0;
+    L.UA = o; o = hc_align32(o + (long long)M * k);
+    L.VB = o; o = hc_align32(o + (long long)M * k);
+    L.tauA = o; o = hc_align32(o + k);
+    L.tauB = o; o = hc_align32(o + k);
+    L.sig = o; o = hc_align32(o + k);
+    L.F = o; o = hc_align32(o + (long long)a * b);
+    L.W = o; o = hc_align32(o + (long long)k * k);
+    L.V = o; o = hc_align32(o + (long long)k * k);
+    L.Uo = o; o = hc_align32(o + (long long)k * k);
+    L.Vo = o; o = hc_align32(o + (long long)k * k);
+    L.total = o;
+    return L;
+}
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxSweeps = 60;
+constexpr int kMaxRowsPerLane = 64;  // apply kernel keeps a column in registers: M <= 2048
+
+constexpr unsigned kPhaseStack = 1u, kPhaseQR = 2u, kPhaseSVD = 4u, kPhaseApply = 8u;
+constexpr unsigned kPhaseAll = 15u;
+constexpr int kMaxK = 512;  // largest a + c a plan accepts
+
+// launchers (hc_kernels.cu)
+template <typename T>
+cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int *d_status,
+                              int maxM, int maxK, cudaStream_t s, unsigned phases);
+
+// dense-C updates (hc_dense.cu): per-task rank-K' form coef * P Q^T
+struct DenseWork {
+    const double *P;  // M x K' (ldp): computed into the workspace, or an input factor
+    const double *Q;  // M x K' (ldq)
+    int ldp, ldq, kk;
+    double coef;
+    int syrk;         // 1: zero the strict upper triangle after this task
+    long long ws;     // workspace offset (doubles): S (p x q), then the computed factor
+};
+cudaError_t launch_dense_prep(const hcore_dense_task *d_tasks, const DenseWork *d_work, int n,
+                              double *ws, cudaStream_t s);
+cudaError_t launch_dense_tiles(const hcore_dense_task *d_tasks, const DenseWork *d_work,
+                               const int *d_group_start, const int *d_group_tasks, int ngroups,
+                               int maxM, cudaStream_t s);
+template <typename T>
+cudaError_t launch_gemm_dense(int ta, int tb, int M, int N, int K, T alpha, const T *A, int lda,
+                              const T *B, int ldb, T beta, T *C, int ldc, cudaStream_t s);
+
+}  // namespace hc

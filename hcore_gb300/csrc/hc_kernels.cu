@@ -1,0 +1,455 @@
+// hcore-gb300 — batched low-rank recompression kernels for sm_103a.
+//
+// One Schur update C <- beta*C + alpha*A*B^T (A, B, C in U*V^T form) follows
+// the reference HCORE_dgemm (src/compute/hcore_dgemm.c:703-1012) as four
+// batched phases, each a grid over the updates of the batch:
+//
+//   1. stack  (hcore_dgemm.c:79-225)  UA = [beta*CU | alpha*AU],
+//              F = AV^T BV, G = BU F^T, VB = [CV | G]            -> workspace
+//   2. geqrf  (hcore_dgemm.c:123, :216) Householder QR of UA and VB
+//              (blockIdx.y selects the side), LAPACK dlarfg conventions
+//   3. gesvd  (hcore_dgemm.c:296-503) T = R_A R_B^T, one-sided Jacobi SVD,
+//              singular values sorted, rank rule, U_r and V_r S_r
+//   4. apply  (hcore_dgemm.c:508-696) CU = Q_A [U_r; 0], CV = Q_B [V_r S_r; 0]
+//              written straight into the caller's output factors
+//
+// The scalar type T is double (HCORE_dgemm) or float (HCORE_sgemm); every
+// step computes in T, like the reference's two copies.
+#include <cfloat>
+#include <climits>
+
+#include "hc_internal.h"
+
+namespace hc {
+
+template <typename T>
+struct Lim;
+template <>
+struct Lim<double> {
+    static constexpr double eps = DBL_EPSILON;
+    static constexpr double big_zeta = 1e150;
+};
+template <>
+struct Lim<float> {
+    static constexpr float eps = FLT_EPSILON;
+    static constexpr float big_zeta = 1e18f;
+};
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// phase 1: stack the factors
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kThreads) stack_kernel(const Desc *__restrict__ descs,
+                                                         T *__restrict__ ws) {
+    const Desc d = descs[blockIdx.x];
+    if (d.status0) return;
+    const int M = d.M, a = d.a, b = d.b, c = d.c, k = d.k;
+    const WsLayout L = ws_layout(M, a, b, k);
+    T *UA = ws + d.ws + L.UA;
+    T *VB = ws + d.ws + L.VB;
+    T *F = ws + d.ws + L.F;
+    const T alpha = (T)d.alpha, beta = (T)d.beta;
+    const T *CU = (const T *)d.CU, *CV = (const T *)d.CV;
+    const T *AU = (const T *)d.AU, *AV = (const T *)d.AV;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    // [beta*CU | alpha*AU] and [CV | .] (hcore_dgemm.c:106-114, :199-205)
+    for (long long e = tid; e < (long long)M * c; e += kThreads) {
+        const int i = (int)(e % M), j = (int)(e / M);
+        UA[(size_t)j * M + i] = beta * CU[(size_t)j * d.ldc + i];
+        VB[(size_t)j * M + i] = CV[(size_t)j * d.ldc + i];
+    }
+    for (long long e = tid; e < (long long)M * a; e += kThreads) {
+        const int i = (int)(e % M), j = (int)(e / M);
+        UA[(size_t)(c + j) * M + i] = alpha * AU[(size_t)j * d.lda + i];
+    }
+    if (a == 0) return;
+    T *G = VB + (size_t)c * M;
+    if (d.Bd) {
+        // dense B: G = B * AV (hcore_dgemm.c:262-271)
+        const T *B = (const T *)d.Bd;
+        for (long long e = tid; e < (long long)M * a; e += kThreads) {
+            const int i = (int)(e % M), j = (int)(e / M);
+            T s = 0;
+            for (int l = 0; l < M; ++l) s += B[(size_t)l * d.ldb + i] * AV[(size_t)j * d.lda + l];
+            G[(size_t)j * M + i] = s;
+        }
+        return;
+    }
+    const T *BU = (const T *)d.BU, *BV = (const T *)d.BV;
+    // F = AV^T BV, a x b, one warp per entry (hcore_dgemm.c:175-178)
+    for (int e = warp; e < a * b; e += kWarps) {
+        const int p = e % a, q = e / a;
+        const T *x = AV + (size_t)p * d.lda;
+        const T *y = BV + (size_t)q * d.ldb;
+        T s = 0;
+        for (int l = lane; l < M; l += 32) s += x[l] * y[l];
+        s = warp_sum(s);
+        if (lane == 0) F[(size_t)q * a + p] = s;
+    }
+    __syncthreads();
+    // G = BU F^T, M x a (hcore_dgemm.c:199-205)
+    for (long long e = tid; e < (long long)M * a; e += kThreads) {
+        const int i = (int)(e % M), p = (int)(e / M);
+        T s = 0;
+        for (int q = 0; q < b; ++q) s += BU[(size_t)q * d.ldb + i] * F[(size_t)q * a + p];
+        G[(size_t)p * M + i] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// phase 2: Householder QR of UA (blockIdx.y = 0) or VB (blockIdx.y = 1)
+// ---------------------------------------------------------------------------
+// Reflector j is H_j = I - tau_j v v^T with v(j) = 1, v(i<j) = 0 and v(i>j)
+// stored below the diagonal, beta = -sign(alpha)*||x||, tau = (beta-alpha)/beta
+// (LAPACK dlarfg); ||x|| = 0 gives tau = 0.  R ends up on and above the
+// diagonal, as dgeqrf leaves it.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) geqrf_kernel(const Desc *__restrict__ descs,
+                                                         T *__restrict__ ws) {
+    extern __shared__ unsigned char smem_raw[];
+    T *sv = reinterpret_cast<T *>(smem_raw);  // current reflector, M entries
+    __shared__ T s_tau;
+    const Desc d = descs[blockIdx.x];
+    if (d.status0) return;
+    const int M = d.M, k = d.k;
+    const WsLayout L = ws_layout(M, d.a, d.b, k);
+    const int side = blockIdx.y;
+    T *A = ws + d.ws + (side ? L.VB : L.UA);
+    T *tau = ws + d.ws + (side ? L.tauB : L.tauA);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    for (int j = 0; j < k; ++j) {
+        T *Aj = A + (size_t)j * M;
+        if (warp == 0) {
+            const T alpha = Aj[j];
+            T amax = 0;
+            for (int i = j + 1 + lane; i < M; i += 32) amax = max(amax, abs(Aj[i]));
+            amax = warp_max(amax);
+            T xnorm = 0;
+            if (amax > 0) {
+                const T inv = T(1) / amax;
+                T ss = 0;
+                for (int i = j + 1 + lane; i < M; i += 32) {
+                    const T t = Aj[i] * inv;
+                    ss += t * t;
+                }
+                xnorm = amax * sqrt(warp_sum(ss));
+            }
+            T tj = 0, beta = alpha;
+            if (xnorm > 0) {
+                beta = -copysign(hypot(alpha, xnorm), alpha);
+                tj = (beta - alpha) / beta;
+                const T scal = T(1) / (alpha - beta);
+                for (int i = j + 1 + lane; i < M; i += 32) {
+                    const T v = Aj[i] * scal;
+                    Aj[i] = v;
+                    sv[i] = v;
+                }
+            } else {
+                for (int i = j + 1 + lane; i < M; i += 32) sv[i] = Aj[i];
+            }
+            if (lane == 0) {
+                Aj[j] = beta;
+                tau[j] = tj;
+                s_tau = tj;
+                sv[j] = T(1);
+            }
+        }
+        __syncthreads();
+        const T tj = s_tau;
+        if (tj != T(0)) {
+            for (int col = j + 1 + warp; col < k; col += kWarps) {
+                T *Ac = A + (size_t)col * M;
+                T dot = 0;
+                for (int i = j + lane; i < M; i += 32) dot += sv[i] * Ac[i];
+                const T s = tj * warp_sum(dot);
+                for (int i = j + lane; i < M; i += 32) Ac[i] -= s * sv[i];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// phase 3: T = R_A R_B^T, one-sided Jacobi SVD, rank rule
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void rr_pair(int round, int pi, int n, int &p, int &q) {
+    // circle-method tournament on n (even) columns: n/2 disjoint pairs per
+    // round, every pair exactly once in n-1 rounds
+    if (pi == 0) {
+        p = n - 1;
+        q = round;
+    } else {
+        p = (round + pi) % (n - 1);
+        q = (round - pi + (n - 1)) % (n - 1);
+    }
+}
+
+
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict__ descs,
+                                                         T *__restrict__ ws, int *__restrict__ rank,
+                                                         int *__restrict__ status, int smem_kmax) {
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ T s_sig[kMaxK];
+    __shared__ int s_perm[kMaxK];
+    __shared__ int s_rot;
+    const Desc d = descs[blockIdx.x];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (d.status0) {
+        if (tid == 0) {
+            status[d.idx] = d.status0;
+            rank[d.idx] = 0;
+        }
+        return;
+    }
+    const int M = d.M, k = d.k;
+    const WsLayout L = ws_layout(M, d.a, d.b, k);
+    T *base = ws + d.ws;
+    const T *UA = base + L.UA, *VB = base + L.VB;
+    const bool in_smem = k <= smem_kmax;
+    T *W = in_smem ? reinterpret_cast<T *>(smem_raw) : base + L.W;
+    T *V = in_smem ? W + (size_t)k * k : base + L.V;
+
+    // T = triu(R_A) triu(R_B)^T  (hcore_dgemm.c:330-387)
+    for (int e = tid; e < k * k; e += kThreads) {
+        const int i = e % k, j = e / k;
+        T s = 0;
+        for (int l = max(i, j); l < k; ++l) s += UA[(size_t)l * M + i] * VB[(size_t)l * M + j];
+        W[(size_t)j * k + i] = s;
+        V[(size_t)j * k + i] = (i == j) ? T(1) : T(0);
+    }
+    __syncthreads();
+
+    // one-sided (Hestenes) Jacobi: rotate column pairs of W until all are
+    // orthogonal to tol; V accumulates the rotations, so T V = W throughout
+    const int n = k + (k & 1);
+    const T tol = sqrt(T(k)) * Lim<T>::eps;
+    bool converged = (k == 1);
+    for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
+        if (tid == 0) s_rot = 0;
+        __syncthreads();
+        for (int round = 0; round < n - 1; ++round) {
+            for (int pi = warp; pi < n / 2; pi += kWarps) {
+                int p, q;
+                rr_pair(round, pi, n, p, q);
+                if (p >= k || q >= k) continue;
+                T *wp = W + (size_t)p * k, *wq = W + (size_t)q * k;
+                T app = 0, aqq = 0, apq = 0;
+                for (int i = lane; i < k; i += 32) {
+                    const T x = wp[i], y = wq[i];
+                    app += x * x;
+                    aqq += y * y;
+                    apq += x * y;
+                }
+                app = warp_sum(app);
+                aqq = warp_sum(aqq);
+                apq = warp_sum(apq);
+                if (apq != T(0) && abs(apq) > tol * sqrt(app) * sqrt(aqq)) {
+                    const T zeta = (aqq - app) / (T(2) * apq);
+                    const T az = abs(zeta);
+                    const T t = az > Lim<T>::big_zeta ? T(0.5) / zeta
+                                                      : copysign(T(1), zeta) / (az + sqrt(T(1) + az * az));
+                    const T cs = T(1) / sqrt(T(1) + t * t);
+                    const T sn = cs * t;
+                    for (int i = lane; i < k; i += 32) {
+                        const T x = wp[i], y = wq[i];
+                        wp[i] = cs * x - sn * y;
+                        wq[i] = sn * x + cs * y;
+                    }
+                    T *vp = V + (size_t)p * k, *vq = V + (size_t)q * k;
+                    for (int i = lane; i < k; i += 32) {
+                        const T x = vp[i], y = vq[i];
+                        vp[i] = cs * x - sn * y;
+                        vq[i] = sn * x + cs * y;
+                    }
+                    if (lane == 0) s_rot = 1;
+                }
+                __syncwarp();
+            }
+            __syncthreads();
+        }
+        const int rot = s_rot;
+        __syncthreads();
+        converged = (rot == 0);
+    }
+
+    // singular values = column norms; sort descending (ties by index)
+    for (int j = warp; j < k; j += kWarps) {
+        const T *wj = W + (size_t)j * k;
+        T s = 0;
+        for (int i = lane; i < k; i += 32) s += wj[i] * wj[i];
+        s = warp_sum(s);
+        if (lane == 0) s_sig[j] = sqrt(s);
+    }
+    __syncthreads();
+    for (int j = tid; j < k; j += kThreads) {
+        const T sj = s_sig[j];
+        int pos = 0;
+        for (int i = 0; i < k; ++i) {
+            const T si = s_sig[i];
+            pos += (si > sj) || (si == sj && i < j);
+        }
+        s_perm[pos] = j;
+    }
+    __syncthreads();
+    T *sig_out = base + L.sig;
+    for (int t = tid; t < k; t += kThreads) sig_out[t] = s_sig[s_perm[t]];
+
+    // rank rule (hcore_dgemm.c:444-464; the fast rules start at i = 2)
+    int r;
+    if (d.rk != 0) {
+        r = d.rk < k ? d.rk : k;
+    } else {
+        r = k;
+        for (int i = d.rank_start; i < k; ++i)
+            if (s_sig[s_perm[i]] < (T)d.acc) {
+                r = i;
+                break;
+            }
+    }
+    int st = HCORE_GPU_S_OK;
+    if (!converged) st = HCORE_GPU_S_NOCONV;
+    else if (r > d.max_rank) st = HCORE_GPU_S_RANK_MAX;
+    else if (r > d.storage_rank) st = HCORE_GPU_S_STORAGE;
+
+    // U_r = W(:, perm) / sigma, V_r S_r = V(:, perm) * sigma  (:484-489)
+    T *Uo = base + L.Uo, *Vo = base + L.Vo;
+    for (int e = tid; e < k * r; e += kThreads) {
+        const int i = e % k, t = e / k;
+        const int j = s_perm[t];
+        const T s = s_sig[j];
+        Uo[(size_t)t * k + i] = s > T(0) ? W[(size_t)j * k + i] / s : T(0);
+        Vo[(size_t)t * k + i] = V[(size_t)j * k + i] * s;
+    }
+    if (tid == 0) {
+        rank[d.idx] = r;
+        status[d.idx] = st;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// phase 4: CU = Q_A [U_r; 0], CV = Q_B [V_r S_r; 0]   (dormqr 'L','N')
+// ---------------------------------------------------------------------------
+// One warp owns one output column and keeps it in registers (RPL rows per
+// lane, row i = lane + 32*t); the k reflectors are applied last to first and
+// the column is stored once, coalesced, into the caller's factor.
+template <typename T, int RPL>
+__global__ void __launch_bounds__(kThreads) apply_kernel(const Desc *__restrict__ descs,
+                                                         const T *__restrict__ ws,
+                                                         const int *__restrict__ rank,
+                                                         const int *__restrict__ status) {
+    __shared__ T s_tau[kMaxK];
+    const Desc d = descs[blockIdx.x];
+    if (d.status0 || status[d.idx] != HCORE_GPU_S_OK) return;
+    const int side = blockIdx.y;
+    const int M = d.M, k = d.k, r = rank[d.idx];
+    const WsLayout L = ws_layout(M, d.a, d.b, k);
+    const T *base = ws + d.ws;
+    const T *Y = base + (side ? L.VB : L.UA);
+    const T *tau = base + (side ? L.tauB : L.tauA);
+    const T *X0 = base + (side ? L.Vo : L.Uo);
+    T *out = (T *)(side ? d.CVo : d.CUo);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < k; i += kThreads) s_tau[i] = tau[i];
+    __syncthreads();
+
+    for (int col = warp; col < r; col += kWarps) {
+        T x[RPL];
+#pragma unroll
+        for (int t = 0; t < RPL; ++t) {
+            const int i = lane + 32 * t;
+            x[t] = (i < k) ? X0[(size_t)col * k + i] : T(0);
+        }
+        for (int j = k - 1; j >= 0; --j) {
+            const T tj = s_tau[j];
+            if (tj == T(0)) continue;
+            const T *y = Y + (size_t)j * M;
+            T dot = 0;
+#pragma unroll
+            for (int t = 0; t < RPL; ++t) {
+                const int i = lane + 32 * t;
+                if (i >= j && i < M) dot += (i == j ? T(1) : y[i]) * x[t];
+            }
+            const T s = tj * warp_sum(dot);
+#pragma unroll
+            for (int t = 0; t < RPL; ++t) {
+                const int i = lane + 32 * t;
+                if (i >= j && i < M) x[t] -= s * (i == j ? T(1) : y[i]);
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < RPL; ++t) {
+            const int i = lane + 32 * t;
+            if (i < M) out[(size_t)col * d.ldco + i] = x[t];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+static size_t svd_smem_bytes(int k) {
+    return 2 * (size_t)k * k * sizeof(T);
+}
+
+template <typename T, int RPL>
+static void launch_apply(const Desc *d_desc, int n, const T *ws, const int *d_rank,
+                         const int *d_status, cudaStream_t s) {
+    apply_kernel<T, RPL><<<dim3(n, 2), kThreads, 0, s>>>(d_desc, ws, d_rank, d_status);
+}
+
+template <typename T>
+cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int *d_status,
+                              int maxM, int maxK, cudaStream_t s, unsigned phases) {
+    if (n <= 0) return cudaSuccess;
+    if (maxK > kMaxK || maxM > 32 * kMaxRowsPerLane) return cudaErrorInvalidValue;
+    if (phases & kPhaseStack) stack_kernel<T><<<n, kThreads, 0, s>>>(d_desc, ws);
+    if (phases & kPhaseQR)
+        geqrf_kernel<T><<<dim3(n, 2), kThreads, (size_t)maxM * sizeof(T), s>>>(d_desc, ws);
+    if (phases & kPhaseSVD) {
+        // Jacobi matrices in shared memory when both fit (k <= 117 in FP64)
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        const size_t static_smem = kMaxK * (sizeof(T) + sizeof(int)) + 64;
+        int smem_kmax = 0;
+        while (smem_kmax < maxK && svd_smem_bytes<T>(smem_kmax + 1) + static_smem <= (size_t)optin)
+            ++smem_kmax;
+        const size_t dyn = svd_smem_bytes<T>(smem_kmax < maxK ? smem_kmax : maxK);
+        cudaFuncSetAttribute(gesvd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)dyn);
+        gesvd_kernel<T><<<n, kThreads, dyn, s>>>(d_desc, ws, d_rank, d_status, smem_kmax);
+    }
+    if (phases & kPhaseApply) {
+        const int rpl = (maxM + 31) / 32;
+        if (rpl <= 4) launch_apply<T, 4>(d_desc, n, ws, d_rank, d_status, s);
+        else if (rpl <= 8) launch_apply<T, 8>(d_desc, n, ws, d_rank, d_status, s);
+        else if (rpl <= 16) launch_apply<T, 16>(d_desc, n, ws, d_rank, d_status, s);
+        else if (rpl <= 32) launch_apply<T, 32>(d_desc, n, ws, d_rank, d_status, s);
+        else launch_apply<T, 64>(d_desc, n, ws, d_rank, d_status, s);
+    }
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_recompress<double>(const Desc *, int, double *, int *, int *, int,
+                                               int, cudaStream_t, unsigned);
+template cudaError_t launch_recompress<float>(const Desc *, int, float *, int *, int *, int, int,
+                                              cudaStream_t, unsigned);
+
+}  // namespace hc

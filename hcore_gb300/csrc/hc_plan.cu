@@ -1,0 +1,344 @@
+// hcore-gb300 — batched plan API (include/hcore_gb300.h) and shared host
+// helpers for the drop-in entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hc_host.h"
+
+namespace hc {
+
+static thread_local std::string g_last_error;
+
+void set_error(const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+const char *last_error() { return g_last_error.c_str(); }
+
+// Device-accessible alias of p: device/managed memory as is, pinned host
+// memory through its device pointer; pageable host memory yields nullptr.
+const void *device_alias(const void *p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    switch (at.type) {
+        case cudaMemoryTypeDevice:
+        case cudaMemoryTypeManaged:
+            return p;
+        case cudaMemoryTypeHost:
+            return at.devicePointer ? at.devicePointer : p;
+        default:
+            return nullptr;
+    }
+}
+
+bool is_device_memory(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Validate one task and fill its descriptor; returns the task status
+// (0 = runnable).  Mirrors the reference's exit(-1) conditions, in the order
+// HCORE_dgemm checks them.
+int fill_desc(const hcore_lr_task &t, unsigned flags, bool translate, Desc &d, int &k_out) {
+    memset(&d, 0, sizeof d);
+    const bool fast = flags & HCORE_GPU_FAST_RULES;
+    const int a = t.a, b = t.b, c = t.c, M = t.M;
+    const int k = a + c;
+    k_out = k > 0 ? k : 0;
+    d.M = M;
+    d.a = a;
+    d.b = b;
+    d.c = c;
+    d.k = k_out;
+    d.alpha = t.alpha;
+    d.beta = t.beta;
+    d.acc = t.acc;
+    d.rk = t.rk;
+    d.lda = t.lda;
+    d.ldb = t.ldb;
+    d.ldc = t.ldc;
+    d.ldco = t.ldco;
+    d.rank_start = fast ? 2 : 1;
+    d.max_rank = fast ? INT_MAX : t.maxrk;
+    d.storage_rank = t.storage_maxrank > 0 ? t.storage_maxrank : INT_MAX;
+    if (a < 0 || b < 0 || c < 0 || M < 1) return HCORE_GPU_S_SHAPE;
+    if (k == 0) return HCORE_GPU_S_ZERO_RANK;
+    if (!fast && k > 2 * t.maxrk) return HCORE_GPU_S_RANK_SUM;
+    const int ld_newv = t.ld_newv > 0 ? t.ld_newv : 2 * t.maxrk;
+    if (!fast && ld_newv < k) return HCORE_GPU_S_LDNEWV;
+    if (k > M || k > kMaxK || M > 32 * kMaxRowsPerLane) return HCORE_GPU_S_SHAPE;
+    if ((a > 0 && t.lda < M) || (b > 0 && t.ldb < M && !t.Bdense) || (c > 0 && t.ldc < M) ||
+        t.ldco < M)
+        return HCORE_GPU_S_SHAPE;
+    auto tr = [&](const void *p) { return translate ? device_alias(p) : p; };
+    d.AU = a ? tr(t.AU) : nullptr;
+    d.AV = a ? tr(t.AV) : nullptr;
+    if (t.Bdense) {
+        d.Bd = a ? tr(t.Bdense) : nullptr;
+        if (a && !d.Bd) return HCORE_GPU_S_SHAPE;
+    } else {
+        d.BU = (a && b) ? tr(t.BU) : nullptr;
+        d.BV = (a && b) ? tr(t.BV) : nullptr;
+        if (a && b && (!d.BU || !d.BV)) return HCORE_GPU_S_SHAPE;
+    }
+    d.CU = c ? tr(t.CU) : nullptr;
+    d.CV = c ? tr(t.CV) : nullptr;
+    d.CUo = const_cast<void *>(tr(t.CUo));
+    d.CVo = const_cast<void *>(tr(t.CVo));
+    if ((a && (!d.AU || !d.AV)) || (c && (!d.CU || !d.CV)) || !d.CUo || !d.CVo)
+        return HCORE_GPU_S_SHAPE;
+    return HCORE_GPU_S_OK;
+}
+
+// Build the descriptors of a batch, sorted by decreasing cost so that the
+// long updates start first (longest-processing-time order).
+bool build_descs(int n, const hcore_lr_task *tasks, unsigned flags, bool translate,
+                 std::vector<Desc> &descs, long long &ws_elems, int &maxM, int &maxK,
+                 std::vector<int> *status0) {
+    descs.resize(n);
+    std::vector<double> cost(n);
+    maxM = 1;
+    maxK = 1;
+    for (int i = 0; i < n; ++i) {
+        int k = 0;
+        const int st = fill_desc(tasks[i], flags, translate, descs[i], k);
+        descs[i].status0 = st;
+        descs[i].idx = i;
+        if (status0) (*status0)[i] = st;
+        cost[i] = st ? 0.0 : (double)tasks[i].M * k * k + (double)k * k * k;
+        if (!st) {
+            maxM = std::max(maxM, tasks[i].M);
+            maxK = std::max(maxK, k);
+        }
+    }
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+    std::vector<Desc> sorted(n);
+    long long off = 0;
+    for (int j = 0; j < n; ++j) {
+        Desc d = descs[order[j]];
+        d.ws = off;
+        if (!d.status0) off += ws_layout(d.M, d.a, d.b, d.k).total;
+        sorted[j] = d;
+    }
+    descs.swap(sorted);
+    ws_elems = off;
+    return true;
+}
+
+}  // namespace hc
+
+using namespace hc;
+
+struct hcore_gpu_plan_s {
+    int prec = 0;
+    int n = 0;
+    unsigned flags = 0;
+    int maxM = 1, maxK = 1;
+    Desc *d_desc = nullptr;
+    int *d_rank = nullptr;
+    int *d_status = nullptr;
+    void *d_ws = nullptr;
+    size_t ws_bytes = 0;
+    std::vector<long long> ws_of_task;
+    std::vector<int> k_of_task;
+};
+
+static void plan_free(hcore_gpu_plan p) {
+    if (!p) return;
+    cudaFree(p->d_desc);
+    cudaFree(p->d_rank);
+    cudaFree(p->d_status);
+    cudaFree(p->d_ws);
+    delete p;
+}
+
+extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
+                                     const hcore_lr_task *tasks, unsigned flags) {
+    if (!plan || n < 0 || (n > 0 && !tasks) ||
+        (precision != HCORE_GPU_F64 && precision != HCORE_GPU_F32)) {
+        set_error("hcore_gpu_plan_create: invalid argument");
+        return HCORE_GPU_EINVAL;
+    }
+    *plan = nullptr;
+    auto *p = new hcore_gpu_plan_s;
+    p->prec = precision;
+    p->n = n;
+    p->flags = flags;
+    std::vector<Desc> descs;
+    long long ws_elems = 0;
+    build_descs(n, tasks, flags, true, descs, ws_elems, p->maxM, p->maxK, nullptr);
+    p->ws_of_task.assign(n, -1);
+    p->k_of_task.assign(n, 0);
+    for (const Desc &d : descs) {
+        p->ws_of_task[d.idx] = d.status0 ? -1 : d.ws;
+        p->k_of_task[d.idx] = d.k;
+    }
+    const size_t esz = precision == HCORE_GPU_F64 ? sizeof(double) : sizeof(float);
+    p->ws_bytes = (size_t)ws_elems * esz;
+    const size_t nn = (size_t)(n > 0 ? n : 1);
+    cudaError_t e = cudaMalloc(&p->d_desc, nn * sizeof(Desc));
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_rank, nn * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_status, nn * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_ws, p->ws_bytes > 0 ? p->ws_bytes : 256);
+    if (e != cudaSuccess) {
+        set_error("hcore_gpu_plan_create: cudaMalloc failed (%s), workspace %zu bytes",
+                  cudaGetErrorString(e), p->ws_bytes);
+        cudaGetLastError();
+        plan_free(p);
+        return HCORE_GPU_ENOMEM;
+    }
+    if (n > 0) {
+        e = cudaMemcpy(p->d_desc, descs.data(), n * sizeof(Desc), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemset(p->d_rank, 0, n * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, n * sizeof(int));
+    }
+    if (e != cudaSuccess) {
+        set_error("hcore_gpu_plan_create: %s", cudaGetErrorString(e));
+        plan_free(p);
+        return HCORE_GPU_ECUDA;
+    }
+    *plan = p;
+    return HCORE_GPU_OK;
+}
+
+extern "C" int hcore_gpu_plan_execute(hcore_gpu_plan p, void *stream) {
+    if (!p) {
+        set_error("hcore_gpu_plan_execute: null plan");
+        return HCORE_GPU_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e;
+    if (p->prec == HCORE_GPU_F64)
+        e = launch_recompress<double>(p->d_desc, p->n, (double *)p->d_ws, p->d_rank, p->d_status,
+                                      p->maxM, p->maxK, s, kPhaseAll);
+    else
+        e = launch_recompress<float>(p->d_desc, p->n, (float *)p->d_ws, p->d_rank, p->d_status,
+                                     p->maxM, p->maxK, s, kPhaseAll);
+    if (e != cudaSuccess) {
+        set_error("hcore_gpu_plan_execute: %s", cudaGetErrorString(e));
+        return HCORE_GPU_ECUDA;
+    }
+    return HCORE_GPU_OK;
+}
+
+extern "C" const int *hcore_gpu_plan_device_ranks(hcore_gpu_plan p) {
+    return p ? p->d_rank : nullptr;
+}
+extern "C" const int *hcore_gpu_plan_device_status(hcore_gpu_plan p) {
+    return p ? p->d_status : nullptr;
+}
+extern "C" size_t hcore_gpu_plan_workspace_bytes(hcore_gpu_plan p) { return p ? p->ws_bytes : 0; }
+
+extern "C" int hcore_gpu_plan_results(hcore_gpu_plan p, int *ranks, int *status, void *stream) {
+    if (!p) {
+        set_error("hcore_gpu_plan_results: null plan");
+        return HCORE_GPU_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaSuccess;
+    if (ranks && p->n)
+        e = cudaMemcpyAsync(ranks, p->d_rank, p->n * sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && status && p->n)
+        e = cudaMemcpyAsync(status, p->d_status, p->n * sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_error("hcore_gpu_plan_results: %s", cudaGetErrorString(e));
+        return HCORE_GPU_ECUDA;
+    }
+    if (status)
+        for (int i = 0; i < p->n; ++i)
+            if (status[i]) return HCORE_GPU_ETASK;
+    return HCORE_GPU_OK;
+}
+
+extern "C" int hcore_gpu_plan_sigma(hcore_gpu_plan p, int i, double *sigma, int *k, void *stream) {
+    if (!p || i < 0 || i >= p->n) {
+        set_error("hcore_gpu_plan_sigma: invalid argument");
+        return HCORE_GPU_EINVAL;
+    }
+    const int kk = p->k_of_task[i];
+    if (k) *k = kk;
+    if (!sigma || p->ws_of_task[i] < 0 || kk == 0) return HCORE_GPU_OK;
+    // task i's descriptor holds its layout; recompute the sigma offset
+    std::vector<Desc> one(1);
+    cudaStream_t s = (cudaStream_t)stream;
+    // locate the descriptor of task i
+    std::vector<Desc> all(p->n);
+    cudaError_t e = cudaMemcpy(all.data(), p->d_desc, p->n * sizeof(Desc), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_error("hcore_gpu_plan_sigma: %s", cudaGetErrorString(e));
+        return HCORE_GPU_ECUDA;
+    }
+    for (const Desc &d : all)
+        if (d.idx == i) one[0] = d;
+    const WsLayout L = ws_layout(one[0].M, one[0].a, one[0].b, one[0].k);
+    const long long off = one[0].ws + L.sig;
+    if (p->prec == HCORE_GPU_F64) {
+        e = cudaMemcpyAsync(sigma, (double *)p->d_ws + off, kk * sizeof(double),
+                            cudaMemcpyDeviceToHost, s);
+    } else {
+        std::vector<float> tmp(kk);
+        e = cudaMemcpyAsync(tmp.data(), (float *)p->d_ws + off, kk * sizeof(float),
+                            cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        for (int j = 0; j < kk; ++j) sigma[j] = tmp[j];
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_error("hcore_gpu_plan_sigma: %s", cudaGetErrorString(e));
+        return HCORE_GPU_ECUDA;
+    }
+    return HCORE_GPU_OK;
+}
+
+extern "C" int hcore_gpu_plan_destroy(hcore_gpu_plan p) {
+    plan_free(p);
+    return HCORE_GPU_OK;
+}
+
+static int batched_once(int prec, int n, const hcore_lr_task *tasks, int *ranks, int *status,
+                        void *stream) {
+    hcore_gpu_plan p = nullptr;
+    int rc = hcore_gpu_plan_create(&p, prec, n, tasks, 0);
+    if (rc) return rc;
+    rc = hcore_gpu_plan_execute(p, stream);
+    if (!rc) rc = hcore_gpu_plan_results(p, ranks, status, stream);
+    hcore_gpu_plan_destroy(p);
+    return rc;
+}
+
+extern "C" int hcore_gpu_dgemm_batched(int n, const hcore_lr_task *tasks, int *ranks, int *status,
+                                       void *stream) {
+    return batched_once(HCORE_GPU_F64, n, tasks, ranks, status, stream);
+}
+
+extern "C" int hcore_gpu_sgemm_batched(int n, const hcore_lr_task *tasks, int *ranks, int *status,
+                                       void *stream) {
+    return batched_once(HCORE_GPU_F32, n, tasks, ranks, status, stream);
+}
+
+extern "C" const char *hcore_gpu_last_error(void) { return last_error(); }
+extern "C" int hcore_gpu_version(void) { return 100; }

@@ -1,0 +1,133 @@
+/*
+ * hcore-gb300 — batched GPU API (new; the reference has no batched entry
+ * point, every HCORE_* call there recompresses one tile on one CPU thread).
+ *
+ * A batch is a list of independent low-rank updates
+ *     C_i <- beta_i * C_i + alpha_i * A_i * B_i^T
+ * (the Schur updates of a TLR Cholesky panel, for instance), each with the
+ * semantics of HCORE_dgemm (src/compute/hcore_dgemm.c:703-1012): stack,
+ * Householder QR of both stacked factors, SVD of R_A R_B^T, truncation with the
+ * absolute threshold acc (first i >= min_rank_start with sigma_i < acc), and
+ * rebuild CU = Q_A U_r, CV = Q_B V_r S_r.
+ *
+ * Pointers in a task may be device memory or pinned (page-locked) host
+ * memory; both are read and written directly by the kernels.  Outputs may
+ * alias the task's own C inputs (in-place update, as in the reference): every
+ * input of the whole batch is consumed before any output is written.
+ *
+ * Usage without a GPU-side rank array in the caller's hands:
+ *     hcore_gpu_dgemm_batched(n, tasks, ranks, status, stream)   (synchronous)
+ * Capturable form (no host work, no allocation inside execute):
+ *     hcore_gpu_plan_create(&p, HCORE_GPU_F64, n, tasks, flags);
+ *     hcore_gpu_plan_execute(p, stream);      // may be captured in a graph
+ *     hcore_gpu_plan_results(p, ranks, status, stream);
+ *     hcore_gpu_plan_destroy(p);
+ *
+ * Return values: 0 on success, a negative HCORE_GPU_E* code otherwise (the
+ * message is available from hcore_gpu_last_error()).  Per-task outcomes are
+ * reported in the status array (HCORE_GPU_S*).
+ */
+#ifndef HCORE_GB300_H
+#define HCORE_GB300_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* precision of a plan */
+#define HCORE_GPU_F64 0 /* HCORE_dgemm semantics, everything in FP64 */
+#define HCORE_GPU_F32 1 /* HCORE_sgemm semantics, everything in FP32 */
+
+/* return codes */
+#define HCORE_GPU_OK 0
+#define HCORE_GPU_EINVAL (-1)   /* bad argument (see hcore_gpu_last_error) */
+#define HCORE_GPU_ECUDA (-2)    /* CUDA runtime error */
+#define HCORE_GPU_ENOMEM (-3)   /* device allocation failed */
+#define HCORE_GPU_ETASK (-4)    /* at least one task reported a non-zero status */
+
+/* per-task status (what the reference would have exit(-1)-ed on) */
+#define HCORE_GPU_S_OK 0
+#define HCORE_GPU_S_ZERO_RANK 1 /* hcore_dgemm.c:743-746 */
+#define HCORE_GPU_S_RANK_SUM 2  /* a + c > 2*maxrk, hcore_dgemm.c:91-95 */
+#define HCORE_GPU_S_LDNEWV 3    /* a + c > ld_newV, hcore_dgemm.c:924-927 */
+#define HCORE_GPU_S_RANK_MAX 4  /* new rank > maxrk, hcore_dgemm.c:465-468 */
+#define HCORE_GPU_S_STORAGE 5   /* new rank > storage maxrank, :1648-1651 */
+#define HCORE_GPU_S_NOCONV 6    /* Jacobi SVD did not converge */
+#define HCORE_GPU_S_SHAPE 7     /* a + c > M */
+
+/* flags of a plan */
+#define HCORE_GPU_FAST_RULES 0x1 /* HCORE_dgemm_fast: rank search from i=2, no maxrk checks */
+
+/* One low-rank update.  Factors are column-major with the given leading
+ * dimensions; every factor has M rows.  Ranks are plain ints. */
+typedef struct hcore_lr_task {
+    int M;
+    int a, b, c;          /* ranks of A, B and C (c may be 0) */
+    int rk;               /* fixed output rank (0: decided by acc) */
+    int maxrk;            /* computational max rank: a + c <= 2*maxrk, new rank <= maxrk */
+    int ld_newv;          /* reference's ld_newV rule: a + c must not exceed it (0: 2*maxrk) */
+    int storage_maxrank;  /* new rank must not exceed it (0: no extra limit) */
+    double alpha, beta, acc;
+    const void *AU, *AV;
+    int lda;
+    const void *BU, *BV; /* BU == NULL and Bdense != NULL selects dense B */
+    int ldb;
+    const void *Bdense;  /* M x M dense B (HCORE_dgemm_qr_svd_b_dense form) or NULL */
+    const void *CU, *CV;
+    int ldc;
+    void *CUo, *CVo;     /* outputs: the first r columns are written */
+    int ldco;
+} hcore_lr_task;
+
+typedef struct hcore_gpu_plan_s *hcore_gpu_plan;
+
+int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n, const hcore_lr_task *tasks,
+                          unsigned flags);
+int hcore_gpu_plan_execute(hcore_gpu_plan plan, void *stream);
+/* device array of the n new ranks / statuses (valid after execute completes) */
+const int *hcore_gpu_plan_device_ranks(hcore_gpu_plan plan);
+const int *hcore_gpu_plan_device_status(hcore_gpu_plan plan);
+/* copy ranks and statuses to host arrays (either may be NULL) and wait */
+int hcore_gpu_plan_results(hcore_gpu_plan plan, int *ranks, int *status, void *stream);
+/* copy the k singular values of task i (descending) to host (diagnostics) */
+int hcore_gpu_plan_sigma(hcore_gpu_plan plan, int i, double *sigma, int *k, void *stream);
+/* bytes of device workspace the plan holds */
+size_t hcore_gpu_plan_workspace_bytes(hcore_gpu_plan plan);
+int hcore_gpu_plan_destroy(hcore_gpu_plan plan);
+
+/* one-shot synchronous batch: create, execute, results, destroy */
+int hcore_gpu_dgemm_batched(int n, const hcore_lr_task *tasks, int *ranks, int *status,
+                            void *stream);
+int hcore_gpu_sgemm_batched(int n, const hcore_lr_task *tasks, int *ranks, int *status,
+                            void *stream);
+
+/* Dense-C updates (HCORE_dsyrk / HCORE_dgemmcd semantics) batched over
+ * output tiles.  Each task adds to one dense M x M tile CD (ld ldcd):
+ *   kind 0 (syrk):   CD += alpha * U (V^T V) U^T, strict upper set to 0
+ *   kind 1 (gemmcd): CD -= Au (Av^T Bv) Bu^T
+ * Tasks that share a CD are applied in list order by one CTA group, so the
+ * result is that of running them one after another. */
+typedef struct hcore_dense_task {
+    int kind;
+    int M;
+    int a, b;             /* ranks (b unused for syrk) */
+    double alpha;
+    const double *Au, *Av;
+    int lda;              /* leading dimension of Au/Av (syrk: also the row count of Av) */
+    const double *Bu, *Bv;
+    int ldb;
+    double *CD;
+    int ldcd;
+} hcore_dense_task;
+
+int hcore_gpu_dense_batched(int n, const hcore_dense_task *tasks, void *stream);
+
+/* library-owned per-thread stream used by the drop-in HCORE_* entry points */
+void *hcore_gpu_thread_stream(void);
+const char *hcore_gpu_last_error(void);
+int hcore_gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,103 @@
+/*
+ * ORACLE — CPU restatement of the reference HCORE low-rank path (test
+ * infrastructure; never part of the GPU product).
+ *
+ * Built by oracle/build.py into oracle/_build/libhcore_port.so on whichever
+ * machine runs the tests, linked against the LAPACK/BLAS that SciPy bundles
+ * (OpenBLAS, symbols prefixed "scipy_").  The reference itself pins no
+ * LAPACK version (CMakeLists.txt:49-144 accepts any CBLAS/LAPACKE); the
+ * oracle's is whatever SciPy wheel is installed, and its results are pinned
+ * against the reference's own known-answer tests and against outputs of the
+ * reference compiled from source (tests/golden/).
+ *
+ * The double and float bodies come from hcore_port_impl.h.
+ */
+#include <stdlib.h>
+#include <string.h>
+
+#include "hcore_port.h"
+
+enum { CblasColMajor = 102 };
+enum { CblasNoTrans = 111, CblasTrans = 112 };
+#define LAPACK_COL_MAJOR 102
+
+void scipy_cblas_dgemm(int, int, int, int, int, int, double, const double *, int,
+                       const double *, int, double, double *, int);
+void scipy_cblas_sgemm(int, int, int, int, int, int, float, const float *, int,
+                       const float *, int, float, float *, int);
+int scipy_LAPACKE_dgeqrf(int, int, int, double *, int, double *);
+int scipy_LAPACKE_sgeqrf(int, int, int, float *, int, float *);
+int scipy_LAPACKE_dgesvd(int, char, char, int, int, double *, int, double *, double *,
+                         int, double *, int, double *);
+int scipy_LAPACKE_sgesvd(int, char, char, int, int, float *, int, float *, float *, int,
+                         float *, int, float *);
+int scipy_LAPACKE_dormqr(int, char, char, int, int, int, const double *, int,
+                         const double *, double *, int);
+int scipy_LAPACKE_sormqr(int, char, char, int, int, int, const float *, int,
+                         const float *, float *, int);
+int scipy_LAPACKE_dlatms(int, int, int, char, int *, char, double *, int, double, double,
+                         int, int, char, double *, int);
+void scipy_openblas_set_num_threads(int);
+
+/* src/misc/descutil/flop_counts.c:3-70, restated.  The 'q' formula divides
+ * in single precision (2*n*n*n/3.0f) exactly as the reference does, so the
+ * integer totals agree bit for bit. */
+unsigned long port_flop_counts(char op, unsigned long a, unsigned long b, unsigned long c,
+                               unsigned long d)
+{
+    unsigned long res = 0;
+    if (op == 'q') {
+        unsigned long m = a, n = b;
+        res = 2 * m * n * n - (unsigned long)((float)(2 * n * n * n) / 3.0f) + 2 * m * n +
+              (unsigned long)((float)(17 * n) / 3.0f);
+    } else if (op == 'm') {
+        res = a * b * c * 2;
+    } else if (op == 's') {
+        res = 22 * a * a * a;
+    } else if (op == 'o') {
+        unsigned long m = a, n = b, k = c;
+        if (d == 1)
+            res = 4 * n * m * k - 2 * n * k * k + 3 * n * k;
+        else if (d == 2)
+            res = 4 * n * m * k - 2 * m * k * k + 2 * m * k + n * k - k * k / 2 + k / 2;
+    } else if (op == 'c') {
+        unsigned long n = a;
+        res = (unsigned long)(n * n * n / 3 - n * n / 2.0 + n / 6);
+    } else if (op == 't' || op == 'r') {
+        unsigned long m = a, n = b;
+        if (c == 1) res = n * m * m;
+        else if (c == 2) res = m * n * n;
+    }
+    return res;
+}
+
+void port_set_threads(int n) { scipy_openblas_set_num_threads(n); }
+
+/* LAPACKE_dlatms, used by the reference tests' generate_compress
+ * (testing/testing_dgemm.c:159) to build their known-answer inputs. */
+int port_dlatms(int m, int n, char dist, int *iseed, char sym, double *d, int mode,
+                double cond, double dmax, int kl, int ku, char pack, double *a, int lda)
+{
+    return scipy_LAPACKE_dlatms(LAPACK_COL_MAJOR, m, n, dist, iseed, sym, d, mode, cond,
+                                dmax, kl, ku, pack, a, lda);
+}
+
+#define REAL double
+#define PFX(name) port_d##name
+#define LAPACKE_(name) scipy_LAPACKE_d##name
+#define cblas_(name) scipy_cblas_d##name
+#include "hcore_port_impl.h"
+#undef REAL
+#undef PFX
+#undef LAPACKE_
+#undef cblas_
+
+#define REAL float
+#define PFX(name) port_s##name
+#define LAPACKE_(name) scipy_LAPACKE_s##name
+#define cblas_(name) scipy_cblas_s##name
+#include "hcore_port_impl.h"
+#undef REAL
+#undef PFX
+#undef LAPACKE_
+#undef cblas_

@@ -1,0 +1,125 @@
+"""The oracle (C restatement, oracle/hcore_port_impl.h) against the reference.
+
+The fixtures in tests/golden/ were produced by the reference HCORE compiled
+from its own sources (tests/golden/make_golden.py); these tests pin the
+restatement to them on whatever machine runs them.  CPU only.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def test_known_answer_programs_recorded(golden):
+    """The reference's own four ctest programs passed when the fixtures were made."""
+    meta, _ = golden
+    ka = meta["known_answer"]
+    assert ka["testing_dgemm"]["rc"] == 0 and ka["testing_dgemm"]["crank_out"] == 6
+    assert ka["testing_dgemm"]["inf_norm_err"] < 10 * 1e-4          # testing_dgemm.c:378
+    assert ka["testing_sgemm"]["rc"] == 0 and ka["testing_sgemm"]["crank_out"] == 6
+    assert ka["testing_dsyrk"]["inf_norm_err"] < 1000 * 2.2e-16     # testing_dsyrk.c:205
+    assert ka["testing_dgemmcd"]["inf_norm_err"] < 1000 * 2.2e-16
+
+
+def test_port_reproduces_dgemm_known_answer(port, golden):
+    """testing_dgemm.c:250-392 rebuilt: dlatms(iseed 0,0,0,1) -> compress -> update."""
+    meta, g = golden
+    kat = meta["kat_dgemm"]
+    iseed = np.array([0, 0, 0, 1], dtype=np.int32)
+    M = kat["M"]
+    A, AU, AV, ar = O.generate_compress(port, M, iseed, 1e-4, 6)
+    B, BU, BV, br = O.generate_compress(port, M, iseed, 1e-4, 6)
+    Cd, CU, CV, cr = O.generate_compress(port, M, iseed, 1e-4, 6)
+    assert [ar, br, cr] == kat["ranks"]
+    np.testing.assert_allclose(A, g["kat_dgemm_A"], rtol=0, atol=1e-13)
+    out = port.gemm(M, 1.0, AU, AV, ar, BU, BV, br, 1.0, CU, CV, cr, maxrk=M, acc=1e-4)
+    assert out["status"] == 0 and out["rank"] == kat["rank_out"] == 6
+    assert out["flops"] == kat["flops"]
+    ref_C = Cd + A @ B.T
+    err = np.abs(out["CU"] @ out["CV"].T - ref_C).sum(axis=1).max()   # inf norm
+    assert err < 10 * 1e-4
+    P_ref = g["kat_dgemm_CUo"] @ g["kat_dgemm_CVo"].T
+    assert O.rel_fro(out["CU"] @ out["CV"].T, P_ref) < 1e-12
+
+
+@pytest.mark.parametrize("i", range(11))
+def test_port_matches_reference_cases(port, golden, i):
+    meta, g = golden
+    case = meta["gemm"][i]
+    name, kind = case["name"], case["kind"]
+    dtype = np.float32 if kind == "sgemm" else np.float64
+    AU, AV, BU, BV, CU, CV = (g[f"{name}_{f}"] for f in ("AU", "AV", "BU", "BV", "CU", "CV"))
+    out = port.gemm(case["M"], case["alpha"], AU, AV, case["a"], BU, BV, case["b"], case["beta"],
+                    CU, CV, case["c"], rk=case["rk"], maxrk=case["maxrk"], acc=case["acc"],
+                    variant=1 if kind == "fast" else 0, dtype=dtype)
+    assert out["status"] == 0
+    assert out["rank"] == case["rank_out"]
+    if case["flops"] is not None:
+        assert out["flops"] == case["flops"]
+    P = out["CU"].astype(np.float64) @ out["CV"].T.astype(np.float64)
+    P_ref = g[f"{name}_CUo"].astype(np.float64) @ g[f"{name}_CVo"].T.astype(np.float64)
+    tol = 2e-5 if dtype == np.float32 else 1e-12
+    assert O.rel_fro(P, P_ref) < tol
+
+
+def test_port_config512_fingerprint(port, golden):
+    """nb=512, ranks 32, sigma_i = 10^(-8i/32), acc 1e-8, maxrk 64."""
+    meta, g = golden
+    c = meta["cfg512"]
+    rng = np.random.default_rng(c["seed"])
+    AU, AV = O.graded_lowrank(rng, 512, 32)
+    BU, BV = O.graded_lowrank(rng, 512, 32)
+    CU, CV = O.graded_lowrank(rng, 512, 32)
+    out = port.gemm(512, 1.0, AU, AV, 32, BU, BV, 32, 1.0, CU, CV, 32, maxrk=64, acc=1e-8)
+    assert out["rank"] == c["rank_out"] and out["flops"] == c["flops"]
+    omega = np.random.default_rng(c["omega_seed"]).standard_normal((512, 8))
+    fp = (out["CU"] @ out["CV"].T) @ omega
+    assert O.rel_fro(fp, g["cfg512_fingerprint"]) < 1e-10
+    D = O.dense_update(1.0, AU, AV, BU, BV, 1.0, CU, CV)
+    assert O.rel_fro(out["CU"] @ out["CV"].T, D) < 1e-8
+
+
+@pytest.mark.parametrize("i", range(2))
+def test_port_dsyrk_matches_reference(port, golden, i):
+    meta, g = golden
+    c = meta["syrk"][i]
+    n = c["name"]
+    CDo, fl = port.dsyrk(c["M"], c["K"], c["alpha"], g[f"{n}_AU"], g[f"{n}_AV"], g[f"{n}_CD"])
+    np.testing.assert_allclose(CDo, g[f"{n}_CDo"], rtol=1e-12, atol=1e-12)
+    assert fl == c["flops"]
+
+
+@pytest.mark.parametrize("i", range(2))
+def test_port_dgemmcd_matches_reference(port, golden, i):
+    meta, g = golden
+    c = meta["gemmcd"][i]
+    n = c["name"]
+    CDo = port.dgemmcd(c["M"], g[f"{n}_Au"], g[f"{n}_Av"], c["a"], g[f"{n}_Bu"], g[f"{n}_Bv"],
+                       c["b"], g[f"{n}_CD"])
+    np.testing.assert_allclose(CDo, g[f"{n}_CDo"], rtol=1e-12, atol=1e-12)
+
+
+def test_port_error_statuses(port):
+    """The reference's exit(-1) conditions become status codes in the oracle."""
+    rng = np.random.default_rng(5)
+    AU, AV = O.graded_lowrank(rng, 64, 8)
+    out = port.gemm(64, 1.0, AU, AV, 8, AU, AV, 8, 1.0, AU, AV, 0, maxrk=16, acc=1e-8)
+    assert out["status"] == 1                                   # zero rank (hcore_dgemm.c:743)
+    out = port.gemm(64, 1.0, AU, AV, 8, AU, AV, 8, 1.0, AU, AV, 8, maxrk=7, acc=1e-8)
+    assert out["status"] == 2                                   # a + c > 2*maxrk (:91)
+    out = port.gemm(64, 1.0, AU, AV, 8, AU, AV, 8, 1.0, AU, AV, 8, maxrk=12, acc=1e-8)
+    assert out["status"] == 3                                   # ld_newV < k (:924)
+    out = port.gemm(64, 1.0, AU, AV, 8, AU, AV, 8, 1.0, AU, AV, 8, maxrk=16, acc=0.0)
+    assert out["status"] == 0 and out["rank"] == 16
+    out = port.gemm(64, 1.0, AU, AV, 8, AU, AV, 8, 1.0, AU, AV, 8, maxrk=16, acc=0.0, rk=20)
+    assert out["rank"] == 16                                    # rk capped at k (:448-450)
+
+
+def test_flop_model_matches_reference_formula(port):
+    """flop_counts.c:3-70 restated; the survey's config-1 total 2.7635e7."""
+    M, a, b, c, r = 512, 32, 32, 32, 47
+    k = a + c
+    tot = (2 * port.flop_counts("q", M, k) + port.flop_counts("m", a, b, M) +
+           port.flop_counts("m", M, a, b) + port.flop_counts("s", k) + r * k +
+           port.flop_counts("o", M, r, k, 1) + port.flop_counts("o", r, M, k, 2))
+    assert tot == 27634720
