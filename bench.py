@@ -1,0 +1,502 @@
+"""Benchmark: TLR-GEMM updates/s, batched vs plain per-tile, on one GB300.
+
+Workload (one "step"): every Schur update of panel 0 of a TLR Cholesky,
+C_ij <- C_ij - A_i0 A_j0^T for 1 <= j < i < 64, i.e. 1953 HCORE_dgemm
+recompressions at once: 65536 seeded uniform points in [0,1]^2, Morton
+sorted, nb = 1024, kernel exp(-|x-y|^2/0.01), tiles compressed to acc 1e-8
+(relative to each tile's largest singular value), maxrank 128, FP64.  The
+update itself uses the reference's absolute rule sigma_i < 1e-8.
+
+Arms:
+  default           the batched GPU plan (hcore_gb300, C ABI), graph-captured
+  --impl reference  the reference's CPU algorithm (the oracle's LAPACK
+                    restatement, oracle/) on all host cores, same workload
+
+Output: one JSON line (see the keys below).  Multi-GPU: launched under
+torchrun, each rank takes an equal share of the update list (independent
+updates, no collective: weak scaling); value = all ranks' updates / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TLR-GEMM updates/s batched vs plain per-tile on 1 GB300 at rel err <= acc"
+WORKLOAD = dict(workload="TLR Cholesky panel-0 Schur updates (HCORE_dgemm recompression)",
+                points=65536, dim=2, nb=1024, tiles_per_dim=64, kernel="exp(-|x-y|^2/0.01)",
+                acc=1e-8, maxrank=128, tile_compression="relative sigma >= acc*sigma_max",
+                update_truncation="absolute sigma_i < acc (reference rule)")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--max-updates", type=int, default=None, help="truncate the update list")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--per-tile-sample", type=int, default=48)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    return p.parse_args()
+
+
+def dist_init():
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def shard(updates, rank, world):
+    """Contiguous equal shares of the update list (independent updates)."""
+    n = len(updates)
+    lo = rank * n // world
+    hi = (rank + 1) * n // world
+    return updates[lo:hi]
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+
+    def start(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}",
+                                          f"--query-gpu={self.FIELDS}", "--format=csv,noheader",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, mx, reasons, pw = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1].split()[0]))
+                mx.append(float(parts[2].split()[0]))
+                pw.append(float(parts[3].split()[0]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def build_tasks(hc, panel, updates, out_U, out_V, out_off, host=None):
+    """LrTask list for the updates (device arenas, or pinned host copies)."""
+    nb = panel.nb
+    U = host["U"] if host else panel.U
+    V = host["V"] if host else panel.V
+    oU = host["oU"] if host else out_U
+    oV = host["oV"] if host else out_V
+    esz = 8
+    bU, bV, boU, boV = U.data_ptr(), V.data_ptr(), oU.data_ptr(), oV.data_ptr()
+    tasks = []
+    for u, (i, j) in enumerate(updates):
+        sa, sb, sc = panel.index[(i, 0)], panel.index[(j, 0)], panel.index[(i, j)]
+        a, b, c = int(panel.rank[sa]), int(panel.rank[sb]), int(panel.rank[sc])
+        tasks.append(hc.LrTask(
+            M=nb, a=a, b=b, c=c, rk=0, maxrk=panel.maxrank, ld_newv=0,
+            storage_maxrank=panel.maxrank, alpha=-1.0, beta=1.0, acc=panel.acc,
+            AU=bU + esz * int(panel.offset[sa]), AV=bV + esz * int(panel.offset[sa]), lda=nb,
+            BU=bU + esz * int(panel.offset[sb]), BV=bV + esz * int(panel.offset[sb]), ldb=nb,
+            Bdense=None,
+            CU=bU + esz * int(panel.offset[sc]), CV=bV + esz * int(panel.offset[sc]), ldc=nb,
+            CUo=boU + esz * int(out_off[u]), CVo=boV + esz * int(out_off[u]), ldco=nb))
+    return tasks
+
+
+def input_bytes(panel, updates):
+    tot = 0
+    for (i, j) in updates:
+        a = int(panel.rank[panel.index[(i, 0)]])
+        b = int(panel.rank[panel.index[(j, 0)]])
+        c = int(panel.rank[panel.index[(i, j)]])
+        tot += 2 * panel.nb * (a + b + c) * 8
+    return tot
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    import hcore_gb300 as hc
+    from hcore_gb300 import build as hbuild
+    from hcore_gb300 import panel as pnl
+
+    rank, world, local = dist_init()
+    if not os.path.exists(hbuild.LIB):
+        hbuild.build()
+    L = hc.lib()
+    dev = torch.device("cuda", local)
+    t0 = time.time()
+    panel = pnl.build_panel(device=str(dev), max_updates=args.max_updates)
+    gen_s = time.time() - t0
+    updates = shard(panel.updates, rank, world)
+    n = len(updates)
+    nb, maxrank = panel.nb, panel.maxrank
+    # out-of-place outputs: maxrank columns per update, so steps repeat on
+    # the same inputs
+    out_off = np.arange(n + 1, dtype=np.int64) * nb * maxrank
+    out_U = torch.empty(int(out_off[-1]) + 1, dtype=torch.float64, device=dev)
+    out_V = torch.empty_like(out_U)
+    tasks = build_tasks(hc, panel, updates, out_U, out_V, out_off)
+    stream = torch.cuda.current_stream(dev)
+    batch = hc.Batch(tasks)
+    batch.execute(stream.cuda_stream)
+    ranks, status = batch.results(stream.cuda_stream)
+    if (status != 0).any():
+        bad = {int(s): int((status == s).sum()) for s in set(status.tolist()) if s}
+        raise SystemExit(f"tasks failed: {bad}")
+
+    # capture the four launches in one CUDA graph
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(graph, stream=side):
+            batch.execute(side.cuda_stream)
+    stream.wait_stream(side)
+    torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        graph.replay()
+    torch.cuda.synchronize(dev)
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        graph.replay()
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms_max = max_over_ranks(ms, world)
+    total_updates = sum_over_ranks(n, world)
+    value = total_updates / (ms_max / 1e3)
+
+    # reference flop model of what this rank did (ranks from the first run)
+    flops_model, phase_model = 0, {"stack": 0, "qr": 0, "svd": 0, "rebuild": 0}
+    for u, (i, j) in enumerate(updates):
+        a = int(panel.rank[panel.index[(i, 0)]])
+        b = int(panel.rank[panel.index[(j, 0)]])
+        c = int(panel.rank[panel.index[(i, j)]])
+        r = int(ranks[u])
+        flops_model += pnl.update_flops(nb, a, b, c, r)
+        for key, v in pnl.phase_flops(nb, a, b, c, r).items():
+            phase_model[key] += v
+
+    result = {"metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world,
+              "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
+              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+              "data": "synthetic (seeded points, covariance tiles compressed on the GPU)",
+              "config": dict(WORKLOAD, updates_per_step=int(total_updates), parallelism=f"dp{world}",
+                             l2="inputs+outputs+workspace larger than L2 (no flush needed)",
+                             graph="4 kernel launches captured in one CUDA graph"),
+              "gpu_launches": 4 * args.steps,
+              "gflops_model": flops_model / (ms / 1e3) / 1e9,
+              "clocks": clk}
+    if rank != 0:
+        barrier(world)
+        return
+
+    # ---- per-phase timing: the four phases back to back, events between ----
+    phases = [("stack", 1), ("qr", 2), ("svd", 4), ("rebuild", 8)]
+    reps = 3
+    ph_ms = {nm: 0.0 for nm, _ in phases}
+    L.hcore_gpu_plan_execute_phases.argtypes = [hc.C.c_void_p, hc.C.c_void_p, hc.C.c_uint]
+    for _ in range(reps):
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(len(phases) + 1)]
+        torch.cuda.synchronize(dev)
+        evs[0].record(stream)
+        for q, (nm, bit) in enumerate(phases):
+            L.hcore_gpu_plan_execute_phases(batch._plan, stream.cuda_stream, bit)
+            evs[q + 1].record(stream)
+        torch.cuda.synchronize(dev)
+        for q, (nm, _) in enumerate(phases):
+            ph_ms[nm] += evs[q].elapsed_time(evs[q + 1]) / reps
+    dom = max(ph_ms, key=ph_ms.get)
+    peak = fp64_peak(L, torch, dev)
+    achieved = phase_model[dom] / (ph_ms[dom] / 1e3) / 1e12
+    result["phases_ms"] = ph_ms
+    result["roofline"] = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak,
+                          "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                          "peak_source": "fp64 DMMA m16n8k16 issue-rate probe timed live "
+                                         "(MEASURED_PEAKS.json has no FP64 figure)",
+                          "flops_basis": "reference flop model (flop_counts.c) of that phase"}
+
+    # ---- plain per-tile loop: one plan per update, device pointers ----
+    k = min(args.per_tile_sample, n)
+    singles = [hc.Batch([t]) for t in tasks[:k]]
+    for s in singles[:2]:
+        s.execute(stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for s in singles:
+        s.execute(stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    pt_ms = e0.elapsed_time(e1)
+    result["per_tile"] = {"value": k / (pt_ms / 1e3), "unit": "updates/s", "sample": k,
+                          "how": "one single-update plan launched per tile on one stream"}
+    result["batched_vs_per_tile"] = value / result["per_tile"]["value"]
+    for s in singles:
+        s.close()
+
+    # ---- e2e: the same plan over pinned host buffers (zero-copy C2C) ----
+    if not args.no_e2e:
+        result["e2e"] = e2e_pinned(hc, panel, updates, stream, dev, args)
+    batch.close()
+
+    # ---- CPU baseline: the reference algorithm on the host cores ----
+    if not args.no_cpu:
+        result["cpu_baseline"] = cpu_baseline(panel, updates, args.cpu_seconds)
+    result["generation_s"] = gen_s
+    print(json.dumps(result))
+    sys.stdout.flush()
+    barrier(world)
+
+
+def e2e_pinned(hc, panel, updates, stream, dev, args):
+    import numpy as np
+    import torch
+
+    n = len(updates)
+    nb, maxrank = panel.nb, panel.maxrank
+    out_off = np.arange(n + 1, dtype=np.int64) * nb * maxrank
+    host = {"U": panel.U.cpu().pin_memory(), "V": panel.V.cpu().pin_memory(),
+            "oU": torch.empty(int(out_off[-1]) + 1, dtype=torch.float64).pin_memory(),
+            "oV": torch.empty(int(out_off[-1]) + 1, dtype=torch.float64).pin_memory()}
+    tasks = build_tasks(hc, panel, updates, None, None, out_off, host=host)
+    batch = hc.Batch(tasks)
+    for _ in range(max(args.warmup, 1)):
+        batch.execute(stream.cuda_stream)
+    ranks, status = batch.results(stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(args.steps // 2, 1)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(steps):
+        batch.execute(stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / steps
+    out_bytes = int(sum(2 * nb * int(r) * 8 for r in ranks))
+    batch.close()
+    return {"value": n / (ms / 1e3), "unit": "updates/s", "h2d_bytes_per_step": input_bytes(panel, updates),
+            "d2h_bytes_per_step": out_bytes,
+            "how": "plan over pinned host factors: kernels read inputs and write results "
+                   "over NVLink-C2C (zero-copy), no device-resident input",
+            "all_ok": bool((status == 0).all())}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the reference algorithm (oracle/, LAPACK restatement)
+# ---------------------------------------------------------------------------
+
+def _cpu_worker(args):
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    sys.path.insert(0, ROOT)
+    import numpy as np
+
+    from oracle import oracle as O
+
+    folder, items, nb, acc, maxrk, deadline = args
+    U = np.load(os.path.join(folder, "U.npy"), mmap_mode="r")
+    V = np.load(os.path.join(folder, "V.npy"), mmap_mode="r")
+    off = np.load(os.path.join(folder, "off.npy"))
+    port = O.Port()
+    port.set_threads(1)
+
+    def fac(s):
+        o0, o1 = int(off[s]), int(off[s + 1])
+        r = (o1 - o0) // nb
+        return (np.asfortranarray(U[o0:o1].reshape(r, nb).T),
+                np.asfortranarray(V[o0:o1].reshape(r, nb).T), r)
+
+    done = 0
+    t0 = time.time()
+    while True:
+        for (sa, sb, sc) in items:
+            AU, AV, a = fac(sa)
+            BU, BV, b = fac(sb)
+            CU, CV, c = fac(sc)
+            port.gemm(nb, -1.0, AU, AV, a, BU, BV, b, 1.0, CU, CV, c, maxrk=maxrk, acc=acc,
+                      variant=2)
+            done += 1
+            if time.time() - t0 > deadline:
+                return done, time.time() - t0
+        if deadline <= 0:
+            return done, time.time() - t0
+
+
+def cpu_run(panel, updates, seconds):
+    """Time the reference algorithm over the update list on all host cores
+    (one single-threaded process per core, factors memory-mapped from a
+    scratch folder); returns (updates/s, cores, updates done)."""
+    import multiprocessing as mp
+    import tempfile
+
+    import numpy as np
+
+    cores = os.cpu_count() or 1
+    slots = [(panel.index[(i, 0)], panel.index[(j, 0)], panel.index[(i, j)]) for i, j in updates]
+    with tempfile.TemporaryDirectory() as folder:
+        np.save(os.path.join(folder, "U.npy"), panel.U.cpu().numpy())
+        np.save(os.path.join(folder, "V.npy"), panel.V.cpu().numpy())
+        np.save(os.path.join(folder, "off.npy"), panel.offset)
+        ctx = mp.get_context("spawn")
+        chunks = [slots[w::cores] for w in range(cores)]
+        chunks = [c for c in chunks if c]
+        with ctx.Pool(len(chunks)) as pool:
+            pool.map(_cpu_worker, [(folder, ch[:1], panel.nb, panel.acc, panel.maxrank, 0)
+                                   for ch in chunks])
+            t0 = time.time()
+            res = pool.map(_cpu_worker, [(folder, ch, panel.nb, panel.acc, panel.maxrank, seconds)
+                                         for ch in chunks])
+            wall = time.time() - t0
+    done = sum(d for d, _ in res)
+    return done / wall, len(chunks), done
+
+
+def cpu_baseline(panel, updates, seconds):
+    v, cores, done = cpu_run(panel, updates, seconds)
+    return {"value": v, "unit": "updates/s", "cores": cores, "kind": "port",
+            "sample": f"{done} of the step's {len(updates)} updates, one single-threaded "
+                      f"process per core, OpenBLAS LAPACK (oracle/hcore_port.c)"}
+
+
+def run_reference(args):
+    import torch
+
+    rank, world, local = dist_init()
+    if rank != 0:
+        barrier(world)
+        return
+    from hcore_gb300 import panel as pnl
+
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    panel = pnl.build_panel(device=dev, max_updates=args.max_updates)
+    updates = panel.updates
+    vals = []
+    per_step = max(args.cpu_seconds / max(args.steps, 1), 2.0)
+    for s in range(args.warmup + args.steps):
+        v, cores, done = cpu_run(panel, updates, per_step)
+        if s >= args.warmup:
+            vals.append(v)
+    v = statistics.median(vals)
+    kind = "port"
+    line = {"metric": METRIC, "value": v, "unit": "updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": len(updates) / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": dict(WORKLOAD, updates_per_step=len(updates), parallelism="cpu"),
+            "cpu_baseline": {"value": v, "unit": "updates/s", "cores": cores, "kind": kind,
+                             "sample": f"bounded sample per step (~{per_step:.0f} s) of the "
+                                       f"{len(updates)}-update panel; the reference compiled "
+                                       "from source is not on this machine, so the oracle's "
+                                       "LAPACK restatement of it runs"},
+            "e2e": {"value": v, "unit": "updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    sys.stdout.flush()
+    barrier(world)
+
+
+def fp64_peak(L, torch, dev) -> float:
+    """FP64 tensor-pipe (DMMA m16n8k16) throughput in TFLOP/s, measured now."""
+    import ctypes as C
+
+    fn = L.hcore_gpu_fp64_peak
+    fn.restype = C.c_double
+    fn.argtypes = [C.c_void_p]
+    return float(fn(torch.cuda.current_stream(dev).cuda_stream))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

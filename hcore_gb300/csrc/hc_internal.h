@@ -67,10 +67,15 @@ constexpr unsigned kPhaseStack = 1u, kPhaseQR = 2u, kPhaseSVD = 4u, kPhaseApply 
 constexpr unsigned kPhaseAll = 15u;
 constexpr int kMaxK = 512;  // largest a + c a plan accepts
 
-// launchers (hc_kernels.cu)
+// launchers (hc_kernels.cu).  configure_recompress sets kernel attributes
+// (not capturable) and returns the largest k whose Jacobi matrices fit in
+// shared memory; launch_recompress only launches (capturable).
+template <typename T>
+cudaError_t configure_recompress(int maxK, int *svd_smem_kmax);
 template <typename T>
 cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int *d_status,
-                              int maxM, int maxK, cudaStream_t s, unsigned phases);
+                              int maxM, int maxK, int svd_smem_kmax, cudaStream_t s,
+                              unsigned phases);
 
 // dense-C updates (hc_dense.cu): per-task rank-K' form coef * P Q^T
 struct DenseWork {

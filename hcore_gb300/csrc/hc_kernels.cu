@@ -415,26 +415,34 @@ static void launch_apply(const Desc *d_desc, int n, const T *ws, const int *d_ra
 }
 
 template <typename T>
+cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
+    // Jacobi matrices in shared memory when both fit (k <= 117 in FP64)
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    const size_t static_smem = kMaxK * (sizeof(T) + sizeof(int)) + 64;
+    int kmax = 0;
+    while (kmax < maxK && svd_smem_bytes<T>(kmax + 1) + static_smem <= (size_t)optin) ++kmax;
+    *svd_smem_kmax = kmax;
+    const size_t dyn = svd_smem_bytes<T>(kmax);
+    return cudaFuncSetAttribute(gesvd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)dyn);
+}
+
+template <typename T>
 cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int *d_status,
-                              int maxM, int maxK, cudaStream_t s, unsigned phases) {
+                              int maxM, int maxK, int svd_smem_kmax, cudaStream_t s,
+                              unsigned phases) {
     if (n <= 0) return cudaSuccess;
     if (maxK > kMaxK || maxM > 32 * kMaxRowsPerLane) return cudaErrorInvalidValue;
     if (phases & kPhaseStack) stack_kernel<T><<<n, kThreads, 0, s>>>(d_desc, ws);
     if (phases & kPhaseQR)
         geqrf_kernel<T><<<dim3(n, 2), kThreads, (size_t)maxM * sizeof(T), s>>>(d_desc, ws);
     if (phases & kPhaseSVD) {
-        // Jacobi matrices in shared memory when both fit (k <= 117 in FP64)
-        int dev = 0, optin = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        const size_t static_smem = kMaxK * (sizeof(T) + sizeof(int)) + 64;
-        int smem_kmax = 0;
-        while (smem_kmax < maxK && svd_smem_bytes<T>(smem_kmax + 1) + static_smem <= (size_t)optin)
-            ++smem_kmax;
-        const size_t dyn = svd_smem_bytes<T>(smem_kmax < maxK ? smem_kmax : maxK);
-        cudaFuncSetAttribute(gesvd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)dyn);
-        gesvd_kernel<T><<<n, kThreads, dyn, s>>>(d_desc, ws, d_rank, d_status, smem_kmax);
+        const size_t dyn = svd_smem_bytes<T>(svd_smem_kmax < maxK ? svd_smem_kmax : maxK);
+        gesvd_kernel<T><<<n, kThreads, dyn, s>>>(d_desc, ws, d_rank, d_status, svd_smem_kmax);
     }
     if (phases & kPhaseApply) {
         const int rpl = (maxM + 31) / 32;
@@ -447,9 +455,69 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
     return cudaGetLastError();
 }
 
+template cudaError_t configure_recompress<double>(int, int *);
+template cudaError_t configure_recompress<float>(int, int *);
 template cudaError_t launch_recompress<double>(const Desc *, int, double *, int *, int *, int,
-                                               int, cudaStream_t, unsigned);
+                                               int, int, cudaStream_t, unsigned);
 template cudaError_t launch_recompress<float>(const Desc *, int, float *, int *, int *, int, int,
-                                              cudaStream_t, unsigned);
+                                              int, cudaStream_t, unsigned);
 
 }  // namespace hc
+
+// ---------------------------------------------------------------------------
+// FP64 tensor-pipe calibration: sustained DMMA m16n8k16 throughput, used as
+// the roofline denominator of the FP64 phases (the driver's measured peaks
+// cover HBM and bf16 only).  Fixed trip count, no memory traffic.
+// ---------------------------------------------------------------------------
+namespace hc {
+__global__ void __launch_bounds__(256) fp64_peak_kernel(double *out, int iters) {
+    double a[8], b[4], c[4][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = 1e-3 * (threadIdx.x + i);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) b[i] = 0.999 - 1e-4 * i;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) c[j][i] = 0.0;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            asm volatile(
+                "mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, "
+                "{%4,%5,%6,%7,%8,%9,%10,%11}, {%12,%13,%14,%15}, {%0,%1,%2,%3};"
+                : "+d"(c[j][0]), "+d"(c[j][1]), "+d"(c[j][2]), "+d"(c[j][3])
+                : "d"(a[0]), "d"(a[1]), "d"(a[2]), "d"(a[3]), "d"(a[4]), "d"(a[5]), "d"(a[6]),
+                  "d"(a[7]), "d"(b[0]), "d"(b[1]), "d"(b[2]), "d"(b[3]));
+    }
+    double s = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) s += c[j][0] + c[j][1] + c[j][2] + c[j][3];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace hc
+
+extern "C" double hcore_gpu_fp64_peak(void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 4, threads = 256, iters = 2048;
+    double *out = nullptr;
+    if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return -1.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    hc::fp64_peak_kernel<<<blocks, threads, 0, s>>>(out, 64);
+    cudaEventRecord(e0, s);
+    hc::fp64_peak_kernel<<<blocks, threads, 0, s>>>(out, iters);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    const double flops = 2.0 * 16 * 8 * 16 * 4 * (double)iters * ((double)blocks * threads / 32);
+    return ms > 0 ? flops / (ms * 1e-3) / 1e12 : -1.0;
+}

@@ -157,6 +157,7 @@ struct hcore_gpu_plan_s {
     int n = 0;
     unsigned flags = 0;
     int maxM = 1, maxK = 1;
+    int svd_smem_kmax = 0;
     Desc *d_desc = nullptr;
     int *d_rank = nullptr;
     int *d_status = nullptr;
@@ -196,6 +197,16 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
         p->ws_of_task[d.idx] = d.status0 ? -1 : d.ws;
         p->k_of_task[d.idx] = d.k;
     }
+    {
+        const cudaError_t ce = precision == HCORE_GPU_F64
+                                   ? configure_recompress<double>(p->maxK, &p->svd_smem_kmax)
+                                   : configure_recompress<float>(p->maxK, &p->svd_smem_kmax);
+        if (ce != cudaSuccess) {
+            set_error("hcore_gpu_plan_create: %s", cudaGetErrorString(ce));
+            plan_free(p);
+            return HCORE_GPU_ECUDA;
+        }
+    }
     const size_t esz = precision == HCORE_GPU_F64 ? sizeof(double) : sizeof(float);
     p->ws_bytes = (size_t)ws_elems * esz;
     const size_t nn = (size_t)(n > 0 ? n : 1);
@@ -224,7 +235,7 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
     return HCORE_GPU_OK;
 }
 
-extern "C" int hcore_gpu_plan_execute(hcore_gpu_plan p, void *stream) {
+extern "C" int hcore_gpu_plan_execute_phases(hcore_gpu_plan p, void *stream, unsigned phases) {
     if (!p) {
         set_error("hcore_gpu_plan_execute: null plan");
         return HCORE_GPU_EINVAL;
@@ -233,15 +244,19 @@ extern "C" int hcore_gpu_plan_execute(hcore_gpu_plan p, void *stream) {
     cudaError_t e;
     if (p->prec == HCORE_GPU_F64)
         e = launch_recompress<double>(p->d_desc, p->n, (double *)p->d_ws, p->d_rank, p->d_status,
-                                      p->maxM, p->maxK, s, kPhaseAll);
+                                      p->maxM, p->maxK, p->svd_smem_kmax, s, phases & kPhaseAll);
     else
         e = launch_recompress<float>(p->d_desc, p->n, (float *)p->d_ws, p->d_rank, p->d_status,
-                                     p->maxM, p->maxK, s, kPhaseAll);
+                                     p->maxM, p->maxK, p->svd_smem_kmax, s, phases & kPhaseAll);
     if (e != cudaSuccess) {
         set_error("hcore_gpu_plan_execute: %s", cudaGetErrorString(e));
         return HCORE_GPU_ECUDA;
     }
     return HCORE_GPU_OK;
+}
+
+extern "C" int hcore_gpu_plan_execute(hcore_gpu_plan p, void *stream) {
+    return hcore_gpu_plan_execute_phases(p, stream, kPhaseAll);
 }
 
 extern "C" const int *hcore_gpu_plan_device_ranks(hcore_gpu_plan p) {

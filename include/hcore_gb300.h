@@ -84,6 +84,14 @@ typedef struct hcore_gpu_plan_s *hcore_gpu_plan;
 int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n, const hcore_lr_task *tasks,
                           unsigned flags);
 int hcore_gpu_plan_execute(hcore_gpu_plan plan, void *stream);
+/* run only some of the four phases (bit 0 stack, 1 QR, 2 SVD, 3 rebuild),
+ * in that order; for per-phase timing.  Phases read what earlier phases left
+ * in the plan's workspace. */
+#define HCORE_GPU_PHASE_STACK 0x1
+#define HCORE_GPU_PHASE_QR 0x2
+#define HCORE_GPU_PHASE_SVD 0x4
+#define HCORE_GPU_PHASE_REBUILD 0x8
+int hcore_gpu_plan_execute_phases(hcore_gpu_plan plan, void *stream, unsigned phases);
 /* device array of the n new ranks / statuses (valid after execute completes) */
 const int *hcore_gpu_plan_device_ranks(hcore_gpu_plan plan);
 const int *hcore_gpu_plan_device_status(hcore_gpu_plan plan);
@@ -121,6 +129,11 @@ typedef struct hcore_dense_task {
 } hcore_dense_task;
 
 int hcore_gpu_dense_batched(int n, const hcore_dense_task *tasks, void *stream);
+
+/* measured FP64 tensor-pipe (DMMA m16n8k16) throughput of this GPU in
+ * TFLOP/s, timed on `stream` (about 0.1 s); the roofline denominator of the
+ * FP64 phases */
+double hcore_gpu_fp64_peak(void *stream);
 
 /* library-owned per-thread stream used by the drop-in HCORE_* entry points */
 void *hcore_gpu_thread_stream(void);
