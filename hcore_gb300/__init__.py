@@ -97,6 +97,10 @@ def lib() -> C.CDLL:
     L.hcore_gpu_plan_results.argtypes = [vp, _ip, _ip, vp]
     L.hcore_gpu_plan_sigma.argtypes = [vp, C.c_int, _dp, _ip, vp]
     L.hcore_gpu_plan_destroy.argtypes = [vp]
+    L.hcore_gpu_plan_sweeps.argtypes = [vp, _ip, vp]
+    L.hcore_gpu_plan_execute_phases.argtypes = [vp, vp, C.c_uint]
+    L.hcore_gpu_fp64_peak.argtypes = [vp]
+    L.hcore_gpu_fp64_peak.restype = C.c_double
     L.hcore_gpu_plan_device_ranks.argtypes = [vp]
     L.hcore_gpu_plan_device_ranks.restype = vp
     L.hcore_gpu_plan_device_status.argtypes = [vp]
@@ -231,6 +235,16 @@ class Batch:
         _check(lib().hcore_gpu_plan_sigma(self._plan, i, out.ctypes.data_as(_dp), C.byref(k),
                                           stream or None), "hcore_gpu_plan_sigma")
         return out[:k.value]
+
+    def sweeps(self, stream=None):
+        out = np.zeros(max(self.n, 1), dtype=np.int32)
+        _check(lib().hcore_gpu_plan_sweeps(self._plan, out.ctypes.data_as(_ip), stream or None),
+               "hcore_gpu_plan_sweeps")
+        return out[:self.n]
+
+    def execute_phases(self, phases, stream=None):
+        _check(lib().hcore_gpu_plan_execute_phases(self._plan, stream or None, phases),
+               "hcore_gpu_plan_execute_phases")
 
     @property
     def device_ranks_ptr(self) -> int:

@@ -241,8 +241,8 @@ struct Single {
         int kmax = 0;
         cudaError_t e = configure_recompress<T>(k, &kmax);
         if (e == cudaSuccess)
-            e = launch_recompress<T>(d_desc, 1, ws, d_rs, d_rs + 1, t.M, k, kmax, tc.stream,
-                                     phases);
+            e = launch_recompress<T>(d_desc, 1, ws, d_rs, d_rs + 1, nullptr, t.M, k, kmax,
+                                     tc.stream, phases);
         int *pin = (int *)((char *)tc.pin_ensure(kPinBytes) + kPinRankOff);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(pin, d_rs, 2 * sizeof(int), cudaMemcpyDeviceToHost, tc.stream);

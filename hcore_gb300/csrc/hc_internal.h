@@ -60,7 +60,7 @@ __host__ __device__ inline WsLayout ws_layout(int M, int a, int b, int k) {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kMaxSweeps = 60;
+constexpr int kMaxSweeps = 40;
 constexpr int kMaxRowsPerLane = 64;  // apply kernel keeps a column in registers: M <= 2048
 
 constexpr unsigned kPhaseStack = 1u, kPhaseQR = 2u, kPhaseSVD = 4u, kPhaseApply = 8u;
@@ -74,7 +74,7 @@ template <typename T>
 cudaError_t configure_recompress(int maxK, int *svd_smem_kmax);
 template <typename T>
 cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int *d_status,
-                              int maxM, int maxK, int svd_smem_kmax, cudaStream_t s,
+                              int *d_info, int maxM, int maxK, int svd_smem_kmax, cudaStream_t s,
                               unsigned phases);
 
 // dense-C updates (hc_dense.cu): per-task rank-K' form coef * P Q^T

@@ -118,12 +118,96 @@ __global__ void __launch_bounds__(kThreads) stack_kernel(const Desc *__restrict_
 // stored below the diagonal, beta = -sign(alpha)*||x||, tau = (beta-alpha)/beta
 // (LAPACK dlarfg); ||x|| = 0 gives tau = 0.  R ends up on and above the
 // diagonal, as dgeqrf leaves it.
+//
+// FP64 issue slots are the scarce resource on this GPU, so a warp keeps the
+// column it updates in registers (RPL rows per lane, row = lane + 32 t): one
+// load, one dot, one axpy, one store per column and reflector.  The reflector
+// vector is published in shared memory, zero outside rows j..M-1, so the dot
+// and the axpy need no predicates.  Look-ahead: warp 0 updates column j+1
+// first and turns it into reflector j+1 while the other warps finish step j,
+// so there is a single barrier per column.
 template <typename T>
+struct NormLim;
+template <>
+struct NormLim<double> {
+    static constexpr double lo = 1e-280, hi = 1e280;
+};
+template <>
+struct NormLim<float> {
+    static constexpr float lo = 1e-30f, hi = 1e30f;
+};
+
+// Build reflector j from the register column x (already updated by all
+// earlier reflectors); store the column back and publish v and tau.
+template <typename T, int RPL>
+__device__ __forceinline__ void make_reflector(T (&x)[RPL], int j, int M, int lane, T *Aj,
+                                               T *sv, T *s_tau, T *tau_out) {
+    T alpha_l = 0, ss = 0;
+#pragma unroll
+    for (int t = 0; t < RPL; ++t) {
+        const int i = lane + 32 * t;
+        if (i == j) alpha_l = x[t];
+        if (i > j && i < M) ss += x[t] * x[t];
+    }
+    const T alpha = __shfl_sync(0xffffffffu, alpha_l, j & 31);
+    ss = warp_sum(ss);
+    T xnorm;
+    if (ss > NormLim<T>::lo && ss < NormLim<T>::hi) {
+        xnorm = sqrt(ss);
+    } else {  // scaled recomputation (dnrm2's guard against under/overflow)
+        T amax = 0;
+#pragma unroll
+        for (int t = 0; t < RPL; ++t) {
+            const int i = lane + 32 * t;
+            if (i > j && i < M) amax = max(amax, abs(x[t]));
+        }
+        amax = warp_max(amax);
+        T s2 = 0;
+        if (amax > T(0)) {
+            const T inv = T(1) / amax;
+#pragma unroll
+            for (int t = 0; t < RPL; ++t) {
+                const int i = lane + 32 * t;
+                if (i > j && i < M) {
+                    const T y = x[t] * inv;
+                    s2 += y * y;
+                }
+            }
+        }
+        xnorm = amax * sqrt(warp_sum(s2));
+    }
+    T tj = 0, beta = alpha, scal = 1;
+    if (xnorm > T(0)) {
+        beta = -copysign(hypot(alpha, xnorm), alpha);
+        tj = (beta - alpha) / beta;
+        scal = T(1) / (alpha - beta);
+    }
+#pragma unroll
+    for (int t = 0; t < RPL; ++t) {
+        const int i = lane + 32 * t;
+        T v = 0;
+        if (i > j && i < M) {
+            v = x[t] * scal;
+            Aj[i] = v;
+        } else if (i == j) {
+            v = T(1);
+            Aj[i] = beta;
+        } else if (i < j) {
+            Aj[i] = x[t];  // R entries above the diagonal
+        }
+        sv[i] = v;
+    }
+    if (lane == 0) {
+        *s_tau = tj;
+        tau_out[j] = tj;
+    }
+}
+
+template <typename T, int RPL>
 __global__ void __launch_bounds__(kThreads) geqrf_kernel(const Desc *__restrict__ descs,
                                                          T *__restrict__ ws) {
-    extern __shared__ unsigned char smem_raw[];
-    T *sv = reinterpret_cast<T *>(smem_raw);  // current reflector, M entries
-    __shared__ T s_tau;
+    __shared__ T sv[2][32 * RPL];
+    __shared__ T s_tau[2];
     const Desc d = descs[blockIdx.x];
     if (d.status0) return;
     const int M = d.M, k = d.k;
@@ -131,54 +215,45 @@ __global__ void __launch_bounds__(kThreads) geqrf_kernel(const Desc *__restrict_
     const int side = blockIdx.y;
     T *A = ws + d.ws + (side ? L.VB : L.UA);
     T *tau = ws + d.ws + (side ? L.tauB : L.tauA);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T x[RPL];
 
-    for (int j = 0; j < k; ++j) {
-        T *Aj = A + (size_t)j * M;
-        if (warp == 0) {
-            const T alpha = Aj[j];
-            T amax = 0;
-            for (int i = j + 1 + lane; i < M; i += 32) amax = max(amax, abs(Aj[i]));
-            amax = warp_max(amax);
-            T xnorm = 0;
-            if (amax > 0) {
-                const T inv = T(1) / amax;
-                T ss = 0;
-                for (int i = j + 1 + lane; i < M; i += 32) {
-                    const T t = Aj[i] * inv;
-                    ss += t * t;
-                }
-                xnorm = amax * sqrt(warp_sum(ss));
-            }
-            T tj = 0, beta = alpha;
-            if (xnorm > 0) {
-                beta = -copysign(hypot(alpha, xnorm), alpha);
-                tj = (beta - alpha) / beta;
-                const T scal = T(1) / (alpha - beta);
-                for (int i = j + 1 + lane; i < M; i += 32) {
-                    const T v = Aj[i] * scal;
-                    Aj[i] = v;
-                    sv[i] = v;
-                }
-            } else {
-                for (int i = j + 1 + lane; i < M; i += 32) sv[i] = Aj[i];
-            }
-            if (lane == 0) {
-                Aj[j] = beta;
-                tau[j] = tj;
-                s_tau = tj;
-                sv[j] = T(1);
-            }
+    if (warp == 0) {
+#pragma unroll
+        for (int t = 0; t < RPL; ++t) {
+            const int i = lane + 32 * t;
+            x[t] = i < M ? A[i] : T(0);
         }
-        __syncthreads();
-        const T tj = s_tau;
-        if (tj != T(0)) {
-            for (int col = j + 1 + warp; col < k; col += kWarps) {
-                T *Ac = A + (size_t)col * M;
+        make_reflector<T, RPL>(x, 0, M, lane, A, sv[0], &s_tau[0], tau);
+    }
+    __syncthreads();
+    for (int j = 0; j + 1 < k; ++j) {
+        const int cur = j & 1;
+        const T *v = sv[cur];
+        const T tj = s_tau[cur];
+        for (int col = j + 1 + warp; col < k; col += kWarps) {
+            T *Ac = A + (size_t)col * M;
+#pragma unroll
+            for (int t = 0; t < RPL; ++t) {
+                const int i = lane + 32 * t;
+                x[t] = i < M ? Ac[i] : T(0);
+            }
+            if (tj != T(0)) {
                 T dot = 0;
-                for (int i = j + lane; i < M; i += 32) dot += sv[i] * Ac[i];
-                const T s = tj * warp_sum(dot);
-                for (int i = j + lane; i < M; i += 32) Ac[i] -= s * sv[i];
+#pragma unroll
+                for (int t = 0; t < RPL; ++t) dot += v[lane + 32 * t] * x[t];
+                const T sc = tj * warp_sum(dot);
+#pragma unroll
+                for (int t = 0; t < RPL; ++t) x[t] -= sc * v[lane + 32 * t];
+            }
+            if (col == j + 1) {
+                make_reflector<T, RPL>(x, j + 1, M, lane, Ac, sv[cur ^ 1], &s_tau[cur ^ 1], tau);
+            } else {
+#pragma unroll
+                for (int t = 0; t < RPL; ++t) {
+                    const int i = lane + 32 * t;
+                    if (i >= j && i < M) Ac[i] = x[t];
+                }
             }
         }
         __syncthreads();
@@ -200,15 +275,31 @@ __device__ __forceinline__ void rr_pair(int round, int pi, int n, int &p, int &q
     }
 }
 
+// Dynamic shared memory of the SVD kernel for a plan whose largest k is K:
+// W (K x K) when it fits, five per-pair arrays, the singular values and the
+// sort permutation.
+template <typename T>
+__host__ __device__ inline size_t svd_smem_bytes(int K, bool w_in_smem) {
+    const size_t np = (size_t)(K + 1) / 2 + 1;
+    return (w_in_smem ? (size_t)K * K * sizeof(T) : 0) + (5 * np + K + 1) * sizeof(T) +
+           (size_t)(K + 1) * sizeof(int) + 64;
+}
 
-
+// One-sided (Hestenes) Jacobi on W = T: column pairs are rotated until every
+// pair is orthogonal to tol = k*eps relative to its column norms (LAPACK
+// dgesvj's criterion).  A round of the circle tournament (k/2 disjoint pairs)
+// runs in three steps: the warps form the three dot products of their pairs
+// (lanes over rows), warp 0 turns all pairs into rotations at once (one lane
+// per pair, so the square roots and divisions are not repeated 32 times), the
+// warps rotate.  The right singular vectors are not accumulated:
+// V_r S_r = T^T U_r = R_B (R_A^T U_r) is formed once at the end.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict__ descs,
                                                          T *__restrict__ ws, int *__restrict__ rank,
-                                                         int *__restrict__ status, int smem_kmax) {
+                                                         int *__restrict__ status,
+                                                         int *__restrict__ info, int smem_kmax,
+                                                         int maxK) {
     extern __shared__ unsigned char smem_raw[];
-    __shared__ T s_sig[kMaxK];
-    __shared__ int s_perm[kMaxK];
     __shared__ int s_rot;
     const Desc d = descs[blockIdx.x];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -216,6 +307,7 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         if (tid == 0) {
             status[d.idx] = d.status0;
             rank[d.idx] = 0;
+            if (info) info[d.idx] = 0;
         }
         return;
     }
@@ -223,71 +315,97 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     const WsLayout L = ws_layout(M, d.a, d.b, k);
     T *base = ws + d.ws;
     const T *UA = base + L.UA, *VB = base + L.VB;
-    const bool in_smem = k <= smem_kmax;
+    const bool in_smem = maxK <= smem_kmax;
     T *W = in_smem ? reinterpret_cast<T *>(smem_raw) : base + L.W;
-    T *V = in_smem ? W + (size_t)k * k : base + L.V;
+    const int npmax = (maxK + 1) / 2 + 1;
+    T *aux = reinterpret_cast<T *>(smem_raw + (in_smem ? (size_t)maxK * maxK * sizeof(T) : 0));
+    T *s_app = aux, *s_aqq = aux + npmax, *s_apq = aux + 2 * npmax;
+    T *s_c = aux + 3 * npmax, *s_s = aux + 4 * npmax;
+    T *s_sig = aux + 5 * npmax;
+    int *s_perm = reinterpret_cast<int *>(s_sig + maxK + 1);
 
-    // T = triu(R_A) triu(R_B)^T  (hcore_dgemm.c:330-387)
-    for (int e = tid; e < k * k; e += kThreads) {
-        const int i = e % k, j = e / k;
-        T s = 0;
-        for (int l = max(i, j); l < k; ++l) s += UA[(size_t)l * M + i] * VB[(size_t)l * M + j];
-        W[(size_t)j * k + i] = s;
-        V[(size_t)j * k + i] = (i == j) ? T(1) : T(0);
+    // T = triu(R_A) triu(R_B)^T (hcore_dgemm.c:330-387): warp per column j,
+    // lanes over rows i (coalesced in UA, a broadcast in VB)
+    for (int j = warp; j < k; j += kWarps) {
+        for (int i = lane; i < k; i += 32) {
+            T s = 0;
+            for (int l = max(i, j); l < k; ++l) s += UA[(size_t)l * M + i] * VB[(size_t)l * M + j];
+            W[(size_t)j * k + i] = s;
+        }
     }
     __syncthreads();
 
-    // one-sided (Hestenes) Jacobi: rotate column pairs of W until all are
-    // orthogonal to tol; V accumulates the rotations, so T V = W throughout
     const int n = k + (k & 1);
-    const T tol = sqrt(T(k)) * Lim<T>::eps;
+    const int np = n / 2;
+    const T tol = T(k > 8 ? k : 8) * Lim<T>::eps;
     bool converged = (k == 1);
+    int sweeps = 0;
     for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
         if (tid == 0) s_rot = 0;
-        __syncthreads();
         for (int round = 0; round < n - 1; ++round) {
-            for (int pi = warp; pi < n / 2; pi += kWarps) {
+            for (int pi = warp; pi < np; pi += kWarps) {
                 int p, q;
                 rr_pair(round, pi, n, p, q);
-                if (p >= k || q >= k) continue;
-                T *wp = W + (size_t)p * k, *wq = W + (size_t)q * k;
                 T app = 0, aqq = 0, apq = 0;
-                for (int i = lane; i < k; i += 32) {
-                    const T x = wp[i], y = wq[i];
-                    app += x * x;
-                    aqq += y * y;
-                    apq += x * y;
-                }
-                app = warp_sum(app);
-                aqq = warp_sum(aqq);
-                apq = warp_sum(apq);
-                if (apq != T(0) && abs(apq) > tol * sqrt(app) * sqrt(aqq)) {
-                    const T zeta = (aqq - app) / (T(2) * apq);
-                    const T az = abs(zeta);
-                    const T t = az > Lim<T>::big_zeta ? T(0.5) / zeta
-                                                      : copysign(T(1), zeta) / (az + sqrt(T(1) + az * az));
-                    const T cs = T(1) / sqrt(T(1) + t * t);
-                    const T sn = cs * t;
+                if (p < k && q < k) {
+                    const T *wp = W + (size_t)p * k, *wq = W + (size_t)q * k;
                     for (int i = lane; i < k; i += 32) {
                         const T x = wp[i], y = wq[i];
-                        wp[i] = cs * x - sn * y;
-                        wq[i] = sn * x + cs * y;
+                        app += x * x;
+                        aqq += y * y;
+                        apq += x * y;
                     }
-                    T *vp = V + (size_t)p * k, *vq = V + (size_t)q * k;
-                    for (int i = lane; i < k; i += 32) {
-                        const T x = vp[i], y = vq[i];
-                        vp[i] = cs * x - sn * y;
-                        vq[i] = sn * x + cs * y;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        app += __shfl_xor_sync(0xffffffffu, app, o);
+                        aqq += __shfl_xor_sync(0xffffffffu, aqq, o);
+                        apq += __shfl_xor_sync(0xffffffffu, apq, o);
                     }
-                    if (lane == 0) s_rot = 1;
                 }
-                __syncwarp();
+                if (lane == 0) {
+                    s_app[pi] = app;
+                    s_aqq[pi] = aqq;
+                    s_apq[pi] = apq;
+                }
+            }
+            __syncthreads();
+            if (warp == 0) {
+                for (int pi = lane; pi < np; pi += 32) {
+                    const T app = s_app[pi], aqq = s_aqq[pi], apq = s_apq[pi];
+                    T cs = 1, sn = 0;
+                    if (apq != T(0) && abs(apq) > tol * sqrt(app) * sqrt(aqq)) {
+                        const T zeta = (aqq - app) / (T(2) * apq);
+                        const T az = abs(zeta);
+                        const T t = az > Lim<T>::big_zeta
+                                        ? T(0.5) / zeta
+                                        : copysign(T(1), zeta) / (az + sqrt(T(1) + az * az));
+                        cs = T(1) / sqrt(T(1) + t * t);
+                        sn = cs * t;
+                        s_rot = 1;
+                    }
+                    s_c[pi] = cs;
+                    s_s[pi] = sn;
+                }
+            }
+            __syncthreads();
+            for (int pi = warp; pi < np; pi += kWarps) {
+                const T sn = s_s[pi];
+                if (sn == T(0)) continue;
+                const T cs = s_c[pi];
+                int p, q;
+                rr_pair(round, pi, n, p, q);
+                T *wp = W + (size_t)p * k, *wq = W + (size_t)q * k;
+                for (int i = lane; i < k; i += 32) {
+                    const T x = wp[i], y = wq[i];
+                    wp[i] = cs * x - sn * y;
+                    wq[i] = sn * x + cs * y;
+                }
             }
             __syncthreads();
         }
-        const int rot = s_rot;
+        ++sweeps;
+        converged = (s_rot == 0);
         __syncthreads();
-        converged = (rot == 0);
     }
 
     // singular values = column norms; sort descending (ties by index)
@@ -329,18 +447,35 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     else if (r > d.max_rank) st = HCORE_GPU_S_RANK_MAX;
     else if (r > d.storage_rank) st = HCORE_GPU_S_STORAGE;
 
-    // U_r = W(:, perm) / sigma, V_r S_r = V(:, perm) * sigma  (:484-489)
+    // U_r = W(:, perm) / sigma  (k x r, ld k)
     T *Uo = base + L.Uo, *Vo = base + L.Vo;
     for (int e = tid; e < k * r; e += kThreads) {
         const int i = e % k, t = e / k;
         const int j = s_perm[t];
         const T s = s_sig[j];
         Uo[(size_t)t * k + i] = s > T(0) ? W[(size_t)j * k + i] / s : T(0);
-        Vo[(size_t)t * k + i] = V[(size_t)j * k + i] * s;
+    }
+    __syncthreads();
+    // V_r S_r = T^T U_r = R_B (R_A^T U_r): the rows S V^T of
+    // hcore_dgemm.c:484-489, transposed.  Z = R_A^T U_r reuses W's storage.
+    T *Z = W;
+    for (int e = tid; e < k * r; e += kThreads) {
+        const int l = e % k, t = e / k;
+        T s = 0;
+        for (int i = 0; i <= l; ++i) s += UA[(size_t)l * M + i] * Uo[(size_t)t * k + i];
+        Z[(size_t)t * k + l] = s;
+    }
+    __syncthreads();
+    for (int e = tid; e < k * r; e += kThreads) {
+        const int j = e % k, t = e / k;
+        T s = 0;
+        for (int l = j; l < k; ++l) s += VB[(size_t)l * M + j] * Z[(size_t)t * k + l];
+        Vo[(size_t)t * k + j] = s;
     }
     if (tid == 0) {
         rank[d.idx] = r;
         status[d.idx] = st;
+        if (info) info[d.idx] = sweeps;
     }
 }
 
@@ -403,49 +538,56 @@ __global__ void __launch_bounds__(kThreads) apply_kernel(const Desc *__restrict_
 }
 
 // ---------------------------------------------------------------------------
-template <typename T>
-static size_t svd_smem_bytes(int k) {
-    return 2 * (size_t)k * k * sizeof(T);
-}
-
 template <typename T, int RPL>
 static void launch_apply(const Desc *d_desc, int n, const T *ws, const int *d_rank,
                          const int *d_status, cudaStream_t s) {
     apply_kernel<T, RPL><<<dim3(n, 2), kThreads, 0, s>>>(d_desc, ws, d_rank, d_status);
 }
 
+template <typename T, int RPL>
+static void launch_geqrf(const Desc *d_desc, int n, T *ws, cudaStream_t s) {
+    geqrf_kernel<T, RPL><<<dim3(n, 2), kThreads, 0, s>>>(d_desc, ws);
+}
+
 template <typename T>
 cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
-    // Jacobi matrices in shared memory when both fit (k <= 117 in FP64)
+    // the Jacobi matrix W lives in shared memory when it fits (k <= 166 in FP64)
+    (void)maxK;
     int dev = 0, optin = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return e;
-    const size_t static_smem = kMaxK * (sizeof(T) + sizeof(int)) + 64;
     int kmax = 0;
-    while (kmax < maxK && svd_smem_bytes<T>(kmax + 1) + static_smem <= (size_t)optin) ++kmax;
+    while (kmax < kMaxK && svd_smem_bytes<T>(kmax + 1, true) + 64 <= (size_t)optin) ++kmax;
     *svd_smem_kmax = kmax;
-    const size_t dyn = svd_smem_bytes<T>(kmax);
+    // the attribute is per kernel, not per plan: allow the largest size any
+    // plan may launch with, so plans of different k coexist
     return cudaFuncSetAttribute(gesvd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)dyn);
+                                optin - 64);
 }
 
 template <typename T>
 cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int *d_status,
-                              int maxM, int maxK, int svd_smem_kmax, cudaStream_t s,
+                              int *d_info, int maxM, int maxK, int svd_smem_kmax, cudaStream_t s,
                               unsigned phases) {
     if (n <= 0) return cudaSuccess;
     if (maxK > kMaxK || maxM > 32 * kMaxRowsPerLane) return cudaErrorInvalidValue;
+    const int rpl = (maxM + 31) / 32;
     if (phases & kPhaseStack) stack_kernel<T><<<n, kThreads, 0, s>>>(d_desc, ws);
-    if (phases & kPhaseQR)
-        geqrf_kernel<T><<<dim3(n, 2), kThreads, (size_t)maxM * sizeof(T), s>>>(d_desc, ws);
+    if (phases & kPhaseQR) {
+        if (rpl <= 4) launch_geqrf<T, 4>(d_desc, n, ws, s);
+        else if (rpl <= 8) launch_geqrf<T, 8>(d_desc, n, ws, s);
+        else if (rpl <= 16) launch_geqrf<T, 16>(d_desc, n, ws, s);
+        else if (rpl <= 32) launch_geqrf<T, 32>(d_desc, n, ws, s);
+        else launch_geqrf<T, 64>(d_desc, n, ws, s);
+    }
     if (phases & kPhaseSVD) {
-        const size_t dyn = svd_smem_bytes<T>(svd_smem_kmax < maxK ? svd_smem_kmax : maxK);
-        gesvd_kernel<T><<<n, kThreads, dyn, s>>>(d_desc, ws, d_rank, d_status, svd_smem_kmax);
+        const bool w_smem = maxK <= svd_smem_kmax;
+        gesvd_kernel<T><<<n, kThreads, svd_smem_bytes<T>(maxK, w_smem), s>>>(
+            d_desc, ws, d_rank, d_status, d_info, svd_smem_kmax, maxK);
     }
     if (phases & kPhaseApply) {
-        const int rpl = (maxM + 31) / 32;
         if (rpl <= 4) launch_apply<T, 4>(d_desc, n, ws, d_rank, d_status, s);
         else if (rpl <= 8) launch_apply<T, 8>(d_desc, n, ws, d_rank, d_status, s);
         else if (rpl <= 16) launch_apply<T, 16>(d_desc, n, ws, d_rank, d_status, s);
@@ -457,10 +599,10 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
 
 template cudaError_t configure_recompress<double>(int, int *);
 template cudaError_t configure_recompress<float>(int, int *);
-template cudaError_t launch_recompress<double>(const Desc *, int, double *, int *, int *, int,
-                                               int, int, cudaStream_t, unsigned);
-template cudaError_t launch_recompress<float>(const Desc *, int, float *, int *, int *, int, int,
-                                              int, cudaStream_t, unsigned);
+template cudaError_t launch_recompress<double>(const Desc *, int, double *, int *, int *, int *,
+                                               int, int, int, cudaStream_t, unsigned);
+template cudaError_t launch_recompress<float>(const Desc *, int, float *, int *, int *, int *, int,
+                                              int, int, cudaStream_t, unsigned);
 
 }  // namespace hc
 
@@ -502,7 +644,7 @@ extern "C" double hcore_gpu_fp64_peak(void *stream) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int blocks = sms * 4, threads = 256, iters = 2048;
+    const int blocks = sms * 8, threads = 256, iters = 2048;
     double *out = nullptr;
     if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return -1.0;
     cudaEvent_t e0, e1;

@@ -161,6 +161,7 @@ struct hcore_gpu_plan_s {
     Desc *d_desc = nullptr;
     int *d_rank = nullptr;
     int *d_status = nullptr;
+    int *d_info = nullptr;  // Jacobi sweeps per task
     void *d_ws = nullptr;
     size_t ws_bytes = 0;
     std::vector<long long> ws_of_task;
@@ -172,6 +173,7 @@ static void plan_free(hcore_gpu_plan p) {
     cudaFree(p->d_desc);
     cudaFree(p->d_rank);
     cudaFree(p->d_status);
+    cudaFree(p->d_info);
     cudaFree(p->d_ws);
     delete p;
 }
@@ -213,6 +215,7 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
     cudaError_t e = cudaMalloc(&p->d_desc, nn * sizeof(Desc));
     if (e == cudaSuccess) e = cudaMalloc(&p->d_rank, nn * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&p->d_status, nn * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_info, nn * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&p->d_ws, p->ws_bytes > 0 ? p->ws_bytes : 256);
     if (e != cudaSuccess) {
         set_error("hcore_gpu_plan_create: cudaMalloc failed (%s), workspace %zu bytes",
@@ -225,6 +228,7 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
         e = cudaMemcpy(p->d_desc, descs.data(), n * sizeof(Desc), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemset(p->d_rank, 0, n * sizeof(int));
         if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, n * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(p->d_info, 0, n * sizeof(int));
     }
     if (e != cudaSuccess) {
         set_error("hcore_gpu_plan_create: %s", cudaGetErrorString(e));
@@ -244,10 +248,12 @@ extern "C" int hcore_gpu_plan_execute_phases(hcore_gpu_plan p, void *stream, uns
     cudaError_t e;
     if (p->prec == HCORE_GPU_F64)
         e = launch_recompress<double>(p->d_desc, p->n, (double *)p->d_ws, p->d_rank, p->d_status,
-                                      p->maxM, p->maxK, p->svd_smem_kmax, s, phases & kPhaseAll);
+                                      p->d_info, p->maxM, p->maxK, p->svd_smem_kmax, s,
+                                      phases & kPhaseAll);
     else
         e = launch_recompress<float>(p->d_desc, p->n, (float *)p->d_ws, p->d_rank, p->d_status,
-                                     p->maxM, p->maxK, p->svd_smem_kmax, s, phases & kPhaseAll);
+                                     p->d_info, p->maxM, p->maxK, p->svd_smem_kmax, s,
+                                     phases & kPhaseAll);
     if (e != cudaSuccess) {
         set_error("hcore_gpu_plan_execute: %s", cudaGetErrorString(e));
         return HCORE_GPU_ECUDA;
@@ -265,6 +271,22 @@ extern "C" const int *hcore_gpu_plan_device_ranks(hcore_gpu_plan p) {
 extern "C" const int *hcore_gpu_plan_device_status(hcore_gpu_plan p) {
     return p ? p->d_status : nullptr;
 }
+extern "C" int hcore_gpu_plan_sweeps(hcore_gpu_plan p, int *sweeps, void *stream) {
+    if (!p || !sweeps) {
+        set_error("hcore_gpu_plan_sweeps: invalid argument");
+        return HCORE_GPU_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaSuccess;
+    if (p->n) e = cudaMemcpyAsync(sweeps, p->d_info, p->n * sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_error("hcore_gpu_plan_sweeps: %s", cudaGetErrorString(e));
+        return HCORE_GPU_ECUDA;
+    }
+    return HCORE_GPU_OK;
+}
+
 extern "C" size_t hcore_gpu_plan_workspace_bytes(hcore_gpu_plan p) { return p ? p->ws_bytes : 0; }
 
 extern "C" int hcore_gpu_plan_results(hcore_gpu_plan p, int *ranks, int *status, void *stream) {

@@ -16,11 +16,11 @@ builds the workload the batched path is measured on:
 * the panel-0 update list C_ij <- C_ij - A_i0 A_j0^T for 1 <= j < i < T.
 
 Compression of the input tiles is set-up work, not the measured path: it
-runs once, on the GPU through torch (randomized range finder + small SVD).
+runs once, on the host cores (randomized range finder + small SVD, LAPACK).
 """
 from __future__ import annotations
 
-import math
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -67,76 +67,108 @@ class Panel:
     index: dict = field(default_factory=dict)    # (i, j) -> tile slot
 
 
-def _kernel(X, Y, kind: str, ell: float):
-    import torch
-
-    d2 = (X * X).sum(-1)[..., :, None] + (Y * Y).sum(-1)[..., None, :] - 2.0 * X @ Y.transpose(-1, -2)
-    d2 = torch.clamp(d2, min=0.0)
+def _kernel_np(X: np.ndarray, Y: np.ndarray, kind: str, ell: float) -> np.ndarray:
+    d2 = (X * X).sum(-1)[:, None] + (Y * Y).sum(-1)[None, :] - 2.0 * X @ Y.T
+    np.maximum(d2, 0.0, out=d2)
     if kind == "sqexp":
-        return torch.exp(-d2 / ell)
+        return np.exp(-d2 / ell)
     if kind == "exp":
-        return torch.exp(-torch.sqrt(d2) / ell)
+        return np.exp(-np.sqrt(d2) / ell)
     raise ValueError(kind)
 
 
-def compress_tiles(K, acc: float, maxrank: int, seed: int, oversample: int = 32):
-    """Randomized compression of a batch of nb x nb tiles (torch, fp64, GPU).
+def compress_tile(K: np.ndarray, acc: float, maxrank: int, seed: int, oversample: int = 32):
+    """Randomized compression of one nb x nb tile (host, LAPACK): range
+    finder with p = maxrank + oversample Gaussian vectors, QR, small SVD.
+    Returns (U, V, rank) with U orthonormal and V = (S V^T)^T, truncated at
+    sigma >= acc * sigma_max and capped at maxrank."""
+    import scipy.linalg as sl
 
-    Returns (U, V, ranks) with U, V of shape (batch, nb, p) whose first
-    ranks[t] columns are the factors (U orthonormal, V = (S V^T)^T)."""
-    import torch
-
-    T, nb, _ = K.shape
+    nb = K.shape[0]
     p = min(nb, maxrank + oversample)
-    g = torch.Generator(device=K.device)
-    g.manual_seed(seed)
-    omega = torch.randn((nb, p), generator=g, dtype=K.dtype, device=K.device)
-    Y = K @ omega
-    Q, _ = torch.linalg.qr(Y)
-    B = Q.transpose(-1, -2) @ K
-    Ub, S, Vh = torch.linalg.svd(B, full_matrices=False)
-    U = Q @ Ub
-    thr = acc * S[:, :1]
-    ranks = torch.clamp((S >= thr).sum(-1), max=maxrank)
-    V = (S[:, :, None] * Vh).transpose(-1, -2)
-    return U, V, ranks
+    omega = np.random.default_rng(seed).standard_normal((nb, p))
+    Q, _ = sl.qr(K @ omega, mode="economic")
+    Ub, S, Vh = sl.svd(Q.T @ K, full_matrices=False, lapack_driver="gesvd")
+    r = int(min(maxrank, (S >= acc * S[0]).sum())) if S[0] > 0 else 1
+    r = max(r, 1)
+    U = Q @ Ub[:, :r]
+    V = (S[:r, None] * Vh[:r]).T
+    return U, V, r
+
+
+def _compress_job(args):
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    folder, slots, nb, kind, ell, acc, maxrank, seed = args
+    P = np.load(os.path.join(folder, "points.npy"), mmap_mode="r")
+    out = []
+    for s, i, j in slots:
+        K = _kernel_np(np.asarray(P[i * nb:(i + 1) * nb]), np.asarray(P[j * nb:(j + 1) * nb]),
+                       kind, ell)
+        U, V, r = compress_tile(K, acc, maxrank, seed * 100003 + s)
+        out.append((s, np.ascontiguousarray(U.T), np.ascontiguousarray(V.T), r))
+    return out
 
 
 def build_panel(n_points: int = 65536, dim: int = 2, nb: int = 1024, kernel: str = "sqexp",
                 ell: float = 0.01, acc: float = 1e-8, maxrank: int = 128, seed: int = 0,
-                device: str = "cuda", batch: int = 32, max_updates: int | None = None) -> Panel:
-    """Generate and compress the tiles that panel 0's Schur updates touch."""
+                device: str = "cuda", max_updates: int | None = None,
+                workers: int | None = None) -> Panel:
+    """Generate and compress the tiles that panel 0's Schur updates touch.
+
+    Compression runs on the host cores (one single-threaded LAPACK process
+    per core, spawn start method so a CUDA context in the parent is safe);
+    the factors are then uploaded to ``device`` (or kept on the host when
+    device is "cpu")."""
+    import multiprocessing as mp
+    import tempfile
+
     import torch
 
     T = n_points // nb
-    P = torch.from_numpy(morton_points(n_points, dim, seed)).to(device)
+    P = morton_points(n_points, dim, seed)
     tiles = [(i, 0) for i in range(1, T)]
     updates = [(i, j) for j in range(1, T) for i in range(j + 1, T)]
     if max_updates is not None:
         updates = updates[:max_updates]
-    need_c = sorted({u for u in updates})
-    tiles += need_c
+    tiles += sorted(set(updates))
     index = {t: s for s, t in enumerate(tiles)}
-    ranks = np.zeros(len(tiles), dtype=np.int32)
-    Us, Vs = [], []
-    for s0 in range(0, len(tiles), batch):
-        chunk = tiles[s0:s0 + batch]
-        X = torch.stack([P[i * nb:(i + 1) * nb] for i, _ in chunk])
-        Yp = torch.stack([P[j * nb:(j + 1) * nb] for _, j in chunk])
-        K = _kernel(X, Yp, kernel, ell)
-        U, V, r = compress_tiles(K, acc, maxrank, seed + s0)
-        r = r.cpu().numpy()
-        ranks[s0:s0 + len(chunk)] = r
-        for t in range(len(chunk)):
-            Us.append(U[t, :, :r[t]].transpose(0, 1).contiguous())   # (r, nb): column-major
-            Vs.append(V[t, :, :r[t]].transpose(0, 1).contiguous())
-        del K, U, V
+    workers = workers or os.cpu_count() or 1
+    jobs = [(s, i, j) for s, (i, j) in enumerate(tiles)]
+    results = [None] * len(tiles)
+    with tempfile.TemporaryDirectory() as folder:
+        np.save(os.path.join(folder, "points.npy"), P)
+        chunks = [jobs[w::workers] for w in range(workers)]
+        chunks = [c for c in chunks if c]
+        args = [(folder, c, nb, kernel, ell, acc, maxrank, seed) for c in chunks]
+        if len(chunks) == 1:
+            parts = [_compress_job(args[0])]
+        else:
+            # children inherit the environment: one BLAS thread per process
+            saved = {v: os.environ.get(v) for v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS")}
+            os.environ.update(OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+            try:
+                with mp.get_context("spawn").Pool(len(chunks)) as pool:
+                    parts = pool.map(_compress_job, args)
+            finally:
+                for v, old in saved.items():
+                    if old is None:
+                        os.environ.pop(v, None)
+                    else:
+                        os.environ[v] = old
+    for part in parts:
+        for s, Ut, Vt, r in part:
+            results[s] = (Ut, Vt, r)
+    ranks = np.array([r for _, _, r in results], dtype=np.int32)
     offset = np.zeros(len(tiles) + 1, dtype=np.int64)
     offset[1:] = np.cumsum(ranks.astype(np.int64) * nb)
-    Uflat = torch.cat([u.reshape(-1) for u in Us]) if Us else torch.zeros(1, device=device)
-    Vflat = torch.cat([v.reshape(-1) for v in Vs]) if Vs else torch.zeros(1, device=device)
+    Uflat = np.concatenate([u.reshape(-1) for u, _, _ in results])
+    Vflat = np.concatenate([v.reshape(-1) for _, v, _ in results])
+    Ut = torch.from_numpy(Uflat)
+    Vt = torch.from_numpy(Vflat)
+    if device != "cpu":
+        Ut, Vt = Ut.to(device), Vt.to(device)
     return Panel(nb=nb, ntiles=T, acc=acc, maxrank=maxrank, tiles=tiles, rank=ranks,
-                 offset=offset, U=Uflat, V=Vflat, updates=updates, index=index)
+                 offset=offset, U=Ut, V=Vt, updates=updates, index=index)
 
 
 def update_flops(M: int, a: int, b: int, c: int, r: int) -> int:

@@ -99,6 +99,8 @@ const int *hcore_gpu_plan_device_status(hcore_gpu_plan plan);
 int hcore_gpu_plan_results(hcore_gpu_plan plan, int *ranks, int *status, void *stream);
 /* copy the k singular values of task i (descending) to host (diagnostics) */
 int hcore_gpu_plan_sigma(hcore_gpu_plan plan, int i, double *sigma, int *k, void *stream);
+/* Jacobi sweeps each task's SVD took (diagnostics; valid after execute) */
+int hcore_gpu_plan_sweeps(hcore_gpu_plan plan, int *sweeps, void *stream);
 /* bytes of device workspace the plan holds */
 size_t hcore_gpu_plan_workspace_bytes(hcore_gpu_plan plan);
 int hcore_gpu_plan_destroy(hcore_gpu_plan plan);
