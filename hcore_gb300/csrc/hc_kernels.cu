@@ -275,24 +275,47 @@ __device__ __forceinline__ void rr_pair(int round, int pi, int n, int &p, int &q
     }
 }
 
-// Dynamic shared memory of the SVD kernel for a plan whose largest k is K:
-// W (K x K) when it fits, five per-pair arrays, the singular values and the
-// sort permutation.
+template <typename T>
+struct JacobiLim;
+template <>
+struct JacobiLim<double> {
+    static constexpr double tiny_scale = 1e-60;  // fold a column scale below this
+};
+template <>
+struct JacobiLim<float> {
+    static constexpr float tiny_scale = 1e-12f;
+};
+
+// Threads per CTA of the SVD kernel for a plan whose largest k is K: one lane
+// per column pair.
+__host__ __device__ inline int svd_threads(int K) {
+    const int np = (K + 1) / 2;
+    return np <= 32 ? 32 : (np <= 64 ? 64 : (np <= 128 ? 128 : 256));
+}
+__host__ __device__ inline int svd_ldw(int k) { return k | 1; }
+
+// Dynamic shared memory of the SVD kernel: W (K x ldw) when it fits, then the
+// column scales, the squared column norms, the singular values and the sort
+// permutation.
 template <typename T>
 __host__ __device__ inline size_t svd_smem_bytes(int K, bool w_in_smem) {
-    const size_t np = (size_t)(K + 1) / 2 + 1;
-    return (w_in_smem ? (size_t)K * K * sizeof(T) : 0) + (5 * np + K + 1) * sizeof(T) +
+    return (w_in_smem ? (size_t)K * svd_ldw(K) * sizeof(T) : 0) + (size_t)3 * (K + 1) * sizeof(T) +
            (size_t)(K + 1) * sizeof(int) + 64;
 }
 
-// One-sided (Hestenes) Jacobi on W = T: column pairs are rotated until every
-// pair is orthogonal to tol = k*eps relative to its column norms (LAPACK
-// dgesvj's criterion).  A round of the circle tournament (k/2 disjoint pairs)
-// runs in three steps: the warps form the three dot products of their pairs
-// (lanes over rows), warp 0 turns all pairs into rotations at once (one lane
-// per pair, so the square roots and divisions are not repeated 32 times), the
-// warps rotate.  The right singular vectors are not accumulated:
-// V_r S_r = T^T U_r = R_B (R_A^T U_r) is formed once at the end.
+// One-sided (Hestenes) Jacobi on W = T, written for the FP64 issue rate of
+// this GPU (one warp FP64 instruction per ~80 cycles per SM sub-partition):
+//  * one lane per column pair of the round (the circle tournament gives k/2
+//    disjoint pairs), looping over the rows: no shuffle reductions;
+//  * scaled ("fast") rotations: column j is stored as d_j * x_j, so rotating
+//    a pair costs two FMAs per row (x_p -= t d_q/d_p x_q, x_q += t d_p/d_q x_p)
+//    and the cosine goes into the scales;
+//  * squared norms are tracked (app' = app - t apq, aqq' = aqq + t apq, exact
+//    in exact arithmetic), recomputed on strong cancellation and after every
+//    sweep, so each pair needs one dot product.
+// Convergence: every pair orthogonal to tol = k*eps relative to its norms
+// (LAPACK dgesvj's criterion).  The right singular vectors are not
+// accumulated: V_r S_r = T^T U_r = R_B (R_A^T U_r) is formed once at the end.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict__ descs,
                                                          T *__restrict__ ws, int *__restrict__ rank,
@@ -302,7 +325,7 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     extern __shared__ unsigned char smem_raw[];
     __shared__ int s_rot;
     const Desc d = descs[blockIdx.x];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x, nthr = blockDim.x;
     if (d.status0) {
         if (tid == 0) {
             status[d.idx] = d.status0;
@@ -316,22 +339,27 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     T *base = ws + d.ws;
     const T *UA = base + L.UA, *VB = base + L.VB;
     const bool in_smem = maxK <= smem_kmax;
+    const int ldw = in_smem ? svd_ldw(k) : k;
     T *W = in_smem ? reinterpret_cast<T *>(smem_raw) : base + L.W;
-    const int npmax = (maxK + 1) / 2 + 1;
-    T *aux = reinterpret_cast<T *>(smem_raw + (in_smem ? (size_t)maxK * maxK * sizeof(T) : 0));
-    T *s_app = aux, *s_aqq = aux + npmax, *s_apq = aux + 2 * npmax;
-    T *s_c = aux + 3 * npmax, *s_s = aux + 4 * npmax;
-    T *s_sig = aux + 5 * npmax;
+    T *aux = reinterpret_cast<T *>(smem_raw + (in_smem ? (size_t)maxK * svd_ldw(maxK) * sizeof(T) : 0));
+    T *s_d = aux, *s_nrm = aux + (maxK + 1), *s_sig = aux + 2 * (maxK + 1);
     int *s_perm = reinterpret_cast<int *>(s_sig + maxK + 1);
 
-    // T = triu(R_A) triu(R_B)^T (hcore_dgemm.c:330-387): warp per column j,
-    // lanes over rows i (coalesced in UA, a broadcast in VB)
-    for (int j = warp; j < k; j += kWarps) {
-        for (int i = lane; i < k; i += 32) {
+    // T = triu(R_A) triu(R_B)^T (hcore_dgemm.c:330-387): threads over rows i
+    // (coalesced in UA), VB read as a broadcast
+    for (int j = 0; j < k; ++j) {
+        for (int i = tid; i < k; i += nthr) {
             T s = 0;
             for (int l = max(i, j); l < k; ++l) s += UA[(size_t)l * M + i] * VB[(size_t)l * M + j];
-            W[(size_t)j * k + i] = s;
+            W[(size_t)j * ldw + i] = s;
         }
+    }
+    __syncthreads();
+    for (int j = tid; j < k; j += nthr) {
+        T s = 0;
+        for (int i = 0; i < k; ++i) s += W[(size_t)j * ldw + i] * W[(size_t)j * ldw + i];
+        s_nrm[j] = s;
+        s_d[j] = T(1);
     }
     __syncthreads();
 
@@ -342,82 +370,76 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     int sweeps = 0;
     for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
         if (tid == 0) s_rot = 0;
+        __syncthreads();
         for (int round = 0; round < n - 1; ++round) {
-            for (int pi = warp; pi < np; pi += kWarps) {
+            for (int pi = tid; pi < np; pi += nthr) {
                 int p, q;
                 rr_pair(round, pi, n, p, q);
-                T app = 0, aqq = 0, apq = 0;
-                if (p < k && q < k) {
-                    const T *wp = W + (size_t)p * k, *wq = W + (size_t)q * k;
-                    for (int i = lane; i < k; i += 32) {
-                        const T x = wp[i], y = wq[i];
-                        app += x * x;
-                        aqq += y * y;
-                        apq += x * y;
+                if (p >= k || q >= k) continue;
+                T *xp = W + (size_t)p * ldw, *xq = W + (size_t)q * ldw;
+                T dot = 0;
+                for (int i = 0; i < k; ++i) dot += xp[i] * xq[i];
+                const T dp = s_d[p], dq = s_d[q];
+                const T app = s_nrm[p], aqq = s_nrm[q];
+                const T apq = dp * dq * dot;
+                if (apq != T(0) && abs(apq) > tol * sqrt(app) * sqrt(aqq)) {
+                    const T zeta = (aqq - app) / (T(2) * apq);
+                    const T az = abs(zeta);
+                    const T t = az > Lim<T>::big_zeta
+                                    ? T(0.5) / zeta
+                                    : copysign(T(1), zeta) / (az + sqrt(T(1) + az * az));
+                    const T cs = T(1) / sqrt(T(1) + t * t);
+                    // true columns p' = c (p - t q), q' = c (q + t p)
+                    const T f1 = t * dq / dp, f2 = t * dp / dq;
+                    for (int i = 0; i < k; ++i) {
+                        const T a = xp[i], b = xq[i];
+                        xp[i] = a - f1 * b;
+                        xq[i] = b + f2 * a;
                     }
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        app += __shfl_xor_sync(0xffffffffu, app, o);
-                        aqq += __shfl_xor_sync(0xffffffffu, aqq, o);
-                        apq += __shfl_xor_sync(0xffffffffu, apq, o);
+                    T np_ = app - t * apq, nq_ = aqq + t * apq;
+                    T dp2 = dp * cs, dq2 = dq * cs;
+                    // strong cancellation in a tracked norm: recompute it
+                    if (np_ < app * T(1.0 / 64)) {
+                        T s = 0;
+                        for (int i = 0; i < k; ++i) s += xp[i] * xp[i];
+                        np_ = dp2 * dp2 * s;
                     }
-                }
-                if (lane == 0) {
-                    s_app[pi] = app;
-                    s_aqq[pi] = aqq;
-                    s_apq[pi] = apq;
+                    if (nq_ < aqq * T(1.0 / 64)) {
+                        T s = 0;
+                        for (int i = 0; i < k; ++i) s += xq[i] * xq[i];
+                        nq_ = dq2 * dq2 * s;
+                    }
+                    s_nrm[p] = np_;
+                    s_nrm[q] = nq_;
+                    s_d[p] = dp2;
+                    s_d[q] = dq2;
+                    s_rot = 1;
                 }
             }
             __syncthreads();
-            if (warp == 0) {
-                for (int pi = lane; pi < np; pi += 32) {
-                    const T app = s_app[pi], aqq = s_aqq[pi], apq = s_apq[pi];
-                    T cs = 1, sn = 0;
-                    if (apq != T(0) && abs(apq) > tol * sqrt(app) * sqrt(aqq)) {
-                        const T zeta = (aqq - app) / (T(2) * apq);
-                        const T az = abs(zeta);
-                        const T t = az > Lim<T>::big_zeta
-                                        ? T(0.5) / zeta
-                                        : copysign(T(1), zeta) / (az + sqrt(T(1) + az * az));
-                        cs = T(1) / sqrt(T(1) + t * t);
-                        sn = cs * t;
-                        s_rot = 1;
-                    }
-                    s_c[pi] = cs;
-                    s_s[pi] = sn;
-                }
+        }
+        // exact norms once per sweep; fold scales before they underflow
+        for (int j = tid; j < k; j += nthr) {
+            T *xj = W + (size_t)j * ldw;
+            T dj = s_d[j];
+            if (dj < JacobiLim<T>::tiny_scale) {
+                for (int i = 0; i < k; ++i) xj[i] *= dj;
+                dj = T(1);
+                s_d[j] = dj;
             }
-            __syncthreads();
-            for (int pi = warp; pi < np; pi += kWarps) {
-                const T sn = s_s[pi];
-                if (sn == T(0)) continue;
-                const T cs = s_c[pi];
-                int p, q;
-                rr_pair(round, pi, n, p, q);
-                T *wp = W + (size_t)p * k, *wq = W + (size_t)q * k;
-                for (int i = lane; i < k; i += 32) {
-                    const T x = wp[i], y = wq[i];
-                    wp[i] = cs * x - sn * y;
-                    wq[i] = sn * x + cs * y;
-                }
-            }
-            __syncthreads();
+            T s = 0;
+            for (int i = 0; i < k; ++i) s += xj[i] * xj[i];
+            s_nrm[j] = dj * dj * s;
         }
         ++sweeps;
         converged = (s_rot == 0);
         __syncthreads();
     }
 
-    // singular values = column norms; sort descending (ties by index)
-    for (int j = warp; j < k; j += kWarps) {
-        const T *wj = W + (size_t)j * k;
-        T s = 0;
-        for (int i = lane; i < k; i += 32) s += wj[i] * wj[i];
-        s = warp_sum(s);
-        if (lane == 0) s_sig[j] = sqrt(s);
-    }
+    // singular values = true column norms; sort descending (ties by index)
+    for (int j = tid; j < k; j += nthr) s_sig[j] = sqrt(s_nrm[j]);
     __syncthreads();
-    for (int j = tid; j < k; j += kThreads) {
+    for (int j = tid; j < k; j += nthr) {
         const T sj = s_sig[j];
         int pos = 0;
         for (int i = 0; i < k; ++i) {
@@ -428,7 +450,7 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     }
     __syncthreads();
     T *sig_out = base + L.sig;
-    for (int t = tid; t < k; t += kThreads) sig_out[t] = s_sig[s_perm[t]];
+    for (int t = tid; t < k; t += nthr) sig_out[t] = s_sig[s_perm[t]];
 
     // rank rule (hcore_dgemm.c:444-464; the fast rules start at i = 2)
     int r;
@@ -447,26 +469,26 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     else if (r > d.max_rank) st = HCORE_GPU_S_RANK_MAX;
     else if (r > d.storage_rank) st = HCORE_GPU_S_STORAGE;
 
-    // U_r = W(:, perm) / sigma  (k x r, ld k)
+    // U_r = W(:, perm) d / sigma  (k x r, ld k)
     T *Uo = base + L.Uo, *Vo = base + L.Vo;
-    for (int e = tid; e < k * r; e += kThreads) {
+    for (int e = tid; e < k * r; e += nthr) {
         const int i = e % k, t = e / k;
         const int j = s_perm[t];
         const T s = s_sig[j];
-        Uo[(size_t)t * k + i] = s > T(0) ? W[(size_t)j * k + i] / s : T(0);
+        Uo[(size_t)t * k + i] = s > T(0) ? W[(size_t)j * ldw + i] * (s_d[j] / s) : T(0);
     }
     __syncthreads();
     // V_r S_r = T^T U_r = R_B (R_A^T U_r): the rows S V^T of
     // hcore_dgemm.c:484-489, transposed.  Z = R_A^T U_r reuses W's storage.
     T *Z = W;
-    for (int e = tid; e < k * r; e += kThreads) {
+    for (int e = tid; e < k * r; e += nthr) {
         const int l = e % k, t = e / k;
         T s = 0;
         for (int i = 0; i <= l; ++i) s += UA[(size_t)l * M + i] * Uo[(size_t)t * k + i];
         Z[(size_t)t * k + l] = s;
     }
     __syncthreads();
-    for (int e = tid; e < k * r; e += kThreads) {
+    for (int e = tid; e < k * r; e += nthr) {
         const int j = e % k, t = e / k;
         T s = 0;
         for (int l = j; l < k; ++l) s += VB[(size_t)l * M + j] * Z[(size_t)t * k + l];
@@ -584,7 +606,7 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
     }
     if (phases & kPhaseSVD) {
         const bool w_smem = maxK <= svd_smem_kmax;
-        gesvd_kernel<T><<<n, kThreads, svd_smem_bytes<T>(maxK, w_smem), s>>>(
+        gesvd_kernel<T><<<n, svd_threads(maxK), svd_smem_bytes<T>(maxK, w_smem), s>>>(
             d_desc, ws, d_rank, d_status, d_info, svd_smem_kmax, maxK);
     }
     if (phases & kPhaseApply) {
