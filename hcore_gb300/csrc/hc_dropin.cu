@@ -238,11 +238,15 @@ struct Single {
 
     // run phases, fetch rank and status
     int run(unsigned phases, int *rank, int *status) {
-        int kmax = 0;
-        cudaError_t e = configure_recompress<T>(k, &kmax);
+        LaunchShape shape;
+        shape.maxM = t.M;
+        shape.maxK = k;
+        shape.nbuckets = 1;
+        shape.buckets[0] = Bucket{0, 1, k};
+        cudaError_t e = configure_recompress<T>(k, &shape.svd_smem_kmax);
         if (e == cudaSuccess)
-            e = launch_recompress<T>(d_desc, 1, ws, d_rs, d_rs + 1, nullptr, t.M, k, kmax,
-                                     tc.stream, phases);
+            e = launch_recompress<T>(d_desc, 1, ws, d_rs, d_rs + 1, nullptr, shape, tc.stream,
+                                     phases);
         int *pin = (int *)((char *)tc.pin_ensure(kPinBytes) + kPinRankOff);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(pin, d_rs, 2 * sizeof(int), cudaMemcpyDeviceToHost, tc.stream);

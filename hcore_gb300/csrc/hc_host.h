@@ -14,6 +14,7 @@ const char *last_error();
 const void *device_alias(const void *p);
 bool is_device_memory(const void *p);
 int fill_desc(const hcore_lr_task &t, unsigned flags, bool translate, Desc &d, int &k_out);
+void fill_buckets(const std::vector<Desc> &descs, LaunchShape &shape);
 bool build_descs(int n, const hcore_lr_task *tasks, unsigned flags, bool translate,
                  std::vector<Desc> &descs, long long &ws_elems, int &maxM, int &maxK,
                  std::vector<int> *status0);

@@ -67,6 +67,21 @@ constexpr unsigned kPhaseStack = 1u, kPhaseQR = 2u, kPhaseSVD = 4u, kPhaseApply 
 constexpr unsigned kPhaseAll = 15u;
 constexpr int kMaxK = 512;  // largest a + c a plan accepts
 
+// Rank buckets: the descriptors of a plan are sorted by decreasing k and the
+// SVD phase is launched once per bucket of similar k, each launch sized (CTA
+// width, shared memory) for its own largest k.
+constexpr int kMaxBuckets = 24;
+struct Bucket {
+    int start, count, K;
+};
+struct LaunchShape {
+    int maxM = 1, maxK = 1, svd_smem_kmax = 0;
+    int nbuckets = 0;
+    Bucket buckets[kMaxBuckets];
+};
+// smallest bucket edge >= k
+int bucket_edge(int k);
+
 // launchers (hc_kernels.cu).  configure_recompress sets kernel attributes
 // (not capturable) and returns the largest k whose Jacobi matrices fit in
 // shared memory; launch_recompress only launches (capturable).
@@ -74,7 +89,7 @@ template <typename T>
 cudaError_t configure_recompress(int maxK, int *svd_smem_kmax);
 template <typename T>
 cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int *d_status,
-                              int *d_info, int maxM, int maxK, int svd_smem_kmax, cudaStream_t s,
+                              int *d_info, const LaunchShape &shape, cudaStream_t s,
                               unsigned phases);
 
 // dense-C updates (hc_dense.cu): per-task rank-K' form coef * P Q^T

@@ -589,12 +589,21 @@ cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
                                 optin - 64);
 }
 
+int bucket_edge(int k) {
+    static const int edges[] = {8, 16, 24, 32, 40, 48, 56, 64, 80, 96, 112, 128,
+                                160, 192, 224, 256, 320, 384, 448, 512};
+    for (int e : edges)
+        if (k <= e) return e;
+    return kMaxK;
+}
+
 template <typename T>
 cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int *d_status,
-                              int *d_info, int maxM, int maxK, int svd_smem_kmax, cudaStream_t s,
+                              int *d_info, const LaunchShape &shape, cudaStream_t s,
                               unsigned phases) {
     if (n <= 0) return cudaSuccess;
-    if (maxK > kMaxK || maxM > 32 * kMaxRowsPerLane) return cudaErrorInvalidValue;
+    const int maxM = shape.maxM;
+    if (shape.maxK > kMaxK || maxM > 32 * kMaxRowsPerLane) return cudaErrorInvalidValue;
     const int rpl = (maxM + 31) / 32;
     if (phases & kPhaseStack) stack_kernel<T><<<n, kThreads, 0, s>>>(d_desc, ws);
     if (phases & kPhaseQR) {
@@ -605,9 +614,14 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
         else launch_geqrf<T, 64>(d_desc, n, ws, s);
     }
     if (phases & kPhaseSVD) {
-        const bool w_smem = maxK <= svd_smem_kmax;
-        gesvd_kernel<T><<<n, svd_threads(maxK), svd_smem_bytes<T>(maxK, w_smem), s>>>(
-            d_desc, ws, d_rank, d_status, d_info, svd_smem_kmax, maxK);
+        for (int b = 0; b < shape.nbuckets; ++b) {
+            const Bucket &bk = shape.buckets[b];
+            if (bk.count <= 0) continue;
+            const int K = bk.K;
+            const bool w_smem = K <= shape.svd_smem_kmax;
+            gesvd_kernel<T><<<bk.count, svd_threads(K), svd_smem_bytes<T>(K, w_smem), s>>>(
+                d_desc + bk.start, ws, d_rank, d_status, d_info, shape.svd_smem_kmax, K);
+        }
     }
     if (phases & kPhaseApply) {
         if (rpl <= 4) launch_apply<T, 4>(d_desc, n, ws, d_rank, d_status, s);
@@ -622,9 +636,9 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
 template cudaError_t configure_recompress<double>(int, int *);
 template cudaError_t configure_recompress<float>(int, int *);
 template cudaError_t launch_recompress<double>(const Desc *, int, double *, int *, int *, int *,
-                                               int, int, int, cudaStream_t, unsigned);
-template cudaError_t launch_recompress<float>(const Desc *, int, float *, int *, int *, int *, int,
-                                              int, int, cudaStream_t, unsigned);
+                                               const LaunchShape &, cudaStream_t, unsigned);
+template cudaError_t launch_recompress<float>(const Desc *, int, float *, int *, int *, int *,
+                                              const LaunchShape &, cudaStream_t, unsigned);
 
 }  // namespace hc
 

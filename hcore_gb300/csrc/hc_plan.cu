@@ -111,8 +111,34 @@ int fill_desc(const hcore_lr_task &t, unsigned flags, bool translate, Desc &d, i
     return HCORE_GPU_S_OK;
 }
 
-// Build the descriptors of a batch, sorted by decreasing cost so that the
-// long updates start first (longest-processing-time order).
+// Build the descriptors of a batch, sorted by decreasing k (then cost) so that
+// the long updates start first (longest-processing-time order) and the rank
+// buckets are contiguous; rejected tasks go last.
+void fill_buckets(const std::vector<Desc> &descs, LaunchShape &shape) {
+    shape.nbuckets = 0;
+    const int n = (int)descs.size();
+    int i = 0;
+    while (i < n) {
+        const int K = descs[i].status0 ? bucket_edge(1) : bucket_edge(descs[i].k);
+        int j = i;
+        while (j < n && (descs[j].status0 ? bucket_edge(1) : bucket_edge(descs[j].k)) == K) ++j;
+        if (shape.nbuckets == kMaxBuckets) {  // cannot happen with the fixed edges; merge
+            shape.buckets[kMaxBuckets - 1].count += j - i;
+        } else {
+            shape.buckets[shape.nbuckets++] = Bucket{i, j - i, K};
+        }
+        i = j;
+    }
+    // each launch is sized for the largest k actually present in its bucket
+    for (int b = 0; b < shape.nbuckets; ++b) {
+        int K = 1;
+        const Bucket &bk = shape.buckets[b];
+        for (int x = bk.start; x < bk.start + bk.count; ++x)
+            if (!descs[x].status0) K = std::max(K, descs[x].k);
+        shape.buckets[b].K = K;
+    }
+}
+
 bool build_descs(int n, const hcore_lr_task *tasks, unsigned flags, bool translate,
                  std::vector<Desc> &descs, long long &ws_elems, int &maxM, int &maxK,
                  std::vector<int> *status0) {
@@ -126,7 +152,7 @@ bool build_descs(int n, const hcore_lr_task *tasks, unsigned flags, bool transla
         descs[i].status0 = st;
         descs[i].idx = i;
         if (status0) (*status0)[i] = st;
-        cost[i] = st ? 0.0 : (double)tasks[i].M * k * k + (double)k * k * k;
+        cost[i] = st ? -1.0 : (double)k * 1e12 + (double)tasks[i].M * k * k;
         if (!st) {
             maxM = std::max(maxM, tasks[i].M);
             maxK = std::max(maxK, k);
@@ -157,7 +183,7 @@ struct hcore_gpu_plan_s {
     int n = 0;
     unsigned flags = 0;
     int maxM = 1, maxK = 1;
-    int svd_smem_kmax = 0;
+    LaunchShape shape;
     Desc *d_desc = nullptr;
     int *d_rank = nullptr;
     int *d_status = nullptr;
@@ -193,6 +219,9 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
     std::vector<Desc> descs;
     long long ws_elems = 0;
     build_descs(n, tasks, flags, true, descs, ws_elems, p->maxM, p->maxK, nullptr);
+    fill_buckets(descs, p->shape);
+    p->shape.maxM = p->maxM;
+    p->shape.maxK = p->maxK;
     p->ws_of_task.assign(n, -1);
     p->k_of_task.assign(n, 0);
     for (const Desc &d : descs) {
@@ -201,8 +230,8 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
     }
     {
         const cudaError_t ce = precision == HCORE_GPU_F64
-                                   ? configure_recompress<double>(p->maxK, &p->svd_smem_kmax)
-                                   : configure_recompress<float>(p->maxK, &p->svd_smem_kmax);
+                                   ? configure_recompress<double>(p->maxK, &p->shape.svd_smem_kmax)
+                                   : configure_recompress<float>(p->maxK, &p->shape.svd_smem_kmax);
         if (ce != cudaSuccess) {
             set_error("hcore_gpu_plan_create: %s", cudaGetErrorString(ce));
             plan_free(p);
@@ -248,12 +277,10 @@ extern "C" int hcore_gpu_plan_execute_phases(hcore_gpu_plan p, void *stream, uns
     cudaError_t e;
     if (p->prec == HCORE_GPU_F64)
         e = launch_recompress<double>(p->d_desc, p->n, (double *)p->d_ws, p->d_rank, p->d_status,
-                                      p->d_info, p->maxM, p->maxK, p->svd_smem_kmax, s,
-                                      phases & kPhaseAll);
+                                      p->d_info, p->shape, s, phases & kPhaseAll);
     else
         e = launch_recompress<float>(p->d_desc, p->n, (float *)p->d_ws, p->d_rank, p->d_status,
-                                     p->d_info, p->maxM, p->maxK, p->svd_smem_kmax, s,
-                                     phases & kPhaseAll);
+                                     p->d_info, p->shape, s, phases & kPhaseAll);
     if (e != cudaSuccess) {
         set_error("hcore_gpu_plan_execute: %s", cudaGetErrorString(e));
         return HCORE_GPU_ECUDA;
