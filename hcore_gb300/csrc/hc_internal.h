@@ -78,6 +78,11 @@ struct LaunchShape {
     int maxM = 1, maxK = 1, svd_smem_kmax = 0;
     int nbuckets = 0;
     Bucket buckets[kMaxBuckets];
+    // optional fork/join resources so the bucket launches overlap: one stream
+    // per bucket, a fork event and one join event per bucket (plan-owned)
+    cudaStream_t side[kMaxBuckets] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kMaxBuckets] = {};
 };
 // smallest bucket edge >= k
 int bucket_edge(int k);

@@ -614,13 +614,23 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
         else launch_geqrf<T, 64>(d_desc, n, ws, s);
     }
     if (phases & kPhaseSVD) {
+        // buckets run concurrently (largest k first) when the plan provides
+        // side streams; otherwise back to back on s
+        const bool forked = shape.fork != nullptr && shape.nbuckets > 1;
+        if (forked) cudaEventRecord(shape.fork, s);
         for (int b = 0; b < shape.nbuckets; ++b) {
             const Bucket &bk = shape.buckets[b];
             if (bk.count <= 0) continue;
             const int K = bk.K;
             const bool w_smem = K <= shape.svd_smem_kmax;
-            gesvd_kernel<T><<<bk.count, svd_threads(K), svd_smem_bytes<T>(K, w_smem), s>>>(
+            cudaStream_t sb = forked ? shape.side[b] : s;
+            if (forked) cudaStreamWaitEvent(sb, shape.fork, 0);
+            gesvd_kernel<T><<<bk.count, svd_threads(K), svd_smem_bytes<T>(K, w_smem), sb>>>(
                 d_desc + bk.start, ws, d_rank, d_status, d_info, shape.svd_smem_kmax, K);
+            if (forked) {
+                cudaEventRecord(shape.join[b], sb);
+                cudaStreamWaitEvent(s, shape.join[b], 0);
+            }
         }
     }
     if (phases & kPhaseApply) {

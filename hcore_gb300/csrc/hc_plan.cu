@@ -196,6 +196,11 @@ struct hcore_gpu_plan_s {
 
 static void plan_free(hcore_gpu_plan p) {
     if (!p) return;
+    for (int b = 0; b < kMaxBuckets; ++b) {
+        if (p->shape.side[b]) cudaStreamDestroy(p->shape.side[b]);
+        if (p->shape.join[b]) cudaEventDestroy(p->shape.join[b]);
+    }
+    if (p->shape.fork) cudaEventDestroy(p->shape.fork);
     cudaFree(p->d_desc);
     cudaFree(p->d_rank);
     cudaFree(p->d_status);
@@ -222,6 +227,17 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
     fill_buckets(descs, p->shape);
     p->shape.maxM = p->maxM;
     p->shape.maxK = p->maxK;
+    if (p->shape.nbuckets > 1) {
+        bool ok = cudaEventCreateWithFlags(&p->shape.fork, cudaEventDisableTiming) == cudaSuccess;
+        for (int b = 0; ok && b < p->shape.nbuckets; ++b)
+            ok = cudaStreamCreateWithFlags(&p->shape.side[b], cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&p->shape.join[b], cudaEventDisableTiming) == cudaSuccess;
+        if (!ok) {
+            set_error("hcore_gpu_plan_create: cannot create bucket streams");
+            plan_free(p);
+            return HCORE_GPU_ECUDA;
+        }
+    }
     p->ws_of_task.assign(n, -1);
     p->k_of_task.assign(n, 0);
     for (const Desc &d : descs) {
