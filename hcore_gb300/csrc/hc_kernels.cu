@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(kThreads) geqrf_kernel(const Desc *__restrict_
 }
 
 // ---------------------------------------------------------------------------
-// phase 3: T = R_A R_B^T, one-sided Jacobi SVD, rank rule
+// phase 3: T = R_A R_B^T, SVD, rank rule
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void rr_pair(int round, int pi, int n, int &p, int &q) {
     // circle-method tournament on n (even) columns: n/2 disjoint pairs per
@@ -286,36 +286,37 @@ struct JacobiLim<float> {
     static constexpr float tiny_scale = 1e-12f;
 };
 
-// Threads per CTA of the SVD kernel for a plan whose largest k is K: one lane
-// per column pair.
+// Threads per CTA of the SVD kernel for a bucket whose largest k is K: one
+// lane per column pair.
 __host__ __device__ inline int svd_threads(int K) {
     const int np = (K + 1) / 2;
     return np <= 32 ? 32 : (np <= 64 ? 64 : (np <= 128 ? 128 : 256));
 }
-__host__ __device__ inline int svd_ldw(int k) { return k | 1; }
+__host__ __device__ inline int svd_ld(int k) { return k | 1; }
 
-// Dynamic shared memory of the SVD kernel: W (K x ldw) when it fits, then the
-// column scales, the squared column norms, the singular values and the sort
-// permutation.
+// Dynamic shared memory of the SVD kernel: two K x ld matrices (when they
+// fit), then the column scales, squared norms, singular values, Householder
+// scalars, and two index arrays.
 template <typename T>
-__host__ __device__ inline size_t svd_smem_bytes(int K, bool w_in_smem) {
-    return (w_in_smem ? (size_t)K * svd_ldw(K) * sizeof(T) : 0) + (size_t)3 * (K + 1) * sizeof(T) +
-           (size_t)(K + 1) * sizeof(int) + 64;
+__host__ __device__ inline size_t svd_smem_bytes(int K, bool in_smem) {
+    return (in_smem ? (size_t)2 * K * svd_ld(K) * sizeof(T) : 0) + (size_t)4 * (K + 1) * sizeof(T) +
+           (size_t)2 * (K + 1) * sizeof(int) + 64;
 }
 
-// One-sided (Hestenes) Jacobi on W = T, written for the FP64 issue rate of
-// this GPU (one warp FP64 instruction per ~80 cycles per SM sub-partition):
-//  * one lane per column pair of the round (the circle tournament gives k/2
-//    disjoint pairs), looping over the rows: no shuffle reductions;
-//  * scaled ("fast") rotations: column j is stored as d_j * x_j, so rotating
-//    a pair costs two FMAs per row (x_p -= t d_q/d_p x_q, x_q += t d_p/d_q x_p)
-//    and the cosine goes into the scales;
-//  * squared norms are tracked (app' = app - t apq, aqq' = aqq + t apq, exact
-//    in exact arithmetic), recomputed on strong cancellation and after every
-//    sweep, so each pair needs one dot product.
-// Convergence: every pair orthogonal to tol = k*eps relative to its norms
-// (LAPACK dgesvj's criterion).  The right singular vectors are not
-// accumulated: V_r S_r = T^T U_r = R_B (R_A^T U_r) is formed once at the end.
+// SVD of T = R_A R_B^T (k x k) by QR-preconditioned one-sided Jacobi
+// (Drmac-Veselic): T P = Q R with column pivoting, then one-sided Jacobi on
+// R^T, whose columns are graded by the pivoting, so the sweeps are few.
+// With R^T V_J = U' S (U' orthonormal):  T = (Q V_J) S (P U')^T, hence
+//   left vectors  U_T = Q V_J           (V_J accumulated by the rotations)
+//   V_T S         = P (R^T V_J)         (the rotated columns, rows permuted).
+// Written for the FP64 issue rate of this GPU (one warp FP64 instruction per
+// ~80 cycles per SM sub-partition): lanes work on whole columns or pairs of
+// columns and loop over rows, so no shuffle reductions are needed, and the
+// rotations are scaled ("fast"): column j is d_j x_j in both R^T and V_J, so
+// a rotation costs two FMAs per row and matrix.  Squared norms are tracked
+// (exact in exact arithmetic), recomputed on strong cancellation and after
+// every sweep.  Convergence: every pair orthogonal to k*eps relative to its
+// norms (LAPACK dgesvj's criterion).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict__ descs,
                                                          T *__restrict__ ws, int *__restrict__ rank,
@@ -323,9 +324,9 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
                                                          int *__restrict__ info, int smem_kmax,
                                                          int maxK) {
     extern __shared__ unsigned char smem_raw[];
-    __shared__ int s_rot;
+    __shared__ int s_rot, s_piv;
     const Desc d = descs[blockIdx.x];
-    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
     if (d.status0) {
         if (tid == 0) {
             status[d.idx] = d.status0;
@@ -339,30 +340,132 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     T *base = ws + d.ws;
     const T *UA = base + L.UA, *VB = base + L.VB;
     const bool in_smem = maxK <= smem_kmax;
-    const int ldw = in_smem ? svd_ldw(k) : k;
-    T *W = in_smem ? reinterpret_cast<T *>(smem_raw) : base + L.W;
-    T *aux = reinterpret_cast<T *>(smem_raw + (in_smem ? (size_t)maxK * svd_ldw(maxK) * sizeof(T) : 0));
+    const int ld = in_smem ? svd_ld(k) : k;
+    T *A = in_smem ? reinterpret_cast<T *>(smem_raw) : base + L.W;   // T, then QR, then V_J
+    T *B = in_smem ? A + (size_t)maxK * svd_ld(maxK) : base + L.V;   // R^T, rotated
+    T *aux = reinterpret_cast<T *>(smem_raw + (in_smem ? (size_t)2 * maxK * svd_ld(maxK) * sizeof(T) : 0));
     T *s_d = aux, *s_nrm = aux + (maxK + 1), *s_sig = aux + 2 * (maxK + 1);
-    int *s_perm = reinterpret_cast<int *>(s_sig + maxK + 1);
+    T *s_tau = aux + 3 * (maxK + 1);
+    int *s_perm = reinterpret_cast<int *>(aux + 4 * (maxK + 1));   // Jacobi sort
+    int *s_pcol = s_perm + (maxK + 1);                                // QR pivots
+    T *Yg = base + L.Uo;   // Householder vectors of Q (k x k, ld k), until Uo is written
 
-    // T = triu(R_A) triu(R_B)^T (hcore_dgemm.c:330-387): threads over rows i
-    // (coalesced in UA), VB read as a broadcast
-    for (int j = 0; j < k; ++j) {
+    // T = triu(R_A) triu(R_B)^T (hcore_dgemm.c:330-387)
+    for (int j = 0; j < k; ++j)
         for (int i = tid; i < k; i += nthr) {
             T s = 0;
             for (int l = max(i, j); l < k; ++l) s += UA[(size_t)l * M + i] * VB[(size_t)l * M + j];
-            W[(size_t)j * ldw + i] = s;
+            A[(size_t)j * ld + i] = s;
         }
+    __syncthreads();
+
+    // ---- QR with column pivoting, T P = Q R (lane per column) ----
+    for (int c = tid; c < k; c += nthr) {
+        T s = 0;
+        for (int i = 0; i < k; ++i) s += A[(size_t)c * ld + i] * A[(size_t)c * ld + i];
+        s_nrm[c] = s;   // partial column norms (rows j..k-1), squared
+        s_d[c] = s;     // norms at the last exact computation
+        s_pcol[c] = c;
     }
     __syncthreads();
-    for (int j = tid; j < k; j += nthr) {
+    for (int j = 0; j < k; ++j) {
+        // pivot: the largest remaining partial norm (warp 0)
+        if (tid < 32) {
+            T best = -1;
+            int bi = j;
+            for (int c = j + lane; c < k; c += 32)
+                if (s_nrm[c] > best) {
+                    best = s_nrm[c];
+                    bi = c;
+                }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const T ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) {
+                    best = ob;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) s_piv = bi;
+        }
+        __syncthreads();
+        const int pv = s_piv;
+        if (pv != j) {
+            for (int i = tid; i < k; i += nthr) {
+                const T x = A[(size_t)j * ld + i];
+                A[(size_t)j * ld + i] = A[(size_t)pv * ld + i];
+                A[(size_t)pv * ld + i] = x;
+            }
+            if (tid == 0) {
+                T x = s_nrm[j]; s_nrm[j] = s_nrm[pv]; s_nrm[pv] = x;
+                x = s_d[j]; s_d[j] = s_d[pv]; s_d[pv] = x;
+                const int ci = s_pcol[j]; s_pcol[j] = s_pcol[pv]; s_pcol[pv] = ci;
+            }
+        }
+        __syncthreads();
+        // reflector of column j, rows j..k-1 (dlarfg), by thread 0
+        if (tid == 0) {
+            T *aj = A + (size_t)j * ld;
+            const T alpha = aj[j];
+            T ss = 0;
+            for (int i = j + 1; i < k; ++i) ss += aj[i] * aj[i];
+            T tj = 0;
+            if (ss > T(0)) {
+                const T beta = -copysign(sqrt(alpha * alpha + ss), alpha);
+                tj = (beta - alpha) / beta;
+                const T scal = T(1) / (alpha - beta);
+                for (int i = j + 1; i < k; ++i) aj[i] *= scal;
+                aj[j] = beta;
+            }
+            s_tau[j] = tj;
+        }
+        __syncthreads();
+        // apply to the trailing columns and downdate their norms (lane per column)
+        const T tj = s_tau[j];
+        for (int c = j + 1 + tid; c < k; c += nthr) {
+            T *ac = A + (size_t)c * ld;
+            const T *aj = A + (size_t)j * ld;
+            if (tj != T(0)) {
+                T dot = ac[j];
+                for (int i = j + 1; i < k; ++i) dot += aj[i] * ac[i];
+                const T s = tj * dot;
+                ac[j] -= s;
+                for (int i = j + 1; i < k; ++i) ac[i] -= s * aj[i];
+            }
+            // partial norm of rows j+1..k-1 (dlaqp2's downdate with recomputation)
+            const T rjc = ac[j];
+            T nn = s_nrm[c] - rjc * rjc;
+            if (nn <= s_d[c] * T(1.0 / 1024) || nn <= T(0)) {
+                T s = 0;
+                for (int i = j + 1; i < k; ++i) s += ac[i] * ac[i];
+                nn = s;
+                s_d[c] = s;
+            }
+            s_nrm[c] = nn;
+        }
+        __syncthreads();
+    }
+    // Q's reflectors to global (read back when forming U_T = Q V_J); B = R^T;
+    // A = I (V_J)
+    for (int j = 0; j < k; ++j)
+        for (int i = tid; i < k; i += nthr) {
+            const T x = A[(size_t)j * ld + i];
+            Yg[(size_t)j * k + i] = i > j ? x : T(0);
+            B[(size_t)i * ld + j] = i <= j ? x : T(0);   // B(j, i) = R(i, j)
+        }
+    __syncthreads();
+    for (int j = 0; j < k; ++j)
+        for (int i = tid; i < k; i += nthr) A[(size_t)j * ld + i] = i == j ? T(1) : T(0);
+    for (int c = tid; c < k; c += nthr) {
         T s = 0;
-        for (int i = 0; i < k; ++i) s += W[(size_t)j * ldw + i] * W[(size_t)j * ldw + i];
-        s_nrm[j] = s;
-        s_d[j] = T(1);
+        for (int i = 0; i < k; ++i) s += B[(size_t)c * ld + i] * B[(size_t)c * ld + i];
+        s_nrm[c] = s;
+        s_d[c] = T(1);
     }
     __syncthreads();
 
+    // ---- one-sided Jacobi on B = R^T, rotations accumulated in A ----
     const int n = k + (k & 1);
     const int np = n / 2;
     const T tol = T(k > 8 ? k : 8) * Lim<T>::eps;
@@ -376,7 +479,7 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
                 int p, q;
                 rr_pair(round, pi, n, p, q);
                 if (p >= k || q >= k) continue;
-                T *xp = W + (size_t)p * ldw, *xq = W + (size_t)q * ldw;
+                T *xp = B + (size_t)p * ld, *xq = B + (size_t)q * ld;
                 T dot = 0;
                 for (int i = 0; i < k; ++i) dot += xp[i] * xq[i];
                 const T dp = s_d[p], dq = s_d[q];
@@ -389,17 +492,20 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
                                     ? T(0.5) / zeta
                                     : copysign(T(1), zeta) / (az + sqrt(T(1) + az * az));
                     const T cs = T(1) / sqrt(T(1) + t * t);
-                    // true columns p' = c (p - t q), q' = c (q + t p)
+                    // true columns p' = c (p - t q), q' = c (q + t p), in B and V_J
                     const T f1 = t * dq / dp, f2 = t * dp / dq;
+                    T *vp = A + (size_t)p * ld, *vq = A + (size_t)q * ld;
                     for (int i = 0; i < k; ++i) {
                         const T a = xp[i], b = xq[i];
                         xp[i] = a - f1 * b;
                         xq[i] = b + f2 * a;
+                        const T u = vp[i], v = vq[i];
+                        vp[i] = u - f1 * v;
+                        vq[i] = v + f2 * u;
                     }
                     T np_ = app - t * apq, nq_ = aqq + t * apq;
-                    T dp2 = dp * cs, dq2 = dq * cs;
-                    // strong cancellation in a tracked norm: recompute it
-                    if (np_ < app * T(1.0 / 64)) {
+                    const T dp2 = dp * cs, dq2 = dq * cs;
+                    if (np_ < app * T(1.0 / 64)) {  // strong cancellation: recompute
                         T s = 0;
                         for (int i = 0; i < k; ++i) s += xp[i] * xp[i];
                         np_ = dp2 * dp2 * s;
@@ -420,10 +526,14 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         }
         // exact norms once per sweep; fold scales before they underflow
         for (int j = tid; j < k; j += nthr) {
-            T *xj = W + (size_t)j * ldw;
+            T *xj = B + (size_t)j * ld;
             T dj = s_d[j];
             if (dj < JacobiLim<T>::tiny_scale) {
-                for (int i = 0; i < k; ++i) xj[i] *= dj;
+                T *vj = A + (size_t)j * ld;
+                for (int i = 0; i < k; ++i) {
+                    xj[i] *= dj;
+                    vj[i] *= dj;
+                }
                 dj = T(1);
                 s_d[j] = dj;
             }
@@ -436,7 +546,7 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         __syncthreads();
     }
 
-    // singular values = true column norms; sort descending (ties by index)
+    // singular values = true column norms of B; sort descending (ties by index)
     for (int j = tid; j < k; j += nthr) s_sig[j] = sqrt(s_nrm[j]);
     __syncthreads();
     for (int j = tid; j < k; j += nthr) {
@@ -469,30 +579,39 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     else if (r > d.max_rank) st = HCORE_GPU_S_RANK_MAX;
     else if (r > d.storage_rank) st = HCORE_GPU_S_STORAGE;
 
-    // U_r = W(:, perm) d / sigma  (k x r, ld k)
+    // V_r S_r = P (B's true columns): row P(i) of the output is row i of B
+    // (the rows S V^T of hcore_dgemm.c:484-489, transposed)
     T *Uo = base + L.Uo, *Vo = base + L.Vo;
     for (int e = tid; e < k * r; e += nthr) {
         const int i = e % k, t = e / k;
         const int j = s_perm[t];
-        const T s = s_sig[j];
-        Uo[(size_t)t * k + i] = s > T(0) ? W[(size_t)j * ldw + i] * (s_d[j] / s) : T(0);
+        Vo[(size_t)t * k + s_pcol[i]] = s_d[j] * B[(size_t)j * ld + i];
+    }
+    __syncthreads();  // B's columns are read above and overwritten below
+    // U_r = Q (V_J's true columns), Q = H_0 ... H_{k-1}: lane per output
+    // column, reflectors from last to first; the columns are built in B
+    // (no longer needed) and then stored over the reflectors' slot
+    for (int t = tid; t < r; t += nthr) {
+        const int j = s_perm[t];
+        T *x = B + (size_t)j * ld;   // each lane owns the B column of its own j
+        const T dj = s_d[j];
+        const T *vj = A + (size_t)j * ld;
+        for (int i = 0; i < k; ++i) x[i] = dj * vj[i];
+        for (int h = k - 1; h >= 0; --h) {
+            const T th = s_tau[h];
+            if (th == T(0)) continue;
+            const T *y = Yg + (size_t)h * k;
+            T dot = x[h];
+            for (int i = h + 1; i < k; ++i) dot += y[i] * x[i];
+            const T s = th * dot;
+            x[h] -= s;
+            for (int i = h + 1; i < k; ++i) x[i] -= s * y[i];
+        }
     }
     __syncthreads();
-    // V_r S_r = T^T U_r = R_B (R_A^T U_r): the rows S V^T of
-    // hcore_dgemm.c:484-489, transposed.  Z = R_A^T U_r reuses W's storage.
-    T *Z = W;
     for (int e = tid; e < k * r; e += nthr) {
-        const int l = e % k, t = e / k;
-        T s = 0;
-        for (int i = 0; i <= l; ++i) s += UA[(size_t)l * M + i] * Uo[(size_t)t * k + i];
-        Z[(size_t)t * k + l] = s;
-    }
-    __syncthreads();
-    for (int e = tid; e < k * r; e += nthr) {
-        const int j = e % k, t = e / k;
-        T s = 0;
-        for (int l = j; l < k; ++l) s += VB[(size_t)l * M + j] * Z[(size_t)t * k + l];
-        Vo[(size_t)t * k + j] = s;
+        const int i = e % k, t = e / k;
+        Uo[(size_t)t * k + i] = B[(size_t)s_perm[t] * ld + i];
     }
     if (tid == 0) {
         rank[d.idx] = r;
