@@ -623,19 +623,30 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
 // ---------------------------------------------------------------------------
 // phase 4: CU = Q_A [U_r; 0], CV = Q_B [V_r S_r; 0]   (dormqr 'L','N')
 // ---------------------------------------------------------------------------
-// One warp owns one output column and keeps it in registers (RPL rows per
-// lane, row i = lane + 32*t); the k reflectors are applied last to first and
-// the column is stored once, coalesced, into the caller's factor.
+// A CTA owns up to kWarps output columns of one (update, side), one per warp,
+// each kept in registers (RPL rows per lane, row = lane + 32 t) for the whole
+// product.  The k reflectors are applied last to first, staged through
+// shared memory kApplyChunk at a time (one coalesced load per CTA, zero
+// outside rows j..M-1 so that the dot and the axpy need no predicates); the
+// column is stored once, coalesced, into the caller's factor.  blockIdx.z
+// selects the group of columns; groups past the new rank exit at once.
+constexpr int kApplyChunk = 8;
+
 template <typename T, int RPL>
-__global__ void __launch_bounds__(kThreads) apply_kernel(const Desc *__restrict__ descs,
+__global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) apply_kernel(const Desc *__restrict__ descs,
                                                          const T *__restrict__ ws,
                                                          const int *__restrict__ rank,
                                                          const int *__restrict__ status) {
-    __shared__ T s_tau[kMaxK];
+    extern __shared__ unsigned char smem_raw[];
+    T *sv = reinterpret_cast<T *>(smem_raw);   // kApplyChunk x (32 RPL)
+    __shared__ T s_tau[kApplyChunk];
     const Desc d = descs[blockIdx.x];
     if (d.status0 || status[d.idx] != HCORE_GPU_S_OK) return;
+    const int r = rank[d.idx];
+    const int col0 = blockIdx.z * kWarps;
+    if (col0 >= r) return;
     const int side = blockIdx.y;
-    const int M = d.M, k = d.k, r = rank[d.idx];
+    const int M = d.M, k = d.k;
     const WsLayout L = ws_layout(M, d.a, d.b, k);
     const T *base = ws + d.ws;
     const T *Y = base + (side ? L.VB : L.UA);
@@ -643,33 +654,48 @@ __global__ void __launch_bounds__(kThreads) apply_kernel(const Desc *__restrict_
     const T *X0 = base + (side ? L.Vo : L.Uo);
     T *out = (T *)(side ? d.CVo : d.CUo);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < k; i += kThreads) s_tau[i] = tau[i];
-    __syncthreads();
+    const int col = col0 + warp;
+    const bool active = col < r;
+    constexpr int ROWS = 32 * RPL;
 
-    for (int col = warp; col < r; col += kWarps) {
-        T x[RPL];
+    T x[RPL];
 #pragma unroll
-        for (int t = 0; t < RPL; ++t) {
-            const int i = lane + 32 * t;
-            x[t] = (i < k) ? X0[(size_t)col * k + i] : T(0);
+    for (int t = 0; t < RPL; ++t) {
+        const int i = lane + 32 * t;
+        x[t] = (active && i < k) ? X0[(size_t)col * k + i] : T(0);
+    }
+    const int nch = (k + kApplyChunk - 1) / kApplyChunk;
+    for (int ch = nch - 1; ch >= 0; --ch) {
+        const int j0 = ch * kApplyChunk;
+        const int nj = min(kApplyChunk, k - j0);
+        __syncthreads();  // the previous chunk is no longer read
+        for (int e = tid; e < nj * ROWS; e += kThreads) {
+            const int c = e / ROWS, i = e % ROWS;
+            const int j = j0 + c;
+            T v = T(0);
+            if (i > j && i < M) v = Y[(size_t)j * M + i];
+            else if (i == j) v = T(1);
+            sv[c * ROWS + i] = v;
         }
-        for (int j = k - 1; j >= 0; --j) {
-            const T tj = s_tau[j];
+        if (tid < nj) s_tau[tid] = tau[j0 + tid];
+        __syncthreads();
+        if (!active) continue;
+        for (int c = nj - 1; c >= 0; --c) {
+            const T tj = s_tau[c];
             if (tj == T(0)) continue;
-            const T *y = Y + (size_t)j * M;
-            T dot = 0;
+            const T *v = sv + c * ROWS;
+            T d0 = 0, d1 = 0;
 #pragma unroll
-            for (int t = 0; t < RPL; ++t) {
-                const int i = lane + 32 * t;
-                if (i >= j && i < M) dot += (i == j ? T(1) : y[i]) * x[t];
+            for (int t = 0; t < RPL; t += 2) {
+                d0 += v[lane + 32 * t] * x[t];
+                if (t + 1 < RPL) d1 += v[lane + 32 * (t + 1)] * x[t + 1];
             }
-            const T s = tj * warp_sum(dot);
+            const T s = tj * warp_sum(d0 + d1);
 #pragma unroll
-            for (int t = 0; t < RPL; ++t) {
-                const int i = lane + 32 * t;
-                if (i >= j && i < M) x[t] -= s * (i == j ? T(1) : y[i]);
-            }
+            for (int t = 0; t < RPL; ++t) x[t] -= s * v[lane + 32 * t];
         }
+    }
+    if (active) {
 #pragma unroll
         for (int t = 0; t < RPL; ++t) {
             const int i = lane + 32 * t;
@@ -681,8 +707,10 @@ __global__ void __launch_bounds__(kThreads) apply_kernel(const Desc *__restrict_
 // ---------------------------------------------------------------------------
 template <typename T, int RPL>
 static void launch_apply(const Desc *d_desc, int n, const T *ws, const int *d_rank,
-                         const int *d_status, cudaStream_t s) {
-    apply_kernel<T, RPL><<<dim3(n, 2), kThreads, 0, s>>>(d_desc, ws, d_rank, d_status);
+                         const int *d_status, int maxK, cudaStream_t s) {
+    const int groups = (maxK + kWarps - 1) / kWarps;   // the new rank is at most k
+    const size_t smem = (size_t)kApplyChunk * 32 * RPL * sizeof(T);
+    apply_kernel<T, RPL><<<dim3(n, 2, groups), kThreads, smem, s>>>(d_desc, ws, d_rank, d_status);
 }
 
 template <typename T, int RPL>
@@ -702,6 +730,13 @@ cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
     int kmax = 0;
     while (kmax < kMaxK && svd_smem_bytes<T>(kmax + 1, true) + 64 <= (size_t)optin) ++kmax;
     *svd_smem_kmax = kmax;
+    const int apply_smem64 = kApplyChunk * 32 * 64 * (int)sizeof(T);
+    e = cudaFuncSetAttribute(apply_kernel<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             apply_smem64);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(apply_kernel<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 apply_smem64 / 2);
+    if (e != cudaSuccess) return e;
     // the attribute is per kernel, not per plan: allow the largest size any
     // plan may launch with, so plans of different k coexist
     return cudaFuncSetAttribute(gesvd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -753,11 +788,12 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
         }
     }
     if (phases & kPhaseApply) {
-        if (rpl <= 4) launch_apply<T, 4>(d_desc, n, ws, d_rank, d_status, s);
-        else if (rpl <= 8) launch_apply<T, 8>(d_desc, n, ws, d_rank, d_status, s);
-        else if (rpl <= 16) launch_apply<T, 16>(d_desc, n, ws, d_rank, d_status, s);
-        else if (rpl <= 32) launch_apply<T, 32>(d_desc, n, ws, d_rank, d_status, s);
-        else launch_apply<T, 64>(d_desc, n, ws, d_rank, d_status, s);
+        const int K = shape.maxK;
+        if (rpl <= 4) launch_apply<T, 4>(d_desc, n, ws, d_rank, d_status, K, s);
+        else if (rpl <= 8) launch_apply<T, 8>(d_desc, n, ws, d_rank, d_status, K, s);
+        else if (rpl <= 16) launch_apply<T, 16>(d_desc, n, ws, d_rank, d_status, K, s);
+        else if (rpl <= 32) launch_apply<T, 32>(d_desc, n, ws, d_rank, d_status, K, s);
+        else launch_apply<T, 64>(d_desc, n, ws, d_rank, d_status, K, s);
     }
     return cudaGetLastError();
 }
