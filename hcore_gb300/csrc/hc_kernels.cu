@@ -204,7 +204,7 @@ __device__ __forceinline__ void make_reflector(T (&x)[RPL], int j, int M, int la
 }
 
 template <typename T, int RPL>
-__global__ void __launch_bounds__(kThreads) geqrf_kernel(const Desc *__restrict__ descs,
+__global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) geqrf_kernel(const Desc *__restrict__ descs,
                                                          T *__restrict__ ws) {
     __shared__ T sv[2][32 * RPL];
     __shared__ T s_tau[2];
@@ -239,12 +239,17 @@ __global__ void __launch_bounds__(kThreads) geqrf_kernel(const Desc *__restrict_
                 x[t] = i < M ? Ac[i] : T(0);
             }
             if (tj != T(0)) {
-                T dot = 0;
+                T d0 = 0, d1 = 0;
 #pragma unroll
-                for (int t = 0; t < RPL; ++t) dot += v[lane + 32 * t] * x[t];
-                const T sc = tj * warp_sum(dot);
+                for (int t = 0; t < RPL; t += 2) {
+                    d0 += v[lane + 32 * t] * x[t];
+                    if (t + 1 < RPL) d1 += v[lane + 32 * (t + 1)] * x[t + 1];
+                }
+                const T sc = tj * warp_sum(d0 + d1);
+                // re-read v from shared memory instead of holding RPL values in registers
+                const volatile T *vv = v;
 #pragma unroll
-                for (int t = 0; t < RPL; ++t) x[t] -= sc * v[lane + 32 * t];
+                for (int t = 0; t < RPL; ++t) x[t] -= sc * vv[lane + 32 * t];
             }
             if (col == j + 1) {
                 make_reflector<T, RPL>(x, j + 1, M, lane, Ac, sv[cur ^ 1], &s_tau[cur ^ 1], tau);
@@ -691,8 +696,9 @@ __global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) apply_kernel(cons
                 if (t + 1 < RPL) d1 += v[lane + 32 * (t + 1)] * x[t + 1];
             }
             const T s = tj * warp_sum(d0 + d1);
+            const volatile T *vv = v;  // re-read rather than hold RPL values in registers
 #pragma unroll
-            for (int t = 0; t < RPL; ++t) x[t] -= s * v[lane + 32 * t];
+            for (int t = 0; t < RPL; ++t) x[t] -= s * vv[lane + 32 * t];
         }
     }
     if (active) {
