@@ -30,6 +30,7 @@ __all__ = ["lib", "LrTask", "DenseTask", "Batch", "hcore_dgemm", "hcore_sgemm", 
 
 F64, F32 = 0, 1
 FAST_RULES = 0x1
+STAGE_INPUTS = 0x2
 STATUS = {0: "ok", 1: "zero rank", 2: "rank sum > 2*maxrk", 3: "rank sum > ld_newV",
           4: "new rank > maxrk", 5: "new rank > storage maxrank", 6: "Jacobi did not converge",
           7: "bad shape"}
@@ -107,6 +108,8 @@ def lib() -> C.CDLL:
     L.hcore_gpu_plan_device_status.restype = vp
     L.hcore_gpu_plan_workspace_bytes.argtypes = [vp]
     L.hcore_gpu_plan_workspace_bytes.restype = C.c_size_t
+    L.hcore_gpu_plan_staged_bytes.argtypes = [vp]
+    L.hcore_gpu_plan_staged_bytes.restype = C.c_size_t
     L.hcore_gpu_dgemm_batched.argtypes = [C.c_int, C.POINTER(LrTask), _ip, _ip, vp]
     L.hcore_gpu_sgemm_batched.argtypes = [C.c_int, C.POINTER(LrTask), _ip, _ip, vp]
     L.hcore_gpu_dense_batched.argtypes = [C.c_int, C.POINTER(DenseTask), vp]
@@ -253,6 +256,10 @@ class Batch:
     @property
     def device_status_ptr(self) -> int:
         return lib().hcore_gpu_plan_device_status(self._plan)
+
+    @property
+    def staged_bytes(self) -> int:
+        return int(lib().hcore_gpu_plan_staged_bytes(self._plan))
 
     @property
     def workspace_bytes(self) -> int:

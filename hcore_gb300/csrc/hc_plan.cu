@@ -192,7 +192,105 @@ struct hcore_gpu_plan_s {
     size_t ws_bytes = 0;
     std::vector<long long> ws_of_task;
     std::vector<int> k_of_task;
+    // HCORE_GPU_STAGE_INPUTS: host input ranges merged into segments, each
+    // mirrored in d_mirror and refreshed by one copy per execute
+    struct Segment {
+        const char *host;
+        size_t bytes, off;
+    };
+    std::vector<Segment> segs;
+    char *d_mirror = nullptr;
+    size_t staged_bytes = 0;
 };
+
+namespace {
+bool is_host_memory(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;  // unknown to CUDA: ordinary host memory
+    }
+    return at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeUnregistered;
+}
+
+// Replace every host input pointer of the tasks by its address in a device
+// mirror of the merged host ranges.  Returns false on allocation failure.
+bool stage_inputs(hcore_gpu_plan p, std::vector<hcore_lr_task> &tt, size_t esz) {
+    struct Rng {
+        const char *lo, *hi;
+    };
+    std::vector<Rng> rr;
+    auto add = [&](const void *ptr, int rows, int ld, int ncol) {
+        if (!ptr || ncol <= 0 || rows <= 0 || !is_host_memory(ptr)) return;
+        const char *lo = (const char *)ptr;
+        rr.push_back({lo, lo + ((size_t)(ncol - 1) * ld + rows) * esz});
+    };
+    for (const hcore_lr_task &t : tt) {
+        if (t.a > 0) {
+            add(t.AU, t.M, t.lda, t.a);
+            add(t.AV, t.M, t.lda, t.a);
+        }
+        if (t.Bdense) add(t.Bdense, t.M, t.ldb, t.M);
+        else if (t.b > 0) {
+            add(t.BU, t.M, t.ldb, t.b);
+            add(t.BV, t.M, t.ldb, t.b);
+        }
+        if (t.c > 0) {
+            add(t.CU, t.M, t.ldc, t.c);
+            add(t.CV, t.M, t.ldc, t.c);
+        }
+    }
+    if (rr.empty()) return true;
+    std::sort(rr.begin(), rr.end(), [](const Rng &x, const Rng &y) { return x.lo < y.lo; });
+    std::vector<Rng> merged;
+    for (const Rng &r : rr) {
+        if (!merged.empty() && r.lo <= merged.back().hi)
+            merged.back().hi = std::max(merged.back().hi, r.hi);
+        else
+            merged.push_back(r);
+    }
+    size_t off = 0;
+    for (const Rng &m : merged) {
+        p->segs.push_back({m.lo, (size_t)(m.hi - m.lo), off});
+        off += ((size_t)(m.hi - m.lo) + 255) & ~(size_t)255;
+    }
+    p->staged_bytes = 0;
+    for (const auto &sg : p->segs) p->staged_bytes += sg.bytes;
+    if (cudaMalloc(&p->d_mirror, off) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    // translate: the segment holding each host pointer (binary search)
+    auto tr = [&](const void *ptr) -> const void * {
+        if (!ptr || !is_host_memory(ptr)) return ptr;
+        const char *c = (const char *)ptr;
+        size_t lo = 0, hi = p->segs.size();
+        while (hi - lo > 1) {
+            const size_t mid = (lo + hi) / 2;
+            if (p->segs[mid].host <= c) lo = mid;
+            else hi = mid;
+        }
+        const auto &sg = p->segs[lo];
+        return p->d_mirror + sg.off + (size_t)(c - sg.host);
+    };
+    for (hcore_lr_task &t : tt) {
+        if (t.a > 0) {
+            t.AU = tr(t.AU);
+            t.AV = tr(t.AV);
+        }
+        if (t.Bdense) t.Bdense = tr(t.Bdense);
+        else if (t.b > 0) {
+            t.BU = tr(t.BU);
+            t.BV = tr(t.BV);
+        }
+        if (t.c > 0) {
+            t.CU = tr(t.CU);
+            t.CV = tr(t.CV);
+        }
+    }
+    return true;
+}
+}  // namespace
 
 static void plan_free(hcore_gpu_plan p) {
     if (!p) return;
@@ -206,6 +304,7 @@ static void plan_free(hcore_gpu_plan p) {
     cudaFree(p->d_status);
     cudaFree(p->d_info);
     cudaFree(p->d_ws);
+    cudaFree(p->d_mirror);
     delete p;
 }
 
@@ -223,6 +322,16 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
     p->flags = flags;
     std::vector<Desc> descs;
     long long ws_elems = 0;
+    std::vector<hcore_lr_task> staged;
+    if ((flags & HCORE_GPU_STAGE_INPUTS) && n > 0) {
+        staged.assign(tasks, tasks + n);
+        if (!stage_inputs(p, staged, precision == HCORE_GPU_F64 ? sizeof(double) : sizeof(float))) {
+            set_error("hcore_gpu_plan_create: cannot allocate the input mirror");
+            plan_free(p);
+            return HCORE_GPU_ENOMEM;
+        }
+        tasks = staged.data();
+    }
     build_descs(n, tasks, flags, true, descs, ws_elems, p->maxM, p->maxK, nullptr);
     fill_buckets(descs, p->shape);
     p->shape.maxM = p->maxM;
@@ -290,7 +399,15 @@ extern "C" int hcore_gpu_plan_execute_phases(hcore_gpu_plan p, void *stream, uns
         return HCORE_GPU_EINVAL;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e;
+    cudaError_t e = cudaSuccess;
+    if (phases & kPhaseStack)
+        for (const auto &sg : p->segs) {
+            e = cudaMemcpyAsync(p->d_mirror + sg.off, sg.host, sg.bytes, cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) {
+                set_error("hcore_gpu_plan_execute: staging copy failed: %s", cudaGetErrorString(e));
+                return HCORE_GPU_ECUDA;
+            }
+        }
     if (p->prec == HCORE_GPU_F64)
         e = launch_recompress<double>(p->d_desc, p->n, (double *)p->d_ws, p->d_rank, p->d_status,
                                       p->d_info, p->shape, s, phases & kPhaseAll);
@@ -331,6 +448,7 @@ extern "C" int hcore_gpu_plan_sweeps(hcore_gpu_plan p, int *sweeps, void *stream
 }
 
 extern "C" size_t hcore_gpu_plan_workspace_bytes(hcore_gpu_plan p) { return p ? p->ws_bytes : 0; }
+extern "C" size_t hcore_gpu_plan_staged_bytes(hcore_gpu_plan p) { return p ? p->staged_bytes : 0; }
 
 extern "C" int hcore_gpu_plan_results(hcore_gpu_plan p, int *ranks, int *status, void *stream) {
     if (!p) {

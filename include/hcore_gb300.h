@@ -57,6 +57,13 @@ extern "C" {
 
 /* flags of a plan */
 #define HCORE_GPU_FAST_RULES 0x1 /* HCORE_dgemm_fast: rank search from i=2, no maxrk checks */
+/* Host input factors (pinned or pageable) are merged into contiguous
+ * segments, mirrored on the device, and refreshed by one copy per segment at
+ * the start of every execute; shared factors (a panel tile used by many
+ * updates) cross the host link once.  Pinned segments keep execute
+ * capturable.  Outputs in pinned host memory are written in place by the
+ * rebuild kernel. */
+#define HCORE_GPU_STAGE_INPUTS 0x2
 
 /* One low-rank update.  Factors are column-major with the given leading
  * dimensions; every factor has M rows.  Ranks are plain ints. */
@@ -103,6 +110,8 @@ int hcore_gpu_plan_sigma(hcore_gpu_plan plan, int i, double *sigma, int *k, void
 int hcore_gpu_plan_sweeps(hcore_gpu_plan plan, int *sweeps, void *stream);
 /* bytes of device workspace the plan holds */
 size_t hcore_gpu_plan_workspace_bytes(hcore_gpu_plan plan);
+/* bytes copied host->device by every execute (HCORE_GPU_STAGE_INPUTS) */
+size_t hcore_gpu_plan_staged_bytes(hcore_gpu_plan plan);
 int hcore_gpu_plan_destroy(hcore_gpu_plan plan);
 
 /* one-shot synchronous batch: create, execute, results, destroy */

@@ -294,3 +294,51 @@ def test_dgemm_dense_dropin(hc):
         L.HCORE_dgemm_dense(ta, tb, M, N, K, 0.7, A.ctypes.data_as(dp), A.shape[0],
                             B.ctypes.data_as(dp), B.shape[0], -1.3, Cm.ctypes.data_as(dp), M)
         np.testing.assert_allclose(Cm, ref, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_staged_host_inputs_equal_device_plan(hc, pinned):
+    """HCORE_GPU_STAGE_INPUTS: host factors (pinned or pageable) in one arena,
+    tiles shared between updates; results identical to the device plan's."""
+    import torch
+    from hcore_gb300 import devmem
+
+    rng = np.random.default_rng(77)
+    M, ranks = 128, [9, 12, 7, 15, 10]
+    facs = [O.graded_lowrank(rng, M, r) for r in ranks]
+    arenaU = np.concatenate([u.T.reshape(-1) for u, _ in facs])
+    arenaV = np.concatenate([v.T.reshape(-1) for _, v in facs])
+    offs = np.concatenate([[0], np.cumsum([M * r for r in ranks])])
+    hU, hV = torch.from_numpy(arenaU.copy()), torch.from_numpy(arenaV.copy())
+    if pinned:
+        hU, hV = hU.pin_memory(), hV.pin_memory()
+    dU, dV = hU.cuda(), hV.cuda()
+    pairs = [(0, 1, 2), (0, 3, 4), (1, 3, 2), (4, 0, 1)]   # (A, B, C) slots; tiles shared
+    kmax = max(ranks[x] + ranks[z] for x, _, z in pairs)
+    outs = {}
+    for mode in ("device", "staged"):
+        oU = torch.zeros(len(pairs) * M * kmax, dtype=torch.float64, device="cuda")
+        oV = torch.zeros_like(oU)
+        baseU, baseV = (dU, dV) if mode == "device" else (hU, hV)
+        tasks = []
+        for u, (x, y, z) in enumerate(pairs):
+            e = 8
+            tasks.append(hc.LrTask(
+                M=M, a=ranks[x], b=ranks[y], c=ranks[z], rk=0, maxrk=kmax, ld_newv=0,
+                storage_maxrank=0, alpha=-1.0, beta=1.0, acc=1e-8,
+                AU=baseU.data_ptr() + e * int(offs[x]), AV=baseV.data_ptr() + e * int(offs[x]), lda=M,
+                BU=baseU.data_ptr() + e * int(offs[y]), BV=baseV.data_ptr() + e * int(offs[y]), ldb=M,
+                Bdense=None,
+                CU=baseU.data_ptr() + e * int(offs[z]), CV=baseV.data_ptr() + e * int(offs[z]), ldc=M,
+                CUo=oU.data_ptr() + e * u * M * kmax, CVo=oV.data_ptr() + e * u * M * kmax, ldco=M))
+        b = hc.Batch(tasks, flags=hc.STAGE_INPUTS if mode == "staged" else 0)
+        b.execute()
+        rk, st = b.results()
+        assert (st == 0).all()
+        if mode == "staged":
+            assert b.staged_bytes == (arenaU.nbytes + arenaV.nbytes)   # each tile once
+        outs[mode] = (rk.copy(), oU.cpu().numpy(), oV.cpu().numpy())
+        b.close()
+    assert np.array_equal(outs["device"][0], outs["staged"][0])
+    assert np.array_equal(outs["device"][1], outs["staged"][1])
+    assert np.array_equal(outs["device"][2], outs["staged"][2])
