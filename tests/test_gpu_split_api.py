@@ -79,16 +79,19 @@ def _two_phase(hc, prefix, dtype, M, alpha, AU, AV, a, BU, BV, b, Bd, beta, CU, 
 @pytest.mark.parametrize("prefix,dtype,tol", [("d", np.float64, 1e-11), ("s", np.float32, 5e-5)])
 def test_split_api_matches_oracle(hc, port, prefix, dtype, tol):
     rng = np.random.default_rng(61)
-    M, a, b, c, maxrk, storage = 160, 14, 11, 30, 24, 40           # a + c = 44 <= 2*maxrk
-    AU, AV = O.graded_lowrank(rng, M, a, 6.0)
-    BU, BV = O.graded_lowrank(rng, M, b, 6.0)
-    CU, CV = O.graded_lowrank(rng, M, c, 6.0)
+    # compmaxrank 24: a + c = 44 <= 2*maxrk = ld_newV; the new rank must stay
+    # <= maxrk and <= storage_maxrank, or the reference exits (hcore_dgemm.c:465)
+    M, a, b, c, maxrk, storage = 160, 14, 11, 20, 24, 24
+    AU, AV = O.graded_lowrank(rng, M, a, 12.0)
+    BU, BV = O.graded_lowrank(rng, M, b, 12.0)
+    CU, CV = O.graded_lowrank(rng, M, c, 12.0)
     acc = 1e-4 if dtype == np.float32 else 1e-8
-    r, CUo, CVo, fl1, fl = _two_phase(hc, prefix, dtype, M, -1.0, AU, AV, a, BU, BV, b, None,
-                                      1.0, CU, CV, c, maxrk, storage, acc)
     ref = port.gemm(M, -1.0, AU, AV, a, BU, BV, b, 1.0, CU, CV, c, maxrk=maxrk,
                     storage_maxrank=storage, acc=acc, variant=2, dtype=dtype)
-    assert ref["status"] == 0 and r == ref["rank"]
+    assert ref["status"] == 0, "case must be valid for the reference (it would exit)"
+    r, CUo, CVo, fl1, fl = _two_phase(hc, prefix, dtype, M, -1.0, AU, AV, a, BU, BV, b, None,
+                                      1.0, CU, CV, c, maxrk, storage, acc)
+    assert r == ref["rank"]
     assert fl == ref["flops"]                    # both phases together: the reference model
     P = CUo.astype(np.float64) @ CVo.T.astype(np.float64)
     Pr = ref["CU"].astype(np.float64) @ ref["CV"].T.astype(np.float64)
@@ -98,16 +101,17 @@ def test_split_api_matches_oracle(hc, port, prefix, dtype, tol):
 def test_split_api_dense_b_matches_oracle(hc, port):
     """HCORE_dgemm_qr_svd_b_dense: B is a dense M x M tile, G = B * AV."""
     rng = np.random.default_rng(62)
-    M, a, c, maxrk, storage = 128, 12, 16, 16, 32
+    M, a, c, maxrk, storage = 128, 12, 16, 32, 32
     AU, AV = O.graded_lowrank(rng, M, a, 4.0)
     CU, CV = O.graded_lowrank(rng, M, c, 4.0)
     XU, XV = O.graded_lowrank(rng, M, 40, 10.0)
     Bd = np.asfortranarray(XU @ XV.T)
-    r, CUo, CVo, fl1, fl = _two_phase(hc, "d", np.float64, M, -1.0, AU, AV, a, None, None, 0, Bd,
-                                      1.0, CU, CV, c, maxrk, storage, 1e-8)
     ref = port.gemm(M, -1.0, AU, AV, a, None, np.zeros((M, 1)), 0, 1.0, CU, CV, c, maxrk=maxrk,
                     storage_maxrank=storage, acc=1e-8, variant=2, dense_B=Bd)
-    assert ref["status"] == 0 and r == ref["rank"]
+    assert ref["status"] == 0, "case must be valid for the reference (it would exit)"
+    r, CUo, CVo, fl1, fl = _two_phase(hc, "d", np.float64, M, -1.0, AU, AV, a, None, None, 0, Bd,
+                                      1.0, CU, CV, c, maxrk, storage, 1e-8)
+    assert r == ref["rank"]
     assert fl == ref["flops"]
     D = 1.0 * (CU @ CV.T) - (AU @ AV.T) @ Bd.T
     assert O.rel_fro(CUo @ CVo.T, ref["CU"] @ ref["CV"].T) < 1e-11
