@@ -6,6 +6,7 @@
 #include <climits>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -183,7 +184,18 @@ struct hcore_gpu_plan_s {
     int n = 0;
     unsigned flags = 0;
     int maxM = 1, maxK = 1;
-    LaunchShape shape;
+    LaunchShape shape;  // of the whole plan when it runs as one group
+    // stream groups: the sorted updates are dealt round-robin into groups,
+    // each launched on its own stream so that one group's latency-bound SVD
+    // CTAs share the SMs with another group's FP64-bound QR/rebuild CTAs
+    struct Group {
+        int start = 0, count = 0;
+        LaunchShape shape;
+        cudaStream_t stream = nullptr;
+        cudaEvent_t done = nullptr;
+    };
+    std::vector<Group> groups;
+    cudaEvent_t gfork = nullptr;
     Desc *d_desc = nullptr;
     int *d_rank = nullptr;
     int *d_status = nullptr;
@@ -299,6 +311,11 @@ static void plan_free(hcore_gpu_plan p) {
         if (p->shape.join[b]) cudaEventDestroy(p->shape.join[b]);
     }
     if (p->shape.fork) cudaEventDestroy(p->shape.fork);
+    for (auto &g : p->groups) {
+        if (g.stream) cudaStreamDestroy(g.stream);
+        if (g.done) cudaEventDestroy(g.done);
+    }
+    if (p->gfork) cudaEventDestroy(p->gfork);
     cudaFree(p->d_desc);
     cudaFree(p->d_rank);
     cudaFree(p->d_status);
@@ -333,18 +350,51 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
         tasks = staged.data();
     }
     build_descs(n, tasks, flags, true, descs, ws_elems, p->maxM, p->maxK, nullptr);
-    fill_buckets(descs, p->shape);
-    p->shape.maxM = p->maxM;
-    p->shape.maxK = p->maxK;
-    if (p->shape.nbuckets > 1) {
-        bool ok = cudaEventCreateWithFlags(&p->shape.fork, cudaEventDisableTiming) == cudaSuccess;
-        for (int b = 0; ok && b < p->shape.nbuckets; ++b)
-            ok = cudaStreamCreateWithFlags(&p->shape.side[b], cudaStreamNonBlocking) == cudaSuccess &&
-                 cudaEventCreateWithFlags(&p->shape.join[b], cudaEventDisableTiming) == cudaSuccess;
+    // stream groups (HCORE_GPU_STREAMS, default 4): deal the k-sorted
+    // descriptors round-robin so every group gets the same mix of sizes
+    int ngroups = 4;
+    if (const char *env = getenv("HCORE_GPU_STREAMS")) ngroups = atoi(env);
+    ngroups = std::max(1, std::min(ngroups, std::min(n > 0 ? n : 1, 16)));
+    if (ngroups > 1) {
+        std::vector<Desc> dealt;
+        dealt.reserve(n);
+        for (int g = 0; g < ngroups; ++g) {
+            hcore_gpu_plan_s::Group grp;
+            grp.start = (int)dealt.size();
+            for (int i = g; i < n; i += ngroups) dealt.push_back(descs[i]);
+            grp.count = (int)dealt.size() - grp.start;
+            p->groups.push_back(grp);
+        }
+        descs.swap(dealt);
+        bool ok = cudaEventCreateWithFlags(&p->gfork, cudaEventDisableTiming) == cudaSuccess;
+        for (auto &g : p->groups) {
+            std::vector<Desc> sub(descs.begin() + g.start, descs.begin() + g.start + g.count);
+            fill_buckets(sub, g.shape);
+            g.shape.maxM = p->maxM;
+            g.shape.maxK = p->maxK;
+            ok = ok && cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming) == cudaSuccess;
+        }
         if (!ok) {
-            set_error("hcore_gpu_plan_create: cannot create bucket streams");
+            set_error("hcore_gpu_plan_create: cannot create group streams");
             plan_free(p);
             return HCORE_GPU_ECUDA;
+        }
+    } else {
+        fill_buckets(descs, p->shape);
+        p->shape.maxM = p->maxM;
+        p->shape.maxK = p->maxK;
+        if (p->shape.nbuckets > 1) {
+            bool ok = cudaEventCreateWithFlags(&p->shape.fork, cudaEventDisableTiming) == cudaSuccess;
+            for (int b = 0; ok && b < p->shape.nbuckets; ++b)
+                ok = cudaStreamCreateWithFlags(&p->shape.side[b], cudaStreamNonBlocking) ==
+                         cudaSuccess &&
+                     cudaEventCreateWithFlags(&p->shape.join[b], cudaEventDisableTiming) == cudaSuccess;
+            if (!ok) {
+                set_error("hcore_gpu_plan_create: cannot create bucket streams");
+                plan_free(p);
+                return HCORE_GPU_ECUDA;
+            }
         }
     }
     p->ws_of_task.assign(n, -1);
@@ -357,6 +407,7 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
         const cudaError_t ce = precision == HCORE_GPU_F64
                                    ? configure_recompress<double>(p->maxK, &p->shape.svd_smem_kmax)
                                    : configure_recompress<float>(p->maxK, &p->shape.svd_smem_kmax);
+        for (auto &g : p->groups) g.shape.svd_smem_kmax = p->shape.svd_smem_kmax;
         if (ce != cudaSuccess) {
             set_error("hcore_gpu_plan_create: %s", cudaGetErrorString(ce));
             plan_free(p);
@@ -408,12 +459,25 @@ extern "C" int hcore_gpu_plan_execute_phases(hcore_gpu_plan p, void *stream, uns
                 return HCORE_GPU_ECUDA;
             }
         }
-    if (p->prec == HCORE_GPU_F64)
-        e = launch_recompress<double>(p->d_desc, p->n, (double *)p->d_ws, p->d_rank, p->d_status,
-                                      p->d_info, p->shape, s, phases & kPhaseAll);
-    else
-        e = launch_recompress<float>(p->d_desc, p->n, (float *)p->d_ws, p->d_rank, p->d_status,
-                                     p->d_info, p->shape, s, phases & kPhaseAll);
+    auto launch = [&](const Desc *dd, int cnt, const LaunchShape &sh, cudaStream_t st) {
+        return p->prec == HCORE_GPU_F64
+                   ? launch_recompress<double>(dd, cnt, (double *)p->d_ws, p->d_rank, p->d_status,
+                                               p->d_info, sh, st, phases & kPhaseAll)
+                   : launch_recompress<float>(dd, cnt, (float *)p->d_ws, p->d_rank, p->d_status,
+                                              p->d_info, sh, st, phases & kPhaseAll);
+    };
+    if (p->groups.empty()) {
+        e = launch(p->d_desc, p->n, p->shape, s);
+    } else {
+        e = cudaEventRecord(p->gfork, s);
+        for (auto &g : p->groups) {
+            if (e != cudaSuccess) break;
+            e = cudaStreamWaitEvent(g.stream, p->gfork, 0);
+            if (e == cudaSuccess && g.count > 0) e = launch(p->d_desc + g.start, g.count, g.shape, g.stream);
+            if (e == cudaSuccess) e = cudaEventRecord(g.done, g.stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g.done, 0);
+        }
+    }
     if (e != cudaSuccess) {
         set_error("hcore_gpu_plan_execute: %s", cudaGetErrorString(e));
         return HCORE_GPU_ECUDA;
