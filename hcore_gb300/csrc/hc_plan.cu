@@ -314,6 +314,11 @@ static void plan_free(hcore_gpu_plan p) {
     for (auto &g : p->groups) {
         if (g.stream) cudaStreamDestroy(g.stream);
         if (g.done) cudaEventDestroy(g.done);
+        for (int b = 0; b < kMaxBuckets; ++b) {
+            if (g.shape.side[b]) cudaStreamDestroy(g.shape.side[b]);
+            if (g.shape.join[b]) cudaEventDestroy(g.shape.join[b]);
+        }
+        if (g.shape.fork) cudaEventDestroy(g.shape.fork);
     }
     if (p->gfork) cudaEventDestroy(p->gfork);
     cudaFree(p->d_desc);
@@ -374,6 +379,15 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
             g.shape.maxK = p->maxK;
             ok = ok && cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking) == cudaSuccess &&
                  cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming) == cudaSuccess;
+            // the group's SVD buckets run concurrently too
+            if (ok && g.shape.nbuckets > 1) {
+                ok = cudaEventCreateWithFlags(&g.shape.fork, cudaEventDisableTiming) == cudaSuccess;
+                for (int b = 0; ok && b < g.shape.nbuckets; ++b)
+                    ok = cudaStreamCreateWithFlags(&g.shape.side[b], cudaStreamNonBlocking) ==
+                             cudaSuccess &&
+                         cudaEventCreateWithFlags(&g.shape.join[b], cudaEventDisableTiming) ==
+                             cudaSuccess;
+            }
         }
         if (!ok) {
             set_error("hcore_gpu_plan_create: cannot create group streams");
