@@ -291,11 +291,18 @@ struct JacobiLim<float> {
     static constexpr float tiny_scale = 1e-12f;
 };
 
-// Threads per CTA of the SVD kernel for a bucket whose largest k is K: one
-// lane per column pair.
+// Lanes per column pair in the Jacobi sweeps of a bucket whose largest k is
+// K: a group of G lanes shares a pair's rows, so the per-round latency of one
+// update drops about G-fold while the total work stays the same.
+__host__ __device__ inline int svd_group(int K) {
+    const int np = (K + 1) / 2;
+    return np <= 32 ? 8 : (np <= 64 ? 4 : (np <= 128 ? 2 : 1));
+}
+// Threads per CTA of the SVD kernel: G lanes for each of the K/2 pairs.
 __host__ __device__ inline int svd_threads(int K) {
     const int np = (K + 1) / 2;
-    return np <= 32 ? 32 : (np <= 64 ? 64 : (np <= 128 ? 128 : 256));
+    const int t = ((np * svd_group(K) + 31) / 32) * 32;
+    return t < 32 ? 32 : (t > 256 ? 256 : t);
 }
 __host__ __device__ inline int svd_ld(int k) { return k | 1; }
 
@@ -471,8 +478,12 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     __syncthreads();
 
     // ---- one-sided Jacobi on B = R^T, rotations accumulated in A ----
+    // G lanes per pair (rows i = lig, lig+G, ...); every lane runs the same
+    // number of iterations so that the full-warp shuffles stay converged
     const int n = k + (k & 1);
     const int np = n / 2;
+    const int G = svd_group(maxK);
+    const int grp = tid / G, lig = tid % G, ngrp = nthr / G;
     const T tol = T(k > 8 ? k : 8) * Lim<T>::eps;
     bool converged = (k == 1);
     int sweeps = 0;
@@ -480,27 +491,36 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         if (tid == 0) s_rot = 0;
         __syncthreads();
         for (int round = 0; round < n - 1; ++round) {
-            for (int pi = tid; pi < np; pi += nthr) {
-                int p, q;
-                rr_pair(round, pi, n, p, q);
-                if (p >= k || q >= k) continue;
+            for (int base = 0; base < np; base += ngrp) {
+                const int pi = base + grp;
+                int p = 0, q = 0;
+                if (pi < np) rr_pair(round, pi, n, p, q);
+                const bool valid = pi < np && p < k && q < k;
                 T *xp = B + (size_t)p * ld, *xq = B + (size_t)q * ld;
                 T dot = 0;
-                for (int i = 0; i < k; ++i) dot += xp[i] * xq[i];
-                const T dp = s_d[p], dq = s_d[q];
-                const T app = s_nrm[p], aqq = s_nrm[q];
-                const T apq = dp * dq * dot;
-                if (apq != T(0) && abs(apq) > tol * sqrt(app) * sqrt(aqq)) {
+                if (valid)
+                    for (int i = lig; i < k; i += G) dot += xp[i] * xq[i];
+                for (int o = G / 2; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+                T dp = 1, dq = 1, app = 0, aqq = 0, apq = 0;
+                if (valid) {
+                    dp = s_d[p];
+                    dq = s_d[q];
+                    app = s_nrm[p];
+                    aqq = s_nrm[q];
+                    apq = dp * dq * dot;
+                }
+                const bool rot = valid && apq != T(0) && abs(apq) > tol * sqrt(app) * sqrt(aqq);
+                T t = 0, cs = 1;
+                if (rot) {
                     const T zeta = (aqq - app) / (T(2) * apq);
                     const T az = abs(zeta);
-                    const T t = az > Lim<T>::big_zeta
-                                    ? T(0.5) / zeta
-                                    : copysign(T(1), zeta) / (az + sqrt(T(1) + az * az));
-                    const T cs = T(1) / sqrt(T(1) + t * t);
+                    t = az > Lim<T>::big_zeta ? T(0.5) / zeta
+                                              : copysign(T(1), zeta) / (az + sqrt(T(1) + az * az));
+                    cs = T(1) / sqrt(T(1) + t * t);
                     // true columns p' = c (p - t q), q' = c (q + t p), in B and V_J
                     const T f1 = t * dq / dp, f2 = t * dp / dq;
                     T *vp = A + (size_t)p * ld, *vq = A + (size_t)q * ld;
-                    for (int i = 0; i < k; ++i) {
+                    for (int i = lig; i < k; i += G) {
                         const T a = xp[i], b = xq[i];
                         xp[i] = a - f1 * b;
                         xq[i] = b + f2 * a;
@@ -508,18 +528,27 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
                         vp[i] = u - f1 * v;
                         vq[i] = v + f2 * u;
                     }
-                    T np_ = app - t * apq, nq_ = aqq + t * apq;
-                    const T dp2 = dp * cs, dq2 = dq * cs;
-                    if (np_ < app * T(1.0 / 64)) {  // strong cancellation: recompute
-                        T s = 0;
-                        for (int i = 0; i < k; ++i) s += xp[i] * xp[i];
-                        np_ = dp2 * dp2 * s;
+                }
+                T np_ = app - t * apq, nq_ = aqq + t * apq;
+                const T dp2 = dp * cs, dq2 = dq * cs;
+                // strong cancellation in a tracked norm: recompute (warp-uniform)
+                const bool redo_p = rot && np_ < app * T(1.0 / 64);
+                const bool redo_q = rot && nq_ < aqq * T(1.0 / 64);
+                if (__any_sync(0xffffffffu, redo_p || redo_q)) {
+                    T sp = 0, sq = 0;
+                    if (redo_p || redo_q)
+                        for (int i = lig; i < k; i += G) {
+                            sp += xp[i] * xp[i];
+                            sq += xq[i] * xq[i];
+                        }
+                    for (int o = G / 2; o > 0; o >>= 1) {
+                        sp += __shfl_xor_sync(0xffffffffu, sp, o);
+                        sq += __shfl_xor_sync(0xffffffffu, sq, o);
                     }
-                    if (nq_ < aqq * T(1.0 / 64)) {
-                        T s = 0;
-                        for (int i = 0; i < k; ++i) s += xq[i] * xq[i];
-                        nq_ = dq2 * dq2 * s;
-                    }
+                    if (redo_p) np_ = dp2 * dp2 * sp;
+                    if (redo_q) nq_ = dq2 * dq2 * sq;
+                }
+                if (rot && lig == 0) {
                     s_nrm[p] = np_;
                     s_nrm[q] = nq_;
                     s_d[p] = dp2;
@@ -542,9 +571,9 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
                 dj = T(1);
                 s_d[j] = dj;
             }
-            T s = 0;
-            for (int i = 0; i < k; ++i) s += xj[i] * xj[i];
-            s_nrm[j] = dj * dj * s;
+            T s2 = 0;
+            for (int i = 0; i < k; ++i) s2 += xj[i] * xj[i];
+            s_nrm[j] = dj * dj * s2;
         }
         ++sweeps;
         converged = (s_rot == 0);
