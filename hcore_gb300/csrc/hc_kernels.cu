@@ -292,11 +292,13 @@ struct JacobiLim<float> {
 };
 
 // Lanes per column pair in the Jacobi sweeps of a bucket whose largest k is
-// K: a group of G lanes shares a pair's rows, so the per-round latency of one
-// update drops about G-fold while the total work stays the same.
+// K.  A group of G lanes shares a pair's rows, which divides the per-round
+// latency of one update by about G but repeats the rotation parameters in
+// every lane of the group.  Small updates are throughput-bound (one lane per
+// pair); the few large ones set the phase's critical path (four lanes).
 __host__ __device__ inline int svd_group(int K) {
     const int np = (K + 1) / 2;
-    return np <= 32 ? 8 : (np <= 64 ? 4 : (np <= 128 ? 2 : 1));
+    return np <= 24 ? 1 : (np <= 64 ? 4 : (np <= 128 ? 2 : 1));
 }
 // Threads per CTA of the SVD kernel: G lanes for each of the K/2 pairs.
 __host__ __device__ inline int svd_threads(int K) {
