@@ -30,6 +30,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "TLR-GEMM updates/s batched vs plain per-tile on 1 GB300 at rel err <= acc"
+# DRAM bytes (read + write) per algorithmic byte of each phase's kernel, from
+# one ncu capture of the 300-update case (profiles/recompression_panel_ncu.md
+# section 3); the full launch's traffic is this ratio times its own
+# algorithmic bytes
+DRAM_PER_ALG_BYTE = {"stack": 0.46, "qr": 4.44, "svd": None, "rebuild": 0.97}
 WORKLOAD = dict(workload="TLR Cholesky panel-0 Schur updates (HCORE_dgemm recompression)",
                 points=65536, dim=2, nb=1024, tiles_per_dim=64, kernel="exp(-|x-y|^2/0.01)",
                 acc=1e-8, maxrank=128, tile_compression="relative sigma >= acc*sigma_max",
@@ -293,14 +298,29 @@ def run_gb300(args):
     dom = max(ph_ms, key=ph_ms.get)
     result["phase_tflops_model"] = {nm: phase_model[nm] / (ph_ms[nm] / 1e3) / 1e12 for nm in ph_ms}
     peak = fp64_peak(L, torch, dev)
+    # algorithmic bytes of each phase (see DRAM_PER_ALG_BYTE)
+    alg_bytes = {"stack": 0, "qr": 0, "svd": 0, "rebuild": 0}
+    for u, (i, j) in enumerate(updates):
+        a = int(panel.rank[panel.index[(i, 0)]])
+        b = int(panel.rank[panel.index[(j, 0)]])
+        c = int(panel.rank[panel.index[(i, j)]])
+        kk, r = a + c, int(ranks[u])
+        alg_bytes["stack"] += 8 * nb * (2 * a + 2 * b + 2 * c) + 8 * 2 * nb * kk
+        alg_bytes["qr"] += 2 * 2 * nb * kk * 8
+        alg_bytes["rebuild"] += 2 * nb * kk * 8 + 2 * nb * r * 8
     achieved = phase_model[dom] / (ph_ms[dom] / 1e3) / 1e12
     result["phases_ms"] = ph_ms
     sw = batch.sweeps(stream.cuda_stream)
     kk = np.array([t.a + t.c for t in tasks])
     result["jacobi_sweeps"] = {"mean": float(sw.mean()), "max": int(sw.max()),
                                "k_mean": float(kk.mean()), "k_max": int(kk.max())}
+    ratio = DRAM_PER_ALG_BYTE.get(dom)
     result["roofline"] = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak,
-                          "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                          "unit": "TFLOP/s", "frac": achieved / peak,
+                          "traffic": (ratio * alg_bytes[dom]) if ratio else None,
+                          "traffic_basis": "ncu DRAM bytes per algorithmic byte of this kernel on "
+                                           "the 300-update case, times this launch's algorithmic "
+                                           f"bytes ({alg_bytes[dom]:.3e})",
                           "peak_source": "fp64 DMMA m16n8k16 issue-rate probe timed live "
                                          "(MEASURED_PEAKS.json has no FP64 figure)",
                           "flops_basis": "reference flop model (flop_counts.c) of that phase"}
