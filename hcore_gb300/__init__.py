@@ -25,12 +25,13 @@ import numpy as np
 
 from .build import LIB as _LIB_PATH
 
-__all__ = ["lib", "LrTask", "DenseTask", "Batch", "hcore_dgemm", "hcore_sgemm", "hcore_dgemm_fast",
+__all__ = ["lib", "LrTask", "DenseTask", "Batch", "DensePlan", "hcore_dgemm", "hcore_sgemm", "hcore_dgemm_fast",
            "dense_batched", "HcoreError", "STATUS", "FlopCounter"]
 
 F64, F32 = 0, 1
 FAST_RULES = 0x1
 STAGE_INPUTS = 0x2
+MIXED_FACTORS = 0x4
 STATUS = {0: "ok", 1: "zero rank", 2: "rank sum > 2*maxrk", 3: "rank sum > ld_newV",
           4: "new rank > maxrk", 5: "new rank > storage maxrank", 6: "Jacobi did not converge",
           7: "bad shape"}
@@ -113,6 +114,9 @@ def lib() -> C.CDLL:
     L.hcore_gpu_dgemm_batched.argtypes = [C.c_int, C.POINTER(LrTask), _ip, _ip, vp]
     L.hcore_gpu_sgemm_batched.argtypes = [C.c_int, C.POINTER(LrTask), _ip, _ip, vp]
     L.hcore_gpu_dense_batched.argtypes = [C.c_int, C.POINTER(DenseTask), vp]
+    L.hcore_gpu_dense_plan_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(DenseTask)]
+    L.hcore_gpu_dense_plan_execute.argtypes = [vp, vp]
+    L.hcore_gpu_dense_plan_destroy.argtypes = [vp]
     L.hcore_gpu_last_error.restype = C.c_char_p
     L.hcore_gpu_thread_stream.restype = vp
     for name, rp, real in (("HCORE_dgemm", _dp, C.c_double), ("HCORE_sgemm", _fp, C.c_float)):
@@ -268,6 +272,32 @@ class Batch:
     def close(self):
         if self._plan:
             lib().hcore_gpu_plan_destroy(self._plan)
+            self._plan = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DensePlan:
+    """HCORE_dsyrk / HCORE_dgemmcd tasks (device pointers) as a reusable plan."""
+
+    def __init__(self, tasks):
+        self.n = len(tasks)
+        self._tasks = (DenseTask * max(self.n, 1))(*tasks)
+        self._plan = C.c_void_p()
+        _check(lib().hcore_gpu_dense_plan_create(C.byref(self._plan), self.n, self._tasks),
+               "hcore_gpu_dense_plan_create")
+
+    def execute(self, stream=None):
+        _check(lib().hcore_gpu_dense_plan_execute(self._plan, stream or None),
+               "hcore_gpu_dense_plan_execute")
+
+    def close(self):
+        if self._plan:
+            lib().hcore_gpu_dense_plan_destroy(self._plan)
             self._plan = C.c_void_p()
 
     def __del__(self):

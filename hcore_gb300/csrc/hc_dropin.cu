@@ -477,86 +477,126 @@ struct DenseRun {
     DenseRun() : tc(thread_ctx()) {}
 };
 
-// Run a list of dense tasks (device-accessible pointers) on stream s.
-static int run_dense(int n, const hcore_dense_task *tasks, cudaStream_t s, bool sync) {
-    if (n <= 0) return HCORE_GPU_OK;
-    // group tasks by output tile, keeping list order inside each group
-    std::map<const double *, int> gid;
-    std::vector<std::vector<int>> groups;
-    int maxM = 1;
-    std::vector<DenseWork> work(n);
-    long long ws = 0;
-    for (int i = 0; i < n; ++i) {
-        const hcore_dense_task &t = tasks[i];
-        if ((t.kind != 0 && t.kind != 1) || t.M < 1 || t.a < 0 || t.b < 0 || !t.CD ||
-            t.ldcd < t.M) {
-            set_error("hcore_gpu_dense_batched: invalid task %d", i);
-            return HCORE_GPU_EINVAL;
-        }
-        auto it = gid.find(t.CD);
-        if (it == gid.end()) {
-            gid[t.CD] = (int)groups.size();
-            groups.push_back({i});
-        } else {
-            if (tasks[groups[it->second][0]].M != t.M) {
-                set_error("hcore_gpu_dense_batched: tasks on one tile disagree on M");
+// Host-side preparation of a list of dense tasks (device-accessible
+// pointers): group by output tile (list order kept inside each group), the
+// rank-K' form of every task and the workspace layout.
+struct DensePrep {
+    int n = 0, maxM = 1;
+    std::vector<DenseWork> work;
+    std::vector<int> gstart, gtasks;
+    long long ws = 0;  // doubles
+    size_t b_tasks = 0, b_work = 0, b_gs = 0, b_gt = 0, b_ws = 0;
+    size_t bytes() const { return b_tasks + b_work + b_gs + b_gt + b_ws; }
+    int ngroups() const { return (int)gstart.size() - 1; }
+
+    int build(int n_, const hcore_dense_task *tasks) {
+        n = n_;
+        std::map<const double *, int> gid;
+        std::vector<std::vector<int>> groups;
+        work.assign(n, DenseWork{});
+        ws = 0;
+        for (int i = 0; i < n; ++i) {
+            const hcore_dense_task &t = tasks[i];
+            if ((t.kind != 0 && t.kind != 1) || t.M < 1 || t.a < 0 || t.b < 0 || !t.CD ||
+                t.ldcd < t.M) {
+                set_error("dense tasks: invalid task %d", i);
                 return HCORE_GPU_EINVAL;
             }
-            groups[it->second].push_back(i);
+            auto it = gid.find(t.CD);
+            if (it == gid.end()) {
+                gid[t.CD] = (int)groups.size();
+                groups.push_back({i});
+            } else {
+                if (tasks[groups[it->second][0]].M != t.M) {
+                    set_error("dense tasks: tasks on one tile disagree on M");
+                    return HCORE_GPU_EINVAL;
+                }
+                groups[it->second].push_back(i);
+            }
+            maxM = std::max(maxM, t.M);
+            DenseWork &w = work[i];
+            w.ws = ws;
+            const long long sq = t.kind == 0 ? (long long)t.a * t.a : (long long)t.a * t.b;
+            const int kk = t.kind == 0 ? t.a : std::min(t.a, t.b);
+            ws += ((sq + (long long)t.M * kk + 31) / 32) * 32;
+            w.syrk = t.kind == 0;
+            w.kk = kk;
+            w.coef = t.kind == 0 ? t.alpha : -1.0;
         }
-        maxM = std::max(maxM, t.M);
-        DenseWork &w = work[i];
-        w.ws = ws;
-        const long long sq = t.kind == 0 ? (long long)t.a * t.a : (long long)t.a * t.b;
-        const int kk = t.kind == 0 ? t.a : std::min(t.a, t.b);
-        ws += ((sq + (long long)t.M * kk + 31) / 32) * 32;
-        w.syrk = t.kind == 0;
-        w.kk = kk;
-        w.coef = t.kind == 0 ? t.alpha : -1.0;
+        gstart.assign(groups.size() + 1, 0);
+        gtasks.clear();
+        for (size_t g = 0; g < groups.size(); ++g) {
+            gstart[g + 1] = gstart[g] + (int)groups[g].size();
+            for (int i : groups[g]) gtasks.push_back(i);
+        }
+        b_tasks = al256(n * sizeof(hcore_dense_task));
+        b_work = al256(n * sizeof(DenseWork));
+        b_gs = al256(gstart.size() * sizeof(int));
+        b_gt = al256(gtasks.size() * sizeof(int));
+        b_ws = al256((size_t)ws * sizeof(double));
+        return HCORE_GPU_OK;
     }
-    std::vector<int> gstart(groups.size() + 1, 0), gtasks;
-    for (size_t g = 0; g < groups.size(); ++g) {
-        gstart[g + 1] = gstart[g] + (int)groups[g].size();
-        for (int i : groups[g]) gtasks.push_back(i);
+
+    // point each task's P/Q at its inputs or at its computed factor in the
+    // workspace that starts at d_ws
+    void bind(const hcore_dense_task *tasks, const double *d_ws) {
+        for (int i = 0; i < n; ++i) {
+            const hcore_dense_task &t = tasks[i];
+            DenseWork &w = work[i];
+            const long long sq = t.kind == 0 ? (long long)t.a * t.a : (long long)t.a * t.b;
+            const double *computed = d_ws + w.ws + sq;
+            if (t.kind == 0) {
+                w.P = computed; w.ldp = t.M; w.Q = t.Au; w.ldq = t.lda;
+            } else if (t.a > t.b) {
+                w.P = computed; w.ldp = t.M; w.Q = t.Bu; w.ldq = t.M;
+            } else {
+                w.P = t.Au; w.ldp = t.M; w.Q = computed; w.ldq = t.M;
+            }
+        }
     }
+
+    // copy tasks, work and groups into `host` (pinned or not) laid out as the
+    // device arena's first b_tasks + b_work + b_gs + b_gt bytes
+    void pack(char *host, const hcore_dense_task *tasks) const {
+        memcpy(host, tasks, n * sizeof(hcore_dense_task));
+        memcpy(host + b_tasks, work.data(), n * sizeof(DenseWork));
+        memcpy(host + b_tasks + b_work, gstart.data(), gstart.size() * sizeof(int));
+        memcpy(host + b_tasks + b_work + b_gs, gtasks.data(), gtasks.size() * sizeof(int));
+    }
+
+    cudaError_t launch(char *arena, cudaStream_t s) const {
+        const hcore_dense_task *d_tasks = (const hcore_dense_task *)arena;
+        const DenseWork *d_work = (const DenseWork *)(arena + b_tasks);
+        double *d_ws = (double *)(arena + b_tasks + b_work + b_gs + b_gt);
+        cudaError_t e = launch_dense_prep(d_tasks, d_work, n, d_ws, s);
+        if (e == cudaSuccess)
+            e = launch_dense_tiles(d_tasks, d_work, (const int *)(arena + b_tasks + b_work),
+                                   (const int *)(arena + b_tasks + b_work + b_gs), ngroups(), maxM,
+                                   s);
+        return e;
+    }
+};
+
+// Run a list of dense tasks (device-accessible pointers) on stream s, in the
+// calling thread's arena.
+static int run_dense(int n, const hcore_dense_task *tasks, cudaStream_t s, bool sync) {
+    if (n <= 0) return HCORE_GPU_OK;
+    DensePrep dp;
+    int rc = dp.build(n, tasks);
+    if (rc) return rc;
     ThreadCtx &tc = thread_ctx();
-    const size_t b_tasks = al256(n * sizeof(hcore_dense_task)), b_work = al256(n * sizeof(DenseWork));
-    const size_t b_gs = al256(gstart.size() * sizeof(int)), b_gt = al256(gtasks.size() * sizeof(int));
-    const size_t b_ws = al256((size_t)ws * sizeof(double));
-    char *arena = (char *)tc.dev_ensure(b_tasks + b_work + b_gs + b_gt + b_ws);
-    char *pin = (char *)tc.pin_ensure(b_tasks + b_work + b_gs + b_gt);
+    char *arena = (char *)tc.dev_ensure(dp.bytes());
+    char *pin = (char *)tc.pin_ensure(dp.bytes() - dp.b_ws);
     if (!arena || !pin) {
         set_error("hcore_gpu_dense_batched: out of memory");
         return HCORE_GPU_ENOMEM;
     }
-    double *d_ws = (double *)(arena + b_tasks + b_work + b_gs + b_gt);
-    for (int i = 0; i < n; ++i) {
-        const hcore_dense_task &t = tasks[i];
-        DenseWork &w = work[i];
-        const long long sq = t.kind == 0 ? (long long)t.a * t.a : (long long)t.a * t.b;
-        const double *computed = d_ws + w.ws + sq;
-        if (t.kind == 0) {
-            w.P = computed; w.ldp = t.M; w.Q = t.Au; w.ldq = t.lda;
-        } else if (t.a > t.b) {
-            w.P = computed; w.ldp = t.M; w.Q = t.Bu; w.ldq = t.M;
-        } else {
-            w.P = t.Au; w.ldp = t.M; w.Q = computed; w.ldq = t.M;
-        }
-    }
+    dp.bind(tasks, (const double *)(arena + dp.b_tasks + dp.b_work + dp.b_gs + dp.b_gt));
     // the previous call on this stream may still read the pinned buffer
     cudaStreamSynchronize(s);
-    memcpy(pin, tasks, n * sizeof(hcore_dense_task));
-    memcpy(pin + b_tasks, work.data(), n * sizeof(DenseWork));
-    memcpy(pin + b_tasks + b_work, gstart.data(), gstart.size() * sizeof(int));
-    memcpy(pin + b_tasks + b_work + b_gs, gtasks.data(), gtasks.size() * sizeof(int));
-    cudaMemcpyAsync(arena, pin, b_tasks + b_work + b_gs + b_gt, cudaMemcpyHostToDevice, s);
-    const hcore_dense_task *d_tasks = (const hcore_dense_task *)arena;
-    const DenseWork *d_work = (const DenseWork *)(arena + b_tasks);
-    cudaError_t e = launch_dense_prep(d_tasks, d_work, n, d_ws, s);
-    if (e == cudaSuccess)
-        e = launch_dense_tiles(d_tasks, d_work, (const int *)(arena + b_tasks + b_work),
-                               (const int *)(arena + b_tasks + b_work + b_gs), (int)groups.size(),
-                               maxM, s);
+    dp.pack(pin, tasks);
+    cudaMemcpyAsync(arena, pin, dp.bytes() - dp.b_ws, cudaMemcpyHostToDevice, s);
+    cudaError_t e = dp.launch(arena, s);
     if (e == cudaSuccess && sync) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         set_error("hcore_gpu_dense_batched: %s", cudaGetErrorString(e));
@@ -854,13 +894,8 @@ void HCORE_sgemm_dense(HCORE_enum transA, int transB, int M, int N, int K, float
                       C, LDC);
 }
 
-int hcore_gpu_dense_batched(int n, const hcore_dense_task *tasks, void *stream) {
-    if (n < 0 || (n > 0 && !tasks)) {
-        set_error("hcore_gpu_dense_batched: invalid argument");
-        return HCORE_GPU_EINVAL;
-    }
-    // translate pinned host pointers to their device aliases
-    std::vector<hcore_dense_task> tt(tasks, tasks + n);
+static int translate_dense(int n, const hcore_dense_task *tasks, std::vector<hcore_dense_task> &tt) {
+    tt.assign(tasks, tasks + n);
     for (auto &t : tt) {
         t.Au = (const double *)device_alias(t.Au);
         t.Av = (const double *)device_alias(t.Av);
@@ -878,7 +913,84 @@ int hcore_gpu_dense_batched(int n, const hcore_dense_task *tasks, void *stream) 
             return HCORE_GPU_EINVAL;
         }
     }
+    return HCORE_GPU_OK;
+}
+
+int hcore_gpu_dense_batched(int n, const hcore_dense_task *tasks, void *stream) {
+    if (n < 0 || (n > 0 && !tasks)) {
+        set_error("hcore_gpu_dense_batched: invalid argument");
+        return HCORE_GPU_EINVAL;
+    }
+    std::vector<hcore_dense_task> tt;
+    int rc = translate_dense(n, tasks, tt);
+    if (rc) return rc;
     return run_dense(n, tt.data(), (cudaStream_t)stream, true);
+}
+
+}  // extern "C"
+
+struct hcore_gpu_dense_plan_s {
+    DensePrep prep;
+    char *arena = nullptr;
+};
+
+extern "C" {
+
+int hcore_gpu_dense_plan_create(hcore_gpu_dense_plan *plan, int n, const hcore_dense_task *tasks) {
+    if (!plan || n < 0 || (n > 0 && !tasks)) {
+        set_error("hcore_gpu_dense_plan_create: invalid argument");
+        return HCORE_GPU_EINVAL;
+    }
+    *plan = nullptr;
+    std::vector<hcore_dense_task> tt;
+    int rc = translate_dense(n, tasks, tt);
+    if (rc) return rc;
+    auto *p = new hcore_gpu_dense_plan_s;
+    rc = p->prep.build(n, tt.data());
+    if (rc) {
+        delete p;
+        return rc;
+    }
+    if (cudaMalloc(&p->arena, std::max<size_t>(p->prep.bytes(), 256)) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("hcore_gpu_dense_plan_create: cudaMalloc of %zu bytes failed", p->prep.bytes());
+        delete p;
+        return HCORE_GPU_ENOMEM;
+    }
+    p->prep.bind(tt.data(), (const double *)(p->arena + p->prep.b_tasks + p->prep.b_work +
+                                             p->prep.b_gs + p->prep.b_gt));
+    std::vector<char> host(p->prep.bytes() - p->prep.b_ws);
+    p->prep.pack(host.data(), tt.data());
+    if (cudaMemcpy(p->arena, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        set_error("hcore_gpu_dense_plan_create: upload failed");
+        cudaFree(p->arena);
+        delete p;
+        return HCORE_GPU_ECUDA;
+    }
+    *plan = p;
+    return HCORE_GPU_OK;
+}
+
+int hcore_gpu_dense_plan_execute(hcore_gpu_dense_plan p, void *stream) {
+    if (!p) {
+        set_error("hcore_gpu_dense_plan_execute: null plan");
+        return HCORE_GPU_EINVAL;
+    }
+    if (p->prep.n == 0) return HCORE_GPU_OK;
+    const cudaError_t e = p->prep.launch(p->arena, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        set_error("hcore_gpu_dense_plan_execute: %s", cudaGetErrorString(e));
+        return HCORE_GPU_ECUDA;
+    }
+    return HCORE_GPU_OK;
+}
+
+int hcore_gpu_dense_plan_destroy(hcore_gpu_dense_plan p) {
+    if (p) {
+        cudaFree(p->arena);
+        delete p;
+    }
+    return HCORE_GPU_OK;
 }
 
 void *hcore_gpu_thread_stream(void) { return (void *)thread_ctx().stream; }

@@ -76,6 +76,7 @@ struct Bucket {
 };
 struct LaunchShape {
     int maxM = 1, maxK = 1, svd_smem_kmax = 0;
+    bool mixed = false;  // FP32 factor products and rebuild (HCORE_GPU_MIXED_FACTORS)
     int nbuckets = 0;
     Bucket buckets[kMaxBuckets];
     // optional fork/join resources so the bucket launches overlap: one stream

@@ -14,7 +14,10 @@
 //              written straight into the caller's output factors
 //
 // The scalar type T is double (HCORE_dgemm) or float (HCORE_sgemm); every
-// step computes in T, like the reference's two copies.
+// step computes in T, like the reference's two copies.  With the plan flag
+// HCORE_GPU_MIXED_FACTORS an FP64 plan computes the factor products (stack)
+// and the Q.U rebuild in FP32 (compute type Tc = float, FP32 accumulation,
+// FP64 storage) while the QRs, the SVD and the truncation stay FP64.
 #include <cfloat>
 #include <climits>
 
@@ -52,7 +55,7 @@ __device__ __forceinline__ T warp_max(T v) {
 // ---------------------------------------------------------------------------
 // phase 1: stack the factors
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, typename Tc>
 __global__ void __launch_bounds__(kThreads) stack_kernel(const Desc *__restrict__ descs,
                                                          T *__restrict__ ws) {
     const Desc d = descs[blockIdx.x];
@@ -84,9 +87,10 @@ __global__ void __launch_bounds__(kThreads) stack_kernel(const Desc *__restrict_
         const T *B = (const T *)d.Bd;
         for (long long e = tid; e < (long long)M * a; e += kThreads) {
             const int i = (int)(e % M), j = (int)(e / M);
-            T s = 0;
-            for (int l = 0; l < M; ++l) s += B[(size_t)l * d.ldb + i] * AV[(size_t)j * d.lda + l];
-            G[(size_t)j * M + i] = s;
+            Tc s = 0;
+            for (int l = 0; l < M; ++l)
+                s += (Tc)B[(size_t)l * d.ldb + i] * (Tc)AV[(size_t)j * d.lda + l];
+            G[(size_t)j * M + i] = (T)s;
         }
         return;
     }
@@ -96,18 +100,18 @@ __global__ void __launch_bounds__(kThreads) stack_kernel(const Desc *__restrict_
         const int p = e % a, q = e / a;
         const T *x = AV + (size_t)p * d.lda;
         const T *y = BV + (size_t)q * d.ldb;
-        T s = 0;
-        for (int l = lane; l < M; l += 32) s += x[l] * y[l];
+        Tc s = 0;
+        for (int l = lane; l < M; l += 32) s += (Tc)x[l] * (Tc)y[l];
         s = warp_sum(s);
-        if (lane == 0) F[(size_t)q * a + p] = s;
+        if (lane == 0) F[(size_t)q * a + p] = (T)s;
     }
     __syncthreads();
     // G = BU F^T, M x a (hcore_dgemm.c:199-205)
     for (long long e = tid; e < (long long)M * a; e += kThreads) {
         const int i = (int)(e % M), p = (int)(e / M);
-        T s = 0;
-        for (int q = 0; q < b; ++q) s += BU[(size_t)q * d.ldb + i] * F[(size_t)q * a + p];
-        G[(size_t)p * M + i] = s;
+        Tc s = 0;
+        for (int q = 0; q < b; ++q) s += (Tc)BU[(size_t)q * d.ldb + i] * (Tc)F[(size_t)q * a + p];
+        G[(size_t)p * M + i] = (T)s;
     }
 }
 
@@ -668,14 +672,14 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
 // selects the group of columns; groups past the new rank exit at once.
 constexpr int kApplyChunk = 8;
 
-template <typename T, int RPL>
+template <typename T, int RPL, typename Tc>
 __global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) apply_kernel(const Desc *__restrict__ descs,
                                                          const T *__restrict__ ws,
                                                          const int *__restrict__ rank,
                                                          const int *__restrict__ status) {
     extern __shared__ unsigned char smem_raw[];
-    T *sv = reinterpret_cast<T *>(smem_raw);   // kApplyChunk x (32 RPL)
-    __shared__ T s_tau[kApplyChunk];
+    Tc *sv = reinterpret_cast<Tc *>(smem_raw);   // kApplyChunk x (32 RPL)
+    __shared__ Tc s_tau[kApplyChunk];
     const Desc d = descs[blockIdx.x];
     if (d.status0 || status[d.idx] != HCORE_GPU_S_OK) return;
     const int r = rank[d.idx];
@@ -694,11 +698,11 @@ __global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) apply_kernel(cons
     const bool active = col < r;
     constexpr int ROWS = 32 * RPL;
 
-    T x[RPL];
+    Tc x[RPL];
 #pragma unroll
     for (int t = 0; t < RPL; ++t) {
         const int i = lane + 32 * t;
-        x[t] = (active && i < k) ? X0[(size_t)col * k + i] : T(0);
+        x[t] = (active && i < k) ? (Tc)X0[(size_t)col * k + i] : Tc(0);
     }
     const int nch = (k + kApplyChunk - 1) / kApplyChunk;
     for (int ch = nch - 1; ch >= 0; --ch) {
@@ -708,26 +712,26 @@ __global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) apply_kernel(cons
         for (int e = tid; e < nj * ROWS; e += kThreads) {
             const int c = e / ROWS, i = e % ROWS;
             const int j = j0 + c;
-            T v = T(0);
-            if (i > j && i < M) v = Y[(size_t)j * M + i];
-            else if (i == j) v = T(1);
+            Tc v = Tc(0);
+            if (i > j && i < M) v = (Tc)Y[(size_t)j * M + i];
+            else if (i == j) v = Tc(1);
             sv[c * ROWS + i] = v;
         }
-        if (tid < nj) s_tau[tid] = tau[j0 + tid];
+        if (tid < nj) s_tau[tid] = (Tc)tau[j0 + tid];
         __syncthreads();
         if (!active) continue;
         for (int c = nj - 1; c >= 0; --c) {
-            const T tj = s_tau[c];
-            if (tj == T(0)) continue;
-            const T *v = sv + c * ROWS;
-            T d0 = 0, d1 = 0;
+            const Tc tj = s_tau[c];
+            if (tj == Tc(0)) continue;
+            const Tc *v = sv + c * ROWS;
+            Tc d0 = 0, d1 = 0;
 #pragma unroll
             for (int t = 0; t < RPL; t += 2) {
                 d0 += v[lane + 32 * t] * x[t];
                 if (t + 1 < RPL) d1 += v[lane + 32 * (t + 1)] * x[t + 1];
             }
-            const T s = tj * warp_sum(d0 + d1);
-            const volatile T *vv = v;  // re-read rather than hold RPL values in registers
+            const Tc s = tj * warp_sum(d0 + d1);
+            const volatile Tc *vv = v;  // re-read rather than hold RPL values in registers
 #pragma unroll
             for (int t = 0; t < RPL; ++t) x[t] -= s * vv[lane + 32 * t];
         }
@@ -736,18 +740,40 @@ __global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) apply_kernel(cons
 #pragma unroll
         for (int t = 0; t < RPL; ++t) {
             const int i = lane + 32 * t;
-            if (i < M) out[(size_t)col * d.ldco + i] = x[t];
+            if (i < M) out[(size_t)col * d.ldco + i] = (T)x[t];
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-template <typename T, int RPL>
+template <typename T, int RPL, typename Tc>
 static void launch_apply(const Desc *d_desc, int n, const T *ws, const int *d_rank,
                          const int *d_status, int maxK, cudaStream_t s) {
     const int groups = (maxK + kWarps - 1) / kWarps;   // the new rank is at most k
-    const size_t smem = (size_t)kApplyChunk * 32 * RPL * sizeof(T);
-    apply_kernel<T, RPL><<<dim3(n, 2, groups), kThreads, smem, s>>>(d_desc, ws, d_rank, d_status);
+    const size_t smem = (size_t)kApplyChunk * 32 * RPL * sizeof(Tc);
+    apply_kernel<T, RPL, Tc><<<dim3(n, 2, groups), kThreads, smem, s>>>(d_desc, ws, d_rank,
+                                                                       d_status);
+}
+
+template <typename T, typename Tc>
+static void launch_apply_all(const Desc *d_desc, int n, const T *ws, const int *d_rank,
+                             const int *d_status, int maxK, int rpl, cudaStream_t s) {
+    if (rpl <= 4) launch_apply<T, 4, Tc>(d_desc, n, ws, d_rank, d_status, maxK, s);
+    else if (rpl <= 8) launch_apply<T, 8, Tc>(d_desc, n, ws, d_rank, d_status, maxK, s);
+    else if (rpl <= 16) launch_apply<T, 16, Tc>(d_desc, n, ws, d_rank, d_status, maxK, s);
+    else if (rpl <= 32) launch_apply<T, 32, Tc>(d_desc, n, ws, d_rank, d_status, maxK, s);
+    else launch_apply<T, 64, Tc>(d_desc, n, ws, d_rank, d_status, maxK, s);
+}
+
+template <typename T, typename Tc>
+static cudaError_t set_apply_smem() {
+    const int s64 = kApplyChunk * 32 * 64 * (int)sizeof(Tc);
+    cudaError_t e = cudaFuncSetAttribute(apply_kernel<T, 64, Tc>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, s64);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(apply_kernel<T, 32, Tc>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, s64 / 2);
+    return e;
 }
 
 template <typename T, int RPL>
@@ -767,12 +793,8 @@ cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
     int kmax = 0;
     while (kmax < kMaxK && svd_smem_bytes<T>(kmax + 1, true) + 64 <= (size_t)optin) ++kmax;
     *svd_smem_kmax = kmax;
-    const int apply_smem64 = kApplyChunk * 32 * 64 * (int)sizeof(T);
-    e = cudaFuncSetAttribute(apply_kernel<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             apply_smem64);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(apply_kernel<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 apply_smem64 / 2);
+    e = set_apply_smem<T, T>();
+    if (e == cudaSuccess) e = set_apply_smem<T, float>();
     if (e != cudaSuccess) return e;
     // the attribute is per kernel, not per plan: allow the largest size any
     // plan may launch with, so plans of different k coexist
@@ -796,7 +818,11 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
     const int maxM = shape.maxM;
     if (shape.maxK > kMaxK || maxM > 32 * kMaxRowsPerLane) return cudaErrorInvalidValue;
     const int rpl = (maxM + 31) / 32;
-    if (phases & kPhaseStack) stack_kernel<T><<<n, kThreads, 0, s>>>(d_desc, ws);
+    const bool mixed = shape.mixed && sizeof(T) == sizeof(double);
+    if (phases & kPhaseStack) {
+        if (mixed) stack_kernel<T, float><<<n, kThreads, 0, s>>>(d_desc, ws);
+        else stack_kernel<T, T><<<n, kThreads, 0, s>>>(d_desc, ws);
+    }
     if (phases & kPhaseQR) {
         if (rpl <= 4) launch_geqrf<T, 4>(d_desc, n, ws, s);
         else if (rpl <= 8) launch_geqrf<T, 8>(d_desc, n, ws, s);
@@ -825,12 +851,8 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
         }
     }
     if (phases & kPhaseApply) {
-        const int K = shape.maxK;
-        if (rpl <= 4) launch_apply<T, 4>(d_desc, n, ws, d_rank, d_status, K, s);
-        else if (rpl <= 8) launch_apply<T, 8>(d_desc, n, ws, d_rank, d_status, K, s);
-        else if (rpl <= 16) launch_apply<T, 16>(d_desc, n, ws, d_rank, d_status, K, s);
-        else if (rpl <= 32) launch_apply<T, 32>(d_desc, n, ws, d_rank, d_status, K, s);
-        else launch_apply<T, 64>(d_desc, n, ws, d_rank, d_status, K, s);
+        if (mixed) launch_apply_all<T, float>(d_desc, n, ws, d_rank, d_status, shape.maxK, rpl, s);
+        else launch_apply_all<T, T>(d_desc, n, ws, d_rank, d_status, shape.maxK, rpl, s);
     }
     return cudaGetLastError();
 }

@@ -422,6 +422,9 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
                                    ? configure_recompress<double>(p->maxK, &p->shape.svd_smem_kmax)
                                    : configure_recompress<float>(p->maxK, &p->shape.svd_smem_kmax);
         for (auto &g : p->groups) g.shape.svd_smem_kmax = p->shape.svd_smem_kmax;
+        const bool mixed = (flags & HCORE_GPU_MIXED_FACTORS) && precision == HCORE_GPU_F64;
+        p->shape.mixed = mixed;
+        for (auto &g : p->groups) g.shape.mixed = mixed;
         if (ce != cudaSuccess) {
             set_error("hcore_gpu_plan_create: %s", cudaGetErrorString(ce));
             plan_free(p);

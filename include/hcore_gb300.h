@@ -64,6 +64,11 @@ extern "C" {
  * capturable.  Outputs in pinned host memory are written in place by the
  * rebuild kernel. */
 #define HCORE_GPU_STAGE_INPUTS 0x2
+/* FP64 plans only: the factor products F = AV^T BV, G = BU F^T and the Q.U
+ * rebuild run in FP32 with FP32 accumulation (FP64 storage), the QRs, the SVD
+ * and the truncation stay FP64.  Meant for loose accuracies (1e-4 .. 1e-6);
+ * the rebuild's FP32 rounding (~1e-7 relative) is far below such acc. */
+#define HCORE_GPU_MIXED_FACTORS 0x4
 
 /* One low-rank update.  Factors are column-major with the given leading
  * dimensions; every factor has M rows.  Ranks are plain ints. */
@@ -140,6 +145,13 @@ typedef struct hcore_dense_task {
 } hcore_dense_task;
 
 int hcore_gpu_dense_batched(int n, const hcore_dense_task *tasks, void *stream);
+
+/* The same as a plan: create validates, groups and uploads once; execute only
+ * launches (capturable) and applies every task again to the current tiles. */
+typedef struct hcore_gpu_dense_plan_s *hcore_gpu_dense_plan;
+int hcore_gpu_dense_plan_create(hcore_gpu_dense_plan *plan, int n, const hcore_dense_task *tasks);
+int hcore_gpu_dense_plan_execute(hcore_gpu_dense_plan plan, void *stream);
+int hcore_gpu_dense_plan_destroy(hcore_gpu_dense_plan plan);
 
 /* measured FP64 tensor-pipe (DMMA m16n8k16) throughput of this GPU in
  * TFLOP/s, timed on `stream` (about 0.1 s); the roofline denominator of the

@@ -342,3 +342,33 @@ def test_staged_host_inputs_equal_device_plan(hc, pinned):
     assert np.array_equal(outs["device"][0], outs["staged"][0])
     assert np.array_equal(outs["device"][1], outs["staged"][1])
     assert np.array_equal(outs["device"][2], outs["staged"][2])
+
+
+@pytest.mark.parametrize("acc", [1e-4, 1e-6])
+def test_mixed_factors_vs_fp64_oracle(hc, port, acc):
+    """HCORE_GPU_MIXED_FACTORS at loose accuracies: factor products and the
+    rebuild in FP32, QR/SVD/truncation in FP64.  Same rank as the FP64
+    oracle on cases without a singular value near acc; error against the
+    exact update no more than the oracle's truncation error + 2e-6 relative
+    (FP32 rounding of the products)."""
+    rng = np.random.default_rng(91)
+    cases = []
+    for i in range(10):
+        a, b, c = (int(x) for x in rng.integers(4, 30, size=3))
+        cases.append(dict(M=256, a=a, b=b, c=c, alpha=-1.0, beta=1.0, maxrk=64, acc=acc,
+                          arrays=_batch_case(rng, 256, a, b, c, decades=10.0)))
+    _, ranks, status, outs = _run_batch(hc, cases, flags=hc.MIXED_FACTORS)
+    assert (status == 0).all()
+    for cs, r, (CUo, CVo) in zip(cases, ranks, outs):
+        AU, AV, BU, BV, CU, CV = cs["arrays"]
+        ref = port.gemm(256, -1.0, AU, AV, cs["a"], BU, BV, cs["b"], 1.0, CU, CV, cs["c"],
+                        maxrk=64, acc=acc)
+        sig = ref["sigma"]
+        near = np.any(np.abs(sig - acc) < 1e-3 * acc)
+        if not near:
+            assert r == ref["rank"]
+        D = O.dense_update(-1.0, AU, AV, BU, BV, 1.0, CU, CV)
+        nd = np.linalg.norm(D)
+        eg = np.linalg.norm(CUo @ CVo.T - D)
+        er = np.linalg.norm(ref["CU"] @ ref["CV"].T - D)
+        assert eg <= 1.01 * er + 2e-6 * nd
