@@ -699,19 +699,27 @@ def run_dense(args):
         o = int(panel.offset[s_])
         return panel.U.data_ptr() + 8 * o, panel.V.data_ptr() + 8 * o, int(panel.rank[s_])
 
-    tasks, flops = [], 0
+    # flops: the reference's model (three GEMMs per task over the full tile)
+    # and what the kernels execute (a syrk skips the 64 x 64 blocks strictly
+    # above the diagonal, whose result is zero)
+    tpd = (nb + 63) // 64
+    lower = tpd * (tpd + 1) / 2 / (tpd * tpd)
+    tasks, flops, flops_exec = [], 0, 0
     for i in range(T):
         for j in range(1, T):
             u, v, r = fac(j)
             tasks.append(hc.DenseTask(kind=0, M=nb, a=r, b=0, alpha=-1.0, Au=u, Av=v, lda=nb,
                                       Bu=None, Bv=None, ldb=nb, CD=diag[i].data_ptr(), ldcd=nb))
-            flops += 2 * r * r * nb + 2 * nb * r * r + 2 * nb * nb * r   # reference model
+            flops += 2 * r * r * nb + 2 * nb * r * r + 2 * nb * nb * r
+            flops_exec += 2 * r * r * nb + 2 * nb * r * r + 2 * nb * nb * r * lower
     for t, i in enumerate(range(2, T)):
         ua, va, ra = fac(i)
         ub, vb, rb = fac(i - 1)
         tasks.append(hc.DenseTask(kind=1, M=nb, a=ra, b=rb, alpha=-1.0, Au=ua, Av=va, lda=nb,
                                   Bu=ub, Bv=vb, ldb=nb, CD=offd[t].data_ptr(), ldcd=nb))
-        flops += 2 * ra * rb * nb + 2 * nb * min(ra, rb) * max(ra, rb) + 2 * nb * nb * min(ra, rb)
+        f = 2 * ra * rb * nb + 2 * nb * min(ra, rb) * max(ra, rb) + 2 * nb * nb * min(ra, rb)
+        flops += f
+        flops_exec += f
     plan = hc.DensePlan(tasks)
     stream = torch.cuda.current_stream(dev)
     # correctness on a sample: tiles 0 and 63 and one off-diagonal tile after one step
@@ -751,9 +759,11 @@ def run_dense(args):
             "config": {"workload": "64 diagonal 1024^2 tiles x 63 syrk updates + 62 gemmcd updates",
                        "syrk_tasks": T * (T - 1), "gemmcd_tasks": len(offd), "nb": nb},
             "gflops_model": flops / (ms / 1e3) / 1e9,
-            "roofline": {"bound": "fp64", "achieved": flops / (ms / 1e3) / 1e12, "peak": peak,
-                         "unit": "TFLOP/s", "frac": flops / (ms / 1e3) / 1e12 / peak,
-                         "flops_basis": "reference model (three GEMMs per task, full tile)",
+            "roofline": {"bound": "fp64", "achieved": flops_exec / (ms / 1e3) / 1e12, "peak": peak,
+                         "unit": "TFLOP/s", "frac": flops_exec / (ms / 1e3) / 1e12 / peak,
+                         "flops_basis": "flops the kernels execute: the reference's three GEMMs "
+                                        "per task, syrk tiles without the 64x64 blocks strictly "
+                                        "above the diagonal (gflops_model counts full tiles)",
                          "tile_bytes_per_step": tiles_bytes},
             "accuracy": {"max_rel_err_vs_oracle_sequential_dsyrk": max(errs),
                          "tiles_checked": [0, T - 1]}}

@@ -52,6 +52,26 @@ __device__ __forceinline__ T warp_max(T v) {
     return v;
 }
 
+// binary exponent (floor(log2|x|), subnormals included), per precision
+__device__ __forceinline__ int binary_exponent(double x) { return ilogb(x); }
+__device__ __forceinline__ int binary_exponent(float x) { return ilogbf(x); }
+// 2^n built from its bits, n within the normal exponent range
+template <typename T>
+__device__ __forceinline__ T exp2i(int n);
+template <>
+__device__ __forceinline__ double exp2i<double>(int n) {
+    return __longlong_as_double((long long)(n + 1023) << 52);
+}
+template <>
+__device__ __forceinline__ float exp2i<float>(int n) {
+    return __int_as_float((n + 127) << 23);
+}
+// x * 2^n for |n| up to twice the normal exponent range: two exact multiplies
+template <typename T>
+__device__ __forceinline__ T mul_exp2(T x, int n) {
+    return (x * exp2i<T>(n / 2)) * exp2i<T>(n - n / 2);
+}
+
 // ---------------------------------------------------------------------------
 // phase 1: stack the factors
 // ---------------------------------------------------------------------------
@@ -130,19 +150,52 @@ __global__ void __launch_bounds__(kThreads) stack_kernel(const Desc *__restrict_
 // and the axpy need no predicates.  Look-ahead: warp 0 updates column j+1
 // first and turns it into reflector j+1 while the other warps finish step j,
 // so there is a single barrier per column.
+// lo/hi: range in which a plain sum of squares neither under- nor overflows;
+// safmin = (smallest normal) / eps, the LAPACK dlamch('S')/dlamch('E')
+// threshold below which 1/beta is not safe (a power of two).
 template <typename T>
 struct NormLim;
 template <>
 struct NormLim<double> {
     static constexpr double lo = 1e-280, hi = 1e280;
+    static constexpr double safmin = DBL_MIN / DBL_EPSILON;
+    static constexpr int max_shift = 1000;   // 2^(+-max_shift) is a normal double
 };
 template <>
 struct NormLim<float> {
     static constexpr float lo = 1e-30f, hi = 1e30f;
+    static constexpr float safmin = FLT_MIN / FLT_EPSILON;
+    static constexpr int max_shift = 120;
 };
+
+// dlarfg's rescaling for a column whose beta is below safmin (subnormal
+// entries; warp-uniform and rare, so kept out of line to spare the
+// registers of the common path).  With alpha and ||x|| scaled by 2^s
+// (|beta| -> ~1) tau follows, and v = x 2^s / (as - bs) is applied in two
+// exact factors to the x that make_reflector published; beta stays
+// unscaled.  Each lane rescales the rows it stored.  Returns tau.
+template <typename T>
+__device__ __noinline__ T rescale_reflector(T alpha, T xnorm, T beta, int j, int M, int lane,
+                                            T *Aj, T *sv) {
+    const int sh = -binary_exponent(beta);
+    const T as = mul_exp2(alpha, sh);
+    const T xs = mul_exp2(xnorm, sh);   // as, xs <= ~1: no overflow below
+    const T bs = -copysign(sqrt(as * as + xs * xs), as);
+    const T sc = exp2i<T>(sh - sh / 2) / (as - bs), post = exp2i<T>(sh / 2);
+    for (int i = lane; i < M; i += 32) {
+        if (i <= j) continue;
+        const T v = (sv[i] * sc) * post;
+        sv[i] = v;
+        Aj[i] = v;
+    }
+    return (bs - as) / bs;
+}
 
 // Build reflector j from the register column x (already updated by all
 // earlier reflectors); store the column back and publish v and tau.
+// Tiny columns (subnormal entries, e.g. far-field interactions in FP32)
+// take a scaled norm (dnrm2) and dlarfg's rescaling, so that no reciprocal
+// overflows; both scale by powers of two only (exact, no division).
 template <typename T, int RPL>
 __device__ __forceinline__ void make_reflector(T (&x)[RPL], int j, int M, int lane, T *Aj,
                                                T *sv, T *s_tau, T *tau_out) {
@@ -167,24 +220,32 @@ __device__ __forceinline__ void make_reflector(T (&x)[RPL], int j, int M, int la
         }
         amax = warp_max(amax);
         T s2 = 0;
+        int sc = 0;
         if (amax > T(0)) {
-            const T inv = T(1) / amax;
+            // y = x 2^sc with |y| < 2 (sc clamped to a representable power)
+            sc = min(max(-binary_exponent(amax), -NormLim<T>::max_shift), NormLim<T>::max_shift);
+            const T f = exp2i<T>(sc);
 #pragma unroll
             for (int t = 0; t < RPL; ++t) {
                 const int i = lane + 32 * t;
                 if (i > j && i < M) {
-                    const T y = x[t] * inv;
+                    const T y = x[t] * f;
                     s2 += y * y;
                 }
             }
         }
-        xnorm = amax * sqrt(warp_sum(s2));
+        xnorm = mul_exp2(sqrt(warp_sum(s2)), -sc);
     }
     T tj = 0, beta = alpha, scal = 1;
+    bool rescale = false;
     if (xnorm > T(0)) {
         beta = -copysign(hypot(alpha, xnorm), alpha);
-        tj = (beta - alpha) / beta;
-        scal = T(1) / (alpha - beta);
+        if (abs(beta) >= NormLim<T>::safmin) {
+            tj = (beta - alpha) / beta;
+            scal = T(1) / (alpha - beta);
+        } else if (beta == beta) {
+            rescale = true;   // 1/(alpha - beta) would overflow: x is published as is
+        }
     }
 #pragma unroll
     for (int t = 0; t < RPL; ++t) {
@@ -201,6 +262,7 @@ __device__ __forceinline__ void make_reflector(T (&x)[RPL], int j, int M, int la
         }
         sv[i] = v;
     }
+    if (rescale) tj = rescale_reflector(alpha, xnorm, beta, j, M, lane, Aj, sv);
     if (lane == 0) {
         *s_tau = tj;
         tau_out[j] = tj;
@@ -335,6 +397,12 @@ __host__ __device__ inline size_t svd_smem_bytes(int K, bool in_smem) {
 // (exact in exact arithmetic), recomputed on strong cancellation and after
 // every sweep.  Convergence: every pair orthogonal to k*eps relative to its
 // norms (LAPACK dgesvj's criterion).
+// Range safety (as LAPACK's sgesvd/dgesvd scale the matrix first): T is
+// scaled by 2^-e so that its largest entry lies in [1, 2) (exact; the
+// singular values and V S are scaled back by 2^e), and a column whose squared
+// norm is below safmin is negligible (< 2^-485 relative in FP64, 2^-51 in
+// FP32) and not rotated.  A non-finite singular value marks the update
+// NOCONV; the sort below is a total order even then.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict__ descs,
                                                          T *__restrict__ ws, int *__restrict__ rank,
@@ -342,7 +410,8 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
                                                          int *__restrict__ info, int smem_kmax,
                                                          int maxK) {
     extern __shared__ unsigned char smem_raw[];
-    __shared__ int s_rot, s_piv;
+    __shared__ int s_rot, s_piv, s_exp;
+    __shared__ T s_wmax[kWarps];
     const Desc d = descs[blockIdx.x];
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
     if (d.status0) {
@@ -369,12 +438,28 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     T *Yg = base + L.Uo;   // Householder vectors of Q (k x k, ld k), until Uo is written
 
     // T = triu(R_A) triu(R_B)^T (hcore_dgemm.c:330-387)
+    T amax = 0;
     for (int j = 0; j < k; ++j)
         for (int i = tid; i < k; i += nthr) {
             T s = 0;
             for (int l = max(i, j); l < k; ++l) s += UA[(size_t)l * M + i] * VB[(size_t)l * M + j];
             A[(size_t)j * ld + i] = s;
+            amax = max(amax, abs(s));
         }
+    // scale T by 2^-e, e = exponent of its largest entry (nthr is a multiple of 32)
+    amax = warp_max(amax);
+    if (lane == 0) s_wmax[tid >> 5] = amax;
+    __syncthreads();
+    if (tid == 0) {
+        T m = 0;
+        for (int w = 0; w < nthr / 32; ++w) m = max(m, s_wmax[w]);
+        s_exp = (m > T(0) && isfinite(m)) ? binary_exponent(m) : 0;
+    }
+    __syncthreads();
+    const int sexp = s_exp;
+    if (sexp != 0)
+        for (int j = 0; j < k; ++j)
+            for (int i = tid; i < k; i += nthr) A[(size_t)j * ld + i] = mul_exp2(A[(size_t)j * ld + i], -sexp);
     __syncthreads();
 
     // ---- QR with column pivoting, T P = Q R (lane per column) ----
@@ -481,6 +566,7 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         s_nrm[c] = s;
         s_d[c] = T(1);
     }
+    if (tid == 0) s_piv = 0;   // reused below: set when a singular value is not finite
     __syncthreads();
 
     // ---- one-sided Jacobi on B = R^T, rotations accumulated in A ----
@@ -515,7 +601,8 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
                     aqq = s_nrm[q];
                     apq = dp * dq * dot;
                 }
-                const bool rot = valid && apq != T(0) && abs(apq) > tol * sqrt(app) * sqrt(aqq);
+                const bool rot = valid && app > NormLim<T>::safmin && aqq > NormLim<T>::safmin &&
+                                 apq != T(0) && abs(apq) > tol * sqrt(app) * sqrt(aqq);
                 T t = 0, cs = 1;
                 if (rot) {
                     const T zeta = (aqq - app) / (T(2) * apq);
@@ -586,21 +673,28 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         __syncthreads();
     }
 
-    // singular values = true column norms of B; sort descending (ties by index)
-    for (int j = tid; j < k; j += nthr) s_sig[j] = sqrt(s_nrm[j]);
-    __syncthreads();
+    // singular values = true column norms of B (of the scaled T); sort
+    // descending, ties by index, NaN last: a total order, so s_perm is a
+    // permutation whatever the values
     for (int j = tid; j < k; j += nthr) {
-        const T sj = s_sig[j];
+        const T s = sqrt(s_nrm[j]);
+        s_sig[j] = s;
+        if (!isfinite(s)) s_piv = 1;
+    }
+    __syncthreads();
+    const bool finite = s_piv == 0;
+    for (int j = tid; j < k; j += nthr) {
+        const T sj = s_sig[j] == s_sig[j] ? s_sig[j] : T(-1);
         int pos = 0;
         for (int i = 0; i < k; ++i) {
-            const T si = s_sig[i];
+            const T si = s_sig[i] == s_sig[i] ? s_sig[i] : T(-1);
             pos += (si > sj) || (si == sj && i < j);
         }
         s_perm[pos] = j;
     }
     __syncthreads();
     T *sig_out = base + L.sig;
-    for (int t = tid; t < k; t += nthr) sig_out[t] = s_sig[s_perm[t]];
+    for (int t = tid; t < k; t += nthr) sig_out[t] = mul_exp2(s_sig[s_perm[t]], sexp);
 
     // rank rule (hcore_dgemm.c:444-464; the fast rules start at i = 2)
     int r;
@@ -609,13 +703,13 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     } else {
         r = k;
         for (int i = d.rank_start; i < k; ++i)
-            if (s_sig[s_perm[i]] < (T)d.acc) {
+            if (mul_exp2(s_sig[s_perm[i]], sexp) < (T)d.acc) {
                 r = i;
                 break;
             }
     }
     int st = HCORE_GPU_S_OK;
-    if (!converged) st = HCORE_GPU_S_NOCONV;
+    if (!converged || !finite) st = HCORE_GPU_S_NOCONV;
     else if (r > d.max_rank) st = HCORE_GPU_S_RANK_MAX;
     else if (r > d.storage_rank) st = HCORE_GPU_S_STORAGE;
 
@@ -625,7 +719,7 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     for (int e = tid; e < k * r; e += nthr) {
         const int i = e % k, t = e / k;
         const int j = s_perm[t];
-        Vo[(size_t)t * k + s_pcol[i]] = s_d[j] * B[(size_t)j * ld + i];
+        Vo[(size_t)t * k + s_pcol[i]] = mul_exp2(s_d[j] * B[(size_t)j * ld + i], sexp);
     }
     __syncthreads();  // B's columns are read above and overwritten below
     // U_r = Q (V_J's true columns), Q = H_0 ... H_{k-1}: lane per output
@@ -790,8 +884,13 @@ cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return e;
+    // dynamic shared memory the SVD kernel may take next to its static arrays
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, gesvd_kernel<T>);
+    if (e != cudaSuccess) return e;
+    const int dyn_max = optin - (int)fa.sharedSizeBytes;
     int kmax = 0;
-    while (kmax < kMaxK && svd_smem_bytes<T>(kmax + 1, true) + 64 <= (size_t)optin) ++kmax;
+    while (kmax < kMaxK && svd_smem_bytes<T>(kmax + 1, true) <= (size_t)dyn_max) ++kmax;
     *svd_smem_kmax = kmax;
     e = set_apply_smem<T, T>();
     if (e == cudaSuccess) e = set_apply_smem<T, float>();
@@ -799,7 +898,7 @@ cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
     // the attribute is per kernel, not per plan: allow the largest size any
     // plan may launch with, so plans of different k coexist
     return cudaFuncSetAttribute(gesvd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                optin - 64);
+                                dyn_max);
 }
 
 int bucket_edge(int k) {

@@ -372,3 +372,63 @@ def test_mixed_factors_vs_fp64_oracle(hc, port, acc):
         eg = np.linalg.norm(CUo @ CVo.T - D)
         er = np.linalg.norm(ref["CU"] @ ref["CV"].T - D)
         assert eg <= 1.01 * er + 2e-6 * nd
+
+
+# Tiny-magnitude updates: far-field interactions whose factor products reach
+# the subnormal range (FP32 tiles of a covariance kernel between distant
+# clusters).  The QR takes the scaled-norm / dlarfg-rescaling paths and the
+# SVD its power-of-two pre-scaling; the rank, the singular values and the
+# product must still match the oracle (LAPACK scales the same way).
+# (scale of every factor, acc, precision)
+_TINY = [(1e-12, 1e-4, 1), (1e-12, 1e-28, 1), (3e-17, 1e-4, 1), (1e-20, 1e-4, 1),
+         (1e-100, 1e-8, 0), (1e-100, 1e-208, 0), (1e-152, 1e-8, 0), (1e-160, 1e-8, 0)]
+
+
+@pytest.mark.parametrize("scale,acc,precision", _TINY)
+def test_tiny_magnitude_updates_vs_oracle(hc, port, scale, acc, precision):
+    dtype = np.float32 if precision else np.float64
+    rng = np.random.default_rng(5)
+    M, a, b, c = 256, 12, 10, 14
+    arrays = tuple(x * scale for x in _batch_case(rng, M, a, b, c, decades=6.0))
+    cases = [dict(M=M, a=a, b=b, c=c, alpha=-1.0, beta=1.0, maxrk=64, acc=acc, arrays=arrays)]
+    batch, ranks, status, outs = _run_batch(hc, cases, dtype=dtype, precision=precision)
+    assert status[0] == 0
+    AU, AV, BU, BV, CU, CV = (x.astype(dtype) for x in arrays)
+    ref = port.gemm(M, -1.0, AU, AV, a, BU, BV, b, 1.0, CU, CV, c, maxrk=64, acc=acc, dtype=dtype)
+    assert ranks[0] == ref["rank"]
+    tol = FP32_TOL if precision else FP64_TOL
+    tiny = float(np.finfo(dtype).smallest_subnormal)
+    sig, sig_ref = batch.sigma(0), np.asarray(ref["sigma"], dtype=np.float64)
+    smax = np.abs(sig_ref).max()
+    # subnormal results carry fewer bits: allow a few units of the smallest subnormal
+    assert np.abs(sig - sig_ref).max() <= tol * smax + 64 * tiny
+    CUo, CVo = outs[0]
+    P = CUo.astype(np.float64) @ CVo.T.astype(np.float64)
+    P_ref = ref["CU"].astype(np.float64) @ ref["CV"].T.astype(np.float64)
+    assert np.linalg.norm(P - P_ref) <= tol * np.linalg.norm(P_ref) + 64 * tiny * M
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_nonfinite_input_marks_update_noconv(hc, port, precision):
+    """A NaN or Inf in an update's factors gives that update the NOCONV
+    status (its outputs are not written); the other updates of the batch
+    are unaffected."""
+    dtype = np.float32 if precision else np.float64
+    rng = np.random.default_rng(23)
+    M, a, b, c = 128, 10, 9, 11
+    good = _batch_case(rng, M, a, b, c, decades=6.0)
+    with_nan = tuple(x.copy() for x in good)
+    with_nan[0][5, 3] = np.nan
+    with_inf = tuple(x.copy() for x in good)
+    with_inf[3][7, 2] = np.inf
+    cases = [dict(M=M, a=a, b=b, c=c, alpha=-1.0, beta=1.0, maxrk=40, acc=1e-4, arrays=arr)
+             for arr in (with_nan, good, with_inf)]
+    _, ranks, status, outs = _run_batch(hc, cases, dtype=dtype, precision=precision)
+    assert list(status) == [6, 0, 6]
+    AU, AV, BU, BV, CU, CV = (x.astype(dtype) for x in good)
+    ref = port.gemm(M, -1.0, AU, AV, a, BU, BV, b, 1.0, CU, CV, c, maxrk=40, acc=1e-4, dtype=dtype)
+    assert ranks[1] == ref["rank"]
+    CUo, CVo = outs[1]
+    P = CUo.astype(np.float64) @ CVo.T.astype(np.float64)
+    P_ref = ref["CU"].astype(np.float64) @ ref["CV"].T.astype(np.float64)
+    assert O.rel_fro(P, P_ref) < (FP32_TOL if precision else FP64_TOL)
