@@ -10,7 +10,9 @@ interface so tests and benchmarks read like the reference's own:
   on numpy arrays, through the drop-in C entry points;
 * :class:`Batch` — many independent updates in one plan (device tensors),
   executed by the batched GPU kernels and capturable in a CUDA graph;
-* :func:`dense_batched` — HCORE_dsyrk / HCORE_dgemmcd tile updates.
+* :func:`dense_batched` — HCORE_dsyrk / HCORE_dgemmcd tile updates;
+* :class:`RankMLP` — the rank predictor's network, trained and run by the
+  library's own CUDA kernels (see :mod:`hcore_gb300.predictor`).
 
 There is no CPU fallback: importing works without a GPU, but every call into
 the library needs the compiled extension and a CUDA device, and raises
@@ -26,7 +28,7 @@ import numpy as np
 from .build import LIB as _LIB_PATH
 
 __all__ = ["lib", "LrTask", "DenseTask", "Batch", "DensePlan", "hcore_dgemm", "hcore_sgemm", "hcore_dgemm_fast",
-           "dense_batched", "HcoreError", "STATUS", "FlopCounter"]
+           "dense_batched", "HcoreError", "STATUS", "FlopCounter", "RankMLP"]
 
 F64, F32 = 0, 1
 FAST_RULES = 0x1
@@ -117,6 +119,13 @@ def lib() -> C.CDLL:
     L.hcore_gpu_dense_plan_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(DenseTask)]
     L.hcore_gpu_dense_plan_execute.argtypes = [vp, vp]
     L.hcore_gpu_dense_plan_destroy.argtypes = [vp]
+    L.hcore_gpu_mlp_create.argtypes = [C.POINTER(vp), C.c_ulonglong]
+    L.hcore_gpu_mlp_params.argtypes = [vp, _fp, C.c_int]
+    L.hcore_gpu_mlp_gradient.argtypes = [vp, vp, vp, C.c_int, _fp, _fp, vp]
+    L.hcore_gpu_mlp_train.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_float,
+                                      C.c_ulonglong, _fp, vp]
+    L.hcore_gpu_mlp_predict.argtypes = [vp, vp, C.c_int, vp, vp]
+    L.hcore_gpu_mlp_destroy.argtypes = [vp]
     L.hcore_gpu_last_error.restype = C.c_char_p
     L.hcore_gpu_thread_stream.restype = vp
     for name, rp, real in (("HCORE_dgemm", _dp, C.c_double), ("HCORE_sgemm", _fp, C.c_float)):
@@ -311,3 +320,60 @@ def dense_batched(tasks, stream=None):
     """Run HCORE_dsyrk / HCORE_dgemmcd tasks (device pointers) in one batch."""
     arr = (DenseTask * max(len(tasks), 1))(*tasks)
     _check(lib().hcore_gpu_dense_batched(len(tasks), arr, stream or None), "hcore_gpu_dense_batched")
+
+
+class RankMLP:
+    """The rank predictor's 6 -> 64 -> 64 -> 1 MLP (FP32 weights, BF16
+    activations) held on the GPU by the library (hcore_gpu_mlp_*).  Inputs
+    are (n, 6) float32 CUDA tensors, targets and outputs (n,) float32."""
+
+    NPARAMS = 6 * 64 + 64 + 64 * 64 + 64 + 64 + 1
+
+    def __init__(self, seed: int = 0):
+        self._m = C.c_void_p()
+        _check(lib().hcore_gpu_mlp_create(C.byref(self._m), seed), "hcore_gpu_mlp_create")
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.NPARAMS, dtype=np.float32)
+        _check(lib().hcore_gpu_mlp_params(self._m, out.ctypes.data_as(_fp), 0), "hcore_gpu_mlp_params")
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.NPARAMS
+        _check(lib().hcore_gpu_mlp_params(self._m, p.ctypes.data_as(_fp), 1), "hcore_gpu_mlp_params")
+
+    def gradient(self, X, T, stream=None):
+        g = np.zeros(self.NPARAMS, dtype=np.float32)
+        loss = C.c_float(0)
+        _check(lib().hcore_gpu_mlp_gradient(self._m, X.data_ptr(), T.data_ptr(), X.shape[0],
+                                            g.ctypes.data_as(_fp), C.byref(loss), stream),
+               "hcore_gpu_mlp_gradient")
+        return float(loss.value), g
+
+    def train(self, X, T, epochs: int, batch: int, lr: float, seed: int = 0, stream=None):
+        losses = np.zeros(epochs, dtype=np.float32)
+        _check(lib().hcore_gpu_mlp_train(self._m, X.data_ptr(), T.data_ptr(), X.shape[0], epochs,
+                                         batch, lr, seed, losses.ctypes.data_as(_fp), stream),
+               "hcore_gpu_mlp_train")
+        return losses
+
+    def predict(self, X, out=None, stream=None):
+        import torch
+
+        if out is None:
+            out = torch.empty(X.shape[0], dtype=torch.float32, device=X.device)
+        _check(lib().hcore_gpu_mlp_predict(self._m, X.data_ptr(), X.shape[0], out.data_ptr(), stream),
+               "hcore_gpu_mlp_predict")
+        return out
+
+    def close(self) -> None:
+        if self._m:
+            lib().hcore_gpu_mlp_destroy(self._m)
+            self._m = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -177,6 +177,39 @@ int hcore_gpu_dgemm_noalloc(int M, double alpha, const double *AU, const double 
                             double beta, double *CU, double *CV, int c, int ldc, int rk,
                             int maxrk, double acc, int *new_rank, int *status, void *stream);
 
+/* Rank predictor (no counterpart in the reference): a 6 -> 64 -> 64 -> 1
+ * MLP with ReLU, FP32 weights and BF16 activations, trained and run by the
+ * library's own CUDA kernels.  It predicts an update's output rank from cheap
+ * features so that output slots, workspace and launch shapes can be sized
+ * before the batch runs; the SVD still decides every rank (a task whose rank
+ * exceeds its predicted capacity gets HCORE_GPU_S_STORAGE and is rerun).
+ * Parameters (FP32): W1[6][64] (in x out), b1[64], W2[64][64], b2[64],
+ * w3[64], b3.  Inputs are row-major n x 6 FP32 device arrays, targets and
+ * outputs n FP32 device arrays.  Loss: mean of 0.5 (y - t)^2; optimiser Adam
+ * (0.9, 0.999, 1e-8). */
+#define HCORE_MLP_INPUTS 6
+#define HCORE_MLP_HIDDEN 64
+#define HCORE_MLP_PARAMS (6 * 64 + 64 + 64 * 64 + 64 + 64 + 1)
+typedef struct hcore_gpu_mlp_s *hcore_gpu_mlp;
+/* He-uniform weights from a seeded generator, zero biases */
+int hcore_gpu_mlp_create(hcore_gpu_mlp *mlp, unsigned long long seed);
+/* copy the HCORE_MLP_PARAMS parameters to (set = 0) or from (set = 1) host;
+ * setting them also clears the optimiser state */
+int hcore_gpu_mlp_params(hcore_gpu_mlp mlp, float *params, int set);
+/* gradient of the mean loss over all n samples (host array of
+ * HCORE_MLP_PARAMS) and the loss itself; synchronous */
+int hcore_gpu_mlp_gradient(hcore_gpu_mlp mlp, const float *x, const float *y, int n, float *grad,
+                           float *loss, void *stream);
+/* minibatch Adam: `epochs` passes over the n samples in a fresh seeded order
+ * each time; epoch_loss (host, may be NULL) receives each epoch's mean
+ * training loss; synchronous */
+int hcore_gpu_mlp_train(hcore_gpu_mlp mlp, const float *x, const float *y, int n, int epochs,
+                        int batch, float lr, unsigned long long seed, float *epoch_loss,
+                        void *stream);
+/* forward pass of n samples into out (device); asynchronous on stream */
+int hcore_gpu_mlp_predict(hcore_gpu_mlp mlp, const float *x, int n, float *out, void *stream);
+int hcore_gpu_mlp_destroy(hcore_gpu_mlp mlp);
+
 /* library-owned per-thread stream used by the drop-in HCORE_* entry points */
 void *hcore_gpu_thread_stream(void);
 const char *hcore_gpu_last_error(void);
