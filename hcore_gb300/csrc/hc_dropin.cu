@@ -177,7 +177,7 @@ struct Single {
         const int st = fill_desc(t, flags, false, d, k);
         if (st) return st;
         const int M = t.M, a = t.a, b = t.b, c = t.c;
-        L = ws_layout(M, a, b, k);
+        L = ws_layout(d);
         const bool dense_b = t.Bdense != nullptr;
         bool dev_in = true;
         for (const void *p : {a ? t.AU : nullptr, a ? t.AV : nullptr,

@@ -26,22 +26,35 @@ struct Desc {
     int pad_;
 };
 
-// Workspace layout of one update (element offsets from Desc::ws), k = a + c:
+// Columns of the Uo / Vo slots of an update with k = a + c: an accepted
+// update's new rank is at most min(k, storage_rank), so a caller that knows
+// a smaller bound (storage_maxrank, e.g. a predicted capacity) gets smaller
+// slots; at least ceil(k/2), because Uo and Vo together also hold the k x k
+// reflectors of the SVD's QR until the outputs are written.
+__host__ __device__ inline int uo_cols(int k, int storage_rank) {
+    const int cap = storage_rank < k ? storage_rank : k;
+    const int half = (k + 1) / 2;
+    return cap > half ? cap : half;
+}
+
+// Workspace layout of one update (element offsets from Desc::ws), k = a + c,
+// u = uo_cols(k, storage_rank):
 //   UA  M*k   stacked [beta CU | alpha AU], then its QR (R on top, reflectors below)
 //   VB  M*k   stacked [CV | G], then its QR
 //   tauA k, tauB k, sig k
 //   F   a*b   AV^T BV
 //   W   k*k   Jacobi working matrix (used when it does not fit shared memory)
 //   V   k*k   Jacobi right vectors (same)
-//   Uo  k*k   U_r (k x r, ld k)
-//   Vo  k*k   V_r S_r (k x r, ld k)
+//   Uo  k*u   U_r (k x r, ld k)       } the SVD's QR reflectors (k x k, ld k)
+//   Vo  k*u   V_r S_r (k x r, ld k)   } span both until U_r and V_r S_r are written
 struct WsLayout {
     long long UA, VB, tauA, tauB, sig, F, W, V, Uo, Vo, total;
 };
 
 __host__ __device__ inline long long hc_align32(long long x) { return (x + 31) & ~31LL; }
 
-__host__ __device__ inline WsLayout ws_layout(int M, int a, int b, int k) {
+__host__ __device__ inline WsLayout ws_layout(int M, int a, int b, int k, int storage_rank) {
+    const long long u = uo_cols(k, storage_rank);
     WsLayout L;
     long long o = 0;
     L.UA = o; o = hc_align32(o + (long long)M * k);
@@ -52,10 +65,13 @@ __host__ __device__ inline WsLayout ws_layout(int M, int a, int b, int k) {
     L.F = o; o = hc_align32(o + (long long)a * b);
     L.W = o; o = hc_align32(o + (long long)k * k);
     L.V = o; o = hc_align32(o + (long long)k * k);
-    L.Uo = o; o = hc_align32(o + (long long)k * k);
-    L.Vo = o; o = hc_align32(o + (long long)k * k);
+    L.Uo = o; o = hc_align32(o + (long long)k * u);
+    L.Vo = o; o = hc_align32(o + (long long)k * u);
     L.total = o;
     return L;
+}
+__host__ __device__ inline WsLayout ws_layout(const Desc &d) {
+    return ws_layout(d.M, d.a, d.b, d.k, d.storage_rank);
 }
 
 constexpr int kThreads = 256;
@@ -76,6 +92,9 @@ struct Bucket {
 };
 struct LaunchShape {
     int maxM = 1, maxK = 1, svd_smem_kmax = 0;
+    // most output columns an accepted update may have, max of
+    // min(k, storage_rank): the rebuild's grid (0: maxK)
+    int maxR = 0;
     bool mixed = false;  // FP32 factor products and rebuild (HCORE_GPU_MIXED_FACTORS)
     int nbuckets = 0;
     Bucket buckets[kMaxBuckets];

@@ -18,6 +18,7 @@
 // HCORE_GPU_MIXED_FACTORS an FP64 plan computes the factor products (stack)
 // and the Q.U rebuild in FP32 (compute type Tc = float, FP32 accumulation,
 // FP64 storage) while the QRs, the SVD and the truncation stay FP64.
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 
@@ -81,7 +82,7 @@ __global__ void __launch_bounds__(kThreads) stack_kernel(const Desc *__restrict_
     const Desc d = descs[blockIdx.x];
     if (d.status0) return;
     const int M = d.M, a = d.a, b = d.b, c = d.c, k = d.k;
-    const WsLayout L = ws_layout(M, a, b, k);
+    const WsLayout L = ws_layout(d);
     T *UA = ws + d.ws + L.UA;
     T *VB = ws + d.ws + L.VB;
     T *F = ws + d.ws + L.F;
@@ -277,7 +278,7 @@ __global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) geqrf_kernel(cons
     const Desc d = descs[blockIdx.x];
     if (d.status0) return;
     const int M = d.M, k = d.k;
-    const WsLayout L = ws_layout(M, d.a, d.b, k);
+    const WsLayout L = ws_layout(d);
     const int side = blockIdx.y;
     T *A = ws + d.ws + (side ? L.VB : L.UA);
     T *tau = ws + d.ws + (side ? L.tauB : L.tauA);
@@ -423,7 +424,7 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         return;
     }
     const int M = d.M, k = d.k;
-    const WsLayout L = ws_layout(M, d.a, d.b, k);
+    const WsLayout L = ws_layout(d);
     T *base = ws + d.ws;
     const T *UA = base + L.UA, *VB = base + L.VB;
     const bool in_smem = maxK <= smem_kmax;
@@ -435,7 +436,7 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     T *s_tau = aux + 3 * (maxK + 1);
     int *s_perm = reinterpret_cast<int *>(aux + 4 * (maxK + 1));   // Jacobi sort
     int *s_pcol = s_perm + (maxK + 1);                                // QR pivots
-    T *Yg = base + L.Uo;   // Householder vectors of Q (k x k, ld k), until Uo is written
+    T *Yg = base + L.Uo;   // reflectors of Q (k x k, ld k) over the Uo and Vo slots
 
     // T = triu(R_A) triu(R_B)^T (hcore_dgemm.c:330-387)
     T amax = 0;
@@ -713,39 +714,38 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     else if (r > d.max_rank) st = HCORE_GPU_S_RANK_MAX;
     else if (r > d.storage_rank) st = HCORE_GPU_S_STORAGE;
 
-    // V_r S_r = P (B's true columns): row P(i) of the output is row i of B
-    // (the rows S V^T of hcore_dgemm.c:484-489, transposed)
-    T *Uo = base + L.Uo, *Vo = base + L.Vo;
-    for (int e = tid; e < k * r; e += nthr) {
-        const int i = e % k, t = e / k;
-        const int j = s_perm[t];
-        Vo[(size_t)t * k + s_pcol[i]] = mul_exp2(s_d[j] * B[(size_t)j * ld + i], sexp);
-    }
-    __syncthreads();  // B's columns are read above and overwritten below
-    // U_r = Q (V_J's true columns), Q = H_0 ... H_{k-1}: lane per output
-    // column, reflectors from last to first; the columns are built in B
-    // (no longer needed) and then stored over the reflectors' slot
-    for (int t = tid; t < r; t += nthr) {
-        const int j = s_perm[t];
-        T *x = B + (size_t)j * ld;   // each lane owns the B column of its own j
-        const T dj = s_d[j];
-        const T *vj = A + (size_t)j * ld;
-        for (int i = 0; i < k; ++i) x[i] = dj * vj[i];
-        for (int h = k - 1; h >= 0; --h) {
-            const T th = s_tau[h];
-            if (th == T(0)) continue;
-            const T *y = Yg + (size_t)h * k;
-            T dot = x[h];
-            for (int i = h + 1; i < k; ++i) dot += y[i] * x[i];
-            const T s = th * dot;
-            x[h] -= s;
-            for (int i = h + 1; i < k; ++i) x[i] -= s * y[i];
+    // Outputs of an accepted update only (a rejected one leaves its slots
+    // alone; they may be smaller than its rank).  st is uniform in the CTA.
+    if (st == HCORE_GPU_S_OK) {
+        // U_r = Q (V_J's true columns), Q = H_0 ... H_{k-1}: lane per output
+        // column, in place in V_J's column, reflectors from last to first.
+        // The reflectors span the Uo and Vo slots, so this comes first.
+        for (int t = tid; t < r; t += nthr) {
+            const int j = s_perm[t];
+            T *x = A + (size_t)j * ld;   // each lane owns the column of its own j
+            const T dj = s_d[j];
+            for (int i = 0; i < k; ++i) x[i] *= dj;
+            for (int h = k - 1; h >= 0; --h) {
+                const T th = s_tau[h];
+                if (th == T(0)) continue;
+                const T *y = Yg + (size_t)h * k;
+                T dot = x[h];
+                for (int i = h + 1; i < k; ++i) dot += y[i] * x[i];
+                const T s = th * dot;
+                x[h] -= s;
+                for (int i = h + 1; i < k; ++i) x[i] -= s * y[i];
+            }
         }
-    }
-    __syncthreads();
-    for (int e = tid; e < k * r; e += nthr) {
-        const int i = e % k, t = e / k;
-        Uo[(size_t)t * k + i] = B[(size_t)s_perm[t] * ld + i];
+        __syncthreads();   // the reflectors are dead from here on
+        // V_r S_r = P (B's true columns): row P(i) of the output is row i of
+        // B (the rows S V^T of hcore_dgemm.c:484-489, transposed); U_r
+        T *Uo = base + L.Uo, *Vo = base + L.Vo;
+        for (int e = tid; e < k * r; e += nthr) {
+            const int i = e % k, t = e / k;
+            const int j = s_perm[t];
+            Vo[(size_t)t * k + s_pcol[i]] = mul_exp2(s_d[j] * B[(size_t)j * ld + i], sexp);
+            Uo[(size_t)t * k + i] = A[(size_t)j * ld + i];
+        }
     }
     if (tid == 0) {
         rank[d.idx] = r;
@@ -781,7 +781,7 @@ __global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) apply_kernel(cons
     if (col0 >= r) return;
     const int side = blockIdx.y;
     const int M = d.M, k = d.k;
-    const WsLayout L = ws_layout(M, d.a, d.b, k);
+    const WsLayout L = ws_layout(d);
     const T *base = ws + d.ws;
     const T *Y = base + (side ? L.VB : L.UA);
     const T *tau = base + (side ? L.tauB : L.tauA);
@@ -950,8 +950,9 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
         }
     }
     if (phases & kPhaseApply) {
-        if (mixed) launch_apply_all<T, float>(d_desc, n, ws, d_rank, d_status, shape.maxK, rpl, s);
-        else launch_apply_all<T, T>(d_desc, n, ws, d_rank, d_status, shape.maxK, rpl, s);
+        const int ncols = shape.maxR > 0 ? std::min(shape.maxR, shape.maxK) : shape.maxK;
+        if (mixed) launch_apply_all<T, float>(d_desc, n, ws, d_rank, d_status, ncols, rpl, s);
+        else launch_apply_all<T, T>(d_desc, n, ws, d_rank, d_status, ncols, rpl, s);
     }
     return cudaGetLastError();
 }

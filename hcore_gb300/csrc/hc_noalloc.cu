@@ -25,7 +25,8 @@
 namespace hc {
 
 // workspace capacity in doubles: M = 1024 rows with a + c <= 128 and
-// a*b <= 128*128 (ws_layout(1024, 128, 128, 128) fits)
+// a*b <= 128*128 fit (ws_layout(1024, 128, 128, 128, no storage limit) is
+// 344448 doubles)
 constexpr long long kNoAllocWsElems = 393216;                // 3 MiB
 constexpr size_t kNoAllocDescOff = kNoAllocWsElems * sizeof(double);
 constexpr size_t kNoAllocRankOff = kNoAllocDescOff + 512;   // rank, status
@@ -106,7 +107,7 @@ extern "C" int hcore_gpu_dgemm_noalloc(int M, double alpha, const double *AU, co
         set_error("hcore_gpu_dgemm_noalloc: task rejected (status %d)", st0);
         return HCORE_GPU_ETASK;
     }
-    const long long need = ws_layout(M, a, b, k).total;
+    const long long need = ws_layout(d).total;
     if (need > kNoAllocWsElems) {
         set_error("hcore_gpu_dgemm_noalloc: M=%d, a+c=%d, a*b=%d needs %lld doubles of "
                   "workspace; the fixed scratch holds %lld (e.g. M=1024 with a+c <= 128)",

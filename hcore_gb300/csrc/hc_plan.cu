@@ -130,6 +130,11 @@ void fill_buckets(const std::vector<Desc> &descs, LaunchShape &shape) {
         }
         i = j;
     }
+    // the rebuild launch is sized for the most columns an accepted update
+    // can have (a predicted capacity passed as storage_maxrank shrinks it)
+    shape.maxR = 1;
+    for (const Desc &d : descs)
+        if (!d.status0) shape.maxR = std::max(shape.maxR, std::min(d.k, d.storage_rank));
     // each launch is sized for the largest k actually present in its bucket
     for (int b = 0; b < shape.nbuckets; ++b) {
         int K = 1;
@@ -167,7 +172,7 @@ bool build_descs(int n, const hcore_lr_task *tasks, unsigned flags, bool transla
     for (int j = 0; j < n; ++j) {
         Desc d = descs[order[j]];
         d.ws = off;
-        if (!d.status0) off += ws_layout(d.M, d.a, d.b, d.k).total;
+        if (!d.status0) off += ws_layout(d).total;
         sorted[j] = d;
     }
     descs.swap(sorted);
@@ -573,7 +578,7 @@ extern "C" int hcore_gpu_plan_sigma(hcore_gpu_plan p, int i, double *sigma, int 
     }
     for (const Desc &d : all)
         if (d.idx == i) one[0] = d;
-    const WsLayout L = ws_layout(one[0].M, one[0].a, one[0].b, one[0].k);
+    const WsLayout L = ws_layout(one[0]);
     const long long off = one[0].ws + L.sig;
     if (p->prec == HCORE_GPU_F64) {
         e = cudaMemcpyAsync(sigma, (double *)p->d_ws + off, kk * sizeof(double),

@@ -171,6 +171,86 @@ def build_panel(n_points: int = 65536, dim: int = 2, nb: int = 1024, kernel: str
                  offset=offset, U=Ut, V=Vt, updates=updates, index=index)
 
 
+def compress_tiles(points: np.ndarray, nb: int, tiles: list, kernel: str, ell: float, acc: float,
+                   maxrank: int, seed: int = 0, workers: int | None = None) -> list:
+    """Compress the covariance tiles (i, j) of `points` (host spawn pool, one
+    single-threaded LAPACK process per core).  Returns, per tile, (U^T, V^T,
+    rank) with U^T, V^T of shape (rank, nb) (column-major factors)."""
+    import multiprocessing as mp
+    import tempfile
+
+    workers = workers or os.cpu_count() or 1
+    jobs = [(s, i, j) for s, (i, j) in enumerate(tiles)]
+    results = [None] * len(tiles)
+    with tempfile.TemporaryDirectory() as folder:
+        np.save(os.path.join(folder, "points.npy"), points)
+        chunks = [c for c in (jobs[w::workers] for w in range(workers)) if c]
+        args = [(folder, c, nb, kernel, ell, acc, maxrank, seed) for c in chunks]
+        if len(chunks) <= 1:
+            parts = [_compress_job(a) for a in args]
+        else:
+            saved = {v: os.environ.get(v) for v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS")}
+            os.environ.update(OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+            try:
+                with mp.get_context("spawn").Pool(len(chunks)) as pool:
+                    parts = pool.map(_compress_job, args)
+            finally:
+                for v, old in saved.items():
+                    if old is None:
+                        os.environ.pop(v, None)
+                    else:
+                        os.environ[v] = old
+    for part in parts:
+        for s_, Ut, Vt, r in part:
+            results[s_] = (Ut, Vt, r)
+    return results
+
+
+class TileStore:
+    """Low-rank tiles of a TLR matrix on the device: tile (i, j) -> its
+    factors as (U arena, V arena, element offset, rank), column-major nb x
+    rank blocks with ld = nb.  Updates replace a tile's entry with the slot
+    their new factors were written to."""
+
+    def __init__(self, nb: int, points: np.ndarray, dtype=None, device: str = "cuda"):
+        self.nb, self.points, self.device = nb, points, device
+        self.dtype = dtype
+        self.tiles = {}
+        self.norm = {}
+
+    @staticmethod
+    def build(points: np.ndarray, nb: int, tiles: list, kernel: str, ell: float, acc: float,
+              maxrank: int, seed: int = 0, device: str = "cuda") -> "TileStore":
+        import torch
+
+        comp = compress_tiles(points, nb, tiles, kernel, ell, acc, maxrank, seed)
+        ranks = np.array([r for _, _, r in comp], dtype=np.int64)
+        off = np.zeros(len(tiles) + 1, dtype=np.int64)
+        off[1:] = np.cumsum(ranks * nb)
+        U = torch.from_numpy(np.concatenate([u.reshape(-1) for u, _, _ in comp]))
+        V = torch.from_numpy(np.concatenate([v.reshape(-1) for _, v, _ in comp]))
+        if device != "cpu":
+            U, V = U.to(device), V.to(device)
+        st = TileStore(nb, points, dtype=U.dtype, device=device)
+        for s_, t in enumerate(tiles):
+            st.tiles[t] = (U, V, int(off[s_]), int(ranks[s_]))
+            st.norm[t] = float(np.linalg.norm(comp[s_][1]))   # ||U V^T||_F = ||V||_F
+        return st
+
+    def ptrs(self, t):
+        U, V, o, r = self.tiles[t]
+        e = U.element_size()
+        return U.data_ptr() + e * o, V.data_ptr() + e * o, r
+
+    def factors(self, t):
+        """(U, V) of tile t as host Fortran arrays (nb x rank)."""
+        U, V, o, r = self.tiles[t]
+        n = self.nb * r
+        u = U[o:o + n].cpu().numpy().reshape(r, self.nb).T
+        v = V[o:o + n].cpu().numpy().reshape(r, self.nb).T
+        return np.asfortranarray(u), np.asfortranarray(v)
+
+
 def update_flops(M: int, a: int, b: int, c: int, r: int) -> int:
     """Reference flop model of one HCORE_dgemm update (flop_counts.c:3-70 as
     accumulated at hcore_dgemm.c:125,179,208,224,434,493,595,666)."""
