@@ -47,14 +47,17 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="panel", choices=["panel", "precision", "dense"],
+    p.add_argument("--workload", default="panel", choices=["panel", "precision", "dense", "predictor"],
                    help="panel: the headline (config 2); precision: acc sweep (config 3); "
-                        "dense: batched dsyrk/dgemmcd tile updates (config 4)")
+                        "dense: batched dsyrk/dgemmcd tile updates (config 4); predictor: "
+                        "learned rank predictor on 3D exponential-kernel sweeps (config 5)")
     p.add_argument("--max-updates", type=int, default=None, help="truncate the update list")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--per-tile-sample", type=int, default=48)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--c5-shape", default=None,
+                   help="predictor workload at a reduced shape 'block_tiles,nb,sweeps' (a quick check)")
     return p.parse_args()
 
 
@@ -774,6 +777,399 @@ def run_dense(args):
     barrier(world)
 
 
+C5 = dict(workload="learned rank predictor: 16 panel sweeps of a TLR Cholesky factorization",
+          points=262144, dim=3, nb=2048, tiles_per_dim=128, block_tiles=64,
+          kernel="exp(-|x-y|/0.1) (Matern 1/2)", nugget=1e-2, acc=1e-7, maxrank=256, maxrk=512,
+          sweeps=16,
+          tile_compression="relative sigma >= 1e-7*sigma_max, capped at maxrank",
+          update_truncation="absolute sigma_i < acc (reference rule); new rank above the "
+                            "tile storage maxrank (256) reported as STORAGE and the tile kept",
+          sweep="POTRF of the dense diagonal tile and TRSM of the panel's V factors (torch, "
+                "set-up side), HCORE_dsyrk of the diagonal tiles (batched dense plan), "
+                "HCORE_dgemm Schur updates (batched plan: the timed, compared step)",
+          region="leading 64 x 64 tiles (the first 131072 of the 262144 Morton-sorted points); "
+                 "their factorization does not depend on the rest of the matrix")
+
+
+def _time_execute(batch, torch, stream):
+    """Warm execute, then one timed execute of the same plan (ms)."""
+    batch.execute(stream.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    batch.execute(stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def _panel_logs(hc, torch, dev, pnl, P):
+    """Recompression logs of the panel workload (2D squared-exponential,
+    nb 1024): features and new ranks of its Schur updates at acc 1e-8 (FP64),
+    1e-6 and 1e-4 (FP32 factor products) and 1e-4 (FP32 end to end)."""
+    import numpy as np
+
+    panel = pnl.build_panel(device=str(dev))
+    nb = panel.nb
+    cen, diam = P.cluster_geometry(pnl.morton_points(WORKLOAD["points"], 2, 0), nb)
+    norm = [float(panel.V[int(panel.offset[s]):int(panel.offset[s + 1])].norm()) for s in range(len(panel.tiles))]
+    ups = panel.updates
+    sa = [panel.index[(i, 0)] for i, j in ups]
+    sb = [panel.index[(j, 0)] for i, j in ups]
+    sc = [panel.index[(i, j)] for i, j in ups]
+    out_off = np.arange(len(ups) + 1, dtype=np.int64) * nb * panel.maxrank
+    F, R = [], []
+    for acc, prec, flags in ((1e-8, hc.F64, 0), (1e-6, hc.F64, hc.MIXED_FACTORS),
+                             (1e-4, hc.F64, hc.MIXED_FACTORS), (1e-4, hc.F32, 0)):
+        dt = torch.float64 if prec == hc.F64 else torch.float32
+        src = (panel.U, panel.V) if prec == hc.F64 else (panel.U.float(), panel.V.float())
+        oU = torch.empty(int(out_off[-1]) + 1, dtype=dt, device=dev)
+        oV = torch.empty_like(oU)
+        b = hc.Batch(build_tasks(hc, panel, ups, oU, oV, out_off, acc=acc, src=src),
+                     precision=prec, flags=flags)
+        b.execute()
+        r, st = b.results()
+        b.close()
+        ok = st == 0
+        f = P.features(panel.rank[sa], panel.rank[sb], panel.rank[sc], [norm[x] for x in sa],
+                       [norm[x] for x in sb], [norm[x] for x in sc],
+                       [np.linalg.norm(cen[i] - cen[j]) for i, j in ups],
+                       [(diam[i] + diam[j]) / 2 for i, j in ups], acc)
+        F.append(f[ok])
+        R.append(r[ok])
+        del oU, oV
+    return np.concatenate(F), np.concatenate(R)
+
+
+def _compact(store, torch, keys=None):
+    """Copy the listed tiles (default: all) into one fresh arena of exact
+    ranks; arenas no tile refers to any more are released."""
+    import numpy as np
+
+    keys = list(store.tiles) if keys is None else list(keys)
+    if not keys:
+        return
+    ranks = np.array([store.tiles[t][3] for t in keys], dtype=np.int64)
+    off = np.zeros(len(keys) + 1, dtype=np.int64)
+    off[1:] = np.cumsum(ranks * store.nb)
+    dev = next(iter(store.tiles.values()))[0].device
+    U = torch.empty(int(off[-1]) + 1, dtype=torch.float64, device=dev)
+    V = torch.empty_like(U)
+    for q, t in enumerate(keys):
+        u, v, o, r = store.tiles[t]
+        n = r * store.nb
+        U[int(off[q]):int(off[q]) + n] = u[o:o + n]
+        V[int(off[q]):int(off[q]) + n] = v[o:o + n]
+    for q, t in enumerate(keys):
+        store.tiles[t] = (U, V, int(off[q]), int(ranks[q]))
+
+
+def run_predictor(args):
+    """Config 5: the learned rank predictor against pad-to-maxrank and the
+    per-tile launch loop, in the first 16 panel sweeps of a TLR Cholesky
+    factorization of a 3D exponential-kernel covariance matrix (nb 2048,
+    maxrank 256, acc 1e-7).  Both batched arms run the same kernels, so
+    every rank is the SVD's; the predictor only sizes the Schur updates'
+    output slots (and the rebuild grid); updates above their predicted
+    capacity are rebuilt from the workspace into exact-size slots.  The
+    network is trained on the GPU (library kernels) on the panel workload's
+    logs (2D, nb 1024, acc 1e-8 .. 1e-4), then fine-tuned after every sweep
+    on the ranks this factorization produced so far."""
+    import copy
+
+    import numpy as np
+    import torch
+
+    import hcore_gb300 as hc
+    from hcore_gb300 import build as hbuild
+    from hcore_gb300 import panel as pnl
+    from hcore_gb300 import predictor as P
+    from oracle import oracle as O
+
+    rank, world, local = dist_init()
+    if not os.path.exists(hbuild.LIB):
+        hbuild.build()
+    hc.lib()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    t0 = time.time()
+    F2, R2 = _panel_logs(hc, torch, dev, pnl, P)
+    t_logs = time.time() - t0
+
+    nb, B, S = C5["nb"], C5["block_tiles"], C5["sweeps"]
+    if args.c5_shape:
+        B, nb, S = (int(x) for x in args.c5_shape.split(","))
+    MAXR, MAXRK, ACC = C5["maxrank"], C5["maxrk"], C5["acc"]
+    pts = pnl.morton_points(C5["points"], C5["dim"], 0)[:B * nb]
+    t0 = time.time()
+    tiles = [(i, j) for i in range(B) for j in range(i)]
+    store0 = pnl.TileStore.build(pts, nb, tiles, "exp", 0.1, 1e-7, MAXR, seed=0, device=str(dev))
+    Pd = torch.from_numpy(pts).to(dev)
+
+    def dense_tile(i):   # column-major storage of the symmetric diagonal tile (+ nugget)
+        X = Pd[i * nb:(i + 1) * nb]
+        d2 = (X * X).sum(1)[:, None] + (X * X).sum(1)[None, :] - 2.0 * X @ X.T
+        K = torch.exp(-torch.sqrt(torch.clamp(d2, min=0.0)) / 0.1)
+        return (K + C5["nugget"] * torch.eye(nb, dtype=K.dtype, device=K.device)).contiguous()
+
+    D0 = [dense_tile(i) for i in range(B)]
+    t_tiles = time.time() - t0
+    cen, diam = P.cluster_geometry(pts, nb)
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    def feats(store, ups, k):
+        return P.features([store.tiles[(i, k)][3] for i, j in ups], [store.tiles[(j, k)][3] for i, j in ups],
+                          [store.tiles[(i, j)][3] for i, j in ups], [store.norm[(i, k)] for i, j in ups],
+                          [store.norm[(j, k)] for i, j in ups], [store.norm[(i, j)] for i, j in ups],
+                          [np.linalg.norm(cen[i] - cen[j]) for i, j in ups],
+                          [(diam[i] + diam[j]) / 2 for i, j in ups], ACC)
+
+    def maker(store, ups, k):
+        def make(u, storage, oU, oV):
+            i, j = ups[u]
+            au, av, a = store.ptrs((i, k))
+            bu, bv, b = store.ptrs((j, k))
+            cu, cv, c = store.ptrs((i, j))
+            return hc.LrTask(M=nb, a=a, b=b, c=c, rk=0, maxrk=MAXRK, ld_newv=0,
+                             storage_maxrank=storage, alpha=-1.0, beta=1.0, acc=ACC, AU=au, AV=av,
+                             lda=nb, BU=bu, BV=bv, ldb=nb, Bdense=None, CU=cu, CV=cv, ldc=nb,
+                             CUo=oU, CVo=oV, ldco=nb)
+        return make
+
+    def gemm_step(store, ups, k, caps):
+        """The batched Schur updates of one sweep with output capacities caps:
+        warm execute, timed execute, rebuild of capacity overflows (timed)."""
+        n = len(ups)
+        make = maker(store, ups, k)
+        off = P.slot_offsets(caps, nb)
+        oU = torch.empty(int(off[-1]) + 1, dtype=torch.float64, device=dev)
+        oV = torch.empty_like(oU)
+        tasks = [make(u, int(caps[u]), oU.data_ptr() + 8 * int(off[u]), oV.data_ptr() + 8 * int(off[u]))
+                 for u in range(n)]
+        b = hc.Batch(tasks)
+        ms = _time_execute(b, torch, stream)
+        r, st = b.results(stream.cuda_stream)
+        where = {u: (oU, oV, int(off[u])) for u in range(n)}
+        # STORAGE: above the predicted capacity (rebuilt at its rank) or above
+        # the tiles' maxrank (rebuilt truncated to maxrank, as HCORE_dgemm
+        # with rk = maxrank; the same updates in both arms)
+        over = np.nonzero(st == 5)[0]
+        n_over = int(((r[over] <= MAXR) & (caps[over] < MAXR)).sum())
+        n_trunc = int((r[over] > MAXR).sum())
+        arena = 2 * oU.numel() * 8
+        ms_over = 0.0
+        if len(over):
+            off2 = P.slot_offsets(np.minimum(r[over], MAXR), nb)
+            xU = torch.empty(int(off2[-1]) + 1, dtype=torch.float64, device=dev)
+            xV = torch.empty_like(xU)
+            e0, e1 = ev(), ev()
+            e0.record(stream)
+            b.rebuild(over, [xU.data_ptr() + 8 * int(off2[q]) for q in range(len(over))],
+                      [xV.data_ptr() + 8 * int(off2[q]) for q in range(len(over))], [nb] * len(over),
+                      max_rank=[MAXR] * len(over), stream=stream.cuda_stream)
+            e1.record(stream)
+            r, st = b.results(stream.cuda_stream)
+            ms_over = e0.elapsed_time(e1)
+            for q, u in enumerate(over):
+                where[u] = (xU, xV, int(off2[q]))
+            arena += 2 * xU.numel() * 8
+        ws = b.workspace_bytes
+        b.close()
+        return ms, ms_over, r, st, where, n_over, n_trunc, arena, ws
+
+    net = P.RankPredictor(seed=5)
+    t0 = time.time()
+    base_loss = net.fit(F2, R2, epochs=150, batch=256, lr=2e-3, seed=1)
+    t_train = time.time() - t0
+    policy0 = P.CapacityPolicy.fit(net.predict(F2), R2, target_overflow=0.02)
+    net_state0 = net.state()
+
+    arms, sample_out, extra = {}, {}, {}
+    for arm in ("pad", "predictor"):
+        net.load(net_state0)
+        policy = policy0
+        store = copy.copy(store0)
+        store.tiles, store.norm = dict(store0.tiles), dict(store0.norm)
+        D = [d.clone() for d in D0]
+        logF, logR = [F2], [R2]
+        tot = dict(ms_gemm=0.0, ms_predict=0.0, ms_rebuild=0.0, ms_potrf_trsm=0.0, ms_syrk=0.0,
+                   updates=0, ok=0, truncated=0, overflow=0, arena_bytes_max=0, arena_bytes_sum=0,
+                   ws_bytes_max=0, per_sweep=[])
+        for k in range(S):
+            # POTRF + TRSM of panel k (V <- L^-1 V for every tile (i, k), i > k)
+            e0, e1 = ev(), ev()
+            e0.record(stream)
+            # D[k] holds the lower triangle of the tile (column-major; dsyrk
+            # zeroes the strict upper part): symmetrise before POTRF
+            Dk = torch.tril(D[k].T)
+            Lk, info = torch.linalg.cholesky_ex(Dk + torch.tril(Dk, -1).T)
+            if int(info) != 0:
+                raise SystemExit(f"POTRF of diagonal tile {k} failed (info {int(info)})")
+            col = [(i, k) for i in range(k + 1, B)]
+            if col:
+                Vs = torch.cat([store.tiles[t][1][store.tiles[t][2]:store.tiles[t][2] + nb * store.tiles[t][3]]
+                                .view(store.tiles[t][3], nb) for t in col], 0)
+                Vs = torch.linalg.solve_triangular(Lk, Vs.T, upper=False).T.contiguous()
+                Us = torch.cat([store.tiles[t][0][store.tiles[t][2]:store.tiles[t][2] + nb * store.tiles[t][3]]
+                                for t in col])
+                Vflat = Vs.reshape(-1)
+                o = 0
+                for t in col:
+                    r_ = store.tiles[t][3]
+                    store.tiles[t] = (Us, Vflat, o, r_)
+                    o += nb * r_
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot["ms_potrf_trsm"] += e0.elapsed_time(e1)
+            for t in col:
+                U_, V_, o_, r_ = store.tiles[t]
+                store.norm[t] = float(V_[o_:o_ + nb * r_].norm())
+            # HCORE_dsyrk of the trailing diagonal tiles (batched dense plan)
+            if col:
+                dts = []
+                for j in range(k + 1, B):
+                    au, av, a = store.ptrs((j, k))
+                    dts.append(hc.DenseTask(kind=0, M=nb, a=a, b=0, alpha=-1.0, Au=au, Av=av, lda=nb,
+                                            Bu=None, Bv=None, ldb=nb, CD=D[j].data_ptr(), ldcd=nb))
+                dp = hc.DensePlan(dts)
+                e0, e1 = ev(), ev()
+                e0.record(stream)
+                dp.execute(stream.cuda_stream)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                tot["ms_syrk"] += e0.elapsed_time(e1)
+                dp.close()
+            # HCORE_dgemm Schur updates of the trailing low-rank tiles
+            ups = [(i, j) for j in range(k + 1, B) for i in range(j + 1, B)]
+            n = len(ups)
+            if n == 0:
+                continue
+            F = feats(store, ups, k)
+            ms_pred = 0.0
+            if arm == "pad":
+                caps = np.full(n, MAXR, dtype=np.int64)
+            else:
+                Xd = net._x(F)
+                e0, e1 = ev(), ev()
+                e0.record(stream)
+                y = net.net.predict(Xd, stream=stream.cuda_stream)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms_pred = e0.elapsed_time(e1)
+                caps = policy(P.rank_from_output(y.cpu().numpy()), MAXR)
+            ms, ms_over, r, st, where, nover, ntrunc, arena, ws = gemm_step(store, ups, k, caps)
+            ok = st == 0
+            if k == 0:
+                samp = list(range(0, n, max(1, n // 24)))[:24]
+                sample_out[arm] = {u: (where[u], int(r[u])) for u in samp if ok[u]}
+                if arm == "pad":
+                    # plain per-tile launch loop and the oracle, on sweep 0's inputs
+                    make0 = maker(store, ups, 0)
+                    per_ms = 0.0
+                    for u in samp:
+                        oU1 = torch.empty(nb * MAXR + 1, dtype=torch.float64, device=dev)
+                        oV1 = torch.empty_like(oU1)
+                        b1 = hc.Batch([make0(u, MAXR, oU1.data_ptr(), oV1.data_ptr())])
+                        per_ms += _time_execute(b1, torch, stream)
+                        b1.close()
+                    extra["per_tile"] = {"updates_per_s": len(samp) / (per_ms / 1e3), "sample": len(samp)}
+                    accs = []
+                    for u in samp[:4]:
+                        i, j = ups[u]
+                        AU, AV = store.factors((i, 0))
+                        BU, BV = store.factors((j, 0))
+                        CU, CV = store.factors((i, j))
+                        ref = O.Port().gemm(nb, -1.0, AU, AV, AU.shape[1], BU, BV, BU.shape[1], 1.0,
+                                            CU, CV, CU.shape[1], maxrk=MAXRK, acc=ACC)
+                        if not ok[u] or ref["status"] != 0:
+                            continue
+                        (U_, V_, o_), r_ = where[u], int(r[u])
+                        Pg = (U_[o_:o_ + nb * r_].view(r_, nb).T @ V_[o_:o_ + nb * r_].view(r_, nb)).cpu().numpy()
+                        accs.append(dict(rank=r_, oracle_rank=int(ref["rank"]),
+                                         rel_fro_vs_oracle=float(O.rel_fro(Pg, ref["CU"] @ ref["CV"].T))))
+                    extra["accuracy_vs_oracle"] = accs
+            for u in np.nonzero(ok)[0]:
+                U_, V_, o_ = where[u]
+                store.tiles[ups[u]] = (U_, V_, o_, int(r[u]))
+                store.norm[ups[u]] = float(V_[o_:o_ + nb * int(r[u])].norm())
+            tot["ms_gemm"] += ms
+            tot["ms_predict"] += ms_pred
+            tot["ms_rebuild"] += ms_over
+            tot["updates"] += n
+            tot["ok"] += int(ok.sum())
+            tot["truncated"] += ntrunc
+            tot["overflow"] += nover
+            tot["arena_bytes_max"] = max(tot["arena_bytes_max"], arena)
+            tot["arena_bytes_sum"] += arena
+            tot["ws_bytes_max"] = max(tot["ws_bytes_max"], ws)
+            tot["per_sweep"].append(dict(k=k, updates=n, gemm_ms=round(ms + ms_over + ms_pred, 3),
+                                         overflow=nover, truncated=ntrunc, mean_rank=round(float(r[ok].mean()), 2) if ok.any() else 0.0,
+                                         max_rank=int(r[ok].max()) if ok.any() else 0,
+                                         arena_gb=round(arena / 1e9, 3)))
+            if arm == "predictor":
+                # online: fine-tune on every rank produced so far (fixed standardisation)
+                logF.append(F[ok])
+                logR.append(r[ok])
+                Xall = net._x(np.concatenate(logF))
+                Tall = torch.from_numpy(P.rank_target(np.concatenate(logR))).cuda()
+                net.net.train(Xall, Tall, epochs=8, batch=256, lr=1e-3, seed=100 + k)
+                recent_F, recent_R = np.concatenate(logF[-2:]), np.concatenate(logR[-2:])
+                policy = P.CapacityPolicy.fit(net.predict(recent_F), recent_R, target_overflow=0.02)
+            del where
+            _compact(store, torch)
+        arms[arm] = tot
+        del D
+
+    # equal results: sampled sweep-0 products of both arms
+    max_diff, same = 0.0, True
+    for u, ((U_, V_, o), r) in sample_out["pad"].items():
+        if u not in sample_out["predictor"]:
+            same = False
+            continue
+        (U2, V2, o2), r2 = sample_out["predictor"][u]
+        if r2 != r:
+            same = False
+            continue
+        n_ = nb * r
+        P1 = U_[o:o + n_].view(r, nb).T @ V_[o:o + n_].view(r, nb)
+        P2 = U2[o2:o2 + n_].view(r, nb).T @ V2[o2:o2 + n_].view(r, nb)
+        max_diff = max(max_diff, float((P1 - P2).norm() / P1.norm()))
+
+    def gemm_ups(t):
+        return t["ok"] / ((t["ms_gemm"] + t["ms_rebuild"] + t["ms_predict"]) / 1e3)
+
+    pad, prd = arms["pad"], arms["predictor"]
+    line = {"metric": "config-5 TLR Schur updates/s: predictor-sized vs pad-to-maxrank vs per-tile",
+            "value": gemm_ups(prd), "unit": "updates/s", "n_gpus": world, "steps": 1,
+            "warmup": 1, "ms_per_step": prd["ms_gemm"] + prd["ms_rebuild"] + prd["ms_predict"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded 3D points, tiles compressed on the host cores)",
+            "config": dict(C5, block_tiles=B, nb=nb, sweeps=S),
+            "pad_to_maxrank": {"updates_per_s": gemm_ups(pad),
+                               **{k: v for k, v in pad.items() if k != "per_sweep"}},
+            "predictor": {k: v for k, v in prd.items() if k != "per_sweep"},
+            "per_sweep": {"pad": pad["per_sweep"], "predictor": prd["per_sweep"]},
+            "per_tile": extra.get("per_tile"),
+            "output_memory_ratio_max": prd["arena_bytes_max"] / pad["arena_bytes_max"],
+            "output_memory_ratio_sum": prd["arena_bytes_sum"] / pad["arena_bytes_sum"],
+            "overflow_rate": prd["overflow"] / max(prd["updates"], 1),
+            "same_results": {"ok_counts_equal": pad["ok"] == prd["ok"], "sample_ranks_equal": same,
+                             "max_rel_fro_diff_sweep0_sample": max_diff},
+            "accuracy_vs_oracle": extra.get("accuracy_vs_oracle"),
+            "training": {"samples": int(len(R2)), "epochs": 150, "loss_first": float(base_loss[0]),
+                         "loss_last": float(base_loss[-1]), "train_s": t_train,
+                         "policy_margin_initial": policy0.margin},
+            "setup_s": {"logs": t_logs, "tiles": t_tiles},
+            "timing": "each sweep's batched plan executed twice on the same inputs (warm, timed); "
+                      "predictor arm adds its inference kernel and the rebuild of overflows"}
+    if rank == 0:
+        print(json.dumps(line))
+        sys.stdout.flush()
+    barrier(world)
+
+
 def fp64_peak(L, torch, dev) -> float:
     """FP64 tensor-pipe (DMMA m16n8k16) throughput in TFLOP/s, measured now."""
     return float(L.hcore_gpu_fp64_peak(torch.cuda.current_stream(dev).cuda_stream))
@@ -787,6 +1183,8 @@ def main():
         run_precision(args)
     elif args.workload == "dense":
         run_dense(args)
+    elif args.workload == "predictor":
+        run_predictor(args)
     else:
         run_gb300(args)
 

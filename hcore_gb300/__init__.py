@@ -103,6 +103,8 @@ def lib() -> C.CDLL:
     L.hcore_gpu_plan_destroy.argtypes = [vp]
     L.hcore_gpu_plan_sweeps.argtypes = [vp, _ip, vp]
     L.hcore_gpu_plan_execute_phases.argtypes = [vp, vp, C.c_uint]
+    L.hcore_gpu_plan_rebuild.argtypes = [vp, C.c_int, _ip, C.POINTER(vp), C.POINTER(vp), _ip, _ip,
+                                         vp]
     L.hcore_gpu_fp64_peak.argtypes = [vp]
     L.hcore_gpu_fp64_peak.restype = C.c_double
     L.hcore_gpu_plan_device_ranks.argtypes = [vp]
@@ -257,6 +259,21 @@ class Batch:
         _check(lib().hcore_gpu_plan_sweeps(self._plan, out.ctypes.data_as(_ip), stream or None),
                "hcore_gpu_plan_sweeps")
         return out[:self.n]
+
+    def rebuild(self, idx, CUo, CVo, ldco, max_rank=None, stream=None):
+        """Rebuild STORAGE-status tasks idx[q] into CUo[q]/CVo[q] (pointers,
+        leading dimension ldco[q]) from the last execute's workspace; with
+        max_rank, truncate each to at most max_rank[q] columns."""
+        n = len(idx)
+        if n == 0:
+            return
+        ia = (C.c_int * n)(*[int(i) for i in idx])
+        cu = (C.c_void_p * n)(*[int(x) for x in CUo])
+        cv = (C.c_void_p * n)(*[int(x) for x in CVo])
+        ld = (C.c_int * n)(*[int(x) for x in ldco])
+        mr = (C.c_int * n)(*[int(x) for x in max_rank]) if max_rank is not None else None
+        _check(lib().hcore_gpu_plan_rebuild(self._plan, n, ia, cu, cv, ld, mr, stream or None),
+               "hcore_gpu_plan_rebuild")
 
     def execute_phases(self, phases, stream=None):
         _check(lib().hcore_gpu_plan_execute_phases(self._plan, stream or None, phases),

@@ -26,35 +26,26 @@ struct Desc {
     int pad_;
 };
 
-// Columns of the Uo / Vo slots of an update with k = a + c: an accepted
-// update's new rank is at most min(k, storage_rank), so a caller that knows
-// a smaller bound (storage_maxrank, e.g. a predicted capacity) gets smaller
-// slots; at least ceil(k/2), because Uo and Vo together also hold the k x k
-// reflectors of the SVD's QR until the outputs are written.
-__host__ __device__ inline int uo_cols(int k, int storage_rank) {
-    const int cap = storage_rank < k ? storage_rank : k;
-    const int half = (k + 1) / 2;
-    return cap > half ? cap : half;
-}
-
-// Workspace layout of one update (element offsets from Desc::ws), k = a + c,
-// u = uo_cols(k, storage_rank):
+// Workspace layout of one update (element offsets from Desc::ws), k = a + c:
 //   UA  M*k   stacked [beta CU | alpha AU], then its QR (R on top, reflectors below)
 //   VB  M*k   stacked [CV | G], then its QR
 //   tauA k, tauB k, sig k
 //   F   a*b   AV^T BV
 //   W   k*k   Jacobi working matrix (used when it does not fit shared memory)
 //   V   k*k   Jacobi right vectors (same)
-//   Uo  k*u   U_r (k x r, ld k)       } the SVD's QR reflectors (k x k, ld k)
-//   Vo  k*u   V_r S_r (k x r, ld k)   } span both until U_r and V_r S_r are written
+//   Uo  k*k   U_r (k x r, ld k); the SVD's QR reflectors until U_r is written
+//   Vo  k*k   V_r S_r (k x r, ld k)
+// U_r and V_r S_r are kept for an update whose rank exceeds its storage
+// limit too, so that it can be rebuilt into larger storage without being
+// recompressed (hcore_gpu_plan_rebuild).
 struct WsLayout {
     long long UA, VB, tauA, tauB, sig, F, W, V, Uo, Vo, total;
 };
 
 __host__ __device__ inline long long hc_align32(long long x) { return (x + 31) & ~31LL; }
 
-__host__ __device__ inline WsLayout ws_layout(int M, int a, int b, int k, int storage_rank) {
-    const long long u = uo_cols(k, storage_rank);
+__host__ __device__ inline WsLayout ws_layout(int M, int a, int b, int k) {
+    const long long u = k;
     WsLayout L;
     long long o = 0;
     L.UA = o; o = hc_align32(o + (long long)M * k);
@@ -71,7 +62,7 @@ __host__ __device__ inline WsLayout ws_layout(int M, int a, int b, int k, int st
     return L;
 }
 __host__ __device__ inline WsLayout ws_layout(const Desc &d) {
-    return ws_layout(d.M, d.a, d.b, d.k, d.storage_rank);
+    return ws_layout(d.M, d.a, d.b, d.k);
 }
 
 constexpr int kThreads = 256;
@@ -116,6 +107,12 @@ template <typename T>
 cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int *d_status,
                               int *d_info, const LaunchShape &shape, cudaStream_t s,
                               unsigned phases);
+// rebuild phase only, for listed updates whose status is STORAGE (set to
+// OK; d_cap, if not null, caps their rank)
+template <typename T>
+cudaError_t launch_rebuild(const Desc *d_desc, const int *d_idx, const int *d_cap, int n, T *ws,
+                           int *d_rank, int *d_status, int maxM, int maxK, bool mixed,
+                           cudaStream_t s);
 
 // dense-C updates (hc_dense.cu): per-task rank-K' form coef * P Q^T
 struct DenseWork {

@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     T *s_tau = aux + 3 * (maxK + 1);
     int *s_perm = reinterpret_cast<int *>(aux + 4 * (maxK + 1));   // Jacobi sort
     int *s_pcol = s_perm + (maxK + 1);                                // QR pivots
-    T *Yg = base + L.Uo;   // reflectors of Q (k x k, ld k) over the Uo and Vo slots
+    T *Yg = base + L.Uo;   // reflectors of Q (k x k, ld k) in the Uo slot until U_r is written
 
     // T = triu(R_A) triu(R_B)^T (hcore_dgemm.c:330-387)
     T amax = 0;
@@ -714,12 +714,13 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     else if (r > d.max_rank) st = HCORE_GPU_S_RANK_MAX;
     else if (r > d.storage_rank) st = HCORE_GPU_S_STORAGE;
 
-    // Outputs of an accepted update only (a rejected one leaves its slots
-    // alone; they may be smaller than its rank).  st is uniform in the CTA.
-    if (st == HCORE_GPU_S_OK) {
+    // U_r and V_r S_r of an accepted update, and of one whose rank only
+    // exceeds its storage limit (rebuilt later into larger storage).  st is
+    // uniform in the CTA.
+    if (st == HCORE_GPU_S_OK || st == HCORE_GPU_S_STORAGE) {
         // U_r = Q (V_J's true columns), Q = H_0 ... H_{k-1}: lane per output
-        // column, in place in V_J's column, reflectors from last to first.
-        // The reflectors span the Uo and Vo slots, so this comes first.
+        // column, in place in V_J's column, reflectors (in the Uo slot) from
+        // last to first.
         for (int t = tid; t < r; t += nthr) {
             const int j = s_perm[t];
             T *x = A + (size_t)j * ld;   // each lane owns the column of its own j
@@ -956,6 +957,38 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
     }
     return cudaGetLastError();
 }
+
+// Rebuild of updates that ended with HCORE_GPU_S_STORAGE: their U_r and
+// V_r S_r are still in the workspace, so only the rebuild phase runs again,
+// over descriptors that point at the new output storage.
+// cap[q] > 0 keeps the leading cap[q] singular triplets only (the fixed-rank
+// truncation of HCORE_dgemm's rk argument, applied after the fact).
+__global__ void storage_to_ok_kernel(const int *__restrict__ idx, const int *__restrict__ cap,
+                                     int n, int *__restrict__ status, int *__restrict__ rank) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n || status[idx[q]] != HCORE_GPU_S_STORAGE) return;
+    status[idx[q]] = HCORE_GPU_S_OK;
+    if (cap && cap[q] > 0 && rank[idx[q]] > cap[q]) rank[idx[q]] = cap[q];
+}
+
+template <typename T>
+cudaError_t launch_rebuild(const Desc *d_desc, const int *d_idx, const int *d_cap, int n, T *ws,
+                           int *d_rank, int *d_status, int maxM, int maxK, bool mixed,
+                           cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (maxK > kMaxK || maxM > 32 * kMaxRowsPerLane) return cudaErrorInvalidValue;
+    storage_to_ok_kernel<<<(n + 255) / 256, 256, 0, s>>>(d_idx, d_cap, n, d_status, d_rank);
+    const int rpl = (maxM + 31) / 32;
+    if (mixed && sizeof(T) == sizeof(double))
+        launch_apply_all<T, float>(d_desc, n, ws, d_rank, d_status, maxK, rpl, s);
+    else
+        launch_apply_all<T, T>(d_desc, n, ws, d_rank, d_status, maxK, rpl, s);
+    return cudaGetLastError();
+}
+template cudaError_t launch_rebuild<double>(const Desc *, const int *, const int *, int, double *,
+                                            int *, int *, int, int, bool, cudaStream_t);
+template cudaError_t launch_rebuild<float>(const Desc *, const int *, const int *, int, float *,
+                                           int *, int *, int, int, bool, cudaStream_t);
 
 template cudaError_t configure_recompress<double>(int, int *);
 template cudaError_t configure_recompress<float>(int, int *);

@@ -209,6 +209,11 @@ struct hcore_gpu_plan_s {
     size_t ws_bytes = 0;
     std::vector<long long> ws_of_task;
     std::vector<int> k_of_task;
+    std::vector<Desc> h_desc;        // host copy of d_desc (launch order)
+    std::vector<int> pos_of_task;    // task index -> position in h_desc
+    Desc *d_rdesc = nullptr;         // hcore_gpu_plan_rebuild: descriptors and indices
+    int *d_ridx = nullptr;
+    int rcap = 0;
     // HCORE_GPU_STAGE_INPUTS: host input ranges merged into segments, each
     // mirrored in d_mirror and refreshed by one copy per execute
     struct Segment {
@@ -332,6 +337,8 @@ static void plan_free(hcore_gpu_plan p) {
     cudaFree(p->d_info);
     cudaFree(p->d_ws);
     cudaFree(p->d_mirror);
+    cudaFree(p->d_rdesc);
+    cudaFree(p->d_ridx);
     delete p;
 }
 
@@ -418,10 +425,14 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
     }
     p->ws_of_task.assign(n, -1);
     p->k_of_task.assign(n, 0);
-    for (const Desc &d : descs) {
+    p->pos_of_task.assign(n, -1);
+    for (size_t q = 0; q < descs.size(); ++q) {
+        const Desc &d = descs[q];
         p->ws_of_task[d.idx] = d.status0 ? -1 : d.ws;
         p->k_of_task[d.idx] = d.k;
+        p->pos_of_task[d.idx] = (int)q;
     }
+    p->h_desc = descs;
     {
         const cudaError_t ce = precision == HCORE_GPU_F64
                                    ? configure_recompress<double>(p->maxK, &p->shape.svd_smem_kmax)
@@ -502,6 +513,75 @@ extern "C" int hcore_gpu_plan_execute_phases(hcore_gpu_plan p, void *stream, uns
     }
     if (e != cudaSuccess) {
         set_error("hcore_gpu_plan_execute: %s", cudaGetErrorString(e));
+        return HCORE_GPU_ECUDA;
+    }
+    return HCORE_GPU_OK;
+}
+
+extern "C" int hcore_gpu_plan_rebuild(hcore_gpu_plan p, int n, const int *task_idx,
+                                      void *const *CUo, void *const *CVo, const int *ldco,
+                                      const int *max_rank, void *stream) {
+    if (!p || n < 0 || (n > 0 && (!task_idx || !CUo || !CVo || !ldco))) {
+        set_error("hcore_gpu_plan_rebuild: invalid argument");
+        return HCORE_GPU_EINVAL;
+    }
+    if (n == 0) return HCORE_GPU_OK;
+    std::vector<Desc> sub(n);
+    int maxM = 1, maxK = 1;
+    for (int q = 0; q < n; ++q) {
+        const int i = task_idx[q];
+        if (i < 0 || i >= p->n || p->pos_of_task[i] < 0 || p->h_desc[p->pos_of_task[i]].status0) {
+            set_error("hcore_gpu_plan_rebuild: task %d was not run by this plan", i);
+            return HCORE_GPU_EINVAL;
+        }
+        Desc d = p->h_desc[p->pos_of_task[i]];
+        if (!CUo[q] || !CVo[q] || ldco[q] < d.M) {
+            set_error("hcore_gpu_plan_rebuild: bad output storage for task %d", i);
+            return HCORE_GPU_EINVAL;
+        }
+        d.CUo = const_cast<void *>(device_alias(CUo[q]));
+        d.CVo = const_cast<void *>(device_alias(CVo[q]));
+        d.ldco = ldco[q];
+        d.storage_rank = INT_MAX;
+        sub[q] = d;
+        maxM = std::max(maxM, d.M);
+        maxK = std::max(maxK, d.k);
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaSuccess;
+    if (n > p->rcap) {
+        cudaFree(p->d_rdesc);
+        cudaFree(p->d_ridx);
+        p->d_rdesc = nullptr;
+        p->d_ridx = nullptr;
+        p->rcap = 0;
+        e = cudaMalloc(&p->d_rdesc, (size_t)n * sizeof(Desc));
+        if (e == cudaSuccess) e = cudaMalloc(&p->d_ridx, 2 * (size_t)n * sizeof(int));
+        if (e != cudaSuccess) {
+            set_error("hcore_gpu_plan_rebuild: cudaMalloc: %s", cudaGetErrorString(e));
+            cudaGetLastError();
+            return HCORE_GPU_ENOMEM;
+        }
+        p->rcap = n;
+    }
+    // from pageable host memory: both copies are complete when they return
+    e = cudaMemcpyAsync(p->d_rdesc, sub.data(), (size_t)n * sizeof(Desc), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p->d_ridx, task_idx, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && max_rank)
+        e = cudaMemcpyAsync(p->d_ridx + n, max_rank, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) {
+        const bool mixed = p->shape.mixed;
+        const int *cap = max_rank ? p->d_ridx + n : nullptr;
+        e = p->prec == HCORE_GPU_F64
+                ? launch_rebuild<double>(p->d_rdesc, p->d_ridx, cap, n, (double *)p->d_ws,
+                                         p->d_rank, p->d_status, maxM, maxK, mixed, s)
+                : launch_rebuild<float>(p->d_rdesc, p->d_ridx, cap, n, (float *)p->d_ws,
+                                        p->d_rank, p->d_status, maxM, maxK, mixed, s);
+    }
+    if (e != cudaSuccess) {
+        set_error("hcore_gpu_plan_rebuild: %s", cudaGetErrorString(e));
         return HCORE_GPU_ECUDA;
     }
     return HCORE_GPU_OK;

@@ -8,10 +8,11 @@ This module predicts each rank from cheap features with the library's MLP
 (hcore_gpu_mlp_*, trained by the library's own CUDA kernels on ranks the
 method itself produced), sizes every update's output slot to the predicted
 capacity, and passes that capacity to the plan as the task's
-storage_maxrank, which also shrinks the plan's U/V slots and the rebuild
-grid.  The SVD still decides every rank: an update whose rank exceeds its
+storage_maxrank (the plan then also sizes its rebuild grid by the largest
+capacity).  The SVD still decides every rank: an update whose rank exceeds its
 capacity is reported with HCORE_GPU_S_STORAGE (its slot untouched) and is
-run again in an overflow batch with maxrank-sized slots.
+rebuilt from the plan's workspace into an overflow slot of exactly its rank
+(only the rebuild phase runs again).
 
 Features of update (i, j) of panel k, with A = tile (i, k), B = (j, k),
 C = (i, j) and tile norms ||X||_F = ||V_X||_F (U orthonormal):
@@ -22,7 +23,6 @@ Target: log2(1 + new rank).
 """
 from __future__ import annotations
 
-import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -130,8 +130,10 @@ def slot_offsets(cols: np.ndarray, nb: int) -> np.ndarray:
 
 def run_capacity_batch(hc, make_task, n: int, nb: int, caps: np.ndarray, maxrank: int,
                        dtype=None, device="cuda", precision=0, flags=0):
-    """Run n updates with per-update output capacities `caps`, then rerun
-    the overflowed ones with maxrank slots.
+    """Run n updates with per-update output capacities `caps`; updates whose
+    new rank exceeds their capacity (but not maxrank) are then rebuilt from
+    the plan's workspace into overflow slots of exactly their rank
+    (hcore_gpu_plan_rebuild: the rebuild phase only, no recompression).
 
     make_task(u, storage, CUo_ptr, CVo_ptr) -> LrTask for update u.
     Returns dict(ranks, status, where) where where[u] = (U arena, V arena,
@@ -149,27 +151,21 @@ def run_capacity_batch(hc, make_task, n: int, nb: int, caps: np.ndarray, maxrank
     batch = hc.Batch(tasks, precision=precision, flags=flags)
     batch.execute()
     ranks, status = batch.results()
-    ws_bytes = batch.workspace_bytes
-    batch.close()
     where = [(oU, oV, int(off[u])) for u in range(n)]
-    over = np.nonzero(status == 5)[0]                 # HCORE_GPU_S_STORAGE
+    over = np.nonzero((status == 5) & (ranks <= maxrank) & (caps < maxrank))[0]   # STORAGE
     arena_bytes = 2 * oU.numel() * esz
-    ws2 = 0
     if len(over):
-        off2 = slot_offsets(np.full(len(over), maxrank), nb)
+        off2 = slot_offsets(ranks[over], nb)
         xU = torch.empty(int(off2[-1]) + 1, dtype=dtype, device=device)
         xV = torch.empty_like(xU)
-        t2 = [make_task(int(u), maxrank, xU.data_ptr() + esz * int(off2[q]),
-                        xV.data_ptr() + esz * int(off2[q])) for q, u in enumerate(over)]
-        b2 = hc.Batch(t2, precision=precision, flags=flags)
-        b2.execute()
-        r2, s2 = b2.results()
-        ws2 = b2.workspace_bytes
-        b2.close()
-        ranks, status = ranks.copy(), status.copy()
+        batch.rebuild(over, [xU.data_ptr() + esz * int(off2[q]) for q in range(len(over))],
+                      [xV.data_ptr() + esz * int(off2[q]) for q in range(len(over))],
+                      [nb] * len(over))
+        ranks, status = batch.results()
         for q, u in enumerate(over):
-            ranks[u], status[u] = r2[q], s2[q]
             where[u] = (xU, xV, int(off2[q]))
         arena_bytes += 2 * xU.numel() * esz
+    ws_bytes = batch.workspace_bytes
+    batch.close()
     return dict(ranks=ranks, status=status, where=where, overflow=len(over),
-                arena_bytes=arena_bytes, workspace_bytes=ws_bytes + ws2)
+                arena_bytes=arena_bytes, workspace_bytes=ws_bytes)

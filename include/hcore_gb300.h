@@ -109,6 +109,20 @@ const int *hcore_gpu_plan_device_ranks(hcore_gpu_plan plan);
 const int *hcore_gpu_plan_device_status(hcore_gpu_plan plan);
 /* copy ranks and statuses to host arrays (either may be NULL) and wait */
 int hcore_gpu_plan_results(hcore_gpu_plan plan, int *ranks, int *status, void *stream);
+/* Rebuild tasks that ended with HCORE_GPU_S_STORAGE (new rank above their
+ * storage_maxrank, e.g. a predicted capacity) into new output storage
+ * without recompressing them: the rank, U_r and V_r S_r the last execute
+ * found are still in the plan's workspace, so only the rebuild phase runs,
+ * for these n tasks.  Task task_idx[q] is written to CUo[q]/CVo[q] (leading
+ * dimension ldco[q], room for its new rank) and its status becomes
+ * HCORE_GPU_S_OK.  With max_rank non-NULL, a task whose rank exceeds
+ * max_rank[q] > 0 keeps its leading max_rank[q] singular triplets only (the
+ * truncation HCORE_dgemm's fixed rank rk would have made; its reported rank
+ * becomes max_rank[q]).  Tasks with another status are not written.  Call
+ * after the execute that produced the statuses and before the next one; the
+ * first call (or one with more tasks than any before) allocates. */
+int hcore_gpu_plan_rebuild(hcore_gpu_plan plan, int n, const int *task_idx, void *const *CUo,
+                           void *const *CVo, const int *ldco, const int *max_rank, void *stream);
 /* copy the k singular values of task i (descending) to host (diagnostics) */
 int hcore_gpu_plan_sigma(hcore_gpu_plan plan, int i, double *sigma, int *k, void *stream);
 /* Jacobi sweeps each task's SVD took (diagnostics; valid after execute) */

@@ -432,3 +432,23 @@ def test_nonfinite_input_marks_update_noconv(hc, port, precision):
     P = CUo.astype(np.float64) @ CVo.T.astype(np.float64)
     P_ref = ref["CU"].astype(np.float64) @ ref["CV"].T.astype(np.float64)
     assert O.rel_fro(P, P_ref) < (FP32_TOL if precision else FP64_TOL)
+
+
+@pytest.mark.parametrize("M,a,b,c,maxrk,acc", [
+    (2048, 256, 200, 256, 512, 1e-7),    # k = 512: Jacobi matrices in global memory, 64 rows/lane
+    (1024, 150, 100, 130, 300, 1e-8),    # k = 280
+    (2048, 40, 30, 50, 128, 1e-7)])      # M = 2048 with a small k (shared-memory Jacobi)
+def test_large_rank_updates_vs_oracle(hc, port, M, a, b, c, maxrk, acc):
+    """The largest shapes a plan takes (a + c up to 512, M up to 2048), as in
+    a 3D covariance matrix with nb = 2048 and tiles of rank up to 256."""
+    rng = np.random.default_rng(M + a)
+    arrays = _batch_case(rng, M, a, b, c, decades=10.0)
+    cases = [dict(M=M, a=a, b=b, c=c, alpha=-1.0, beta=1.0, maxrk=maxrk, acc=acc, arrays=arrays)]
+    _, ranks, status, outs = _run_batch(hc, cases)
+    assert status[0] == 0
+    AU, AV, BU, BV, CU, CV = arrays
+    ref = port.gemm(M, -1.0, AU, AV, a, BU, BV, b, 1.0, CU, CV, c, maxrk=maxrk, acc=acc)
+    assert ref["status"] == 0
+    assert ranks[0] == ref["rank"]
+    CUo, CVo = outs[0]
+    assert O.rel_fro(CUo @ CVo.T, ref["CU"] @ ref["CV"].T) < FP64_TOL

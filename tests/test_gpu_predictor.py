@@ -9,11 +9,11 @@ the method produced) and sizes panel 1's output slots:
 * results equal the pad-to-maxrank batch: every rank and status, products
   within 1e-12 relative (the same kernels decide every rank);
 * the output slots take less than half the pad batch's memory, with at most
-  10% of the updates rerun in the overflow batch;
+  10% of the updates rebuilt into overflow slots;
 * an untrained network (same architecture, random weights) sized by the
   same policy loses what the trained one gains;
-* with every capacity forced to 1, all updates overflow and the rerun still
-  reproduces the pad batch.
+* with every capacity forced to 1, all updates overflow and their rebuild
+  from the workspace still reproduces the pad batch.
 """
 import numpy as np
 import pytest
@@ -123,3 +123,35 @@ def test_every_update_overflowing_still_matches(hc, tlr):
     for u in range(len(ups)):
         r = int(ref["ranks"][u])
         assert O.rel_fro(_product(got, u, r), _product(ref, u, r)) < 1e-12
+
+
+def test_rebuild_with_rank_cap_equals_fixed_rank_update(hc, port):
+    """An update whose rank exceeds its storage is rebuilt truncated to
+    max_rank: the result is HCORE_dgemm's fixed-rank update (rk = max_rank)."""
+    import torch
+    from hcore_gb300 import devmem
+
+    rng = np.random.default_rng(31)
+    M, a, b, c, cap = 256, 20, 18, 24, 10
+    AU, AV = O.graded_lowrank(rng, M, a, 10.0)
+    BU, BV = O.graded_lowrank(rng, M, b, 10.0)
+    CU, CV = O.graded_lowrank(rng, M, c, 10.0)
+    d = [devmem.to_device(x) for x in (AU, AV, BU, BV, CU, CV)]
+    oU = torch.zeros((cap, M), dtype=torch.float64, device="cuda")
+    oV = torch.zeros_like(oU)
+    t = hc.LrTask(M=M, a=a, b=b, c=c, rk=0, maxrk=64, ld_newv=0, storage_maxrank=cap,
+                  alpha=-1.0, beta=1.0, acc=1e-12, AU=d[0].data_ptr(), AV=d[1].data_ptr(), lda=M,
+                  BU=d[2].data_ptr(), BV=d[3].data_ptr(), ldb=M, Bdense=None, CU=d[4].data_ptr(),
+                  CV=d[5].data_ptr(), ldc=M, CUo=oU.data_ptr(), CVo=oV.data_ptr(), ldco=M)
+    batch = hc.Batch([t])
+    batch.execute()
+    r, st = batch.results()
+    assert st[0] == 5 and r[0] > cap                      # STORAGE, outputs untouched
+    assert float(oU.abs().max()) == 0.0
+    batch.rebuild([0], [oU.data_ptr()], [oV.data_ptr()], [M], max_rank=[cap])
+    r, st = batch.results()
+    assert st[0] == 0 and r[0] == cap
+    ref = port.gemm(M, -1.0, AU, AV, a, BU, BV, b, 1.0, CU, CV, c, rk=cap, maxrk=64, acc=1e-12)
+    assert ref["status"] == 0 and ref["rank"] == cap
+    P = devmem.to_host(oU, cap) @ devmem.to_host(oV, cap).T
+    assert O.rel_fro(P, ref["CU"] @ ref["CV"].T) < 1e-11
