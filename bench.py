@@ -278,11 +278,12 @@ def run_gb300(args):
     result = {"metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world,
               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-              "data": "synthetic (seeded points, covariance tiles compressed on the GPU)",
+              "data": "synthetic (seeded points, covariance tiles compressed on the host cores)",
               "config": dict(WORKLOAD, updates_per_step=int(total_updates), parallelism=f"dp{world}",
                              l2="inputs+outputs+workspace larger than L2 (no flush needed)",
-                             graph="4 kernel launches captured in one CUDA graph"),
-              "gpu_launches": 4 * args.steps,
+                             graph=f"{batch.launches} kernel launches (4 stream groups: stack, QR, "
+                                   f"one SVD launch per rank bucket, rebuild) captured in one CUDA graph"),
+              "gpu_launches": batch.launches * args.steps,
               "gflops_model": flops_model / (ms / 1e3) / 1e9,
               "clocks": clk}
     if rank != 0:
@@ -538,14 +539,15 @@ def cpu_run(panel, updates, seconds):
                                          for ch in chunks])
             wall = time.time() - t0
     done = sum(d for d, _ in res)
-    return done / wall, len(chunks), done
+    return done / wall, len(chunks), done, wall
 
 
 def cpu_baseline(panel, updates, seconds):
-    v, cores, done = cpu_run(panel, updates, seconds)
+    v, cores, done, wall = cpu_run(panel, updates, seconds)
     return {"value": v, "unit": "updates/s", "cores": cores, "kind": "port",
-            "sample": f"{done} of the step's {len(updates)} updates, one single-threaded "
-                      f"process per core, OpenBLAS LAPACK (oracle/hcore_port.c)"}
+            "sample": f"{done} updates in {wall:.1f} s, the step's {len(updates)} updates dealt "
+                      f"round-robin to one single-threaded process per core and repeated until "
+                      f"the time bound, OpenBLAS LAPACK (oracle/hcore_port.c)"}
 
 
 def run_reference(args):
@@ -563,7 +565,7 @@ def run_reference(args):
     vals = []
     per_step = max(args.cpu_seconds / max(args.steps, 1), 2.0)
     for s in range(args.warmup + args.steps):
-        v, cores, done = cpu_run(panel, updates, per_step)
+        v, cores, done, _ = cpu_run(panel, updates, per_step)
         if s >= args.warmup:
             vals.append(v)
     v = statistics.median(vals)

@@ -111,6 +111,7 @@ def lib() -> C.CDLL:
     L.hcore_gpu_plan_device_ranks.restype = vp
     L.hcore_gpu_plan_device_status.argtypes = [vp]
     L.hcore_gpu_plan_device_status.restype = vp
+    L.hcore_gpu_plan_launches.argtypes = [vp]
     L.hcore_gpu_plan_workspace_bytes.argtypes = [vp]
     L.hcore_gpu_plan_workspace_bytes.restype = C.c_size_t
     L.hcore_gpu_plan_staged_bytes.argtypes = [vp]
@@ -290,6 +291,11 @@ class Batch:
     @property
     def staged_bytes(self) -> int:
         return int(lib().hcore_gpu_plan_staged_bytes(self._plan))
+
+    @property
+    def launches(self) -> int:
+        """Kernel launches of one execute."""
+        return int(lib().hcore_gpu_plan_launches(self._plan))
 
     @property
     def workspace_bytes(self) -> int:

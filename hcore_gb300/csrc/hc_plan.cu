@@ -613,6 +613,20 @@ extern "C" int hcore_gpu_plan_sweeps(hcore_gpu_plan p, int *sweeps, void *stream
     return HCORE_GPU_OK;
 }
 
+extern "C" int hcore_gpu_plan_launches(hcore_gpu_plan p) {
+    if (!p || p->n == 0) return 0;
+    auto count = [](const LaunchShape &sh) {
+        int c = 3;   // stack, QR, rebuild
+        for (int b = 0; b < sh.nbuckets; ++b) c += sh.buckets[b].count > 0;
+        return c;
+    };
+    if (p->groups.empty()) return count(p->shape);
+    int c = 0;
+    for (const auto &g : p->groups)
+        if (g.count > 0) c += count(g.shape);
+    return c;
+}
+
 extern "C" size_t hcore_gpu_plan_workspace_bytes(hcore_gpu_plan p) { return p ? p->ws_bytes : 0; }
 extern "C" size_t hcore_gpu_plan_staged_bytes(hcore_gpu_plan p) { return p ? p->staged_bytes : 0; }
 

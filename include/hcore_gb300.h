@@ -127,6 +127,9 @@ int hcore_gpu_plan_rebuild(hcore_gpu_plan plan, int n, const int *task_idx, void
 int hcore_gpu_plan_sigma(hcore_gpu_plan plan, int i, double *sigma, int *k, void *stream);
 /* Jacobi sweeps each task's SVD took (diagnostics; valid after execute) */
 int hcore_gpu_plan_sweeps(hcore_gpu_plan plan, int *sweeps, void *stream);
+/* kernel launches one execute makes (stack, QR, one SVD launch per rank
+ * bucket, rebuild; per stream group) */
+int hcore_gpu_plan_launches(hcore_gpu_plan plan);
 /* bytes of device workspace the plan holds */
 size_t hcore_gpu_plan_workspace_bytes(hcore_gpu_plan plan);
 /* bytes copied host->device by every execute (HCORE_GPU_STAGE_INPUTS) */
