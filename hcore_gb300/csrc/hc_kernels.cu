@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kThreads) stack_kernel(const Desc *__restrict_
                                                          T *__restrict__ ws) {
     const Desc d = descs[blockIdx.x];
     if (d.status0) return;
-    const int M = d.M, a = d.a, b = d.b, c = d.c, k = d.k;
+    const int M = d.M, a = d.a, b = d.b, c = d.c;
     const WsLayout L = ws_layout(d);
     T *UA = ws + d.ws + L.UA;
     T *VB = ws + d.ws + L.VB;
@@ -361,17 +361,23 @@ struct JacobiLim<float> {
 // Lanes per column pair in the Jacobi sweeps of a bucket whose largest k is
 // K.  A group of G lanes shares a pair's rows, which divides the per-round
 // latency of one update by about G but repeats the rotation parameters in
-// every lane of the group.  Small updates are throughput-bound (one lane per
-// pair); the few large ones set the phase's critical path (four lanes).
-__host__ __device__ inline int svd_group(int K) {
+// every lane of the group.  Shared-memory buckets: small updates are
+// throughput-bound (one lane per pair); the few large ones set the phase's
+// critical path (four lanes).  Workspace buckets (k beyond the shared-memory
+// limit): four lanes per pair, up to 1024 threads, to keep enough loads in
+// flight on the L2-resident matrices.
+constexpr int kSvdMaxThreads = 1024;
+__host__ __device__ inline int svd_group(int K, bool smem) {
     const int np = (K + 1) / 2;
-    return np <= 24 ? 1 : (np <= 64 ? 4 : (np <= 128 ? 2 : 1));
+    if (smem) return np <= 24 ? 1 : (np <= 64 ? 4 : (np <= 128 ? 2 : 1));
+    return np <= kSvdMaxThreads / 4 ? 4 : (np <= kSvdMaxThreads / 2 ? 2 : 1);
 }
 // Threads per CTA of the SVD kernel: G lanes for each of the K/2 pairs.
-__host__ __device__ inline int svd_threads(int K) {
+__host__ __device__ inline int svd_threads(int K, bool smem) {
     const int np = (K + 1) / 2;
-    const int t = ((np * svd_group(K) + 31) / 32) * 32;
-    return t < 32 ? 32 : (t > 256 ? 256 : t);
+    const int cap = smem ? kThreads : kSvdMaxThreads;
+    const int t = ((np * svd_group(K, smem) + 31) / 32) * 32;
+    return t < 32 ? 32 : (t > cap ? cap : t);
 }
 __host__ __device__ inline int svd_ld(int k) { return k | 1; }
 
@@ -404,15 +410,16 @@ __host__ __device__ inline size_t svd_smem_bytes(int K, bool in_smem) {
 // norm is below safmin is negligible (< 2^-485 relative in FP64, 2^-51 in
 // FP32) and not rotated.  A non-finite singular value marks the update
 // NOCONV; the sort below is a total order even then.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict__ descs,
-                                                         T *__restrict__ ws, int *__restrict__ rank,
-                                                         int *__restrict__ status,
-                                                         int *__restrict__ info, int smem_kmax,
-                                                         int maxK) {
+template <typename T, bool SMEM>
+__global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__restrict__ descs,
+                                                               T *__restrict__ ws,
+                                                               int *__restrict__ rank,
+                                                               int *__restrict__ status,
+                                                               int *__restrict__ info, int maxK,
+                                                               int G) {
     extern __shared__ unsigned char smem_raw[];
     __shared__ int s_rot, s_piv, s_exp;
-    __shared__ T s_wmax[kWarps];
+    __shared__ T s_wmax[kSvdMaxThreads / 32];
     const Desc d = descs[blockIdx.x];
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
     if (d.status0) {
@@ -427,11 +434,18 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     const WsLayout L = ws_layout(d);
     T *base = ws + d.ws;
     const T *UA = base + L.UA, *VB = base + L.VB;
-    const bool in_smem = maxK <= smem_kmax;
-    const int ld = in_smem ? svd_ld(k) : k;
-    T *A = in_smem ? reinterpret_cast<T *>(smem_raw) : base + L.W;   // T, then QR, then V_J
-    T *B = in_smem ? A + (size_t)maxK * svd_ld(maxK) : base + L.V;   // R^T, rotated
-    T *aux = reinterpret_cast<T *>(smem_raw + (in_smem ? (size_t)2 * maxK * svd_ld(maxK) * sizeof(T) : 0));
+    // the k x k working matrices: column-major in shared memory (odd ld: a
+    // lane walking its own column is free of bank conflicts), row-major in
+    // the workspace (the lanes of a warp own consecutive columns in the
+    // tournament and in every lane-per-column loop: coalesced)
+    const int ld = SMEM ? svd_ld(k) : k;
+    const size_t rs = SMEM ? 1 : (size_t)ld;   // distance of rows i and i + 1 in a column
+    auto ix = [ld](int i, int j) -> size_t {
+        return SMEM ? (size_t)j * ld + i : (size_t)i * ld + j;
+    };
+    T *A = SMEM ? reinterpret_cast<T *>(smem_raw) : base + L.W;   // T, then QR, then V_J
+    T *B = SMEM ? A + (size_t)maxK * svd_ld(maxK) : base + L.V;   // R^T, rotated
+    T *aux = reinterpret_cast<T *>(smem_raw + (SMEM ? (size_t)2 * maxK * svd_ld(maxK) * sizeof(T) : 0));
     T *s_d = aux, *s_nrm = aux + (maxK + 1), *s_sig = aux + 2 * (maxK + 1);
     T *s_tau = aux + 3 * (maxK + 1);
     int *s_perm = reinterpret_cast<int *>(aux + 4 * (maxK + 1));   // Jacobi sort
@@ -440,11 +454,12 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
 
     // T = triu(R_A) triu(R_B)^T (hcore_dgemm.c:330-387)
     T amax = 0;
-    for (int j = 0; j < k; ++j)
-        for (int i = tid; i < k; i += nthr) {
+    for (int o = 0; o < k; ++o)
+        for (int t = tid; t < k; t += nthr) {   // the lanes walk the contiguous index
+            const int i = SMEM ? t : o, j = SMEM ? o : t;
             T s = 0;
             for (int l = max(i, j); l < k; ++l) s += UA[(size_t)l * M + i] * VB[(size_t)l * M + j];
-            A[(size_t)j * ld + i] = s;
+            A[ix(i, j)] = s;
             amax = max(amax, abs(s));
         }
     // scale T by 2^-e, e = exponent of its largest entry (nthr is a multiple of 32)
@@ -459,14 +474,14 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     __syncthreads();
     const int sexp = s_exp;
     if (sexp != 0)
-        for (int j = 0; j < k; ++j)
-            for (int i = tid; i < k; i += nthr) A[(size_t)j * ld + i] = mul_exp2(A[(size_t)j * ld + i], -sexp);
+        for (int o = 0; o < k; ++o)
+            for (int t = tid; t < k; t += nthr) A[(size_t)o * ld + t] = mul_exp2(A[(size_t)o * ld + t], -sexp);
     __syncthreads();
 
     // ---- QR with column pivoting, T P = Q R (lane per column) ----
     for (int c = tid; c < k; c += nthr) {
         T s = 0;
-        for (int i = 0; i < k; ++i) s += A[(size_t)c * ld + i] * A[(size_t)c * ld + i];
+        for (int i = 0; i < k; ++i) s += A[ix(i, c)] * A[ix(i, c)];
         s_nrm[c] = s;   // partial column norms (rows j..k-1), squared
         s_d[c] = s;     // norms at the last exact computation
         s_pcol[c] = c;
@@ -497,9 +512,9 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         const int pv = s_piv;
         if (pv != j) {
             for (int i = tid; i < k; i += nthr) {
-                const T x = A[(size_t)j * ld + i];
-                A[(size_t)j * ld + i] = A[(size_t)pv * ld + i];
-                A[(size_t)pv * ld + i] = x;
+                const T x = A[ix(i, j)];
+                A[ix(i, j)] = A[ix(i, pv)];
+                A[ix(i, pv)] = x;
             }
             if (tid == 0) {
                 T x = s_nrm[j]; s_nrm[j] = s_nrm[pv]; s_nrm[pv] = x;
@@ -510,17 +525,17 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         __syncthreads();
         // reflector of column j, rows j..k-1 (dlarfg), by thread 0
         if (tid == 0) {
-            T *aj = A + (size_t)j * ld;
-            const T alpha = aj[j];
+            T *aj = A + ix(0, j);
+            const T alpha = aj[j * rs];
             T ss = 0;
-            for (int i = j + 1; i < k; ++i) ss += aj[i] * aj[i];
+            for (int i = j + 1; i < k; ++i) ss += aj[i * rs] * aj[i * rs];
             T tj = 0;
             if (ss > T(0)) {
                 const T beta = -copysign(sqrt(alpha * alpha + ss), alpha);
                 tj = (beta - alpha) / beta;
                 const T scal = T(1) / (alpha - beta);
-                for (int i = j + 1; i < k; ++i) aj[i] *= scal;
-                aj[j] = beta;
+                for (int i = j + 1; i < k; ++i) aj[i * rs] *= scal;
+                aj[j * rs] = beta;
             }
             s_tau[j] = tj;
         }
@@ -528,21 +543,21 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         // apply to the trailing columns and downdate their norms (lane per column)
         const T tj = s_tau[j];
         for (int c = j + 1 + tid; c < k; c += nthr) {
-            T *ac = A + (size_t)c * ld;
-            const T *aj = A + (size_t)j * ld;
+            T *ac = A + ix(0, c);
+            const T *aj = A + ix(0, j);
             if (tj != T(0)) {
-                T dot = ac[j];
-                for (int i = j + 1; i < k; ++i) dot += aj[i] * ac[i];
+                T dot = ac[j * rs];
+                for (int i = j + 1; i < k; ++i) dot += aj[i * rs] * ac[i * rs];
                 const T s = tj * dot;
-                ac[j] -= s;
-                for (int i = j + 1; i < k; ++i) ac[i] -= s * aj[i];
+                ac[j * rs] -= s;
+                for (int i = j + 1; i < k; ++i) ac[i * rs] -= s * aj[i * rs];
             }
             // partial norm of rows j+1..k-1 (dlaqp2's downdate with recomputation)
-            const T rjc = ac[j];
+            const T rjc = ac[j * rs];
             T nn = s_nrm[c] - rjc * rjc;
             if (nn <= s_d[c] * T(1.0 / 1024) || nn <= T(0)) {
                 T s = 0;
-                for (int i = j + 1; i < k; ++i) s += ac[i] * ac[i];
+                for (int i = j + 1; i < k; ++i) s += ac[i * rs] * ac[i * rs];
                 nn = s;
                 s_d[c] = s;
             }
@@ -554,16 +569,16 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     // A = I (V_J)
     for (int j = 0; j < k; ++j)
         for (int i = tid; i < k; i += nthr) {
-            const T x = A[(size_t)j * ld + i];
+            const T x = A[ix(i, j)];
             Yg[(size_t)j * k + i] = i > j ? x : T(0);
-            B[(size_t)i * ld + j] = i <= j ? x : T(0);   // B(j, i) = R(i, j)
+            B[ix(j, i)] = i <= j ? x : T(0);   // B(j, i) = R(i, j)
         }
     __syncthreads();
-    for (int j = 0; j < k; ++j)
-        for (int i = tid; i < k; i += nthr) A[(size_t)j * ld + i] = i == j ? T(1) : T(0);
+    for (int o = 0; o < k; ++o)
+        for (int t = tid; t < k; t += nthr) A[(size_t)o * ld + t] = o == t ? T(1) : T(0);
     for (int c = tid; c < k; c += nthr) {
         T s = 0;
-        for (int i = 0; i < k; ++i) s += B[(size_t)c * ld + i] * B[(size_t)c * ld + i];
+        for (int i = 0; i < k; ++i) s += B[ix(i, c)] * B[ix(i, c)];
         s_nrm[c] = s;
         s_d[c] = T(1);
     }
@@ -575,7 +590,6 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
     // number of iterations so that the full-warp shuffles stay converged
     const int n = k + (k & 1);
     const int np = n / 2;
-    const int G = svd_group(maxK);
     const int grp = tid / G, lig = tid % G, ngrp = nthr / G;
     const T tol = T(k > 8 ? k : 8) * Lim<T>::eps;
     bool converged = (k == 1);
@@ -589,10 +603,10 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
                 int p = 0, q = 0;
                 if (pi < np) rr_pair(round, pi, n, p, q);
                 const bool valid = pi < np && p < k && q < k;
-                T *xp = B + (size_t)p * ld, *xq = B + (size_t)q * ld;
+                T *xp = B + ix(0, p), *xq = B + ix(0, q);
                 T dot = 0;
                 if (valid)
-                    for (int i = lig; i < k; i += G) dot += xp[i] * xq[i];
+                    for (int i = lig; i < k; i += G) dot += xp[i * rs] * xq[i * rs];
                 for (int o = G / 2; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
                 T dp = 1, dq = 1, app = 0, aqq = 0, apq = 0;
                 if (valid) {
@@ -613,14 +627,14 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
                     cs = T(1) / sqrt(T(1) + t * t);
                     // true columns p' = c (p - t q), q' = c (q + t p), in B and V_J
                     const T f1 = t * dq / dp, f2 = t * dp / dq;
-                    T *vp = A + (size_t)p * ld, *vq = A + (size_t)q * ld;
+                    T *vp = A + ix(0, p), *vq = A + ix(0, q);
                     for (int i = lig; i < k; i += G) {
-                        const T a = xp[i], b = xq[i];
-                        xp[i] = a - f1 * b;
-                        xq[i] = b + f2 * a;
-                        const T u = vp[i], v = vq[i];
-                        vp[i] = u - f1 * v;
-                        vq[i] = v + f2 * u;
+                        const T a = xp[i * rs], b = xq[i * rs];
+                        xp[i * rs] = a - f1 * b;
+                        xq[i * rs] = b + f2 * a;
+                        const T u = vp[i * rs], v = vq[i * rs];
+                        vp[i * rs] = u - f1 * v;
+                        vq[i * rs] = v + f2 * u;
                     }
                 }
                 T np_ = app - t * apq, nq_ = aqq + t * apq;
@@ -632,8 +646,8 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
                     T sp = 0, sq = 0;
                     if (redo_p || redo_q)
                         for (int i = lig; i < k; i += G) {
-                            sp += xp[i] * xp[i];
-                            sq += xq[i] * xq[i];
+                            sp += xp[i * rs] * xp[i * rs];
+                            sq += xq[i * rs] * xq[i * rs];
                         }
                     for (int o = G / 2; o > 0; o >>= 1) {
                         sp += __shfl_xor_sync(0xffffffffu, sp, o);
@@ -654,19 +668,19 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         }
         // exact norms once per sweep; fold scales before they underflow
         for (int j = tid; j < k; j += nthr) {
-            T *xj = B + (size_t)j * ld;
+            T *xj = B + ix(0, j);
             T dj = s_d[j];
             if (dj < JacobiLim<T>::tiny_scale) {
-                T *vj = A + (size_t)j * ld;
+                T *vj = A + ix(0, j);
                 for (int i = 0; i < k; ++i) {
-                    xj[i] *= dj;
-                    vj[i] *= dj;
+                    xj[i * rs] *= dj;
+                    vj[i * rs] *= dj;
                 }
                 dj = T(1);
                 s_d[j] = dj;
             }
             T s2 = 0;
-            for (int i = 0; i < k; ++i) s2 += xj[i] * xj[i];
+            for (int i = 0; i < k; ++i) s2 += xj[i * rs] * xj[i * rs];
             s_nrm[j] = dj * dj * s2;
         }
         ++sweeps;
@@ -723,18 +737,18 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         // last to first.
         for (int t = tid; t < r; t += nthr) {
             const int j = s_perm[t];
-            T *x = A + (size_t)j * ld;   // each lane owns the column of its own j
+            T *x = A + ix(0, j);   // each lane owns the column of its own j
             const T dj = s_d[j];
-            for (int i = 0; i < k; ++i) x[i] *= dj;
+            for (int i = 0; i < k; ++i) x[i * rs] *= dj;
             for (int h = k - 1; h >= 0; --h) {
                 const T th = s_tau[h];
                 if (th == T(0)) continue;
                 const T *y = Yg + (size_t)h * k;
-                T dot = x[h];
-                for (int i = h + 1; i < k; ++i) dot += y[i] * x[i];
+                T dot = x[h * rs];
+                for (int i = h + 1; i < k; ++i) dot += y[i] * x[i * rs];
                 const T s = th * dot;
-                x[h] -= s;
-                for (int i = h + 1; i < k; ++i) x[i] -= s * y[i];
+                x[h * rs] -= s;
+                for (int i = h + 1; i < k; ++i) x[i * rs] -= s * y[i];
             }
         }
         __syncthreads();   // the reflectors are dead from here on
@@ -744,8 +758,8 @@ __global__ void __launch_bounds__(kThreads) gesvd_kernel(const Desc *__restrict_
         for (int e = tid; e < k * r; e += nthr) {
             const int i = e % k, t = e / k;
             const int j = s_perm[t];
-            Vo[(size_t)t * k + s_pcol[i]] = mul_exp2(s_d[j] * B[(size_t)j * ld + i], sexp);
-            Uo[(size_t)t * k + i] = A[(size_t)j * ld + i];
+            Vo[(size_t)t * k + s_pcol[i]] = mul_exp2(s_d[j] * B[ix(i, j)], sexp);
+            Uo[(size_t)t * k + i] = A[ix(i, j)];
         }
     }
     if (tid == 0) {
@@ -887,7 +901,7 @@ cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
     if (e != cudaSuccess) return e;
     // dynamic shared memory the SVD kernel may take next to its static arrays
     cudaFuncAttributes fa;
-    e = cudaFuncGetAttributes(&fa, gesvd_kernel<T>);
+    e = cudaFuncGetAttributes(&fa, gesvd_kernel<T, true>);
     if (e != cudaSuccess) return e;
     const int dyn_max = optin - (int)fa.sharedSizeBytes;
     int kmax = 0;
@@ -898,7 +912,7 @@ cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
     if (e != cudaSuccess) return e;
     // the attribute is per kernel, not per plan: allow the largest size any
     // plan may launch with, so plans of different k coexist
-    return cudaFuncSetAttribute(gesvd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(gesvd_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 dyn_max);
 }
 
@@ -942,8 +956,13 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
             const bool w_smem = K <= shape.svd_smem_kmax;
             cudaStream_t sb = forked ? shape.side[b] : s;
             if (forked) cudaStreamWaitEvent(sb, shape.fork, 0);
-            gesvd_kernel<T><<<bk.count, svd_threads(K), svd_smem_bytes<T>(K, w_smem), sb>>>(
-                d_desc + bk.start, ws, d_rank, d_status, d_info, shape.svd_smem_kmax, K);
+            const int G = svd_group(K, w_smem), nt = svd_threads(K, w_smem);
+            if (w_smem)
+                gesvd_kernel<T, true><<<bk.count, nt, svd_smem_bytes<T>(K, true), sb>>>(
+                    d_desc + bk.start, ws, d_rank, d_status, d_info, K, G);
+            else
+                gesvd_kernel<T, false><<<bk.count, nt, svd_smem_bytes<T>(K, false), sb>>>(
+                    d_desc + bk.start, ws, d_rank, d_status, d_info, K, G);
             if (forked) {
                 cudaEventRecord(shape.join[b], sb);
                 cudaStreamWaitEvent(s, shape.join[b], 0);
