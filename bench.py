@@ -449,26 +449,38 @@ def e2e_pinned(hc, panel, updates, stream, dev, args):
             "oV": torch.empty(int(out_off[-1]) + 1, dtype=torch.float64).pin_memory()}
     tasks = build_tasks(hc, panel, updates, None, None, out_off, host=host)
     batch = hc.Batch(tasks, flags=hc.STAGE_INPUTS)
-    for _ in range(max(args.warmup, 1)):
-        batch.execute(stream.cuda_stream)
+    batch.execute(stream.cuda_stream)
     ranks, status = batch.results(stream.cuda_stream)
+    # the execute (its host->device copies included) captured once, replayed per step
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(graph, stream=side):
+            batch.execute(side.cuda_stream)
+    stream.wait_stream(side)
+    for _ in range(max(args.warmup, 1)):
+        graph.replay()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     steps = max(args.steps // 2, 1)
     torch.cuda.synchronize(dev)
     e0.record(stream)
     for _ in range(steps):
-        batch.execute(stream.cuda_stream)
+        graph.replay()
     e1.record(stream)
     torch.cuda.synchronize(dev)
     ms = e0.elapsed_time(e1) / steps
     out_bytes = int(sum(2 * nb * int(r) * 8 for r in ranks))
-    staged = batch.staged_bytes
+    staged, zero_copy = batch.staged_bytes, batch.zero_copy_bytes
     batch.close()
-    return {"value": n / (ms / 1e3), "unit": "updates/s", "h2d_bytes_per_step": int(staged),
+    return {"value": n / (ms / 1e3), "unit": "updates/s", "h2d_bytes_per_step": int(staged + zero_copy),
             "d2h_bytes_per_step": out_bytes, "ms_per_step": ms,
-            "how": "plan over pinned host factors (HCORE_GPU_STAGE_INPUTS): unique input tiles "
-                   "copied host->device each step, new factors written to host memory by the "
-                   "rebuild kernel over NVLink-C2C",
+            "h2d_copied_bytes": int(staged), "h2d_read_in_place_bytes": int(zero_copy),
+            "how": "plan over pinned host factors (HCORE_GPU_STAGE_INPUTS), its execute captured "
+                   "in a CUDA graph and replayed per step: panel tiles shared by many updates "
+                   "copied host->device each step, each update's own C tile read in place by "
+                   "the stack kernel over NVLink-C2C, new factors written to host memory by the "
+                   "rebuild kernel",
             "all_ok": bool((status == 0).all())}
 
 

@@ -116,6 +116,8 @@ def lib() -> C.CDLL:
     L.hcore_gpu_plan_workspace_bytes.restype = C.c_size_t
     L.hcore_gpu_plan_staged_bytes.argtypes = [vp]
     L.hcore_gpu_plan_staged_bytes.restype = C.c_size_t
+    L.hcore_gpu_plan_zero_copy_bytes.argtypes = [vp]
+    L.hcore_gpu_plan_zero_copy_bytes.restype = C.c_size_t
     L.hcore_gpu_dgemm_batched.argtypes = [C.c_int, C.POINTER(LrTask), _ip, _ip, vp]
     L.hcore_gpu_sgemm_batched.argtypes = [C.c_int, C.POINTER(LrTask), _ip, _ip, vp]
     L.hcore_gpu_dense_batched.argtypes = [C.c_int, C.POINTER(DenseTask), vp]
@@ -287,6 +289,11 @@ class Batch:
     @property
     def device_status_ptr(self) -> int:
         return lib().hcore_gpu_plan_device_status(self._plan)
+
+    @property
+    def zero_copy_bytes(self) -> int:
+        """Pinned host input bytes read in place (not staged) by every execute."""
+        return int(lib().hcore_gpu_plan_zero_copy_bytes(self._plan))
 
     @property
     def staged_bytes(self) -> int:

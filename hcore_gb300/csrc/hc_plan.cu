@@ -223,31 +223,98 @@ struct hcore_gpu_plan_s {
     std::vector<Segment> segs;
     char *d_mirror = nullptr;
     size_t staged_bytes = 0;
+    size_t zero_copy_bytes = 0;   // pinned host inputs read in place by the kernels
+    // some task's output overlaps another task's input: the stream groups
+    // finish every stack phase before any later phase starts
+    bool cross_alias = false;
+    std::vector<cudaEvent_t> stacked;   // per group, with cross_alias
 };
 
 namespace {
-bool is_host_memory(const void *p) {
-    cudaPointerAttributes at;
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-        cudaGetLastError();
-        return true;  // unknown to CUDA: ordinary host memory
+
+// Does an output range of one task overlap an input range of another?  (A
+// task's own C may be updated in place: its inputs are read in the stack
+// phase, before its rebuild writes.)  Ranges are conservative: every output
+// of M x max(c, a + c) columns.
+bool outputs_alias_other_inputs(int n, const hcore_lr_task *tasks, size_t esz) {
+    struct Rng {
+        const char *lo, *hi;
+        int task;
+        bool out;
+    };
+    std::vector<Rng> rr;
+    auto add = [&](const void *ptr, int rows, int ld, int ncol, int task, bool out) {
+        if (!ptr || ncol <= 0 || rows <= 0) return;
+        const char *lo = (const char *)ptr;
+        rr.push_back({lo, lo + ((size_t)(ncol - 1) * ld + rows) * esz, task, out});
+    };
+    for (int q = 0; q < n; ++q) {
+        const hcore_lr_task &t = tasks[q];
+        if (t.a > 0) {
+            add(t.AU, t.M, t.lda, t.a, q, false);
+            add(t.AV, t.M, t.lda, t.a, q, false);
+        }
+        if (t.Bdense) add(t.Bdense, t.M, t.ldb, t.M, q, false);
+        else if (t.b > 0) {
+            add(t.BU, t.M, t.ldb, t.b, q, false);
+            add(t.BV, t.M, t.ldb, t.b, q, false);
+        }
+        if (t.c > 0) {
+            add(t.CU, t.M, t.ldc, t.c, q, false);
+            add(t.CV, t.M, t.ldc, t.c, q, false);
+        }
+        const int ncol = std::max(t.c, t.a + t.c);
+        add(t.CUo, t.M, t.ldco, ncol, q, true);
+        add(t.CVo, t.M, t.ldco, ncol, q, true);
     }
-    return at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeUnregistered;
+    std::sort(rr.begin(), rr.end(), [](const Rng &x, const Rng &y) { return x.lo < y.lo; });
+    // sweep: every range against the ranges still open at its start
+    std::vector<const Rng *> open;
+    for (const Rng &r : rr) {
+        size_t w = 0;
+        for (const Rng *o : open)
+            if (o->hi > r.lo) open[w++] = o;
+        open.resize(w);
+        for (const Rng *o : open)
+            if (o->task != r.task && (o->out != r.out || (o->out && r.out))) return true;
+        open.push_back(&r);
+    }
+    return false;
 }
 
-// Replace every host input pointer of the tasks by its address in a device
-// mirror of the merged host ranges.  Returns false on allocation failure.
+// Host inputs of a plan with HCORE_GPU_STAGE_INPUTS.  A host range that
+// several updates read (a panel tile), or that lies in pageable memory, is
+// mirrored on the device and refreshed by one copy per merged segment at the
+// start of every execute; the tasks' pointers are replaced by their mirror
+// addresses.  A pinned range read by one update only (its own C tile) is
+// left in place: the stack kernel reads it over the host link once, as a
+// copy would, but while other stream groups compute.  Returns false on
+// allocation failure.
 bool stage_inputs(hcore_gpu_plan p, std::vector<hcore_lr_task> &tt, size_t esz) {
     struct Rng {
         const char *lo, *hi;
+        int task;
+        bool pinned;
     };
     std::vector<Rng> rr;
+    int cur = 0;
     auto add = [&](const void *ptr, int rows, int ld, int ncol) {
-        if (!ptr || ncol <= 0 || rows <= 0 || !is_host_memory(ptr)) return;
+        if (!ptr || ncol <= 0 || rows <= 0) return;
+        cudaPointerAttributes at;
+        bool pinned = false;
+        if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+            cudaGetLastError();                       // unknown to CUDA: pageable host memory
+        } else if (at.type == cudaMemoryTypeHost) {
+            pinned = at.devicePointer != nullptr;
+        } else if (at.type != cudaMemoryTypeUnregistered) {
+            return;                                   // device or managed memory: used in place
+        }
         const char *lo = (const char *)ptr;
-        rr.push_back({lo, lo + ((size_t)(ncol - 1) * ld + rows) * esz});
+        rr.push_back({lo, lo + ((size_t)(ncol - 1) * ld + rows) * esz, cur, pinned});
     };
-    for (const hcore_lr_task &t : tt) {
+    for (size_t q = 0; q < tt.size(); ++q) {
+        const hcore_lr_task &t = tt[q];
+        cur = (int)q;
         if (t.a > 0) {
             add(t.AU, t.M, t.lda, t.a);
             add(t.AV, t.M, t.lda, t.a);
@@ -262,29 +329,56 @@ bool stage_inputs(hcore_gpu_plan p, std::vector<hcore_lr_task> &tt, size_t esz) 
             add(t.CV, t.M, t.ldc, t.c);
         }
     }
+    p->staged_bytes = 0;
+    p->zero_copy_bytes = 0;
     if (rr.empty()) return true;
     std::sort(rr.begin(), rr.end(), [](const Rng &x, const Rng &y) { return x.lo < y.lo; });
-    std::vector<Rng> merged;
+    // clusters of overlapping ranges: staged when read by two or more tasks
+    // or not pinned; then adjacent staged clusters merge into segments
+    struct Cluster {
+        const char *lo, *hi;
+        int task;
+        bool multi, pinned;
+    };
+    std::vector<Cluster> cl;
     for (const Rng &r : rr) {
-        if (!merged.empty() && r.lo <= merged.back().hi)
-            merged.back().hi = std::max(merged.back().hi, r.hi);
+        if (!cl.empty() && r.lo < cl.back().hi) {
+            Cluster &c = cl.back();
+            c.hi = std::max(c.hi, r.hi);
+            c.multi = c.multi || r.task != c.task;
+            c.pinned = c.pinned && r.pinned;
+        } else {
+            cl.push_back({r.lo, r.hi, r.task, false, r.pinned});
+        }
+    }
+    struct Span {
+        const char *lo, *hi;
+    };
+    std::vector<Span> merged;
+    for (const Cluster &c : cl) {
+        if (!c.multi && c.pinned) {
+            p->zero_copy_bytes += (size_t)(c.hi - c.lo);
+            continue;
+        }
+        if (!merged.empty() && c.lo <= merged.back().hi)
+            merged.back().hi = std::max(merged.back().hi, c.hi);
         else
-            merged.push_back(r);
+            merged.push_back({c.lo, c.hi});
     }
     size_t off = 0;
-    for (const Rng &m : merged) {
+    for (const Span &m : merged) {
         p->segs.push_back({m.lo, (size_t)(m.hi - m.lo), off});
         off += ((size_t)(m.hi - m.lo) + 255) & ~(size_t)255;
     }
-    p->staged_bytes = 0;
     for (const auto &sg : p->segs) p->staged_bytes += sg.bytes;
+    if (p->segs.empty()) return true;
     if (cudaMalloc(&p->d_mirror, off) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
     // translate: the segment holding each host pointer (binary search)
     auto tr = [&](const void *ptr) -> const void * {
-        if (!ptr || !is_host_memory(ptr)) return ptr;
+        if (!ptr) return ptr;
         const char *c = (const char *)ptr;
         size_t lo = 0, hi = p->segs.size();
         while (hi - lo > 1) {
@@ -293,6 +387,7 @@ bool stage_inputs(hcore_gpu_plan p, std::vector<hcore_lr_task> &tt, size_t esz) 
             else hi = mid;
         }
         const auto &sg = p->segs[lo];
+        if (c < sg.host || c >= sg.host + sg.bytes) return ptr;   // not staged: read in place
         return p->d_mirror + sg.off + (size_t)(c - sg.host);
     };
     for (hcore_lr_task &t : tt) {
@@ -331,6 +426,8 @@ static void plan_free(hcore_gpu_plan p) {
         if (g.shape.fork) cudaEventDestroy(g.shape.fork);
     }
     if (p->gfork) cudaEventDestroy(p->gfork);
+    for (cudaEvent_t ev : p->stacked)
+        if (ev) cudaEventDestroy(ev);
     cudaFree(p->d_desc);
     cudaFree(p->d_rank);
     cudaFree(p->d_status);
@@ -366,6 +463,8 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
         }
         tasks = staged.data();
     }
+    p->cross_alias = n > 1 && outputs_alias_other_inputs(
+                                  n, tasks, precision == HCORE_GPU_F64 ? sizeof(double) : sizeof(float));
     build_descs(n, tasks, flags, true, descs, ws_elems, p->maxM, p->maxK, nullptr);
     // stream groups (HCORE_GPU_STREAMS, default 4): deal the k-sorted
     // descriptors round-robin so every group gets the same mix of sizes
@@ -400,6 +499,11 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
                          cudaEventCreateWithFlags(&g.shape.join[b], cudaEventDisableTiming) ==
                              cudaSuccess;
             }
+        }
+        if (ok && p->cross_alias) {
+            p->stacked.assign(p->groups.size(), nullptr);
+            for (auto &ev : p->stacked)
+                ok = ok && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
         }
         if (!ok) {
             set_error("hcore_gpu_plan_create: cannot create group streams");
@@ -492,21 +596,45 @@ extern "C" int hcore_gpu_plan_execute_phases(hcore_gpu_plan p, void *stream, uns
                 return HCORE_GPU_ECUDA;
             }
         }
-    auto launch = [&](const Desc *dd, int cnt, const LaunchShape &sh, cudaStream_t st) {
+    auto launch = [&](const Desc *dd, int cnt, const LaunchShape &sh, cudaStream_t st,
+                      unsigned ph) {
         return p->prec == HCORE_GPU_F64
                    ? launch_recompress<double>(dd, cnt, (double *)p->d_ws, p->d_rank, p->d_status,
-                                               p->d_info, sh, st, phases & kPhaseAll)
+                                               p->d_info, sh, st, ph & kPhaseAll)
                    : launch_recompress<float>(dd, cnt, (float *)p->d_ws, p->d_rank, p->d_status,
-                                              p->d_info, sh, st, phases & kPhaseAll);
+                                              p->d_info, sh, st, ph & kPhaseAll);
     };
     if (p->groups.empty()) {
-        e = launch(p->d_desc, p->n, p->shape, s);
+        e = launch(p->d_desc, p->n, p->shape, s, phases);
+    } else if (p->cross_alias) {
+        // an output of one task overlaps another task's input: every group's
+        // stack phase (which reads all inputs) completes before any group
+        // goes on to the phases that write outputs
+        const size_t ng = p->groups.size();
+        e = cudaEventRecord(p->gfork, s);
+        for (size_t gi = 0; gi < ng && e == cudaSuccess; ++gi) {
+            auto &g = p->groups[gi];
+            e = cudaStreamWaitEvent(g.stream, p->gfork, 0);
+            if (e == cudaSuccess && g.count > 0)
+                e = launch(p->d_desc + g.start, g.count, g.shape, g.stream, phases & kPhaseStack);
+            if (e == cudaSuccess) e = cudaEventRecord(p->stacked[gi], g.stream);
+        }
+        for (size_t gi = 0; gi < ng && e == cudaSuccess; ++gi) {
+            auto &g = p->groups[gi];
+            for (size_t o = 0; o < ng && e == cudaSuccess; ++o)
+                if (o != gi) e = cudaStreamWaitEvent(g.stream, p->stacked[o], 0);
+            if (e == cudaSuccess && g.count > 0)
+                e = launch(p->d_desc + g.start, g.count, g.shape, g.stream, phases & ~kPhaseStack);
+            if (e == cudaSuccess) e = cudaEventRecord(g.done, g.stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g.done, 0);
+        }
     } else {
         e = cudaEventRecord(p->gfork, s);
         for (auto &g : p->groups) {
             if (e != cudaSuccess) break;
             e = cudaStreamWaitEvent(g.stream, p->gfork, 0);
-            if (e == cudaSuccess && g.count > 0) e = launch(p->d_desc + g.start, g.count, g.shape, g.stream);
+            if (e == cudaSuccess && g.count > 0)
+                e = launch(p->d_desc + g.start, g.count, g.shape, g.stream, phases);
             if (e == cudaSuccess) e = cudaEventRecord(g.done, g.stream);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g.done, 0);
         }
@@ -629,6 +757,9 @@ extern "C" int hcore_gpu_plan_launches(hcore_gpu_plan p) {
 
 extern "C" size_t hcore_gpu_plan_workspace_bytes(hcore_gpu_plan p) { return p ? p->ws_bytes : 0; }
 extern "C" size_t hcore_gpu_plan_staged_bytes(hcore_gpu_plan p) { return p ? p->staged_bytes : 0; }
+extern "C" size_t hcore_gpu_plan_zero_copy_bytes(hcore_gpu_plan p) {
+    return p ? p->zero_copy_bytes : 0;
+}
 
 extern "C" int hcore_gpu_plan_results(hcore_gpu_plan p, int *ranks, int *status, void *stream) {
     if (!p) {

@@ -12,8 +12,9 @@
  *
  * Pointers in a task may be device memory or pinned (page-locked) host
  * memory; both are read and written directly by the kernels.  Outputs may
- * alias the task's own C inputs (in-place update, as in the reference): every
- * input of the whole batch is consumed before any output is written.
+ * alias inputs (a task's own C, updated in place as in the reference, or
+ * another task's inputs): the results are those of reading every input of
+ * the batch before writing any output.
  *
  * Usage without a GPU-side rank array in the caller's hands:
  *     hcore_gpu_dgemm_batched(n, tasks, ranks, status, stream)   (synchronous)
@@ -64,6 +65,9 @@ extern "C" {
  * capturable.  Outputs in pinned host memory are written in place by the
  * rebuild kernel. */
 #define HCORE_GPU_STAGE_INPUTS 0x2
+/* (With HCORE_GPU_STAGE_INPUTS, a pinned host range that only one update
+ * reads, such as its own C tile, is not copied: the stack kernel reads it in
+ * place once, overlapped with the other stream groups' work.) */
 /* FP64 plans only: the factor products F = AV^T BV, G = BU F^T and the Q.U
  * rebuild run in FP32 with FP32 accumulation (FP64 storage), the QRs, the SVD
  * and the truncation stay FP64.  Meant for loose accuracies (1e-4 .. 1e-6);
@@ -134,6 +138,9 @@ int hcore_gpu_plan_launches(hcore_gpu_plan plan);
 size_t hcore_gpu_plan_workspace_bytes(hcore_gpu_plan plan);
 /* bytes copied host->device by every execute (HCORE_GPU_STAGE_INPUTS) */
 size_t hcore_gpu_plan_staged_bytes(hcore_gpu_plan plan);
+/* bytes of pinned host inputs that one update each reads in place over the
+ * host link during every execute (HCORE_GPU_STAGE_INPUTS leaves them there) */
+size_t hcore_gpu_plan_zero_copy_bytes(hcore_gpu_plan plan);
 int hcore_gpu_plan_destroy(hcore_gpu_plan plan);
 
 /* one-shot synchronous batch: create, execute, results, destroy */

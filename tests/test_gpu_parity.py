@@ -299,12 +299,14 @@ def test_dgemm_dense_dropin(hc):
 @pytest.mark.parametrize("pinned", [True, False])
 def test_staged_host_inputs_equal_device_plan(hc, pinned):
     """HCORE_GPU_STAGE_INPUTS: host factors (pinned or pageable) in one arena,
-    tiles shared between updates; results identical to the device plan's."""
+    tiles shared between updates (copied once per execute) and one tile read
+    by a single update (read in place when pinned, copied when pageable);
+    results identical to the device plan's."""
     import torch
     from hcore_gb300 import devmem
 
     rng = np.random.default_rng(77)
-    M, ranks = 128, [9, 12, 7, 15, 10]
+    M, ranks = 128, [9, 12, 7, 15, 10, 11]
     facs = [O.graded_lowrank(rng, M, r) for r in ranks]
     arenaU = np.concatenate([u.T.reshape(-1) for u, _ in facs])
     arenaV = np.concatenate([v.T.reshape(-1) for _, v in facs])
@@ -313,7 +315,7 @@ def test_staged_host_inputs_equal_device_plan(hc, pinned):
     if pinned:
         hU, hV = hU.pin_memory(), hV.pin_memory()
     dU, dV = hU.cuda(), hV.cuda()
-    pairs = [(0, 1, 2), (0, 3, 4), (1, 3, 2), (4, 0, 1)]   # (A, B, C) slots; tiles shared
+    pairs = [(0, 1, 2), (0, 3, 4), (1, 3, 2), (4, 0, 1), (3, 1, 5)]   # (A, B, C) slots; 5 private
     kmax = max(ranks[x] + ranks[z] for x, _, z in pairs)
     outs = {}
     for mode in ("device", "staged"):
@@ -336,7 +338,9 @@ def test_staged_host_inputs_equal_device_plan(hc, pinned):
         rk, st = b.results()
         assert (st == 0).all()
         if mode == "staged":
-            assert b.staged_bytes == (arenaU.nbytes + arenaV.nbytes)   # each tile once
+            private = 2 * M * ranks[5] * 8
+            assert b.staged_bytes + b.zero_copy_bytes == arenaU.nbytes + arenaV.nbytes
+            assert b.zero_copy_bytes == (private if pinned else 0)
         outs[mode] = (rk.copy(), oU.cpu().numpy(), oV.cpu().numpy())
         b.close()
     assert np.array_equal(outs["device"][0], outs["staged"][0])
@@ -452,3 +456,47 @@ def test_large_rank_updates_vs_oracle(hc, port, M, a, b, c, maxrk, acc):
     assert ranks[0] == ref["rank"]
     CUo, CVo = outs[0]
     assert O.rel_fro(CUo @ CVo.T, ref["CU"] @ ref["CV"].T) < FP64_TOL
+
+
+def test_output_aliasing_another_tasks_input(hc, port):
+    """Task 0 writes its result over the factors that task 1 reads as its A:
+    task 1 must still see the original A (every input is read before any
+    output is written), whichever stream group each task lands in."""
+    import torch
+    from hcore_gb300 import devmem
+
+    rng = np.random.default_rng(91)
+    M, a, b, c = 128, 10, 8, 12
+    cases = [_batch_case(rng, M, a, b, c, decades=8.0) for _ in range(2)]
+    AU1, AV1 = cases[1][0], cases[1][1]
+    # task 1's A lives in a buffer wide enough to receive task 0's output
+    width = a + c
+    shared_U = devmem.to_device(AU1, ncols=width)
+    shared_V = devmem.to_device(AV1, ncols=width)
+    keep, tasks = [], []
+    for u, (AU, AV, BU, BV, CU, CV) in enumerate(cases):
+        d = [devmem.to_device(x) for x in (AU, AV, BU, BV, CU, CV)]
+        keep.append(d)
+        if u == 1:
+            d[0], d[1] = shared_U, shared_V
+        oU, oV = (shared_U, shared_V) if u == 0 else (torch.zeros((width, M), dtype=torch.float64,
+                                                                   device="cuda"),) * 2
+        if u == 1:
+            oV = torch.zeros_like(oU)
+        keep.append((oU, oV))
+        tasks.append(hc.LrTask(M=M, a=a, b=b, c=c, rk=0, maxrk=width, ld_newv=0, storage_maxrank=0,
+                               alpha=-1.0, beta=1.0, acc=1e-8, AU=d[0].data_ptr(), AV=d[1].data_ptr(),
+                               lda=M, BU=d[2].data_ptr(), BV=d[3].data_ptr(), ldb=M, Bdense=None,
+                               CU=d[4].data_ptr(), CV=d[5].data_ptr(), ldc=M, CUo=oU.data_ptr(),
+                               CVo=oV.data_ptr(), ldco=M))
+    batch = hc.Batch(tasks)
+    batch.execute()
+    ranks, status = batch.results()
+    assert (status == 0).all()
+    AU, AV, BU, BV, CU, CV = cases[1]
+    ref = port.gemm(M, -1.0, AU, AV, a, BU, BV, b, 1.0, CU, CV, c, maxrk=width, acc=1e-8)
+    oU1, oV1 = keep[3]
+    r1 = int(ranks[1])
+    assert r1 == ref["rank"]
+    P = devmem.to_host(oU1, r1) @ devmem.to_host(oV1, r1).T
+    assert O.rel_fro(P, ref["CU"] @ ref["CV"].T) < FP64_TOL
