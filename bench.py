@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "TLR-GEMM updates/s batched vs plain per-tile on 1 GB300 at rel err <= acc"
 # DRAM bytes (read + write) per algorithmic byte of each phase's kernel, from
-# one ncu capture of the 300-update case (profiles/recompression_panel_ncu.md
+# one ncu capture of 300 updates in one launch (profiles/recompression_panel_ncu.md
 # section 3); the full launch's traffic is this ratio times its own
 # algorithmic bytes
 DRAM_PER_ALG_BYTE = {"stack": 0.46, "qr": 4.44, "svd": None, "rebuild": 0.97}
