@@ -24,16 +24,18 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "TLR-GEMM updates/s batched vs plain per-tile on 1 GB300 at rel err <= acc"
-# DRAM bytes (read + write) per algorithmic byte of each phase's kernel, from
-# one ncu capture of 300 updates in one launch (profiles/recompression_panel_ncu.md
-# section 3); the full launch's traffic is this ratio times its own
-# algorithmic bytes
+# DRAM bytes (read + write) per algorithmic byte of each phase's kernel:
+# dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of 300 updates
+# in a single launch (a working set beyond L2, as in each launch of this
+# workload), divided by that launch's algorithmic bytes.  The full phase's
+# traffic is this ratio times its own algorithmic bytes.
 DRAM_PER_ALG_BYTE = {"stack": 0.46, "qr": 4.44, "svd": None, "rebuild": 0.97}
 WORKLOAD = dict(workload="TLR Cholesky panel-0 Schur updates (HCORE_dgemm recompression)",
                 points=65536, dim=2, nb=1024, tiles_per_dim=64, kernel="exp(-|x-y|^2/0.01)",
@@ -126,7 +128,9 @@ class Clocks:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+        # the raw samples go to $HCORE_BENCH_OUT (default: the temp folder)
+        out = os.environ.get("HCORE_BENCH_OUT") or tempfile.gettempdir()
+        self.path = os.path.join(out, f"clocks_rank{index}.csv")
 
     def start(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
