@@ -285,7 +285,7 @@ def run_gb300(args):
               "data": "synthetic (seeded points, covariance tiles compressed on the host cores)",
               "config": dict(WORKLOAD, updates_per_step=int(total_updates), parallelism=f"dp{world}",
                              l2="inputs+outputs+workspace larger than L2 (no flush needed)",
-                             graph=f"{batch.launches} kernel launches (4 stream groups: stack, QR, "
+                             graph=f"{batch.launches} kernel launches (16 stream groups: stack, QR, "
                                    f"one SVD launch per rank bucket, rebuild) captured in one CUDA graph"),
               "gpu_launches": batch.launches * args.steps,
               "gflops_model": flops_model / (ms / 1e3) / 1e9,

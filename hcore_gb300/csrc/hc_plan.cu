@@ -466,11 +466,11 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
     p->cross_alias = n > 1 && outputs_alias_other_inputs(
                                   n, tasks, precision == HCORE_GPU_F64 ? sizeof(double) : sizeof(float));
     build_descs(n, tasks, flags, true, descs, ws_elems, p->maxM, p->maxK, nullptr);
-    // stream groups (HCORE_GPU_STREAMS, default 4): deal the k-sorted
+    // stream groups (HCORE_GPU_STREAMS, default 16): deal the k-sorted
     // descriptors round-robin so every group gets the same mix of sizes
-    int ngroups = 4;
+    int ngroups = 16;
     if (const char *env = getenv("HCORE_GPU_STREAMS")) ngroups = atoi(env);
-    ngroups = std::max(1, std::min(ngroups, std::min(n > 0 ? n : 1, 16)));
+    ngroups = std::max(1, std::min(ngroups, std::min(n > 0 ? n : 1, 64)));
     if (ngroups > 1) {
         std::vector<Desc> dealt;
         dealt.reserve(n);
