@@ -331,9 +331,9 @@ def run_gb300(args):
     result["roofline"] = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak,
                           "unit": "TFLOP/s", "frac": achieved / peak,
                           "traffic": (ratio * alg_bytes[dom]) if ratio else None,
-                          "traffic_basis": "ncu DRAM bytes per algorithmic byte of this kernel on "
-                                           "the 300-update case, times this launch's algorithmic "
-                                           f"bytes ({alg_bytes[dom]:.3e})",
+                          "traffic_basis": "ncu DRAM bytes per algorithmic byte of this kernel in "
+                                           "one 300-update launch (working set beyond L2), times "
+                                           f"this phase's algorithmic bytes ({alg_bytes[dom]:.3e})",
                           "peak_source": "fp64 DMMA m16n8k16 issue-rate probe timed live "
                                          "(MEASURED_PEAKS.json has no FP64 figure)",
                           "flops_basis": "reference flop model (flop_counts.c) of that phase"}
