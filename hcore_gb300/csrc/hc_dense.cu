@@ -112,10 +112,12 @@ __global__ void __launch_bounds__(256) dense_tile_kernel(const hcore_dense_task 
         const DenseWork w = work[group_tasks[gi]];
         if (!(w.syrk && strictly_upper)) {
             for (int k0 = 0; k0 < w.kk; k0 += TK) {
+                // the task's coefficient is folded into P as it is staged
+                // (once per element, not once per use)
                 for (int e = threadIdx.x; e < TK * TB; e += 256) {
                     const int kk = e / TB, r = e % TB;
                     const int kg = k0 + kk;
-                    sP[kk][r] = (kg < w.kk && row0 + r < M) ? w.P[(size_t)kg * w.ldp + row0 + r] : 0.0;
+                    sP[kk][r] = (kg < w.kk && row0 + r < M) ? w.coef * w.P[(size_t)kg * w.ldp + row0 + r] : 0.0;
                     sQ[kk][r] = (kg < w.kk && col0 + r < M) ? w.Q[(size_t)kg * w.ldq + col0 + r] : 0.0;
                 }
                 __syncthreads();
@@ -123,7 +125,7 @@ __global__ void __launch_bounds__(256) dense_tile_kernel(const hcore_dense_task 
                 for (int kk = 0; kk < TK; ++kk) {
                     double pv[4], qv[4];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) pv[u] = w.coef * sP[kk][tx + 16 * u];
+                    for (int u = 0; u < 4; ++u) pv[u] = sP[kk][tx + 16 * u];
 #pragma unroll
                     for (int v = 0; v < 4; ++v) qv[v] = sQ[kk][ty + 16 * v];
 #pragma unroll
