@@ -593,9 +593,10 @@ def run_reference(args):
             "config": dict(WORKLOAD, updates_per_step=len(updates), parallelism="cpu"),
             "cpu_baseline": {"value": v, "unit": "updates/s", "cores": cores, "kind": kind,
                              "sample": f"bounded sample per step (~{per_step:.0f} s) of the "
-                                       f"{len(updates)}-update panel; the reference compiled "
-                                       "from source is not on this machine, so the oracle's "
-                                       "LAPACK restatement of it runs"},
+                                       f"{len(updates)}-update panel, all host cores; the "
+                                       "oracle's restatement of the reference (the same LAPACK "
+                                       "calls in the same order) runs, since the reference "
+                                       "library is built only where its sources are"},
             "e2e": {"value": v, "unit": "updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
