@@ -231,7 +231,12 @@ def run_gb300(args):
     out_V = torch.empty_like(out_U)
     tasks = build_tasks(hc, panel, updates, out_U, out_V, out_off)
     stream = torch.cuda.current_stream(dev)
-    batch = hc.Batch(tasks)
+    # the plan's launch shapes, picked by the library's autotuner on this batch
+    # (set-up, outside the timed region)
+    t0 = time.time()
+    tuning, tuned_ms = hc.autotune(tasks, reps=3, stream=stream.cuda_stream)
+    tune_s = time.time() - t0
+    batch = hc.Batch(tasks, tuning=tuning)
     batch.execute(stream.cuda_stream)
     ranks, status = batch.results(stream.cuda_stream)
     if (status != 0).any():
@@ -285,9 +290,12 @@ def run_gb300(args):
               "data": "synthetic (seeded points, covariance tiles compressed on the host cores)",
               "config": dict(WORKLOAD, updates_per_step=int(total_updates), parallelism=f"dp{world}",
                              l2="inputs+outputs+workspace larger than L2 (no flush needed)",
-                             graph=f"{batch.launches} kernel launches (16 stream groups: stack, QR, "
-                                   f"one SVD launch per rank bucket, rebuild) captured in one CUDA graph"),
+                             graph=f"{batch.launches} kernel launches ({tuning.stream_groups} stream "
+                                   f"groups: stack, QR, one SVD launch per rank bucket, rebuild) "
+                                   f"captured in one CUDA graph"),
               "gpu_launches": batch.launches * args.steps,
+              "tuning": dict(tuning.as_dict(), autotune_ms_per_execute=tuned_ms,
+                             autotune_s=round(tune_s, 2)),
               "gflops_model": flops_model / (ms / 1e3) / 1e9,
               "clocks": clk}
     if rank != 0:
@@ -363,7 +371,7 @@ def run_gb300(args):
 
     # ---- e2e: the same plan over pinned host buffers (zero-copy C2C) ----
     if not args.no_e2e:
-        result["e2e"] = e2e_pinned(hc, panel, updates, stream, dev, args)
+        result["e2e"] = e2e_pinned(hc, panel, updates, stream, dev, args, tuning=tuning)
     batch.close()
 
     # ---- CPU baseline: the reference algorithm on the host cores ----
@@ -435,7 +443,7 @@ def accuracy_sample(panel, updates, ranks, out_U, out_V, out_off, count, acc=Non
                     "tiles whose entries are themselves near acc; the oracle shows the same"}
 
 
-def e2e_pinned(hc, panel, updates, stream, dev, args):
+def e2e_pinned(hc, panel, updates, stream, dev, args, tuning=None):
     """The same workload through the C ABI with every factor in pinned HOST
     memory: each execute copies the unique input tiles host->device (the
     plan's HCORE_GPU_STAGE_INPUTS segments: a panel tile shared by many
@@ -452,7 +460,7 @@ def e2e_pinned(hc, panel, updates, stream, dev, args):
             "oU": torch.empty(int(out_off[-1]) + 1, dtype=torch.float64).pin_memory(),
             "oV": torch.empty(int(out_off[-1]) + 1, dtype=torch.float64).pin_memory()}
     tasks = build_tasks(hc, panel, updates, None, None, out_off, host=host)
-    batch = hc.Batch(tasks, flags=hc.STAGE_INPUTS)
+    batch = hc.Batch(tasks, flags=hc.STAGE_INPUTS, tuning=tuning)
     batch.execute(stream.cuda_stream)
     ranks, status = batch.results(stream.cuda_stream)
     # the execute (its host->device copies included) captured once, replayed per step

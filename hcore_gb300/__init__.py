@@ -28,7 +28,8 @@ import numpy as np
 from .build import LIB as _LIB_PATH
 
 __all__ = ["lib", "LrTask", "DenseTask", "Batch", "DensePlan", "hcore_dgemm", "hcore_sgemm", "hcore_dgemm_fast",
-           "dense_batched", "HcoreError", "STATUS", "FlopCounter", "RankMLP"]
+           "dense_batched", "HcoreError", "STATUS", "FlopCounter", "RankMLP", "Tuning",
+           "make_tuning", "autotune"]
 
 F64, F32 = 0, 1
 FAST_RULES = 0x1
@@ -65,6 +66,16 @@ class DenseTask(C.Structure):
                 ("ldcd", C.c_int)]
 
 
+class Tuning(C.Structure):
+    """Mirror of hcore_gpu_tuning (include/hcore_gb300.h)."""
+
+    _fields_ = [("stream_groups", C.c_int), ("svd_lanes", C.c_int * 3), ("bucket_width", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {"stream_groups": self.stream_groups, "svd_lanes": list(self.svd_lanes),
+                "bucket_width": self.bucket_width}
+
+
 class FlopCounter(C.Structure):
     """Mirror of flop_counter (include/flop_util_structs.h)."""
 
@@ -98,6 +109,11 @@ def lib() -> C.CDLL:
     vp = C.c_void_p
     L.hcore_gpu_plan_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.POINTER(LrTask), C.c_uint]
     L.hcore_gpu_plan_execute.argtypes = [vp, vp]
+    L.hcore_gpu_plan_create_tuned.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.POINTER(LrTask),
+                                              C.c_uint, C.POINTER(Tuning)]
+    L.hcore_gpu_tuning_default.argtypes = [C.POINTER(Tuning)]
+    L.hcore_gpu_autotune.argtypes = [C.c_int, C.c_int, C.POINTER(LrTask), C.c_uint, C.c_int, vp,
+                                     C.POINTER(Tuning), C.POINTER(C.c_double)]
     L.hcore_gpu_plan_results.argtypes = [vp, _ip, _ip, vp]
     L.hcore_gpu_plan_sigma.argtypes = [vp, C.c_int, _dp, _ip, vp]
     L.hcore_gpu_plan_destroy.argtypes = [vp]
@@ -230,13 +246,19 @@ class Batch:
     captured in a CUDA graph.
     """
 
-    def __init__(self, tasks, precision=F64, flags=0):
+    def __init__(self, tasks, precision=F64, flags=0, tuning=None):
         L = lib()
         self.n = len(tasks)
         self._tasks = (LrTask * max(self.n, 1))(*tasks)
         self._plan = C.c_void_p()
-        _check(L.hcore_gpu_plan_create(C.byref(self._plan), precision, self.n, self._tasks, flags),
-               "hcore_gpu_plan_create")
+        if tuning is None:
+            _check(L.hcore_gpu_plan_create(C.byref(self._plan), precision, self.n, self._tasks,
+                                           flags), "hcore_gpu_plan_create")
+        else:
+            t = tuning if isinstance(tuning, Tuning) else make_tuning(**tuning)
+            _check(L.hcore_gpu_plan_create_tuned(C.byref(self._plan), precision, self.n,
+                                                 self._tasks, flags, C.byref(t)),
+                   "hcore_gpu_plan_create_tuned")
 
     def execute(self, stream=None):
         _check(lib().hcore_gpu_plan_execute(self._plan, stream or None), "hcore_gpu_plan_execute")
@@ -407,3 +429,29 @@ class RankMLP:
             self.close()
         except Exception:
             pass
+
+
+def make_tuning(stream_groups=None, svd_lanes=None, bucket_width=None) -> Tuning:
+    """A Tuning from the library default with the given fields replaced."""
+    t = Tuning()
+    _check(lib().hcore_gpu_tuning_default(C.byref(t)), "hcore_gpu_tuning_default")
+    if stream_groups is not None:
+        t.stream_groups = int(stream_groups)
+    if svd_lanes is not None:
+        for q in range(3):
+            t.svd_lanes[q] = int(svd_lanes[q])
+    if bucket_width is not None:
+        t.bucket_width = int(bucket_width)
+    return t
+
+
+def autotune(tasks, precision=F64, flags=0, reps=5, stream=None):
+    """Search the plan's launch-shape parameters on these tasks (the batch runs
+    several times; outputs must not alias inputs).  Returns (Tuning, ms)."""
+    n = len(tasks)
+    arr = (LrTask * max(n, 1))(*tasks)
+    best = Tuning()
+    ms = C.c_double(0)
+    _check(lib().hcore_gpu_autotune(precision, n, arr, flags, reps, stream or None, C.byref(best),
+                                    C.byref(ms)), "hcore_gpu_autotune")
+    return best, float(ms.value)

@@ -86,6 +86,10 @@ struct LaunchShape {
     // most output columns an accepted update may have, max of
     // min(k, storage_rank): the rebuild's grid (0: maxK)
     int maxR = 0;
+    // tuning: lanes per column pair of shared-memory SVD buckets with <= 24,
+    // <= 64 and more pairs; rank-bucket edge spacing
+    int svd_lanes[3] = {1, 4, 2};
+    int bucket_width = 8;
     bool mixed = false;  // FP32 factor products and rebuild (HCORE_GPU_MIXED_FACTORS)
     int nbuckets = 0;
     Bucket buckets[kMaxBuckets];
@@ -95,8 +99,8 @@ struct LaunchShape {
     cudaEvent_t fork = nullptr;
     cudaEvent_t join[kMaxBuckets] = {};
 };
-// smallest bucket edge >= k
-int bucket_edge(int k);
+// smallest bucket edge >= k (edges every `width` up to 64, then coarser)
+int bucket_edge(int k, int width);
 
 // launchers (hc_kernels.cu).  configure_recompress sets kernel attributes
 // (not capturable) and returns the largest k whose Jacobi matrices fit in

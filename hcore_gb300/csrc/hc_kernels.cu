@@ -361,22 +361,23 @@ struct JacobiLim<float> {
 // Lanes per column pair in the Jacobi sweeps of a bucket whose largest k is
 // K.  A group of G lanes shares a pair's rows, which divides the per-round
 // latency of one update by about G but repeats the rotation parameters in
-// every lane of the group.  Shared-memory buckets: small updates are
-// throughput-bound (one lane per pair); the few large ones set the phase's
-// critical path (four lanes).  Workspace buckets (k beyond the shared-memory
-// limit): four lanes per pair, up to 1024 threads, to keep enough loads in
-// flight on the L2-resident matrices.
+// every lane of the group.  Shared-memory buckets take the plan's tuning
+// (default: one lane per pair up to 24 pairs, where small updates are
+// throughput-bound; four up to 64 pairs and two beyond, where the few large
+// updates set the critical path).  Workspace buckets (k beyond the
+// shared-memory limit): four lanes per pair, up to 1024 threads, to keep
+// enough loads in flight on the L2-resident matrices.
 constexpr int kSvdMaxThreads = 1024;
-__host__ __device__ inline int svd_group(int K, bool smem) {
+__host__ __device__ inline int svd_group(int K, bool smem, const int *lanes) {
     const int np = (K + 1) / 2;
-    if (smem) return np <= 24 ? 1 : (np <= 64 ? 4 : (np <= 128 ? 2 : 1));
+    if (smem) return np <= 24 ? lanes[0] : (np <= 64 ? lanes[1] : lanes[2]);
     return np <= kSvdMaxThreads / 4 ? 4 : (np <= kSvdMaxThreads / 2 ? 2 : 1);
 }
 // Threads per CTA of the SVD kernel: G lanes for each of the K/2 pairs.
-__host__ __device__ inline int svd_threads(int K, bool smem) {
+__host__ __device__ inline int svd_threads(int K, bool smem, const int *lanes) {
     const int np = (K + 1) / 2;
     const int cap = smem ? kThreads : kSvdMaxThreads;
-    const int t = ((np * svd_group(K, smem) + 31) / 32) * 32;
+    const int t = ((np * svd_group(K, smem, lanes) + 31) / 32) * 32;
     return t < 32 ? 32 : (t > cap ? cap : t);
 }
 __host__ __device__ inline int svd_ld(int k) { return k | 1; }
@@ -916,11 +917,17 @@ cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
                                 dyn_max);
 }
 
-int bucket_edge(int k) {
-    static const int edges[] = {8, 16, 24, 32, 40, 48, 56, 64, 80, 96, 112, 128,
-                                160, 192, 224, 256, 320, 384, 448, 512};
-    for (int e : edges)
-        if (k <= e) return e;
+int bucket_edge(int k, int width) {
+    static const int fine[] = {8, 16, 24, 32, 40, 48, 56, 64, 80, 96, 112, 128,
+                               160, 192, 224, 256, 320, 384, 448, 512};
+    static const int coarse[] = {16, 32, 48, 64, 96, 128, 192, 256, 384, 512};
+    if (width >= 16) {
+        for (int e : coarse)
+            if (k <= e) return e;
+    } else {
+        for (int e : fine)
+            if (k <= e) return e;
+    }
     return kMaxK;
 }
 
@@ -956,7 +963,8 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
             const bool w_smem = K <= shape.svd_smem_kmax;
             cudaStream_t sb = forked ? shape.side[b] : s;
             if (forked) cudaStreamWaitEvent(sb, shape.fork, 0);
-            const int G = svd_group(K, w_smem), nt = svd_threads(K, w_smem);
+            const int G = svd_group(K, w_smem, shape.svd_lanes);
+            const int nt = svd_threads(K, w_smem, shape.svd_lanes);
             if (w_smem)
                 gesvd_kernel<T, true><<<bk.count, nt, svd_smem_bytes<T>(K, true), sb>>>(
                     d_desc + bk.start, ws, d_rank, d_status, d_info, K, G);

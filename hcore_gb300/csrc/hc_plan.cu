@@ -120,9 +120,10 @@ void fill_buckets(const std::vector<Desc> &descs, LaunchShape &shape) {
     const int n = (int)descs.size();
     int i = 0;
     while (i < n) {
-        const int K = descs[i].status0 ? bucket_edge(1) : bucket_edge(descs[i].k);
+        const int w = shape.bucket_width;
+        const int K = descs[i].status0 ? bucket_edge(1, w) : bucket_edge(descs[i].k, w);
         int j = i;
-        while (j < n && (descs[j].status0 ? bucket_edge(1) : bucket_edge(descs[j].k)) == K) ++j;
+        while (j < n && (descs[j].status0 ? bucket_edge(1, w) : bucket_edge(descs[j].k, w)) == K) ++j;
         if (shape.nbuckets == kMaxBuckets) {  // cannot happen with the fixed edges; merge
             shape.buckets[kMaxBuckets - 1].count += j - i;
         } else {
@@ -439,12 +440,50 @@ static void plan_free(hcore_gpu_plan p) {
     delete p;
 }
 
+extern "C" int hcore_gpu_tuning_default(hcore_gpu_tuning *t) {
+    if (!t) {
+        set_error("hcore_gpu_tuning_default: null argument");
+        return HCORE_GPU_EINVAL;
+    }
+    t->stream_groups = 16;
+    if (const char *env = getenv("HCORE_GPU_STREAMS")) t->stream_groups = atoi(env);
+    t->stream_groups = std::max(1, std::min(t->stream_groups, 64));
+    t->svd_lanes[0] = 1;
+    t->svd_lanes[1] = 4;
+    t->svd_lanes[2] = 2;
+    t->bucket_width = 8;
+    return HCORE_GPU_OK;
+}
+
+static bool valid_tuning(const hcore_gpu_tuning &t) {
+    auto pow2 = [](int x) { return x >= 1 && x <= 32 && (x & (x - 1)) == 0; };
+    return t.stream_groups >= 1 && t.stream_groups <= 64 && pow2(t.svd_lanes[0]) &&
+           pow2(t.svd_lanes[1]) && pow2(t.svd_lanes[2]) &&
+           (t.bucket_width == 8 || t.bucket_width == 16);
+}
+
 extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
                                      const hcore_lr_task *tasks, unsigned flags) {
+    return hcore_gpu_plan_create_tuned(plan, precision, n, tasks, flags, nullptr);
+}
+
+extern "C" int hcore_gpu_plan_create_tuned(hcore_gpu_plan *plan, int precision, int n,
+                                           const hcore_lr_task *tasks, unsigned flags,
+                                           const hcore_gpu_tuning *tuning) {
     if (!plan || n < 0 || (n > 0 && !tasks) ||
         (precision != HCORE_GPU_F64 && precision != HCORE_GPU_F32)) {
         set_error("hcore_gpu_plan_create: invalid argument");
         return HCORE_GPU_EINVAL;
+    }
+    hcore_gpu_tuning tune;
+    hcore_gpu_tuning_default(&tune);
+    if (tuning) {
+        if (!valid_tuning(*tuning)) {
+            set_error("hcore_gpu_plan_create: invalid tuning (groups 1..64, lanes powers of two "
+                      "<= 32, bucket width 8 or 16)");
+            return HCORE_GPU_EINVAL;
+        }
+        tune = *tuning;
     }
     *plan = nullptr;
     auto *p = new hcore_gpu_plan_s;
@@ -468,9 +507,12 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
     build_descs(n, tasks, flags, true, descs, ws_elems, p->maxM, p->maxK, nullptr);
     // stream groups (HCORE_GPU_STREAMS, default 16): deal the k-sorted
     // descriptors round-robin so every group gets the same mix of sizes
-    int ngroups = 16;
-    if (const char *env = getenv("HCORE_GPU_STREAMS")) ngroups = atoi(env);
-    ngroups = std::max(1, std::min(ngroups, std::min(n > 0 ? n : 1, 64)));
+    int ngroups = std::max(1, std::min(tune.stream_groups, n > 0 ? n : 1));
+    auto set_shape_tuning = [&](LaunchShape &sh) {
+        for (int q = 0; q < 3; ++q) sh.svd_lanes[q] = tune.svd_lanes[q];
+        sh.bucket_width = tune.bucket_width;
+    };
+    set_shape_tuning(p->shape);
     if (ngroups > 1) {
         std::vector<Desc> dealt;
         dealt.reserve(n);
@@ -485,6 +527,7 @@ extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
         bool ok = cudaEventCreateWithFlags(&p->gfork, cudaEventDisableTiming) == cudaSuccess;
         for (auto &g : p->groups) {
             std::vector<Desc> sub(descs.begin() + g.start, descs.begin() + g.start + g.count);
+            set_shape_tuning(g.shape);
             fill_buckets(sub, g.shape);
             g.shape.maxM = p->maxM;
             g.shape.maxK = p->maxK;
@@ -851,3 +894,113 @@ extern "C" int hcore_gpu_sgemm_batched(int n, const hcore_lr_task *tasks, int *r
 
 extern "C" const char *hcore_gpu_last_error(void) { return last_error(); }
 extern "C" int hcore_gpu_version(void) { return 100; }
+
+// ---------------------------------------------------------------------------
+// autotuner: coordinate descent over the launch-shape parameters, timing
+// plans of the caller's own batch
+// ---------------------------------------------------------------------------
+extern "C" int hcore_gpu_autotune(int precision, int n, const hcore_lr_task *tasks, unsigned flags,
+                                  int reps, void *stream, hcore_gpu_tuning *best, double *best_ms) {
+    if (n <= 0 || !tasks || !best) {
+        set_error("hcore_gpu_autotune: invalid argument");
+        return HCORE_GPU_EINVAL;
+    }
+    reps = std::max(1, reps);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        set_error("hcore_gpu_autotune: cannot create events");
+        if (e0) cudaEventDestroy(e0);
+        return HCORE_GPU_ECUDA;
+    }
+    // A candidate is timed the way a plan is meant to run: its execute
+    // captured once in a CUDA graph and the graph replayed (launch overhead
+    // then hardly depends on the number of launches).  A plan that cannot be
+    // captured (pageable staged inputs) is timed by direct executes.
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        set_error("hcore_gpu_autotune: cannot create a stream");
+        return HCORE_GPU_ECUDA;
+    }
+    (void)s;
+    auto time_cfg = [&](const hcore_gpu_tuning &t, double &ms) -> int {
+        hcore_gpu_plan p = nullptr;
+        int rc = hcore_gpu_plan_create_tuned(&p, precision, n, tasks, flags, &t);
+        if (rc) return rc;
+        rc = hcore_gpu_plan_execute(p, cs);   // warm-up
+        cudaError_t e = rc ? cudaSuccess : cudaStreamSynchronize(cs);
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        if (!rc && e == cudaSuccess) {
+            bool captured = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            if (captured) {
+                const int xrc = hcore_gpu_plan_execute(p, cs);
+                captured = cudaStreamEndCapture(cs, &g) == cudaSuccess && xrc == 0 &&
+                           cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+            }
+            if (!captured) {
+                cudaGetLastError();
+                if (ge) cudaGraphExecDestroy(ge);
+                if (g) cudaGraphDestroy(g);
+                ge = nullptr;
+                g = nullptr;
+            }
+        }
+        auto run_once = [&]() -> int {
+            if (ge) return cudaGraphLaunch(ge, cs) == cudaSuccess ? 0 : HCORE_GPU_ECUDA;
+            return hcore_gpu_plan_execute(p, cs);
+        };
+        if (!rc && e == cudaSuccess) rc = run_once();   // warm-up of the graph
+        if (!rc && e == cudaSuccess) e = cudaStreamSynchronize(cs);
+        if (!rc && e == cudaSuccess) e = cudaEventRecord(e0, cs);
+        for (int r = 0; r < reps && !rc && e == cudaSuccess; ++r) rc = run_once();
+        if (!rc && e == cudaSuccess) e = cudaEventRecord(e1, cs);
+        if (!rc && e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float f = 0.f;
+        if (!rc && e == cudaSuccess) e = cudaEventElapsedTime(&f, e0, e1);
+        if (ge) cudaGraphExecDestroy(ge);
+        if (g) cudaGraphDestroy(g);
+        hcore_gpu_plan_destroy(p);
+        if (!rc && e != cudaSuccess) {
+            set_error("hcore_gpu_autotune: %s", cudaGetErrorString(e));
+            rc = HCORE_GPU_ECUDA;
+        }
+        ms = (double)f / reps;
+        return rc;
+    };
+    hcore_gpu_tuning cur;
+    hcore_gpu_tuning_default(&cur);
+    double cur_ms = 0;
+    int rc = time_cfg(cur, cur_ms);
+    // one parameter at a time, keeping a change only if it gains 0.5 %
+    const int groups[] = {4, 8, 16, 24, 32};
+    const int lanes0[] = {1, 2}, lanes1[] = {2, 4, 8}, lanes2[] = {1, 2, 4}, widths[] = {8, 16};
+    // field(t) is the parameter being searched, as a reference into t
+    auto try_values = [&](auto field, const int *vals, int nv) {
+        for (int v = 0; v < nv && !rc; ++v) {
+            if (vals[v] == field(cur)) continue;
+            hcore_gpu_tuning t = cur;
+            field(t) = vals[v];
+            double ms = 0;
+            rc = time_cfg(t, ms);
+            if (!rc && ms < cur_ms * 0.995) {
+                cur = t;
+                cur_ms = ms;
+            }
+        }
+    };
+    try_values([](hcore_gpu_tuning &t) -> int & { return t.stream_groups; }, groups, 5);
+    try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[1]; }, lanes1, 3);
+    try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[2]; }, lanes2, 3);
+    try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[0]; }, lanes0, 2);
+    try_values([](hcore_gpu_tuning &t) -> int & { return t.bucket_width; }, widths, 2);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(cs);
+    if (rc) return rc;
+    *best = cur;
+    if (best_ms) *best_ms = cur_ms;
+    return HCORE_GPU_OK;
+}

@@ -143,6 +143,32 @@ size_t hcore_gpu_plan_staged_bytes(hcore_gpu_plan plan);
 size_t hcore_gpu_plan_zero_copy_bytes(hcore_gpu_plan plan);
 int hcore_gpu_plan_destroy(hcore_gpu_plan plan);
 
+/* Launch-shape tuning of a plan (no counterpart in the reference).
+ *   stream_groups      updates are dealt into this many concurrent groups
+ *   svd_lanes[3]       lanes per column pair of the shared-memory SVD buckets
+ *                      with <= 24, <= 64 and more column pairs
+ *   bucket_width       rank-bucket edges every 8 (fine) or 16 (coarse)
+ * hcore_gpu_tuning_default fills the built-in choice (16 groups, lanes 1/4/2,
+ * width 8; HCORE_GPU_STREAMS overrides the groups).  hcore_gpu_autotune
+ * times plans of the given tasks over a search of these parameters
+ * (coordinate descent; each candidate's execute captured in a CUDA graph on
+ * a private stream and replayed `reps` times) and returns the fastest; the
+ * tasks' outputs must not alias their inputs (the batch runs many times)
+ * and are overwritten.  `stream` is not used (reserved).  Results do not
+ * depend on the tuning beyond rounding (the SVD's reduction order follows
+ * the lanes). */
+typedef struct hcore_gpu_tuning {
+    int stream_groups;
+    int svd_lanes[3];
+    int bucket_width;
+} hcore_gpu_tuning;
+int hcore_gpu_tuning_default(hcore_gpu_tuning *tuning);
+int hcore_gpu_plan_create_tuned(hcore_gpu_plan *plan, int precision, int n,
+                                const hcore_lr_task *tasks, unsigned flags,
+                                const hcore_gpu_tuning *tuning);
+int hcore_gpu_autotune(int precision, int n, const hcore_lr_task *tasks, unsigned flags, int reps,
+                       void *stream, hcore_gpu_tuning *best, double *best_ms);
+
 /* one-shot synchronous batch: create, execute, results, destroy */
 int hcore_gpu_dgemm_batched(int n, const hcore_lr_task *tasks, int *ranks, int *status,
                             void *stream);
