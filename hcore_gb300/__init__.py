@@ -69,11 +69,12 @@ class DenseTask(C.Structure):
 class Tuning(C.Structure):
     """Mirror of hcore_gpu_tuning (include/hcore_gb300.h)."""
 
-    _fields_ = [("stream_groups", C.c_int), ("svd_lanes", C.c_int * 3), ("bucket_width", C.c_int)]
+    _fields_ = [("stream_groups", C.c_int), ("svd_lanes", C.c_int * 3), ("bucket_width", C.c_int),
+                ("phase_sync", C.c_int)]
 
     def as_dict(self) -> dict:
         return {"stream_groups": self.stream_groups, "svd_lanes": list(self.svd_lanes),
-                "bucket_width": self.bucket_width}
+                "bucket_width": self.bucket_width, "phase_sync": self.phase_sync}
 
 
 class FlopCounter(C.Structure):
@@ -431,7 +432,7 @@ class RankMLP:
             pass
 
 
-def make_tuning(stream_groups=None, svd_lanes=None, bucket_width=None) -> Tuning:
+def make_tuning(stream_groups=None, svd_lanes=None, bucket_width=None, phase_sync=None) -> Tuning:
     """A Tuning from the library default with the given fields replaced."""
     t = Tuning()
     _check(lib().hcore_gpu_tuning_default(C.byref(t)), "hcore_gpu_tuning_default")
@@ -442,6 +443,8 @@ def make_tuning(stream_groups=None, svd_lanes=None, bucket_width=None) -> Tuning
             t.svd_lanes[q] = int(svd_lanes[q])
     if bucket_width is not None:
         t.bucket_width = int(bucket_width)
+    if phase_sync is not None:
+        t.phase_sync = int(phase_sync)
     return t
 
 

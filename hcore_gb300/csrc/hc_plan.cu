@@ -228,6 +228,7 @@ struct hcore_gpu_plan_s {
     // some task's output overlaps another task's input: the stream groups
     // finish every stack phase before any later phase starts
     bool cross_alias = false;
+    bool phase_sync = false;   // tuning: all groups finish each phase before the next
     std::vector<cudaEvent_t> stacked;   // per group, with cross_alias
 };
 
@@ -452,6 +453,7 @@ extern "C" int hcore_gpu_tuning_default(hcore_gpu_tuning *t) {
     t->svd_lanes[1] = 4;
     t->svd_lanes[2] = 2;
     t->bucket_width = 8;
+    t->phase_sync = 0;
     return HCORE_GPU_OK;
 }
 
@@ -459,7 +461,7 @@ static bool valid_tuning(const hcore_gpu_tuning &t) {
     auto pow2 = [](int x) { return x >= 1 && x <= 32 && (x & (x - 1)) == 0; };
     return t.stream_groups >= 1 && t.stream_groups <= 64 && pow2(t.svd_lanes[0]) &&
            pow2(t.svd_lanes[1]) && pow2(t.svd_lanes[2]) &&
-           (t.bucket_width == 8 || t.bucket_width == 16);
+           (t.bucket_width == 8 || t.bucket_width == 16) && (t.phase_sync == 0 || t.phase_sync == 1);
 }
 
 extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
@@ -480,7 +482,7 @@ extern "C" int hcore_gpu_plan_create_tuned(hcore_gpu_plan *plan, int precision, 
     if (tuning) {
         if (!valid_tuning(*tuning)) {
             set_error("hcore_gpu_plan_create: invalid tuning (groups 1..64, lanes powers of two "
-                      "<= 32, bucket width 8 or 16)");
+                      "<= 32, bucket width 8 or 16, phase sync 0 or 1)");
             return HCORE_GPU_EINVAL;
         }
         tune = *tuning;
@@ -508,6 +510,7 @@ extern "C" int hcore_gpu_plan_create_tuned(hcore_gpu_plan *plan, int precision, 
     // stream groups (HCORE_GPU_STREAMS, default 16): deal the k-sorted
     // descriptors round-robin so every group gets the same mix of sizes
     int ngroups = std::max(1, std::min(tune.stream_groups, n > 0 ? n : 1));
+    p->phase_sync = tune.phase_sync != 0;
     auto set_shape_tuning = [&](LaunchShape &sh) {
         for (int q = 0; q < 3; ++q) sh.svd_lanes[q] = tune.svd_lanes[q];
         sh.bucket_width = tune.bucket_width;
@@ -649,6 +652,22 @@ extern "C" int hcore_gpu_plan_execute_phases(hcore_gpu_plan p, void *stream, uns
     };
     if (p->groups.empty()) {
         e = launch(p->d_desc, p->n, p->shape, s, phases);
+    } else if (p->phase_sync) {
+        // every group finishes a phase before any group starts the next
+        const unsigned order[4] = {kPhaseStack, kPhaseQR, kPhaseSVD, kPhaseApply};
+        for (int q = 0; q < 4 && e == cudaSuccess; ++q) {
+            const unsigned ph = phases & order[q];
+            if (!ph) continue;
+            e = cudaEventRecord(p->gfork, s);
+            for (auto &g : p->groups) {
+                if (e != cudaSuccess) break;
+                e = cudaStreamWaitEvent(g.stream, p->gfork, 0);
+                if (e == cudaSuccess && g.count > 0)
+                    e = launch(p->d_desc + g.start, g.count, g.shape, g.stream, ph);
+                if (e == cudaSuccess) e = cudaEventRecord(g.done, g.stream);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g.done, 0);
+            }
+        }
     } else if (p->cross_alias) {
         // an output of one task overlaps another task's input: every group's
         // stack phase (which reads all inputs) completes before any group
@@ -952,7 +971,7 @@ extern "C" int hcore_gpu_autotune(int precision, int n, const hcore_lr_task *tas
             if (ge) return cudaGraphLaunch(ge, cs) == cudaSuccess ? 0 : HCORE_GPU_ECUDA;
             return hcore_gpu_plan_execute(p, cs);
         };
-        if (!rc && e == cudaSuccess) rc = run_once();   // warm-up of the graph
+        if (!rc && e == cudaSuccess && ge) e = cudaGraphUpload(ge, cs);   // no extra execute
         if (!rc && e == cudaSuccess) e = cudaStreamSynchronize(cs);
         if (!rc && e == cudaSuccess) e = cudaEventRecord(e0, cs);
         for (int r = 0; r < reps && !rc && e == cudaSuccess; ++r) rc = run_once();
@@ -991,6 +1010,8 @@ extern "C" int hcore_gpu_autotune(int precision, int n, const hcore_lr_task *tas
             }
         }
     };
+    const int syncs[] = {0, 1};
+    try_values([](hcore_gpu_tuning &t) -> int & { return t.phase_sync; }, syncs, 2);
     try_values([](hcore_gpu_tuning &t) -> int & { return t.stream_groups; }, groups, 5);
     try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[1]; }, lanes1, 3);
     try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[2]; }, lanes2, 3);

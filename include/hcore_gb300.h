@@ -148,8 +148,12 @@ int hcore_gpu_plan_destroy(hcore_gpu_plan plan);
  *   svd_lanes[3]       lanes per column pair of the shared-memory SVD buckets
  *                      with <= 24, <= 64 and more column pairs
  *   bucket_width       rank-bucket edges every 8 (fine) or 16 (coarse)
+ *   phase_sync         0: each group runs its four phases as soon as it can
+ *                      (phases of different groups overlap); 1: every group
+ *                      finishes a phase before any group starts the next
+ *                      (large tiles, whose phases thrash L2 when mixed)
  * hcore_gpu_tuning_default fills the built-in choice (16 groups, lanes 1/4/2,
- * width 8; HCORE_GPU_STREAMS overrides the groups).  hcore_gpu_autotune
+ * width 8, no phase sync; HCORE_GPU_STREAMS overrides the groups).  hcore_gpu_autotune
  * times plans of the given tasks over a search of these parameters
  * (coordinate descent; each candidate's execute captured in a CUDA graph on
  * a private stream and replayed `reps` times) and returns the fastest; the
@@ -161,6 +165,7 @@ typedef struct hcore_gpu_tuning {
     int stream_groups;
     int svd_lanes[3];
     int bucket_width;
+    int phase_sync;
 } hcore_gpu_tuning;
 int hcore_gpu_tuning_default(hcore_gpu_tuning *tuning);
 int hcore_gpu_plan_create_tuned(hcore_gpu_plan *plan, int precision, int n,

@@ -49,7 +49,8 @@ def test_tunings_give_the_same_results(hc):
     r0, s0, p0 = _run(hc, tasks, keep, None)
     assert (s0 == 0).all()
     for tun in ({"stream_groups": 1}, {"stream_groups": 3, "bucket_width": 16},
-                {"svd_lanes": (2, 8, 4)}, {"stream_groups": 64, "svd_lanes": (1, 2, 1)}):
+                {"svd_lanes": (2, 8, 4)}, {"stream_groups": 64, "svd_lanes": (1, 2, 1)},
+                {"stream_groups": 8, "phase_sync": 1}):
         r, st, p = _run(hc, tasks, keep, tun)
         assert np.array_equal(r, r0) and np.array_equal(st, s0), tun
         for a, b in zip(p, p0):
@@ -63,6 +64,7 @@ def test_autotune_returns_a_valid_tuning(hc):
     t = best.as_dict()
     assert ms > 0
     assert 1 <= t["stream_groups"] <= 64 and t["bucket_width"] in (8, 16)
+    assert t["phase_sync"] in (0, 1)
     assert all(x in (1, 2, 4, 8, 16, 32) for x in t["svd_lanes"])
     r, st, _ = _run(hc, tasks, keep, best)
     assert (st == 0).all()
@@ -71,6 +73,7 @@ def test_autotune_returns_a_valid_tuning(hc):
 def test_invalid_tuning_is_refused(hc):
     rng = np.random.default_rng(73)
     keep, tasks = _tasks(hc, rng, n=4)
-    for bad in ({"stream_groups": 0}, {"svd_lanes": (3, 4, 2)}, {"bucket_width": 12}):
+    for bad in ({"stream_groups": 0}, {"svd_lanes": (3, 4, 2)}, {"bucket_width": 12},
+                {"phase_sync": 2}):
         with pytest.raises(hc.HcoreError):
             hc.Batch(tasks, tuning=bad)
