@@ -53,21 +53,20 @@ extern "C" {
 #define HCORE_GPU_S_LDNEWV 3    /* a + c > ld_newV, hcore_dgemm.c:924-927 */
 #define HCORE_GPU_S_RANK_MAX 4  /* new rank > maxrk, hcore_dgemm.c:465-468 */
 #define HCORE_GPU_S_STORAGE 5   /* new rank > storage maxrank, :1648-1651 */
-#define HCORE_GPU_S_NOCONV 6    /* Jacobi SVD did not converge */
+#define HCORE_GPU_S_NOCONV 6    /* Jacobi SVD did not converge, or a value was not finite */
 #define HCORE_GPU_S_SHAPE 7     /* a + c > M */
 
 /* flags of a plan */
 #define HCORE_GPU_FAST_RULES 0x1 /* HCORE_dgemm_fast: rank search from i=2, no maxrk checks */
-/* Host input factors (pinned or pageable) are merged into contiguous
- * segments, mirrored on the device, and refreshed by one copy per segment at
- * the start of every execute; shared factors (a panel tile used by many
- * updates) cross the host link once.  Pinned segments keep execute
- * capturable.  Outputs in pinned host memory are written in place by the
- * rebuild kernel. */
+/* Host input factors that several updates read (a panel tile) or that are
+ * pageable are merged into contiguous segments, mirrored on the device, and
+ * refreshed by one copy per segment at the start of every execute, so they
+ * cross the host link once.  A pinned host range that only one update reads
+ * (its own C tile) is not copied: its stack kernel reads it in place,
+ * overlapped with the other stream groups' work.  With pinned inputs,
+ * execute stays capturable.  Outputs in pinned host memory are written in
+ * place by the rebuild kernel. */
 #define HCORE_GPU_STAGE_INPUTS 0x2
-/* (With HCORE_GPU_STAGE_INPUTS, a pinned host range that only one update
- * reads, such as its own C tile, is not copied: the stack kernel reads it in
- * place once, overlapped with the other stream groups' work.) */
 /* FP64 plans only: the factor products F = AV^T BV, G = BU F^T and the Q.U
  * rebuild run in FP32 with FP32 accumulation (FP64 storage), the QRs, the SVD
  * and the truncation stay FP64.  Meant for loose accuracies (1e-4 .. 1e-6);
