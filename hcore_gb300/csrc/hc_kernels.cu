@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                                                                int *__restrict__ info, int maxK,
                                                                int G) {
     extern __shared__ unsigned char smem_raw[];
-    __shared__ int s_rot, s_piv, s_exp;
+    __shared__ int s_rot, s_piv, s_exp, s_conv;
     __shared__ T s_wmax[kSvdMaxThreads / 32];
     const Desc d = descs[blockIdx.x];
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
@@ -593,10 +593,17 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
     const int np = n / 2;
     const int grp = tid / G, lig = tid % G, ngrp = nthr / G;
     const T tol = T(k > 8 ? k : 8) * Lim<T>::eps;
+    // Stop after a sweep with no rotation, or after one whose largest relative
+    // off-diagonal |a_pq| / sqrt(a_pp a_qq) was at most sqrt(tol): cyclic
+    // Jacobi converges quadratically, so the next sweep would only rotate by
+    // angles near tol, moving the singular values at second order (the
+    // product U S V^T is exact after every sweep; only orthogonality remains)
+    const T stop_rel = sqrt(tol);
     bool converged = (k == 1);
     int sweeps = 0;
     for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
         if (tid == 0) s_rot = 0;
+        T sweep_rel = 0;   // this thread's largest relative off-diagonal rotated
         __syncthreads();
         for (int round = 0; round < n - 1; ++round) {
             for (int base = 0; base < np; base += ngrp) {
@@ -621,6 +628,7 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                                  apq != T(0) && abs(apq) > tol * sqrt(app) * sqrt(aqq);
                 T t = 0, cs = 1;
                 if (rot) {
+                    sweep_rel = max(sweep_rel, abs(apq) / (sqrt(app) * sqrt(aqq)));
                     const T zeta = (aqq - app) / (T(2) * apq);
                     const T az = abs(zeta);
                     t = az > Lim<T>::big_zeta ? T(0.5) / zeta
@@ -685,7 +693,16 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
             s_nrm[j] = dj * dj * s2;
         }
         ++sweeps;
-        converged = (s_rot == 0);
+        sweep_rel = warp_max(sweep_rel);
+        if (lane == 0) s_wmax[tid >> 5] = sweep_rel;
+        __syncthreads();
+        if (tid == 0) {
+            T m = 0;
+            for (int w = 0; w < nthr / 32; ++w) m = max(m, s_wmax[w]);
+            s_conv = (s_rot == 0 || m <= stop_rel) ? 1 : 0;
+        }
+        __syncthreads();
+        converged = s_conv != 0;
         __syncthreads();
     }
 
