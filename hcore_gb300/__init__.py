@@ -70,11 +70,12 @@ class Tuning(C.Structure):
     """Mirror of hcore_gpu_tuning (include/hcore_gb300.h)."""
 
     _fields_ = [("stream_groups", C.c_int), ("svd_lanes", C.c_int * 3), ("bucket_width", C.c_int),
-                ("phase_sync", C.c_int)]
+                ("phase_sync", C.c_int), ("qr_warps", C.c_int)]
 
     def as_dict(self) -> dict:
         return {"stream_groups": self.stream_groups, "svd_lanes": list(self.svd_lanes),
-                "bucket_width": self.bucket_width, "phase_sync": self.phase_sync}
+                "bucket_width": self.bucket_width, "phase_sync": self.phase_sync,
+                "qr_warps": self.qr_warps}
 
 
 class FlopCounter(C.Structure):
@@ -432,7 +433,8 @@ class RankMLP:
             pass
 
 
-def make_tuning(stream_groups=None, svd_lanes=None, bucket_width=None, phase_sync=None) -> Tuning:
+def make_tuning(stream_groups=None, svd_lanes=None, bucket_width=None, phase_sync=None,
+                qr_warps=None) -> Tuning:
     """A Tuning from the library default with the given fields replaced."""
     t = Tuning()
     _check(lib().hcore_gpu_tuning_default(C.byref(t)), "hcore_gpu_tuning_default")
@@ -445,6 +447,8 @@ def make_tuning(stream_groups=None, svd_lanes=None, bucket_width=None, phase_syn
         t.bucket_width = int(bucket_width)
     if phase_sync is not None:
         t.phase_sync = int(phase_sync)
+    if qr_warps is not None:
+        t.qr_warps = int(qr_warps)
     return t
 
 

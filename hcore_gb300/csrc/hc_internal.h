@@ -88,8 +88,9 @@ struct LaunchShape {
     int maxR = 0;
     // tuning: lanes per column pair of shared-memory SVD buckets with <= 24,
     // <= 64 and more pairs; rank-bucket edge spacing
-    int svd_lanes[3] = {1, 4, 2};
+    int svd_lanes[3] = {2, 2, 2};
     int bucket_width = 8;
+    int qr_warps = 4;   // warps per QR CTA (2, 4 or 8)
     bool mixed = false;  // FP32 factor products and rebuild (HCORE_GPU_MIXED_FACTORS)
     int nbuckets = 0;
     Bucket buckets[kMaxBuckets];

@@ -270,9 +270,12 @@ __device__ __forceinline__ void make_reflector(T (&x)[RPL], int j, int M, int la
     }
 }
 
-template <typename T, int RPL>
-__global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) geqrf_kernel(const Desc *__restrict__ descs,
-                                                         T *__restrict__ ws) {
+// NW warps per CTA (a tuning choice): 8 gives the shortest path per update;
+// 4 or 2 keep the same warps per SM in two or four times as many CTAs, so
+// that one CTA's per-column barrier stall is covered by the others.
+template <typename T, int RPL, int NW>
+__global__ void __launch_bounds__(NW * 32, (RPL <= 32 ? 2 : 1) * (8 / NW))
+    geqrf_kernel(const Desc *__restrict__ descs, T *__restrict__ ws) {
     __shared__ T sv[2][32 * RPL];
     __shared__ T s_tau[2];
     const Desc d = descs[blockIdx.x];
@@ -298,7 +301,7 @@ __global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) geqrf_kernel(cons
         const int cur = j & 1;
         const T *v = sv[cur];
         const T tj = s_tau[cur];
-        for (int col = j + 1 + warp; col < k; col += kWarps) {
+        for (int col = j + 1 + warp; col < k; col += NW) {
             T *Ac = A + (size_t)col * M;
 #pragma unroll
             for (int t = 0; t < RPL; ++t) {
@@ -362,9 +365,8 @@ struct JacobiLim<float> {
 // K.  A group of G lanes shares a pair's rows, which divides the per-round
 // latency of one update by about G but repeats the rotation parameters in
 // every lane of the group.  Shared-memory buckets take the plan's tuning
-// (default: one lane per pair up to 24 pairs, where small updates are
-// throughput-bound; four up to 64 pairs and two beyond, where the few large
-// updates set the critical path).  Workspace buckets (k beyond the
+// (lanes for buckets of up to 24, up to 64 and more pairs; default two
+// throughout, the autotuner's usual pick on a TLR panel).  Workspace buckets (k beyond the
 // shared-memory limit): four lanes per pair, up to 1024 threads, to keep
 // enough loads in flight on the L2-resident matrices.
 constexpr int kSvdMaxThreads = 1024;
@@ -904,8 +906,10 @@ static cudaError_t set_apply_smem() {
 }
 
 template <typename T, int RPL>
-static void launch_geqrf(const Desc *d_desc, int n, T *ws, cudaStream_t s) {
-    geqrf_kernel<T, RPL><<<dim3(n, 2), kThreads, 0, s>>>(d_desc, ws);
+static void launch_geqrf(const Desc *d_desc, int n, T *ws, int warps, cudaStream_t s) {
+    if (warps == 2) geqrf_kernel<T, RPL, 2><<<dim3(n, 2), 64, 0, s>>>(d_desc, ws);
+    else if (warps == 4) geqrf_kernel<T, RPL, 4><<<dim3(n, 2), 128, 0, s>>>(d_desc, ws);
+    else geqrf_kernel<T, RPL, 8><<<dim3(n, 2), 256, 0, s>>>(d_desc, ws);
 }
 
 template <typename T>
@@ -963,11 +967,12 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
         else stack_kernel<T, T><<<n, kThreads, 0, s>>>(d_desc, ws);
     }
     if (phases & kPhaseQR) {
-        if (rpl <= 4) launch_geqrf<T, 4>(d_desc, n, ws, s);
-        else if (rpl <= 8) launch_geqrf<T, 8>(d_desc, n, ws, s);
-        else if (rpl <= 16) launch_geqrf<T, 16>(d_desc, n, ws, s);
-        else if (rpl <= 32) launch_geqrf<T, 32>(d_desc, n, ws, s);
-        else launch_geqrf<T, 64>(d_desc, n, ws, s);
+        const int qw = shape.qr_warps;
+        if (rpl <= 4) launch_geqrf<T, 4>(d_desc, n, ws, qw, s);
+        else if (rpl <= 8) launch_geqrf<T, 8>(d_desc, n, ws, qw, s);
+        else if (rpl <= 16) launch_geqrf<T, 16>(d_desc, n, ws, qw, s);
+        else if (rpl <= 32) launch_geqrf<T, 32>(d_desc, n, ws, qw, s);
+        else launch_geqrf<T, 64>(d_desc, n, ws, qw, s);
     }
     if (phases & kPhaseSVD) {
         // buckets run concurrently (largest k first) when the plan provides

@@ -449,11 +449,12 @@ extern "C" int hcore_gpu_tuning_default(hcore_gpu_tuning *t) {
     t->stream_groups = 16;
     if (const char *env = getenv("HCORE_GPU_STREAMS")) t->stream_groups = atoi(env);
     t->stream_groups = std::max(1, std::min(t->stream_groups, 64));
-    t->svd_lanes[0] = 1;
-    t->svd_lanes[1] = 4;
+    t->svd_lanes[0] = 2;
+    t->svd_lanes[1] = 2;
     t->svd_lanes[2] = 2;
     t->bucket_width = 8;
     t->phase_sync = 0;
+    t->qr_warps = 4;
     return HCORE_GPU_OK;
 }
 
@@ -461,7 +462,8 @@ static bool valid_tuning(const hcore_gpu_tuning &t) {
     auto pow2 = [](int x) { return x >= 1 && x <= 32 && (x & (x - 1)) == 0; };
     return t.stream_groups >= 1 && t.stream_groups <= 64 && pow2(t.svd_lanes[0]) &&
            pow2(t.svd_lanes[1]) && pow2(t.svd_lanes[2]) &&
-           (t.bucket_width == 8 || t.bucket_width == 16) && (t.phase_sync == 0 || t.phase_sync == 1);
+           (t.bucket_width == 8 || t.bucket_width == 16) && (t.phase_sync == 0 || t.phase_sync == 1) &&
+           (t.qr_warps == 2 || t.qr_warps == 4 || t.qr_warps == 8);
 }
 
 extern "C" int hcore_gpu_plan_create(hcore_gpu_plan *plan, int precision, int n,
@@ -482,7 +484,7 @@ extern "C" int hcore_gpu_plan_create_tuned(hcore_gpu_plan *plan, int precision, 
     if (tuning) {
         if (!valid_tuning(*tuning)) {
             set_error("hcore_gpu_plan_create: invalid tuning (groups 1..64, lanes powers of two "
-                      "<= 32, bucket width 8 or 16, phase sync 0 or 1)");
+                      "<= 32, bucket width 8 or 16, phase sync 0 or 1, QR warps 2, 4 or 8)");
             return HCORE_GPU_EINVAL;
         }
         tune = *tuning;
@@ -514,6 +516,7 @@ extern "C" int hcore_gpu_plan_create_tuned(hcore_gpu_plan *plan, int precision, 
     auto set_shape_tuning = [&](LaunchShape &sh) {
         for (int q = 0; q < 3; ++q) sh.svd_lanes[q] = tune.svd_lanes[q];
         sh.bucket_width = tune.bucket_width;
+        sh.qr_warps = tune.qr_warps;
     };
     set_shape_tuning(p->shape);
     if (ngroups > 1) {
@@ -1013,6 +1016,8 @@ extern "C" int hcore_gpu_autotune(int precision, int n, const hcore_lr_task *tas
     const int syncs[] = {0, 1};
     try_values([](hcore_gpu_tuning &t) -> int & { return t.phase_sync; }, syncs, 2);
     try_values([](hcore_gpu_tuning &t) -> int & { return t.stream_groups; }, groups, 5);
+    const int qrw[] = {8, 4, 2};
+    try_values([](hcore_gpu_tuning &t) -> int & { return t.qr_warps; }, qrw, 3);
     try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[1]; }, lanes1, 3);
     try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[2]; }, lanes2, 3);
     try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[0]; }, lanes0, 2);

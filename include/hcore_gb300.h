@@ -150,9 +150,11 @@ int hcore_gpu_plan_destroy(hcore_gpu_plan plan);
  *   phase_sync         0: each group runs its four phases as soon as it can
  *                      (phases of different groups overlap); 1: every group
  *                      finishes a phase before any group starts the next
- *                      (large tiles, whose phases thrash L2 when mixed)
- * hcore_gpu_tuning_default fills the built-in choice (16 groups, lanes 1/4/2,
- * width 8, no phase sync; HCORE_GPU_STREAMS overrides the groups).  hcore_gpu_autotune
+ *   qr_warps           warps per Householder-QR CTA: 8 (shortest path per
+ *                      update), 4 or 2 (two or four times the CTAs per SM)
+ * hcore_gpu_tuning_default fills the built-in choice (16 groups, 2 lanes per
+ * pair, width 8, no phase sync, 4 QR warps: the best measured on a TLR
+ * panel of 1953 updates; HCORE_GPU_STREAMS overrides the groups).  hcore_gpu_autotune
  * times plans of the given tasks over a search of these parameters
  * (coordinate descent; each candidate's execute captured in a CUDA graph on
  * a private stream and replayed `reps` times) and returns the fastest; the
@@ -165,6 +167,7 @@ typedef struct hcore_gpu_tuning {
     int svd_lanes[3];
     int bucket_width;
     int phase_sync;
+    int qr_warps;
 } hcore_gpu_tuning;
 int hcore_gpu_tuning_default(hcore_gpu_tuning *tuning);
 int hcore_gpu_plan_create_tuned(hcore_gpu_plan *plan, int precision, int n,
