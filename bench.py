@@ -1035,20 +1035,24 @@ def run_predictor(args):
                    updates=0, ok=0, truncated=0, overflow=0, arena_bytes_max=0, arena_bytes_sum=0,
                    ws_bytes_max=0, per_sweep=[])
         for k in range(S):
-            # POTRF + TRSM of panel k (V <- L^-1 V for every tile (i, k), i > k)
+            # HCORE_dpotrf + HCORE_dtrsm of panel k (the library's kernels):
+            # D[k] = L L^T in place (D[k] holds the lower triangle, column-major),
+            # then V <- L^-1 V for every tile (i, k), i > k, as one TRSM whose
+            # right-hand sides are all the panel's V columns (copied first: the
+            # factors may be shared with the other arm's starting store)
             e0, e1 = ev(), ev()
             e0.record(stream)
-            # D[k] holds the lower triangle of the tile (column-major; dsyrk
-            # zeroes the strict upper part): symmetrise before POTRF
-            Dk = torch.tril(D[k].T)
-            Lk, info = torch.linalg.cholesky_ex(Dk + torch.tril(Dk, -1).T)
-            if int(info) != 0:
-                raise SystemExit(f"POTRF of diagonal tile {k} failed (info {int(info)})")
+            info = hc.potrf_batched([hc.PotrfTask(uplo=ord("L"), n=nb, A=D[k].data_ptr(), lda=nb)],
+                                    stream=stream.cuda_stream)
+            if int(info[0]) != 0:
+                raise SystemExit(f"POTRF of diagonal tile {k} failed (info {int(info[0])})")
             col = [(i, k) for i in range(k + 1, B)]
             if col:
                 Vs = torch.cat([store.tiles[t][1][store.tiles[t][2]:store.tiles[t][2] + nb * store.tiles[t][3]]
                                 .view(store.tiles[t][3], nb) for t in col], 0)
-                Vs = torch.linalg.solve_triangular(Lk, Vs.T, upper=False).T.contiguous()
+                hc.trsm_batched([hc.TrsmTask(side=141, uplo=122, trans=111, diag=131, M=nb,
+                                             N=Vs.shape[0], alpha=1.0, A=D[k].data_ptr(), lda=nb,
+                                             B=Vs.data_ptr(), ldb=nb)], stream=stream.cuda_stream)
                 Us = torch.cat([store.tiles[t][0][store.tiles[t][2]:store.tiles[t][2] + nb * store.tiles[t][3]]
                                 for t in col])
                 Vflat = Vs.reshape(-1)

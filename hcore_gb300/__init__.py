@@ -10,7 +10,11 @@ interface so tests and benchmarks read like the reference's own:
   on numpy arrays, through the drop-in C entry points;
 * :class:`Batch` — many independent updates in one plan (device tensors),
   executed by the batched GPU kernels and capturable in a CUDA graph;
-* :func:`dense_batched` — HCORE_dsyrk / HCORE_dgemmcd tile updates;
+* :func:`dense_batched` — HCORE_dsyrk / HCORE_dgemmcd / HCORE_duncompress /
+  HCORE_dgemmbdcd tile operations;
+* :func:`trsm_batched` / :func:`potrf_batched` — HCORE_dtrsm on many factors
+  and HCORE_dpotrf on dense tiles, the steps either side of the update in a
+  TLR Cholesky;
 * :class:`RankMLP` — the rank predictor's network, trained and run by the
   library's own CUDA kernels (see :mod:`hcore_gb300.predictor`).
 
@@ -28,7 +32,7 @@ import numpy as np
 from .build import LIB as _LIB_PATH
 
 __all__ = ["lib", "LrTask", "DenseTask", "Batch", "DensePlan", "hcore_dgemm", "hcore_sgemm", "hcore_dgemm_fast",
-           "dense_batched", "HcoreError", "STATUS", "FlopCounter", "RankMLP", "Tuning",
+           "dense_batched", "TrsmTask", "PotrfTask", "trsm_batched", "potrf_batched", "HcoreError", "STATUS", "FlopCounter", "RankMLP", "Tuning",
            "make_tuning", "autotune"]
 
 F64, F32 = 0, 1
@@ -63,7 +67,22 @@ class DenseTask(C.Structure):
     _fields_ = [("kind", C.c_int), ("M", C.c_int), ("a", C.c_int), ("b", C.c_int),
                 ("alpha", C.c_double), ("Au", C.c_void_p), ("Av", C.c_void_p), ("lda", C.c_int),
                 ("Bu", C.c_void_p), ("Bv", C.c_void_p), ("ldb", C.c_int), ("CD", C.c_void_p),
-                ("ldcd", C.c_int)]
+                ("ldcd", C.c_int), ("N", C.c_int), ("beta", C.c_double), ("kdim", C.c_int),
+                ("Bd", C.c_void_p)]
+
+
+class TrsmTask(C.Structure):
+    """Mirror of hcore_trsm_task (include/hcore_gb300.h)."""
+
+    _fields_ = [("side", C.c_int), ("uplo", C.c_int), ("trans", C.c_int), ("diag", C.c_int),
+                ("M", C.c_int), ("N", C.c_int), ("alpha", C.c_double), ("A", C.c_void_p),
+                ("lda", C.c_int), ("B", C.c_void_p), ("ldb", C.c_int)]
+
+
+class PotrfTask(C.Structure):
+    """Mirror of hcore_potrf_task (include/hcore_gb300.h); uplo is 'L' or 'U'."""
+
+    _fields_ = [("uplo", C.c_int), ("n", C.c_int), ("A", C.c_void_p), ("lda", C.c_int)]
 
 
 class Tuning(C.Structure):
@@ -142,6 +161,8 @@ def lib() -> C.CDLL:
     L.hcore_gpu_dense_plan_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(DenseTask)]
     L.hcore_gpu_dense_plan_execute.argtypes = [vp, vp]
     L.hcore_gpu_dense_plan_destroy.argtypes = [vp]
+    L.hcore_gpu_trsm_batched.argtypes = [C.c_int, C.POINTER(TrsmTask), vp]
+    L.hcore_gpu_potrf_batched.argtypes = [C.c_int, C.POINTER(PotrfTask), C.POINTER(C.c_int), vp]
     L.hcore_gpu_mlp_create.argtypes = [C.POINTER(vp), C.c_ulonglong]
     L.hcore_gpu_mlp_params.argtypes = [vp, _fp, C.c_int]
     L.hcore_gpu_mlp_gradient.argtypes = [vp, vp, vp, C.c_int, _fp, _fp, vp]
@@ -168,6 +189,19 @@ def lib() -> C.CDLL:
     L.HCORE_dgemmcd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_int, C.c_int,
                                 _dp, _dp, C.c_int, C.c_int, C.c_double, _dp, C.c_int, C.c_int, _dp,
                                 C.POINTER(FlopCounter)]
+    L.HCORE_duncompress.restype = None
+    L.HCORE_duncompress.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp,
+                                    C.c_int, _dp, _dp, C.c_int, C.c_double, _dp, C.c_int]
+    L.HCORE_dgemmbdcd.restype = None
+    L.HCORE_dgemmbdcd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp,
+                                  C.c_int, _dp, C.c_int, C.c_double, _dp, C.c_int, _dp,
+                                  C.POINTER(FlopCounter)]
+    L.HCORE_dtrsm.restype = None
+    L.HCORE_dtrsm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                              _dp, C.c_int, _dp, C.c_int, C.POINTER(FlopCounter)]
+    L.HCORE_dpotrf.restype = None
+    L.HCORE_dpotrf.argtypes = [C.c_int, C.c_int, _dp, C.c_int, C.POINTER(C.c_int),
+                               C.POINTER(FlopCounter)]
     for name, rp, real in (("HCORE_dgemm_dense", _dp, C.c_double),
                            ("HCORE_sgemm_dense", _fp, C.c_float)):
         f = getattr(L, name)
@@ -374,6 +408,21 @@ def dense_batched(tasks, stream=None):
     """Run HCORE_dsyrk / HCORE_dgemmcd tasks (device pointers) in one batch."""
     arr = (DenseTask * max(len(tasks), 1))(*tasks)
     _check(lib().hcore_gpu_dense_batched(len(tasks), arr, stream or None), "hcore_gpu_dense_batched")
+
+
+def trsm_batched(tasks, stream=None):
+    """Run TrsmTask list (device or pinned pointers); returns when done."""
+    arr = (TrsmTask * max(len(tasks), 1))(*tasks)
+    _check(lib().hcore_gpu_trsm_batched(len(tasks), arr, stream or None), "hcore_gpu_trsm_batched")
+
+
+def potrf_batched(tasks, stream=None) -> np.ndarray:
+    """Factor PotrfTask tiles in place; returns each task's LAPACK info."""
+    arr = (PotrfTask * max(len(tasks), 1))(*tasks)
+    info = (C.c_int * max(len(tasks), 1))()
+    _check(lib().hcore_gpu_potrf_batched(len(tasks), arr, info, stream or None),
+           "hcore_gpu_potrf_batched")
+    return np.array(info[:len(tasks)], dtype=np.int32)
 
 
 class RankMLP:

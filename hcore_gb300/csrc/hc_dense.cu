@@ -3,17 +3,25 @@
 //       CD = alpha * AU (AV^T AV) AU^T + CD, strict upper triangle := 0
 //   HCORE_dgemmcd (src/compute/hcore_dgemmcd.c:36-106)
 //       CD = CD - Au (Av^T Bv) Bu^T (associated by the smaller rank, :72)
+//   HCORE_duncompress (src/compute/hcore_duncompress.c:33-84)
+//       CD = AU BV^T
+//   HCORE_dgemmbdcd (src/compute/hcore_dgemmbdcd.c:35-122)
+//       CD = alpha AU (AV^T BD) + beta CD
 //   HCORE_dgemm_dense (src/compute/hcore_dgemm.c:1701-1715)
 //       C = alpha op(A) op(B) + beta C
 //
-// Every low-rank contribution is first reduced to a rank-K' product
-// coef * P Q^T with P, Q of size M x K' (prep kernel, one CTA per task), and
-// all tasks that hit the same tile are then applied in list order by one
-// tile kernel that keeps a 64 x 64 block of CD in registers.  Zeroing the
+// Every contribution is first reduced to a rank-K' product beta CD +
+// coef * P Q^T with P of size M x K' and Q of size N x K' (prep kernels: one
+// CTA per syrk/gemmcd task, a tiled GEMM for the gemmbdcd product
+// Q = BD^T AV; uncompress needs none), and all tasks that hit the same tile
+// are then applied in list order by one tile kernel that keeps a 64 x 64
+// block of CD in registers.  Zeroing the
 // strict upper triangle after each syrk task reproduces the reference's
 // sequential semantics exactly; the syrk's own upper-triangle products are
 // never computed since they are overwritten by zero.
 #include <cuda_runtime.h>
+
+#include <climits>
 
 #include "hc_internal.h"
 
@@ -33,6 +41,7 @@ __device__ __forceinline__ T wsum(T v) {
 __global__ void __launch_bounds__(256) dense_prep_kernel(const hcore_dense_task *tasks,
                                                          const DenseWork *work, double *ws) {
     const hcore_dense_task t = tasks[blockIdx.x];
+    if (t.kind > 1) return;  // uncompress: no prep; gemmbdcd: bdcd_prep_kernel
     const DenseWork w = work[blockIdx.x];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     double *S = ws + w.ws;
@@ -81,6 +90,57 @@ __global__ void __launch_bounds__(256) dense_prep_kernel(const hcore_dense_task 
 // register block; K' is staged in chunks of 16 through shared memory.
 constexpr int TB = 64, TK = 16;
 
+// gemmbdcd prep: Q = BD^T AV (N x a, ld N) into the task's workspace, i.e.
+// (AV^T BD)^T of hcore_dgemmbdcd.c:80-87/:99-106, summed over kdim rows.
+// One CTA per (64 rows of Q, 64 columns of Q, task); both operands are read
+// along their contiguous dimension (16 consecutive rows of a column).
+__global__ void __launch_bounds__(256) bdcd_prep_kernel(const hcore_dense_task *tasks,
+                                                        const DenseWork *work, const int *idx,
+                                                        int tilesN, int tilesA, double *ws) {
+    __shared__ double sB[TK][TB + 1];
+    __shared__ double sA[TK][TB + 1];
+    const int ti = blockIdx.x % tilesN;
+    const int tj = (blockIdx.x / tilesN) % tilesA;
+    const int q = blockIdx.x / (tilesN * tilesA);
+    const int task = idx[q];
+    const hcore_dense_task t = tasks[task];
+    const int N = t.N ? t.N : t.M, K = t.kdim ? t.kdim : t.M, a = t.a;
+    const int row0 = ti * TB, col0 = tj * TB;  // rows of Q (columns of BD), columns of Q
+    if (row0 >= N || col0 >= a) return;
+    double *Q = ws + work[task].ws;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double acc[4][4] = {};
+    for (int k0 = 0; k0 < K; k0 += TK) {
+        for (int e = threadIdx.x; e < TK * TB; e += 256) {
+            const int kk = e % TK, r = e / TK;
+            const int kg = k0 + kk;
+            sB[kk][r] = (kg < K && row0 + r < N) ? t.Bd[(size_t)(row0 + r) * t.ldb + kg] : 0.0;
+            sA[kk][r] = (kg < K && col0 + r < a) ? t.Av[(size_t)(col0 + r) * t.lda + kg] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < TK; ++kk) {
+            double bv[4], av[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) bv[u] = sB[kk][tx + 16 * u];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) av[v] = sA[kk][ty + 16 * v];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] += bv[u] * av[v];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int i = row0 + tx + 16 * u, j = col0 + ty + 16 * v;
+            if (i < N && j < a) Q[(size_t)j * N + i] = acc[u][v];
+        }
+}
+
 __global__ void __launch_bounds__(256) dense_tile_kernel(const hcore_dense_task *tasks,
                                                          const DenseWork *work,
                                                          const int *group_start,
@@ -93,9 +153,9 @@ __global__ void __launch_bounds__(256) dense_tile_kernel(const hcore_dense_task 
     const int g0 = group_start[g], g1 = group_start[g + 1];
     if (g0 == g1) return;
     const hcore_dense_task t0 = tasks[group_tasks[g0]];
-    const int M = t0.M;
+    const int M = t0.M, N = t0.N ? t0.N : t0.M;
     const int row0 = bi * TB, col0 = bj * TB;
-    if (row0 >= M || col0 >= M) return;
+    if (row0 >= M || col0 >= N) return;
     double *CD = t0.CD;
     const int ldcd = t0.ldcd;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -105,11 +165,17 @@ __global__ void __launch_bounds__(256) dense_tile_kernel(const hcore_dense_task 
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
             const int i = row0 + tx + 16 * u, j = col0 + ty + 16 * v;
-            acc[u][v] = (i < M && j < M) ? CD[(size_t)j * ldcd + i] : 0.0;
+            acc[u][v] = (i < M && j < N) ? CD[(size_t)j * ldcd + i] : 0.0;
         }
     const bool strictly_upper = row0 + TB <= col0;  // every (i, j) here has i < j
     for (int gi = g0; gi < g1; ++gi) {
         const DenseWork w = work[group_tasks[gi]];
+        if (w.beta != 1.0) {  // beta = 0 does not read CD (BLAS convention)
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = w.beta == 0.0 ? 0.0 : w.beta * acc[u][v];
+        }
         if (!(w.syrk && strictly_upper)) {
             for (int k0 = 0; k0 < w.kk; k0 += TK) {
                 // the task's coefficient is folded into P as it is staged
@@ -118,7 +184,7 @@ __global__ void __launch_bounds__(256) dense_tile_kernel(const hcore_dense_task 
                     const int kk = e / TB, r = e % TB;
                     const int kg = k0 + kk;
                     sP[kk][r] = (kg < w.kk && row0 + r < M) ? w.coef * w.P[(size_t)kg * w.ldp + row0 + r] : 0.0;
-                    sQ[kk][r] = (kg < w.kk && col0 + r < M) ? w.Q[(size_t)kg * w.ldq + col0 + r] : 0.0;
+                    sQ[kk][r] = (kg < w.kk && col0 + r < N) ? w.Q[(size_t)kg * w.ldq + col0 + r] : 0.0;
                 }
                 __syncthreads();
 #pragma unroll
@@ -149,7 +215,7 @@ __global__ void __launch_bounds__(256) dense_tile_kernel(const hcore_dense_task 
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
             const int i = row0 + tx + 16 * u, j = col0 + ty + 16 * v;
-            if (i < M && j < M) CD[(size_t)j * ldcd + i] = acc[u][v];
+            if (i < M && j < N) CD[(size_t)j * ldcd + i] = acc[u][v];
         }
 }
 
@@ -160,11 +226,22 @@ cudaError_t launch_dense_prep(const hcore_dense_task *d_tasks, const DenseWork *
     return cudaGetLastError();
 }
 
+cudaError_t launch_bdcd_prep(const hcore_dense_task *d_tasks, const DenseWork *d_work,
+                             const int *d_idx, int n_idx, int maxN, int maxA, double *ws,
+                             cudaStream_t s) {
+    if (n_idx <= 0 || maxN <= 0 || maxA <= 0) return cudaSuccess;
+    const int tn = (maxN + TB - 1) / TB, ta = (maxA + TB - 1) / TB;
+    const long long blocks = (long long)tn * ta * n_idx;
+    if (blocks > INT_MAX) return cudaErrorInvalidValue;
+    bdcd_prep_kernel<<<(unsigned)blocks, 256, 0, s>>>(d_tasks, d_work, d_idx, tn, ta, ws);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_dense_tiles(const hcore_dense_task *d_tasks, const DenseWork *d_work,
                                const int *d_group_start, const int *d_group_tasks, int ngroups,
-                               int maxM, cudaStream_t s) {
+                               int maxDim, cudaStream_t s) {
     if (ngroups <= 0) return cudaSuccess;
-    const int tpd = (maxM + TB - 1) / TB;
+    const int tpd = (maxDim + TB - 1) / TB;
     dense_tile_kernel<<<dim3(tpd * tpd, ngroups), 256, 0, s>>>(d_tasks, d_work, d_group_start,
                                                                d_group_tasks, tpd);
     return cudaGetLastError();

@@ -36,6 +36,8 @@ int syrk_print_index = 0;   // hcore_dsyrk.c:21
 int gemmcd_print_index = 0; // hcore_dgemmcd.c:24
 int gemmcd_print_mat = 0;   // hcore_dgemmcd.c:25
 int gemmcd_use_scratch = 0; // hcore_dgemmcd.c:26
+int gemmbdcd_print_index = 0;  // hcore_dgemmbdcd.c:25
+int gemmbdcd_print_mat = 0;    // hcore_dgemmbdcd.c:26
 // defined by the caller, as in the reference (hcore_dgemm.c:38); weak so that
 // a caller without it still links and reads 0
 extern int use_scratch __attribute__((weak));
@@ -121,6 +123,13 @@ unsigned long flop_counts(char op, unsigned long a, unsigned long b, unsigned lo
         const unsigned long m = a, n = b, k = c;
         if (d == 1) res = 4 * n * m * k - 2 * n * k * k + 3 * n * k;
         else if (d == 2) res = 4 * n * m * k - 2 * m * k * k + 2 * m * k + n * k - k * k / 2 + k / 2;
+    } else if (op == 'c') {  // potrf: integer n^3/3 and n/6, n^2/2 in double (flop_counts.c:11-14)
+        const unsigned long n = a;
+        res = (unsigned long)(n * n * n / 3 - n * n / 2.0 + n / 6);
+    } else if (op == 't') {  // trsm: side 1 (left) n m^2, side 2 (right) m n^2 (flop_counts.c:16-26)
+        const unsigned long m = a, n = b;
+        if (c == 1) res = n * m * m;
+        else if (c == 2) res = m * n * n;
     }
     return res;
 }
@@ -481,47 +490,86 @@ struct DenseRun {
 // pointers): group by output tile (list order kept inside each group), the
 // rank-K' form of every task and the workspace layout.
 struct DensePrep {
-    int n = 0, maxM = 1;
+    int n = 0, maxDim = 1, maxN3 = 0, maxA3 = 0;
     std::vector<DenseWork> work;
-    std::vector<int> gstart, gtasks;
+    std::vector<int> gstart, gtasks, bdcd;  // bdcd: the gemmbdcd tasks
     long long ws = 0;  // doubles
-    size_t b_tasks = 0, b_work = 0, b_gs = 0, b_gt = 0, b_ws = 0;
-    size_t bytes() const { return b_tasks + b_work + b_gs + b_gt + b_ws; }
+    size_t b_tasks = 0, b_work = 0, b_gs = 0, b_gt = 0, b_bd = 0, b_ws = 0;
+    size_t bytes() const { return b_tasks + b_work + b_gs + b_gt + b_bd + b_ws; }
+    size_t ws_offset() const { return b_tasks + b_work + b_gs + b_gt + b_bd; }
     int ngroups() const { return (int)gstart.size() - 1; }
+
+    static bool valid(const hcore_dense_task &t) {
+        const int N = t.N ? t.N : t.M;
+        if (t.M < 1 || N < 1 || t.a < 0 || t.b < 0 || !t.CD || t.ldcd < t.M) return false;
+        switch (t.kind) {
+        case 0:
+        case 1:
+            return N == t.M;
+        case 2:
+            return t.a == 0 || (t.Au && t.Bv && t.lda >= t.M && t.ldb >= N);
+        case 3: {
+            const int K = t.kdim ? t.kdim : t.M;
+            return K >= 1 && (t.a == 0 || (t.Au && t.Av && t.Bd && t.lda >= std::max(t.M, K) &&
+                                           t.ldb >= K));
+        }
+        default:
+            return false;
+        }
+    }
 
     int build(int n_, const hcore_dense_task *tasks) {
         n = n_;
         std::map<const double *, int> gid;
         std::vector<std::vector<int>> groups;
         work.assign(n, DenseWork{});
+        bdcd.clear();
         ws = 0;
         for (int i = 0; i < n; ++i) {
             const hcore_dense_task &t = tasks[i];
-            if ((t.kind != 0 && t.kind != 1) || t.M < 1 || t.a < 0 || t.b < 0 || !t.CD ||
-                t.ldcd < t.M) {
+            if (!valid(t)) {
                 set_error("dense tasks: invalid task %d", i);
                 return HCORE_GPU_EINVAL;
             }
+            const int N = t.N ? t.N : t.M;
             auto it = gid.find(t.CD);
             if (it == gid.end()) {
                 gid[t.CD] = (int)groups.size();
                 groups.push_back({i});
             } else {
-                if (tasks[groups[it->second][0]].M != t.M) {
-                    set_error("dense tasks: tasks on one tile disagree on M");
+                const hcore_dense_task &t0 = tasks[groups[it->second][0]];
+                if (t0.M != t.M || (t0.N ? t0.N : t0.M) != N) {
+                    set_error("dense tasks: tasks on one tile disagree on its shape");
                     return HCORE_GPU_EINVAL;
                 }
                 groups[it->second].push_back(i);
             }
-            maxM = std::max(maxM, t.M);
+            maxDim = std::max(maxDim, std::max(t.M, N));
             DenseWork &w = work[i];
             w.ws = ws;
-            const long long sq = t.kind == 0 ? (long long)t.a * t.a : (long long)t.a * t.b;
-            const int kk = t.kind == 0 ? t.a : std::min(t.a, t.b);
-            ws += ((sq + (long long)t.M * kk + 31) / 32) * 32;
-            w.syrk = t.kind == 0;
-            w.kk = kk;
-            w.coef = t.kind == 0 ? t.alpha : -1.0;
+            w.beta = 1.0;
+            if (t.kind <= 1) {
+                const long long sq = t.kind == 0 ? (long long)t.a * t.a : (long long)t.a * t.b;
+                const int kk = t.kind == 0 ? t.a : std::min(t.a, t.b);
+                ws += ((sq + (long long)t.M * kk + 31) / 32) * 32;
+                w.syrk = t.kind == 0;
+                w.kk = kk;
+                w.coef = t.kind == 0 ? t.alpha : -1.0;
+            } else if (t.kind == 2) {  // alpha = 1, beta = 0 (hcore_duncompress.c:73-79)
+                w.kk = t.a;
+                w.coef = 1.0;
+                w.beta = 0.0;
+            } else {
+                w.kk = t.a;
+                w.coef = t.alpha;
+                w.beta = t.beta;
+                if (t.a > 0) {
+                    ws += (((long long)N * t.a + 31) / 32) * 32;
+                    bdcd.push_back(i);
+                    maxN3 = std::max(maxN3, N);
+                    maxA3 = std::max(maxA3, t.a);
+                }
+            }
         }
         gstart.assign(groups.size() + 1, 0);
         gtasks.clear();
@@ -533,6 +581,7 @@ struct DensePrep {
         b_work = al256(n * sizeof(DenseWork));
         b_gs = al256(gstart.size() * sizeof(int));
         b_gt = al256(gtasks.size() * sizeof(int));
+        b_bd = al256(std::max<size_t>(bdcd.size(), 1) * sizeof(int));
         b_ws = al256((size_t)ws * sizeof(double));
         return HCORE_GPU_OK;
     }
@@ -543,6 +592,15 @@ struct DensePrep {
         for (int i = 0; i < n; ++i) {
             const hcore_dense_task &t = tasks[i];
             DenseWork &w = work[i];
+            const int N = t.N ? t.N : t.M;
+            if (t.kind == 2) {
+                w.P = t.Au; w.ldp = t.lda; w.Q = t.Bv; w.ldq = t.ldb;
+                continue;
+            }
+            if (t.kind == 3) {
+                w.P = t.Au; w.ldp = t.lda; w.Q = d_ws + w.ws; w.ldq = N;
+                continue;
+            }
             const long long sq = t.kind == 0 ? (long long)t.a * t.a : (long long)t.a * t.b;
             const double *computed = d_ws + w.ws + sq;
             if (t.kind == 0) {
@@ -555,24 +613,29 @@ struct DensePrep {
         }
     }
 
-    // copy tasks, work and groups into `host` (pinned or not) laid out as the
-    // device arena's first b_tasks + b_work + b_gs + b_gt bytes
+    // copy tasks, work, groups and the gemmbdcd list into `host` (pinned or
+    // not) laid out as the device arena's first ws_offset() bytes
     void pack(char *host, const hcore_dense_task *tasks) const {
         memcpy(host, tasks, n * sizeof(hcore_dense_task));
         memcpy(host + b_tasks, work.data(), n * sizeof(DenseWork));
         memcpy(host + b_tasks + b_work, gstart.data(), gstart.size() * sizeof(int));
         memcpy(host + b_tasks + b_work + b_gs, gtasks.data(), gtasks.size() * sizeof(int));
+        if (!bdcd.empty())
+            memcpy(host + b_tasks + b_work + b_gs + b_gt, bdcd.data(), bdcd.size() * sizeof(int));
     }
 
     cudaError_t launch(char *arena, cudaStream_t s) const {
         const hcore_dense_task *d_tasks = (const hcore_dense_task *)arena;
         const DenseWork *d_work = (const DenseWork *)(arena + b_tasks);
-        double *d_ws = (double *)(arena + b_tasks + b_work + b_gs + b_gt);
+        double *d_ws = (double *)(arena + ws_offset());
         cudaError_t e = launch_dense_prep(d_tasks, d_work, n, d_ws, s);
+        if (e == cudaSuccess && !bdcd.empty())
+            e = launch_bdcd_prep(d_tasks, d_work, (const int *)(arena + b_tasks + b_work + b_gs + b_gt),
+                                 (int)bdcd.size(), maxN3, maxA3, d_ws, s);
         if (e == cudaSuccess)
             e = launch_dense_tiles(d_tasks, d_work, (const int *)(arena + b_tasks + b_work),
-                                   (const int *)(arena + b_tasks + b_work + b_gs), ngroups(), maxM,
-                                   s);
+                                   (const int *)(arena + b_tasks + b_work + b_gs), ngroups(),
+                                   maxDim, s);
         return e;
     }
 };
@@ -586,16 +649,16 @@ static int run_dense(int n, const hcore_dense_task *tasks, cudaStream_t s, bool 
     if (rc) return rc;
     ThreadCtx &tc = thread_ctx();
     char *arena = (char *)tc.dev_ensure(dp.bytes());
-    char *pin = (char *)tc.pin_ensure(dp.bytes() - dp.b_ws);
+    char *pin = (char *)tc.pin_ensure(dp.ws_offset());
     if (!arena || !pin) {
         set_error("hcore_gpu_dense_batched: out of memory");
         return HCORE_GPU_ENOMEM;
     }
-    dp.bind(tasks, (const double *)(arena + dp.b_tasks + dp.b_work + dp.b_gs + dp.b_gt));
+    dp.bind(tasks, (const double *)(arena + dp.ws_offset()));
     // the previous call on this stream may still read the pinned buffer
     cudaStreamSynchronize(s);
     dp.pack(pin, tasks);
-    cudaMemcpyAsync(arena, pin, dp.bytes() - dp.b_ws, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(arena, pin, dp.ws_offset(), cudaMemcpyHostToDevice, s);
     cudaError_t e = dp.launch(arena, s);
     if (e == cudaSuccess && sync) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
@@ -610,6 +673,43 @@ static void stage(double *dst, const double *src, int rows, int cols, int ld, cu
     if (cols > 0 && rows > 0)
         cudaMemcpy2DAsync(dst, rows * sizeof(double), src, (size_t)ld * sizeof(double),
                           rows * sizeof(double), cols, cudaMemcpyHostToDevice, s);
+}
+
+// the same into dst with leading dimension ldd >= rows
+static void stage_ld(double *dst, int ldd, const double *src, int rows, int cols, int ld,
+                     cudaStream_t s) {
+    if (cols > 0 && rows > 0)
+        cudaMemcpy2DAsync(dst, (size_t)ldd * sizeof(double), src, (size_t)ld * sizeof(double),
+                          rows * sizeof(double), cols, cudaMemcpyHostToDevice, s);
+}
+
+// copy a dense device block (rows x cols, ld rows) back to the caller's host
+// block (ld) and wait for it
+static void unstage(double *dst, int ld, const double *src, int rows, int cols, cudaStream_t s,
+                    const char *fn) {
+    if (rows > 0 && cols > 0)
+        cudaMemcpy2DAsync(dst, (size_t)ld * sizeof(double), src, rows * sizeof(double),
+                          rows * sizeof(double), cols, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) cuda_fatal(fn);
+}
+
+// per-thread device buffer of at least n doubles for the host operands of the
+// dense drop-ins (the dense runner itself uses the thread arena)
+static double *stage_buffer(size_t n, const char *fn) {
+    static thread_local double *buf = nullptr;
+    static thread_local size_t buf_n = 0;
+    if (buf_n < n) {
+        if (buf) {
+            cudaStreamSynchronize(thread_ctx().stream);
+            cudaFree(buf);
+        }
+        buf = nullptr;
+        buf_n = 0;
+        if (cudaMalloc(&buf, std::max<size_t>(n, 1) * sizeof(double)) != cudaSuccess)
+            fatal("%s: cannot allocate %zu bytes of device memory\n", fn, n * sizeof(double));
+        buf_n = n;
+    }
+    return buf;
 }
 
 }  // namespace hc
@@ -765,33 +865,18 @@ void HCORE_dsyrk(HCORE_enum uplo, HCORE_enum trans, int M, int K, double alpha, 
     hcore_dense_task t{};
     t.kind = 0; t.M = M; t.a = K; t.alpha = alpha;
     const bool dev = is_device_memory(AU) && is_device_memory(AV) && is_device_memory(CD);
-    double *stage_cd = nullptr;
     if (dev) {
         t.Au = AU; t.Av = AV; t.lda = LDAU; t.CD = CD; t.ldcd = LDCD;
     } else {
         const size_t nf = (size_t)N * K, nc = (size_t)M * M;
-        // the dense runner uses the thread arena itself; stage into a separate buffer
-        static thread_local double *buf = nullptr;
-        static thread_local size_t buf_n = 0;
-        if (buf_n < 2 * nf + nc) {
-            if (buf) cudaFree(buf);
-            buf = nullptr;
-            buf_n = 0;
-            if (cudaMalloc(&buf, (2 * nf + nc) * sizeof(double)) != cudaSuccess) cuda_fatal("HCORE_dsyrk");
-            buf_n = 2 * nf + nc;
-        }
+        double *buf = stage_buffer(2 * nf + nc, "HCORE_dsyrk");
         stage(buf, AU, N, K, LDAU, tc.stream);
         stage(buf + nf, AV, N, K, LDAU, tc.stream);
         stage(buf + 2 * nf, CD, M, M, LDCD, tc.stream);
         t.Au = buf; t.Av = buf + nf; t.lda = N; t.CD = buf + 2 * nf; t.ldcd = M;
-        stage_cd = buf + 2 * nf;
     }
     if (run_dense(1, &t, tc.stream, true)) fatal("HCORE_dsyrk: %s\n", last_error());
-    if (stage_cd) {
-        cudaMemcpy2DAsync(CD, (size_t)LDCD * sizeof(double), stage_cd, M * sizeof(double),
-                          M * sizeof(double), M, cudaMemcpyDeviceToHost, tc.stream);
-        if (cudaStreamSynchronize(tc.stream) != cudaSuccess) cuda_fatal("HCORE_dsyrk");
-    }
+    if (!dev) unstage(CD, LDCD, t.CD, M, M, tc.stream, "HCORE_dsyrk");
     if (flops)  // hcore_dsyrk.c:104-188
         flops->syrk += flop_counts('m', K, K, N, 0) + flop_counts('m', M, K, K, 0) +
                        flop_counts('m', M, M, K, 0);
@@ -808,21 +893,11 @@ void HCORE_dgemmcd(HCORE_enum transA, HCORE_enum transB, int M, double alpha, do
     t.kind = 1; t.M = M; t.a = Arank; t.b = Brank; t.alpha = -1.0;
     const bool dev = is_device_memory(Au) && is_device_memory(Av) && is_device_memory(Bu) &&
                      is_device_memory(Bv) && is_device_memory(CD);
-    double *stage_cd = nullptr;
     if (dev) {
         t.Au = Au; t.Av = Av; t.Bu = Bu; t.Bv = Bv; t.lda = M; t.ldb = M; t.CD = CD; t.ldcd = M;
     } else {
         const size_t na = (size_t)M * Arank, nb = (size_t)M * Brank, nc = (size_t)M * M;
-        static thread_local double *buf = nullptr;
-        static thread_local size_t buf_n = 0;
-        const size_t need = 2 * na + 2 * nb + nc;
-        if (buf_n < need) {
-            if (buf) cudaFree(buf);
-            buf = nullptr;
-            buf_n = 0;
-            if (cudaMalloc(&buf, need * sizeof(double)) != cudaSuccess) cuda_fatal("HCORE_dgemmcd");
-            buf_n = need;
-        }
+        double *buf = stage_buffer(2 * na + 2 * nb + nc, "HCORE_dgemmcd");
         // every leading dimension is M (hcore_dgemmcd.c:66-99)
         stage(buf, Au, M, Arank, M, tc.stream);
         stage(buf + na, Av, M, Arank, M, tc.stream);
@@ -831,13 +906,84 @@ void HCORE_dgemmcd(HCORE_enum transA, HCORE_enum transB, int M, double alpha, do
         stage(buf + 2 * na + 2 * nb, CD, M, M, M, tc.stream);
         t.Au = buf; t.Av = buf + na; t.Bu = buf + 2 * na; t.Bv = buf + 2 * na + nb;
         t.lda = M; t.ldb = M; t.CD = buf + 2 * na + 2 * nb; t.ldcd = M;
-        stage_cd = t.CD;
     }
     if (run_dense(1, &t, tc.stream, true)) fatal("HCORE_dgemmcd: %s\n", last_error());
-    if (stage_cd) {
-        cudaMemcpyAsync(CD, stage_cd, (size_t)M * M * sizeof(double), cudaMemcpyDeviceToHost, tc.stream);
-        if (cudaStreamSynchronize(tc.stream) != cudaSuccess) cuda_fatal("HCORE_dgemmcd");
+    if (!dev) unstage(CD, M, t.CD, M, M, tc.stream, "HCORE_dgemmcd");
+}
+
+// CD = AU BV^T: M x N from two rank-Ark factors (hcore_duncompress.c:33-84).
+// alpha and beta are not used (the reference passes 1 and 0 to its GEMM) and
+// the two ranks must agree (its assert at :67).
+void HCORE_duncompress(HCORE_enum transA, HCORE_enum transB, int M, int N, double alpha,
+                       double *AU, double *Ark, int LDA, double *BV, double *Brk, int LDB,
+                       double beta, double *CD, int LDC) {
+    (void)transA; (void)transB; (void)alpha; (void)beta;
+    const long long a = (long long)Ark[0], b = (long long)Brk[0];
+    if (a != b) fatal("HCORE_duncompress: Ark (%lld) and Brk (%lld) must be equal\n", a, b);
+    if (M <= 0 || N <= 0) return;
+    ThreadCtx &tc = thread_ctx();
+    hcore_dense_task t{};
+    t.kind = 2; t.M = M; t.N = N; t.a = (int)a;
+    const bool dev = is_device_memory(CD) && (a == 0 || (is_device_memory(AU) && is_device_memory(BV)));
+    if (dev) {
+        t.Au = AU; t.lda = LDA; t.Bv = BV; t.ldb = LDB; t.CD = CD; t.ldcd = LDC;
+    } else {
+        if (LDA < M || LDB < N || LDC < M)
+            fatal("HCORE_duncompress: invalid leading dimension (LDA %d, LDB %d, LDC %d)\n", LDA,
+                  LDB, LDC);
+        const size_t na = (size_t)M * a, nb = (size_t)N * a;
+        double *buf = stage_buffer(na + nb + (size_t)M * N, "HCORE_duncompress");
+        stage(buf, AU, M, (int)a, LDA, tc.stream);
+        stage(buf + na, BV, N, (int)a, LDB, tc.stream);
+        t.Au = buf; t.lda = M; t.Bv = buf + na; t.ldb = N; t.CD = buf + na + nb; t.ldcd = M;
     }
+    if (run_dense(1, &t, tc.stream, true)) fatal("HCORE_duncompress: %s\n", last_error());
+    if (!dev) unstage(CD, LDC, t.CD, M, N, tc.stream, "HCORE_duncompress");
+}
+
+// CD = alpha AU (AV^T BD) + beta CD (hcore_dgemmbdcd.c:35-122).  As in the
+// reference, transA == HCORE_Trans sums AV^T BD over M rows and gives CD LDA
+// rows; otherwise the sum runs over LDB rows and CD has M rows.  Flops:
+// the reference's two GEMM terms (:95-96, :114-115).
+void HCORE_dgemmbdcd(HCORE_enum transA, HCORE_enum transB, int M, int N, double alpha,
+                     double *AU, double *AV, double *Ark, int LDA, double *BD, int LDB,
+                     double beta, double *CD, int LDC, double *work, flop_counter *flops) {
+    (void)transB; (void)work;
+    const long long a = (long long)Ark[0];
+    const bool tr = transA == HCORE_Trans;
+    const int rows = tr ? LDA : M, K = tr ? M : LDB;
+    if (flops)
+        flops->update += flop_counts('m', (unsigned long)a, N, K, 0) +
+                         flop_counts('m', rows, N, (unsigned long)a, 0);
+    // a = 0: the reference hands BLAS a leading dimension of 0 (AVBD, :64),
+    // which it rejects, so CD stays as it was
+    if (rows <= 0 || N <= 0 || a <= 0) return;
+    const int a_eff = K > 0 ? (int)a : 0;  // an empty sum leaves AV^T BD = 0
+    ThreadCtx &tc = thread_ctx();
+    hcore_dense_task t{};
+    t.kind = 3; t.M = rows; t.N = N; t.a = a_eff; t.kdim = std::max(K, 1);
+    t.alpha = alpha; t.beta = beta;
+    const bool dev = is_device_memory(CD) &&
+                     (a_eff == 0 || (is_device_memory(AU) && is_device_memory(AV) &&
+                                     is_device_memory(BD)));
+    if (dev) {
+        t.Au = AU; t.Av = AV; t.lda = LDA; t.Bd = BD; t.ldb = LDB; t.CD = CD; t.ldcd = LDC;
+    } else {
+        if (LDC < rows || (a_eff > 0 && (LDA < std::max(rows, K) || LDB < K)))
+            fatal("HCORE_dgemmbdcd: invalid leading dimension (LDA %d, LDB %d, LDC %d)\n", LDA,
+                  LDB, LDC);
+        const int ld = std::max(rows, K);  // AU and AV share one leading dimension
+        const size_t nf = (size_t)ld * a_eff, nd = (size_t)K * N;
+        double *buf = stage_buffer(2 * nf + nd + (size_t)rows * N, "HCORE_dgemmbdcd");
+        stage_ld(buf, ld, AU, rows, a_eff, LDA, tc.stream);
+        stage_ld(buf + nf, ld, AV, K, a_eff, LDA, tc.stream);
+        if (a_eff) stage(buf + 2 * nf, BD, K, N, LDB, tc.stream);
+        stage(buf + 2 * nf + nd, CD, rows, N, LDC, tc.stream);
+        t.Au = buf; t.Av = buf + nf; t.lda = ld; t.Bd = buf + 2 * nf; t.ldb = K;
+        t.CD = buf + 2 * nf + nd; t.ldcd = rows;
+    }
+    if (run_dense(1, &t, tc.stream, true)) fatal("HCORE_dgemmbdcd: %s\n", last_error());
+    if (!dev) unstage(CD, LDC, t.CD, rows, N, tc.stream, "HCORE_dgemmbdcd");
 }
 
 }  // extern "C"
@@ -897,18 +1043,22 @@ void HCORE_sgemm_dense(HCORE_enum transA, int transB, int M, int N, int K, float
 static int translate_dense(int n, const hcore_dense_task *tasks, std::vector<hcore_dense_task> &tt) {
     tt.assign(tasks, tasks + n);
     for (auto &t : tt) {
-        t.Au = (const double *)device_alias(t.Au);
-        t.Av = (const double *)device_alias(t.Av);
-        if (t.kind == 1) {
-            t.Bu = (const double *)device_alias(t.Bu);
-            t.Bv = (const double *)device_alias(t.Bv);
-            if (!t.Bu || !t.Bv) {
-                set_error("hcore_gpu_dense_batched: B factors are not device-accessible");
-                return HCORE_GPU_EINVAL;
-            }
-        }
+        // only the pointers each kind reads (hcore_dense_task in hcore_gb300.h)
+        const bool uses_av = t.kind != 2, uses_b = t.kind == 1, uses_bv = t.kind == 1 || t.kind == 2;
+        const bool factors = t.kind <= 1 || t.a > 0;
+        bool ok = true;
+        auto tr = [&](const double *&p, bool used) {
+            if (!used) return;
+            p = (const double *)device_alias(p);
+            ok = ok && p != nullptr;
+        };
+        tr(t.Au, factors);
+        tr(t.Av, factors && uses_av);
+        tr(t.Bu, uses_b);
+        tr(t.Bv, factors && uses_bv);
+        tr(t.Bd, t.kind == 3 && t.a > 0);
         t.CD = (double *)device_alias(t.CD);
-        if (!t.Au || !t.Av || !t.CD) {
+        if (!ok || !t.CD) {
             set_error("hcore_gpu_dense_batched: pointers must be device or pinned memory");
             return HCORE_GPU_EINVAL;
         }
@@ -957,9 +1107,8 @@ int hcore_gpu_dense_plan_create(hcore_gpu_dense_plan *plan, int n, const hcore_d
         delete p;
         return HCORE_GPU_ENOMEM;
     }
-    p->prep.bind(tt.data(), (const double *)(p->arena + p->prep.b_tasks + p->prep.b_work +
-                                             p->prep.b_gs + p->prep.b_gt));
-    std::vector<char> host(p->prep.bytes() - p->prep.b_ws);
+    p->prep.bind(tt.data(), (const double *)(p->arena + p->prep.ws_offset()));
+    std::vector<char> host(p->prep.ws_offset());
     p->prep.pack(host.data(), tt.data());
     if (cudaMemcpy(p->arena, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
         set_error("hcore_gpu_dense_plan_create: upload failed");

@@ -122,17 +122,22 @@ cudaError_t launch_rebuild(const Desc *d_desc, const int *d_idx, const int *d_ca
 // dense-C updates (hc_dense.cu): per-task rank-K' form coef * P Q^T
 struct DenseWork {
     const double *P;  // M x K' (ldp): computed into the workspace, or an input factor
-    const double *Q;  // M x K' (ldq)
+    const double *Q;  // N x K' (ldq)
     int ldp, ldq, kk;
-    double coef;
+    double coef;      // CD = beta CD + coef P Q^T
+    double beta;
     int syrk;         // 1: zero the strict upper triangle after this task
     long long ws;     // workspace offset (doubles): S (p x q), then the computed factor
 };
 cudaError_t launch_dense_prep(const hcore_dense_task *d_tasks, const DenseWork *d_work, int n,
                               double *ws, cudaStream_t s);
+// Q = Bd^T Av (N x a) of the gemmbdcd tasks listed in d_idx
+cudaError_t launch_bdcd_prep(const hcore_dense_task *d_tasks, const DenseWork *d_work,
+                             const int *d_idx, int n_idx, int maxN, int maxA, double *ws,
+                             cudaStream_t s);
 cudaError_t launch_dense_tiles(const hcore_dense_task *d_tasks, const DenseWork *d_work,
                                const int *d_group_start, const int *d_group_tasks, int ngroups,
-                               int maxM, cudaStream_t s);
+                               int maxDim, cudaStream_t s);
 template <typename T>
 cudaError_t launch_gemm_dense(int ta, int tb, int M, int N, int K, T alpha, const T *A, int lda,
                               const T *B, int ldb, T beta, T *C, int ldc, cudaStream_t s);

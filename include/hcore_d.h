@@ -32,6 +32,9 @@ extern int syrk_print_index;
 extern int gemmcd_print_index;
 extern int gemmcd_print_mat;
 extern int gemmcd_use_scratch;
+/* hcore_dgemmbdcd.c:25-26 */
+extern int gemmbdcd_print_index;
+extern int gemmbdcd_print_mat;
 
 /* C = beta*C + alpha*A*B^T with A, B, C low rank, then recompression.
  * Replaces src/include/hcore_d.h:25-46 (src/compute/hcore_dgemm.c:703-1012).
@@ -103,6 +106,33 @@ void HCORE_dgemm_ormqr(int transA, int transB, int M, int N, double alpha, doubl
                        int CV_ncols, double *newV, int ld_newV, double *qrtauB,
                        int use_CUV_clone, double *CUclone, int ld_CUclone, double *_CU_save,
                        double *CVclone, int ld_CVclone, double *_CV_save);
+
+/* CD = alpha*AU*(AV^T*BD) + beta*CD, a low-rank A times a dense B.  With
+ * transA == HCORE_Trans the product AV^T*BD sums over M rows and CD has LDA
+ * rows; otherwise it sums over LDB rows and CD has M rows.  Replaces
+ * src/include/hcore_d.h:87-101 (src/compute/hcore_dgemmbdcd.c:35-122). */
+void HCORE_dgemmbdcd(HCORE_enum transA, HCORE_enum transB, int M, int N, double alpha,
+                     double *AU, double *AV, double *Ark, int LDA, double *BD, int LDB,
+                     double beta, double *CD, int LDC, double *work, flop_counter *flops);
+
+/* CD = AU*BV^T (M x N) from factors of rank Ark == Brk; alpha and beta are
+ * not used.  Replaces src/include/hcore_d.h:126-139
+ * (src/compute/hcore_duncompress.c:33-84). */
+void HCORE_duncompress(HCORE_enum transA, HCORE_enum transB, int M, int N, double alpha,
+                       double *AU, double *Ark, int LDA, double *BV, double *Brk, int LDB,
+                       double beta, double *CD, int LDC);
+
+/* Triangular solve on a factor: cblas_dtrsm(ColMajor, side, uplo, transA,
+ * diag, M, Brank, alpha, A, LDA, BV, LDBV).  Replaces
+ * src/include/hcore_d.h:117-125 (src/compute/hcore_dtrsm.c:24-48). */
+void HCORE_dtrsm(HCORE_enum side, HCORE_enum uplo, HCORE_enum transA, HCORE_enum diag, int M,
+                 int Brank, double alpha, double *A, int LDA, double *BV, int LDBV,
+                 flop_counter *flops);
+
+/* Cholesky factorization of a dense tile: *info = LAPACKE_dpotrf_work(
+ * LAPACK_COL_MAJOR, uplo, N, A, LDA), uplo being LAPACK's 'L' or 'U'.
+ * Replaces src/include/hcore_d.h:102-106 (src/compute/hcore_dpotrf.c:23-34). */
+void HCORE_dpotrf(HCORE_enum uplo, int N, double *A, int LDA, int *info, flop_counter *flops);
 
 /* Plain dense C = alpha*op(A)*op(B) + beta*C.  Replaces
  * src/include/hcore_d.h:269-278 (src/compute/hcore_dgemm.c:1701-1715). */

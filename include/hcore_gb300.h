@@ -182,23 +182,33 @@ int hcore_gpu_dgemm_batched(int n, const hcore_lr_task *tasks, int *ranks, int *
 int hcore_gpu_sgemm_batched(int n, const hcore_lr_task *tasks, int *ranks, int *status,
                             void *stream);
 
-/* Dense-C updates (HCORE_dsyrk / HCORE_dgemmcd semantics) batched over
- * output tiles.  Each task adds to one dense M x M tile CD (ld ldcd):
- *   kind 0 (syrk):   CD += alpha * U (V^T V) U^T, strict upper set to 0
- *   kind 1 (gemmcd): CD -= Au (Av^T Bv) Bu^T
+/* Dense-C tile operations batched over output tiles.  Each task writes one
+ * dense M x N tile CD (ld ldcd; N = 0 means N = M):
+ *   kind 0 (syrk, HCORE_dsyrk):       CD += alpha * Au (Av^T Av) Au^T, strict
+ *                                     upper set to 0 (N = M)
+ *   kind 1 (gemmcd, HCORE_dgemmcd):   CD -= Au (Av^T Bv) Bu^T (N = M)
+ *   kind 2 (uncompress, HCORE_duncompress): CD = Au Bv^T, Au M x a (lda),
+ *                                     Bv N x a (ldb); alpha and beta unused
+ *   kind 3 (gemmbdcd, HCORE_dgemmbdcd): CD = alpha Au (Av^T Bd) + beta CD,
+ *                                     Au M x a (lda), Av kdim x a (lda),
+ *                                     Bd kdim x N (ldb); kdim = 0 means M
  * Tasks that share a CD are applied in list order by one CTA group, so the
  * result is that of running them one after another. */
 typedef struct hcore_dense_task {
     int kind;
     int M;
-    int a, b;             /* ranks (b unused for syrk) */
+    int a, b;             /* ranks (b: gemmcd only) */
     double alpha;
     const double *Au, *Av;
     int lda;              /* leading dimension of Au/Av (syrk: also the row count of Av) */
     const double *Bu, *Bv;
-    int ldb;
+    int ldb;              /* leading dimension of Bu/Bv, or of Bd */
     double *CD;
     int ldcd;
+    int N;                /* columns of CD (0: M) */
+    double beta;          /* gemmbdcd only */
+    int kdim;             /* gemmbdcd: rows of Av and Bd (0: M) */
+    const double *Bd;     /* gemmbdcd: dense B */
 } hcore_dense_task;
 
 int hcore_gpu_dense_batched(int n, const hcore_dense_task *tasks, void *stream);
@@ -209,6 +219,39 @@ typedef struct hcore_gpu_dense_plan_s *hcore_gpu_dense_plan;
 int hcore_gpu_dense_plan_create(hcore_gpu_dense_plan *plan, int n, const hcore_dense_task *tasks);
 int hcore_gpu_dense_plan_execute(hcore_gpu_dense_plan plan, void *stream);
 int hcore_gpu_dense_plan_destroy(hcore_gpu_dense_plan plan);
+
+/* Triangular solves with many right-hand sides (HCORE_dtrsm semantics,
+ * cblas_dtrsm column-major): B = alpha op(A)^-1 B (side HCORE_Left, A M x M)
+ * or B = alpha B op(A)^-1 (HCORE_Right, A N x N), B M x N.  side, uplo,
+ * trans and diag take the HCORE_/CBLAS enum values.  In a TLR Cholesky each
+ * task is one V factor of a panel (Left, Lower, NoTrans, M = nb, N = its
+ * rank) and all tasks share the diagonal tile's factor A.  Synchronous. */
+typedef struct hcore_trsm_task {
+    int side, uplo, trans, diag;
+    int M, N;
+    double alpha;
+    const double *A;
+    int lda;
+    double *B;
+    int ldb;
+} hcore_trsm_task;
+int hcore_gpu_trsm_batched(int n, const hcore_trsm_task *tasks, void *stream);
+
+/* Cholesky factorization of dense tiles (HCORE_dpotrf semantics: LAPACK's
+ * dpotrf through LAPACKE_dpotrf_work).  uplo is LAPACK's character, 'L'
+ * (A = L L^T, lower triangle overwritten) or 'U' (A = U^T U, upper); the
+ * other triangle is not touched.  info[i] (host array) receives
+ * LAPACKE_dpotrf_work's value: 0, -2/-3/-5 for a bad uplo/n/lda, or j > 0
+ * when the leading minor of order j is not positive definite (the failing
+ * pivot is left in A(j-1, j-1), and the factorization stops there).
+ * Synchronous. */
+typedef struct hcore_potrf_task {
+    int uplo;
+    int n;
+    double *A;
+    int lda;
+} hcore_potrf_task;
+int hcore_gpu_potrf_batched(int n, const hcore_potrf_task *tasks, int *info, void *stream);
 
 /* measured FP64 tensor-pipe (DMMA m16n8k16) throughput of this GPU in
  * TFLOP/s, timed on `stream` (about 0.1 s); the roofline denominator of the

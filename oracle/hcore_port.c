@@ -101,3 +101,56 @@ int port_dlatms(int m, int n, char dist, int *iseed, char sym, double *d, int mo
 #undef PFX
 #undef LAPACKE_
 #undef cblas_
+
+/* ---- the tile steps either side of the update (FP64 only, as in the
+ * reference): the same BLAS/LAPACK calls in the same order ---- */
+void scipy_cblas_dtrsm(int, int, int, int, int, int, int, double, const double *, int,
+                       double *, int);
+int scipy_LAPACKE_dpotrf_work(int, char, int, double *, int);
+
+/* HCORE_duncompress (src/compute/hcore_duncompress.c:33-84): CD = AU BV^T */
+void port_duncompress(int M, int N, const double *AU, int a, int LDA, const double *BV, int LDB,
+                      double *CD, int LDC)
+{
+    scipy_cblas_dgemm(CblasColMajor, CblasNoTrans, CblasTrans, M, N, a, 1.0, AU, LDA, BV, LDB,
+                      0.0, CD, LDC);
+}
+
+/* HCORE_dgemmbdcd (src/compute/hcore_dgemmbdcd.c:35-122): AVBD = AV^T BD
+ * (a x N, ld a) over K = M rows (transA == Trans) or LDB rows, then
+ * CD = alpha AU AVBD + beta CD with LDA (Trans) or M rows.  With a = 0 the
+ * reference's GEMMs get a leading dimension of 0, which BLAS rejects, so CD
+ * stays as it was. */
+void port_dgemmbdcd(int transA, int M, int N, double alpha, const double *AU, const double *AV,
+                    int a, int LDA, const double *BD, int LDB, double beta, double *CD, int LDC,
+                    unsigned long *flops_update)
+{
+    const int tr = transA == CblasTrans;
+    const int K = tr ? M : LDB, rows = tr ? LDA : M;
+    if (a > 0) {
+        double *AVBD = malloc((size_t)a * (N > 0 ? N : 1) * sizeof(double));
+        scipy_cblas_dgemm(CblasColMajor, CblasTrans, CblasNoTrans, a, N, K, 1.0, AV, LDA, BD,
+                          LDB, 0.0, AVBD, a);
+        scipy_cblas_dgemm(CblasColMajor, CblasNoTrans, CblasNoTrans, rows, N, a, alpha, AU, LDA,
+                          AVBD, a, beta, CD, LDC);
+        free(AVBD);
+    }
+    if (flops_update)
+        *flops_update += port_flop_counts('m', a, N, K, 0) + port_flop_counts('m', rows, N, a, 0);
+}
+
+/* HCORE_dtrsm (src/compute/hcore_dtrsm.c:24-48) */
+void port_dtrsm(int side, int uplo, int transA, int diag, int M, int Brank, double alpha,
+                const double *A, int LDA, double *BV, int LDBV, unsigned long *flops_trsm)
+{
+    scipy_cblas_dtrsm(CblasColMajor, side, uplo, transA, diag, M, Brank, alpha, A, LDA, BV, LDBV);
+    if (flops_trsm) *flops_trsm += port_flop_counts('t', M, Brank, side == 141 ? 1 : 2, 0);
+}
+
+/* HCORE_dpotrf (src/compute/hcore_dpotrf.c:23-34) */
+int port_dpotrf(int uplo, int N, double *A, int LDA, unsigned long *flops_potrf)
+{
+    const int info = scipy_LAPACKE_dpotrf_work(LAPACK_COL_MAJOR, (char)uplo, N, A, LDA);
+    if (flops_potrf) *flops_potrf += port_flop_counts('c', N, 0, 0, 0);
+    return info;
+}

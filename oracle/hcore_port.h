@@ -35,4 +35,12 @@ int port_dsyrk(int M, int K, double alpha, const double *AU, int LDAU, const dou
                double *CD, int LDCD, unsigned long *flops_syrk);
 int port_dgemmcd(int M, const double *Au, const double *Av, int Arank, const double *Bu,
                  const double *Bv, int Brank, double *CD);
+void port_duncompress(int M, int N, const double *AU, int a, int LDA, const double *BV, int LDB,
+                      double *CD, int LDC);
+void port_dgemmbdcd(int transA, int M, int N, double alpha, const double *AU, const double *AV,
+                    int a, int LDA, const double *BD, int LDB, double beta, double *CD, int LDC,
+                    unsigned long *flops_update);
+void port_dtrsm(int side, int uplo, int transA, int diag, int M, int Brank, double alpha,
+                const double *A, int LDA, double *BV, int LDBV, unsigned long *flops_trsm);
+int port_dpotrf(int uplo, int N, double *A, int LDA, unsigned long *flops_potrf);
 #endif

@@ -73,6 +73,17 @@ class Port:
                               rp, _ulp]
             lib.port_dsyrk.argtypes = [C.c_int, C.c_int, C.c_double, _dp, C.c_int, _dp, _dp, C.c_int, _ulp]
             lib.port_dgemmcd.argtypes = [C.c_int, _dp, _dp, C.c_int, _dp, _dp, C.c_int, _dp]
+            lib.port_duncompress.restype = None
+            lib.port_duncompress.argtypes = [C.c_int, C.c_int, _dp, C.c_int, C.c_int, _dp, C.c_int,
+                                             _dp, C.c_int]
+            lib.port_dgemmbdcd.restype = None
+            lib.port_dgemmbdcd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_int,
+                                           C.c_int, _dp, C.c_int, C.c_double, _dp, C.c_int, _ulp]
+            lib.port_dtrsm.restype = None
+            lib.port_dtrsm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_double, _dp, C.c_int, _dp, C.c_int, _ulp]
+            lib.port_dpotrf.restype = C.c_int
+            lib.port_dpotrf.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ulp]
             lib.port_dlatms.argtypes = [C.c_int, C.c_int, C.c_char, _ip, C.c_char, _dp, C.c_int,
                                         C.c_double, C.c_double, C.c_int, C.c_int, C.c_char, _dp,
                                         C.c_int]
@@ -134,6 +145,37 @@ class Port:
         self.lib.port_dgemmcd(M, _ptr(Au), _ptr(Av), Arank, _ptr(Bu), _ptr(Bv), Brank, _ptr(CDo))
         return CDo
 
+    def duncompress(self, M, N, AU, a, BV, CD):
+        AU, BV = fortran(AU), fortran(BV)
+        CDo = fortran(CD).copy(order="F")
+        self.lib.port_duncompress(M, N, _ptr(AU), a, AU.shape[0], _ptr(BV), BV.shape[0], _ptr(CDo),
+                                  CDo.shape[0])
+        return CDo
+
+    def dgemmbdcd(self, transA, M, N, alpha, AU, AV, a, BD, beta, CD):
+        """AU and AV share one leading dimension (their row count)."""
+        AU, AV, BD = fortran(AU), fortran(AV), fortran(BD)
+        assert AU.shape[0] == AV.shape[0]
+        CDo = fortran(CD).copy(order="F")
+        fl = C.c_ulong(0)
+        self.lib.port_dgemmbdcd(transA, M, N, alpha, _ptr(AU), _ptr(AV), a, AU.shape[0], _ptr(BD),
+                                BD.shape[0], beta, _ptr(CDo), CDo.shape[0], C.byref(fl))
+        return CDo, fl.value
+
+    def dtrsm(self, side, uplo, trans, diag, M, N, alpha, A, B):
+        A = fortran(A)
+        Bo = fortran(B).copy(order="F")
+        fl = C.c_ulong(0)
+        self.lib.port_dtrsm(side, uplo, trans, diag, M, N, alpha, _ptr(A), A.shape[0], _ptr(Bo),
+                            Bo.shape[0], C.byref(fl))
+        return Bo, fl.value
+
+    def dpotrf(self, uplo, N, A):
+        Ao = fortran(A).copy(order="F")
+        fl = C.c_ulong(0)
+        info = self.lib.port_dpotrf(uplo, N, _ptr(Ao), Ao.shape[0], C.byref(fl))
+        return Ao, info, fl.value
+
     def dlatms(self, m, n, iseed, d, ld):
         """LAPACKE_dlatms(m, n, 'U', iseed, 'N', d, mode=0, cond=-1, dmax=-1,
         kl=m-1, ku=n-1, 'N') as called at testing/testing_dgemm.c:159."""
@@ -184,6 +226,21 @@ class RefLib:
             lib.HCORE_dgemmcd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_int,
                                           C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_double, _dp,
                                           C.c_int, C.c_int, _dp, C.POINTER(FlopCounter)]
+            lib.HCORE_duncompress.restype = None
+            lib.HCORE_duncompress.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp,
+                                              _dp, C.c_int, _dp, _dp, C.c_int, C.c_double, _dp,
+                                              C.c_int]
+            lib.HCORE_dgemmbdcd.restype = None
+            lib.HCORE_dgemmbdcd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp,
+                                            _dp, _dp, C.c_int, _dp, C.c_int, C.c_double, _dp,
+                                            C.c_int, _dp, C.POINTER(FlopCounter)]
+            lib.HCORE_dtrsm.restype = None
+            lib.HCORE_dtrsm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        C.c_double, _dp, C.c_int, _dp, C.c_int,
+                                        C.POINTER(FlopCounter)]
+            lib.HCORE_dpotrf.restype = None
+            lib.HCORE_dpotrf.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip,
+                                         C.POINTER(FlopCounter)]
             RefLib._lib = lib
         self.lib = RefLib._lib
 
@@ -239,6 +296,39 @@ class RefLib:
         self.lib.HCORE_dgemmcd(111, 112, M, -1.0, _ptr(Au), _ptr(Av), Arank, M, _ptr(Bu),
                                _ptr(Bv), Brank, M, 1.0, _ptr(CDo), M, maxrank, None, C.byref(fc))
         return CDo
+
+    def duncompress(self, M, N, AU, a, BV, CD):
+        AU, BV = fortran(AU), fortran(BV)
+        CDo = fortran(CD).copy(order="F")
+        ra = np.array([a], dtype=np.float64)
+        self.lib.HCORE_duncompress(111, 112, M, N, 1.0, _ptr(AU), _ptr(ra), AU.shape[0], _ptr(BV),
+                                   _ptr(ra), BV.shape[0], 0.0, _ptr(CDo), CDo.shape[0])
+        return CDo
+
+    def dgemmbdcd(self, transA, M, N, alpha, AU, AV, a, BD, beta, CD):
+        AU, AV, BD = fortran(AU), fortran(AV), fortran(BD)
+        CDo = fortran(CD).copy(order="F")
+        ra = np.array([a], dtype=np.float64)
+        fc = FlopCounter()
+        self.lib.HCORE_dgemmbdcd(transA, 111, M, N, alpha, _ptr(AU), _ptr(AV), _ptr(ra), AU.shape[0],
+                                 _ptr(BD), BD.shape[0], beta, _ptr(CDo), CDo.shape[0], None,
+                                 C.byref(fc))
+        return CDo, fc.update
+
+    def dtrsm(self, side, uplo, trans, diag, M, N, alpha, A, B):
+        A = fortran(A)
+        Bo = fortran(B).copy(order="F")
+        fc = FlopCounter()
+        self.lib.HCORE_dtrsm(side, uplo, trans, diag, M, N, alpha, _ptr(A), A.shape[0], _ptr(Bo),
+                             Bo.shape[0], C.byref(fc))
+        return Bo, fc.trsm
+
+    def dpotrf(self, uplo, N, A):
+        Ao = fortran(A).copy(order="F")
+        info = C.c_int(0)
+        fc = FlopCounter()
+        self.lib.HCORE_dpotrf(uplo, N, _ptr(Ao), Ao.shape[0], C.byref(info), C.byref(fc))
+        return Ao, info.value, fc.potrf
 
 
 # --------------------------------------------------------------------------

@@ -58,6 +58,19 @@ def golden():
 
 
 @pytest.fixture(scope="session")
+def golden_tlr():
+    """Reference outputs of HCORE_duncompress / dgemmbdcd / dtrsm / dpotrf."""
+    import json
+
+    import numpy as np
+
+    d = os.path.join(ROOT, "tests", "golden")
+    with open(os.path.join(d, "golden_tlr_meta.json")) as f:
+        meta = json.load(f)
+    return meta, dict(np.load(os.path.join(d, "golden_tlr.npz")))
+
+
+@pytest.fixture(scope="session")
 def hc():
     """The GPU library, built if absent (the GPU machine builds it via build())."""
     import hcore_gb300

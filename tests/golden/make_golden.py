@@ -13,7 +13,12 @@ through ctypes on seeded inputs.  The outputs are committed as
   (rank, Frobenius norm, (CU CV^T) @ Omega for a seeded Omega), since its
   inputs regenerate from the seed.
 
-Usage:  python tests/golden/make_golden.py
+* ``golden_tlr.npz`` / ``golden_tlr_meta.json`` — the same for the tile
+  steps around the update: HCORE_duncompress, HCORE_dgemmbdcd, HCORE_dtrsm
+  (every side/uplo/trans/diag) and HCORE_dpotrf (both triangles, a failing
+  pivot, an invalid uplo).
+
+Usage:  python tests/golden/make_golden.py [--tlr-only]
 """
 from __future__ import annotations
 
@@ -180,5 +185,90 @@ def main():
           os.path.getsize(os.path.join(OUT, "golden_small.npz")))
 
 
+def tlr_spd(rng, n):
+    """Seeded symmetric positive definite n x n (well conditioned)."""
+    X = rng.standard_normal((n, n))
+    return np.asfortranarray(X @ X.T / n + np.eye(n))
+
+
+def tlr_triangle(rng, n, uplo):
+    """Seeded triangular n x n, diagonal in [2, 3] with random signs, the
+    unused triangle NaN (BLAS must not read it)."""
+    T = rng.uniform(-0.5, 0.5, (n, n)) / np.sqrt(n)
+    np.fill_diagonal(T, rng.uniform(2, 3, n) * rng.choice([-1.0, 1.0], n))
+    keep = np.tril(np.ones((n, n), bool)) if uplo == 122 else np.triu(np.ones((n, n), bool))
+    return np.asfortranarray(np.where(keep, T, np.nan))
+
+
+def make_tlr():
+    """Fixtures of HCORE_duncompress, HCORE_dgemmbdcd, HCORE_dtrsm and
+    HCORE_dpotrf (golden_tlr.npz / golden_tlr_meta.json)."""
+    ref = O.RefLib()
+    meta = {"uncompress": [], "gemmbdcd": [], "trsm": [], "potrf": []}
+    arrs = {}
+    for i, (M, N, a) in enumerate([(64, 48, 6), (40, 40, 0)]):
+        rng = np.random.default_rng(500 + i)
+        AU = np.asfortranarray(rng.standard_normal((M, a)))
+        BV = np.asfortranarray(rng.standard_normal((N, a)))
+        CD = np.asfortranarray(rng.standard_normal((M, N)))
+        name = f"unc{i}"
+        arrs.update({f"{name}_AU": AU, f"{name}_BV": BV, f"{name}_CD": CD,
+                     f"{name}_CDo": ref.duncompress(M, N, AU, a, BV, CD)})
+        meta["uncompress"].append(dict(name=name, M=M, N=N, a=a))
+    # (transA, M, N, a, LDA, LDB, LDC): LDB > M and LDA > M exercise the two
+    # branches' row counts (hcore_dgemmbdcd.c:78-117)
+    for i, (tr, M, N, a, lda, ldb, ldc) in enumerate([(111, 64, 40, 9, 64, 64, 64),
+                                                      (112, 64, 40, 9, 64, 64, 64),
+                                                      (111, 48, 33, 7, 60, 56, 50),
+                                                      (112, 48, 33, 7, 52, 48, 52)]):
+        rng = np.random.default_rng(600 + i)
+        AU = np.asfortranarray(rng.standard_normal((lda, a)))
+        AV = np.asfortranarray(rng.standard_normal((lda, a)))
+        BD = np.asfortranarray(rng.standard_normal((ldb, N)))
+        CD = np.asfortranarray(rng.standard_normal((ldc, N)))
+        CDo, fl = ref.dgemmbdcd(tr, M, N, 0.7, AU, AV, a, BD, -1.3, CD)
+        name = f"bdcd{i}"
+        arrs.update({f"{name}_AU": AU, f"{name}_AV": AV, f"{name}_BD": BD, f"{name}_CD": CD,
+                     f"{name}_CDo": CDo})
+        meta["gemmbdcd"].append(dict(name=name, transA=tr, M=M, N=N, a=a, alpha=0.7, beta=-1.3,
+                                     flops=fl))
+    i = 0
+    for side in (141, 142):
+        for uplo in (121, 122):
+            for tr in (111, 112):
+                for dg in (131, 132):
+                    rng = np.random.default_rng(700 + i)
+                    M, N = 40, 7
+                    na = M if side == 141 else N
+                    A = tlr_triangle(rng, na, uplo)
+                    B = np.asfortranarray(rng.standard_normal((M, N)))
+                    Bo, fl = ref.dtrsm(side, uplo, tr, dg, M, N, 0.5, A, B)
+                    name = f"trsm{i}"
+                    arrs.update({f"{name}_A": A, f"{name}_B": B, f"{name}_Bo": Bo})
+                    meta["trsm"].append(dict(name=name, side=side, uplo=uplo, trans=tr, diag=dg,
+                                             M=M, N=N, alpha=0.5, flops=fl))
+                    i += 1
+    for i, (uplo, n, fail_at) in enumerate([(ord("L"), 100, None), (ord("U"), 70, None),
+                                            (ord("L"), 40, 11), (122, 20, None)]):
+        rng = np.random.default_rng(800 + i)
+        S = tlr_spd(rng, n)
+        if fail_at is not None:
+            S[fail_at - 1, fail_at - 1] = -5.0
+        # the triangle dpotrf must not read
+        other = np.triu(np.ones((n, n), bool), 1) if uplo != ord("U") else np.tril(np.ones((n, n), bool), -1)
+        S = np.asfortranarray(np.where(other, np.nan, S))
+        So, info, fl = ref.dpotrf(uplo, n, S)
+        name = f"potrf{i}"
+        arrs.update({f"{name}_A": S, f"{name}_Ao": So})
+        meta["potrf"].append(dict(name=name, uplo=uplo, n=n, info=info, flops=fl))
+    np.savez_compressed(os.path.join(OUT, "golden_tlr.npz"), **arrs)
+    with open(os.path.join(OUT, "golden_tlr_meta.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print("tlr cases:", {k: len(v) for k, v in meta.items()}, "size:",
+          os.path.getsize(os.path.join(OUT, "golden_tlr.npz")))
+
+
 if __name__ == "__main__":
-    main()
+    if "--tlr-only" not in sys.argv:
+        main()
+    make_tlr()

@@ -123,3 +123,58 @@ def test_flop_model_matches_reference_formula(port):
            port.flop_counts("m", M, a, b) + port.flop_counts("s", k) + r * k +
            port.flop_counts("o", M, r, k, 1) + port.flop_counts("o", r, M, k, 2))
     assert tot == 27634720
+
+
+# ---- the tile steps around the update (golden_tlr.npz) ----
+
+def _close(x, y, tol=1e-13):
+    """Equal NaN pattern; finite entries within tol relative to max |y|."""
+    x, y = np.asarray(x), np.asarray(y)
+    assert np.array_equal(np.isnan(x), np.isnan(y))
+    f = ~np.isnan(y)
+    scale = max(np.abs(y[f]).max(), 1.0) if f.any() else 1.0
+    assert np.abs(x[f] - y[f]).max(initial=0.0) <= tol * scale
+
+
+def test_port_duncompress_matches_reference(port, golden_tlr):
+    meta, g = golden_tlr
+    for c in meta["uncompress"]:
+        n = c["name"]
+        out = port.duncompress(c["M"], c["N"], g[f"{n}_AU"], c["a"], g[f"{n}_BV"], g[f"{n}_CD"])
+        _close(out, g[f"{n}_CDo"])
+
+
+def test_port_dgemmbdcd_matches_reference(port, golden_tlr):
+    meta, g = golden_tlr
+    for c in meta["gemmbdcd"]:
+        n = c["name"]
+        out, fl = port.dgemmbdcd(c["transA"], c["M"], c["N"], c["alpha"], g[f"{n}_AU"],
+                                 g[f"{n}_AV"], c["a"], g[f"{n}_BD"], c["beta"], g[f"{n}_CD"])
+        _close(out, g[f"{n}_CDo"])
+        assert fl == c["flops"]
+
+
+def test_port_dtrsm_matches_reference(port, golden_tlr):
+    """Every side/uplo/trans/diag; the unused triangle of A is NaN."""
+    meta, g = golden_tlr
+    assert len(meta["trsm"]) == 16
+    for c in meta["trsm"]:
+        n = c["name"]
+        out, fl = port.dtrsm(c["side"], c["uplo"], c["trans"], c["diag"], c["M"], c["N"],
+                             c["alpha"], g[f"{n}_A"], g[f"{n}_B"])
+        _close(out, g[f"{n}_Bo"], 1e-12)
+        assert fl == c["flops"]
+
+
+def test_port_dpotrf_matches_reference(port, golden_tlr):
+    """Both triangles, a failing pivot (info 11) and uplo = HCORE_Lower, which
+    LAPACKE rejects (info -2): the reference passes uplo through as a char."""
+    meta, g = golden_tlr
+    infos = []
+    for c in meta["potrf"]:
+        n = c["name"]
+        out, info, fl = port.dpotrf(c["uplo"], c["n"], g[f"{n}_A"])
+        assert info == c["info"] and fl == c["flops"]
+        _close(out, g[f"{n}_Ao"], 1e-12)
+        infos.append(info)
+    assert infos == [0, 0, 11, -2]
