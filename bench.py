@@ -49,10 +49,11 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="panel", choices=["panel", "precision", "dense", "predictor"],
+    p.add_argument("--workload", default="panel", choices=["panel", "precision", "dense", "predictor", "tlr"],
                    help="panel: the headline (config 2); precision: acc sweep (config 3); "
                         "dense: batched dsyrk/dgemmcd tile updates (config 4); predictor: "
-                        "learned rank predictor on 3D exponential-kernel sweeps (config 5)")
+                        "learned rank predictor on 3D exponential-kernel sweeps (config 5); "
+                        "tlr: batched POTRF + TRSM, the steps either side of the update")
     p.add_argument("--max-updates", type=int, default=None, help="truncate the update list")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -1232,6 +1233,135 @@ def fp64_peak(L, torch, dev) -> float:
     return float(L.hcore_gpu_fp64_peak(torch.cuda.current_stream(dev).cuda_stream))
 
 
+def run_tlr(args):
+    """The steps either side of the Schur update in a TLR Cholesky, on the
+    panel workload's tiles: HCORE_dpotrf of the 64 diagonal 1024 x 1024
+    covariance tiles (a nugget of 1 on the diagonal keeps them well
+    conditioned) in one batched call, then HCORE_dtrsm V <- L_k^-1 V of the
+    panel's 63 V factors (all their columns as right-hand sides) against
+    each of the 64 factors, one batched call.  One panel step = one POTRF +
+    one panel TRSM; a timed step runs all 64 of them."""
+    import numpy as np
+    import torch
+
+    import hcore_gb300 as hc
+    from hcore_gb300 import build as hbuild
+    from hcore_gb300 import panel as pnl
+    from oracle import oracle as O
+
+    rank, world, local = dist_init()
+    if not os.path.exists(hbuild.LIB):
+        hbuild.build()
+    hc.lib()
+    dev = torch.device("cuda", local)
+    panel = pnl.build_panel(device=str(dev), max_updates=1)
+    nb, T = panel.nb, panel.ntiles
+    P = torch.from_numpy(pnl.morton_points(WORKLOAD["points"], 2, 0)).to(dev)
+
+    def ktile(i):
+        X = P[i * nb:(i + 1) * nb]
+        d2 = (X * X).sum(1)[:, None] + (X * X).sum(1)[None, :] - 2.0 * X @ X.T
+        return torch.exp(-torch.clamp(d2, min=0.0) / 0.01) + torch.eye(nb, dtype=torch.float64, device=dev)
+
+    D0 = torch.stack([ktile(i) for i in range(T)])          # symmetric: storage order is moot
+    D = D0.clone()
+    # the panel's V factors, all columns: column-major nb x R (tensor R x nb)
+    V0 = torch.cat([panel.V[int(panel.offset[panel.index[(j, 0)]]):int(panel.offset[panel.index[(j, 0)] + 1])]
+                    .view(-1, nb) for j in range(1, T)], 0)
+    R = V0.shape[0]
+    Vs0 = V0.unsqueeze(0).expand(T, R, nb).contiguous()
+    Vs = Vs0.clone()
+    ptasks = [hc.PotrfTask(uplo=ord("L"), n=nb, A=D[k].data_ptr(), lda=nb) for k in range(T)]
+    ttasks = [hc.TrsmTask(side=141, uplo=122, trans=111, diag=131, M=nb, N=R, alpha=1.0,
+                          A=D[k].data_ptr(), lda=nb, B=Vs[k].data_ptr(), ldb=nb) for k in range(T)]
+    stream = torch.cuda.current_stream(dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def step():
+        D.copy_(D0)
+        Vs.copy_(Vs0)
+        e0, e1, e2 = ev(), ev(), ev()
+        e0.record(stream)
+        info = hc.potrf_batched(ptasks, stream=stream.cuda_stream)
+        e1.record(stream)
+        hc.trsm_batched(ttasks, stream=stream.cuda_stream)
+        e2.record(stream)
+        torch.cuda.synchronize(dev)
+        assert not info.any(), info
+        return e0.elapsed_time(e1), e1.elapsed_time(e2)
+
+    step()
+    # correctness: tiles 0 and 63 against the oracle
+    port = O.Port()
+    errs = {}
+    for k in (0, T - 1):
+        A = np.asfortranarray(D0[k].cpu().numpy())
+        Lr, info, _ = port.dpotrf(ord("L"), nb, A)
+        Lg = D[k].cpu().numpy().T
+        errs[f"potrf_{k}"] = float(np.abs(np.tril(Lg) - np.tril(Lr)).max() / np.abs(np.tril(Lr)).max())
+        Vr, _ = port.dtrsm(141, 122, 111, 131, nb, R, 1.0, np.asfortranarray(np.tril(Lr)),
+                           np.asfortranarray(V0.cpu().numpy().T))
+        Vg = Vs[k].cpu().numpy().T
+        errs[f"trsm_{k}"] = float(np.abs(Vg - Vr).max() / np.abs(Vr).max())
+    for _ in range(args.warmup):
+        step()
+    tp, tt = [], []
+    for _ in range(args.steps):
+        a, b = step()
+        tp.append(a)
+        tt.append(b)
+    ms_p, ms_t = float(np.mean(tp)), float(np.mean(tt))
+    ms = ms_p + ms_t
+    # library comparison (cuSOLVER / cuBLAS through torch), same work
+    Lt = torch.linalg.cholesky(D0)
+    torch.cuda.synchronize(dev)
+    e0, e1, e2 = ev(), ev(), ev()
+    e0.record(stream)
+    torch.linalg.cholesky_ex(D0)
+    e1.record(stream)
+    torch.linalg.solve_triangular(Lt, Vs0.transpose(1, 2), upper=False)
+    e2.record(stream)
+    torch.cuda.synchronize(dev)
+    lib_p, lib_t = e0.elapsed_time(e1), e1.elapsed_time(e2)
+    # CPU: the oracle (OpenBLAS through the reference's calls) on one panel step
+    cores = os.cpu_count() or 1
+    port.set_threads(cores)
+    A0 = np.asfortranarray(D0[0].cpu().numpy())
+    Vh = np.asfortranarray(V0.cpu().numpy().T)
+    t0 = time.time()
+    Lr, _, _ = port.dpotrf(ord("L"), nb, A0)
+    port.dtrsm(141, 122, 111, 131, nb, R, 1.0, Lr, Vh)
+    cpu_s = time.time() - t0
+    port.set_threads(1)
+    fl_p, fl_t = nb ** 3 / 3, float(nb) * nb * R
+    flops = T * (fl_p + fl_t)
+    peak = fp64_peak(hc.lib(), torch, dev)
+    line = {"metric": "TLR Cholesky panel steps/s (HCORE_dpotrf + HCORE_dtrsm, batched)",
+            "value": T / (ms / 1e3), "unit": "panel-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (covariance tiles of the panel workload, nugget 1)",
+            "config": {"workload": f"{T} x (POTRF of a {nb}^2 diagonal tile + TRSM of the "
+                                   f"panel's {T - 1} V factors, {R} columns)",
+                       "nb": nb, "tiles": T, "rhs_per_panel": R},
+            "phases_ms": {"potrf": round(ms_p, 3), "trsm": round(ms_t, 3)},
+            "roofline": {"bound": "fp64", "achieved": flops / (ms / 1e3) / 1e12, "peak": peak,
+                         "unit": "TFLOP/s", "frac": flops / (ms / 1e3) / 1e12 / peak,
+                         "flops_basis": "n^3/3 per POTRF, n^2 R per TRSM (FMA = 2 flops)",
+                         "potrf_tflops": T * fl_p / (ms_p / 1e3) / 1e12,
+                         "trsm_tflops": T * fl_t / (ms_t / 1e3) / 1e12},
+            "library_comparison_ms": {"potrf_cusolver_batched": round(lib_p, 3),
+                                      "trsm_cublas_batched": round(lib_t, 3)},
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "panel-steps/s", "cores": cores,
+                             "kind": "port", "sample": "one panel step (POTRF + TRSM) through "
+                                                       "OpenBLAS as the reference calls it"},
+            "accuracy": {"max_rel_err_vs_oracle": errs}}
+    if rank == 0:
+        print(json.dumps(line))
+        sys.stdout.flush()
+    barrier(world)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1242,6 +1372,8 @@ def main():
         run_dense(args)
     elif args.workload == "predictor":
         run_predictor(args)
+    elif args.workload == "tlr":
+        run_tlr(args)
     else:
         run_gb300(args)
 

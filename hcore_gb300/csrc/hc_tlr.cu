@@ -25,7 +25,7 @@
 // the factorization and is left in place), the panel below it
 // (A_ik = A_ik L_kk^-T, 64 rows per CTA, the 64 components of a row spread
 // over 4 threads), and the trailing lower triangle (A_ij -= A_ik A_jk^T,
-// 64 x 64 tiles, 4 x 4 register blocks).  Every launch first reads the
+// 32 x 32 tiles, 2 x 2 register blocks).  Every launch first reads the
 // task's info and returns once a pivot has failed.
 #include <cuda_runtime.h>
 
@@ -118,11 +118,13 @@ __global__ void __launch_bounds__(256) trsm_kernel(const hcore_trsm_task *tasks,
         __syncthreads();
         if (warp < w.nv) {  // one warp per vector: forward substitution in the block
             double x = lane < bs ? X[(b0 + lane) * S + warp] : 0.0;
+            // x_j = b_j / T'_jj as a product with the reciprocal (one division
+            // per lane and block instead of one per step)
+            const double rd = (unit || lane >= bs) ? 1.0 : 1.0 / Td[lane][lane];
             for (int j = 0; j < bs; ++j) {
-                double xj = __shfl_sync(0xffffffffu, x, j);
-                if (!unit) xj = xj / Td[j][j];
-                if (lane == j) x = xj;
-                else if (lane > j) x -= Td[lane][j] * xj;
+                if (lane == j) x *= rd;
+                const double xj = __shfl_sync(0xffffffffu, x, j);
+                if (lane > j) x -= Td[lane][j] * xj;
             }
             if (lane < bs) X[(b0 + lane) * S + warp] = x;
         }
@@ -176,6 +178,7 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 __global__ void __launch_bounds__(256) potrf_diag_kernel(const hcore_potrf_task *tasks, int *info,
                                                          int kb) {
     __shared__ double S[kPb][kPb + 1];
+    __shared__ double rpiv;
     __shared__ int fail;
     const hcore_potrf_task t = tasks[blockIdx.x];
     if (info[blockIdx.x] != 0 || kb >= t.n) return;
@@ -200,7 +203,9 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(const hcore_potrf_task 
                     S[j][j] = d;
                     fail = j;
                 } else {
-                    S[j][j] = sqrt(d);
+                    const double l = sqrt(d);
+                    S[j][j] = l;
+                    rpiv = 1.0 / l;  // the column is scaled by the reciprocal, as dpotf2 does
                 }
             }
         }
@@ -211,7 +216,7 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(const hcore_potrf_task 
             for (int l = part; l < j; l += 4) s += S[row][l] * S[j][l];
         s += __shfl_xor_sync(0xffffffffu, s, 1);
         s += __shfl_xor_sync(0xffffffffu, s, 2);
-        if (part == 0 && row > j && row < bs) S[row][j] = (S[row][j] - s) / S[j][j];
+        if (part == 0 && row > j && row < bs) S[row][j] = (S[row][j] - s) * rpiv;
         __syncthreads();
     }
     for (int e = tid; e < kPb * kPb; e += 256) {
@@ -228,6 +233,7 @@ __global__ void __launch_bounds__(256) potrf_panel_kernel(const hcore_potrf_task
                                                           const int *info, int kb) {
     __shared__ double Ls[kPb][kPb + 1];
     __shared__ double Xs[kPb][kPb + 1];
+    __shared__ double rL[kPb];
     const hcore_potrf_task t = tasks[blockIdx.y];
     if (info[blockIdx.y] != 0 || kb >= t.n) return;
     const int bs = min(kPb, t.n - kb);
@@ -247,13 +253,14 @@ __global__ void __launch_bounds__(256) potrf_panel_kernel(const hcore_potrf_task
         const int c = q + 4 * m;
         a[m] = (r < rows && c < bs) ? V.at(r0 + r, kb + c) : 0.0;
     }
+    if (tid < bs) rL[tid] = 1.0 / V.at(kb + tid, kb + tid);
     __syncthreads();
     for (int c = 0; c < bs; ++c) {
         if (q == (c & 3)) {
 #pragma unroll
             for (int m = 0; m < kPb / 4; ++m)
                 if (q + 4 * m == c) {
-                    a[m] = a[m] / Ls[c][c];
+                    a[m] *= rL[c];
                     Xs[r][c] = a[m];
                 }
         }
@@ -273,48 +280,47 @@ __global__ void __launch_bounds__(256) potrf_panel_kernel(const hcore_potrf_task
 }
 
 // trailing lower triangle from row/column t0 = kb + bs: A_ij -= A_ik A_jk^T,
-// one CTA per 64 x 64 tile (bi >= bj), K = bs staged 16 at a time
+// one CTA per 32 x 32 tile (bi >= bj), 2 x 2 outputs per thread, K = bs
+// staged 16 at a time.  Small tiles keep each CTA short: the update is on the
+// factorization's critical path once per block.
+constexpr int kUt = 32;
 __global__ void __launch_bounds__(256) potrf_update_kernel(const hcore_potrf_task *tasks,
                                                            const int *info, int kb, int tiles) {
-    __shared__ double sP[16][kPb + 1];
-    __shared__ double sQ[16][kPb + 1];
+    __shared__ double sP[16][kUt + 1];
+    __shared__ double sQ[16][kUt + 1];
     const hcore_potrf_task t = tasks[blockIdx.y];
     if (info[blockIdx.y] != 0 || kb >= t.n) return;
     const int bs = min(kPb, t.n - kb), t0 = kb + bs;
     const int bi = blockIdx.x % tiles, bj = blockIdx.x / tiles;
     if (bj > bi) return;
-    const int i0 = t0 + bi * kPb, j0 = t0 + bj * kPb;
+    const int i0 = t0 + bi * kUt, j0 = t0 + bj * kUt;
     if (i0 >= t.n) return;
     const PotrfView V{t.A, t.lda, t.uplo == 'U' || t.uplo == 'u'};
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    double acc[4][4] = {};
+    double acc[2][2] = {};
     for (int k0 = 0; k0 < bs; k0 += 16) {
-        for (int e = threadIdx.x; e < 16 * kPb; e += 256) {
+        for (int e = threadIdx.x; e < 2 * 16 * kUt; e += 256) {
+            const int which = e / (16 * kUt), f = e % (16 * kUt);
             int kk, rr;
-            if (V.up) { kk = e % 16; rr = e / 16; } else { rr = e % kPb; kk = e / kPb; }
-            const int kg = k0 + kk;
-            sP[kk][rr] = (kg < bs && i0 + rr < t.n) ? V.at(i0 + rr, kb + kg) : 0.0;
-            sQ[kk][rr] = (kg < bs && j0 + rr < t.n) ? V.at(j0 + rr, kb + kg) : 0.0;
+            if (V.up) { kk = f % 16; rr = f / 16; } else { rr = f % kUt; kk = f / kUt; }
+            const int kg = k0 + kk, base = which ? j0 : i0;
+            const double x = (kg < bs && base + rr < t.n) ? V.at(base + rr, kb + kg) : 0.0;
+            if (which) sQ[kk][rr] = x; else sP[kk][rr] = x;
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk) {
-            double pv[4], qv[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) pv[u] = sP[kk][tx + 16 * u];
-#pragma unroll
-            for (int w = 0; w < 4; ++w) qv[w] = sQ[kk][ty + 16 * w];
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int w = 0; w < 4; ++w) acc[u][w] += pv[u] * qv[w];
+            const double p0 = sP[kk][tx], p1 = sP[kk][tx + 16];
+            const double q0 = sQ[kk][ty], q1 = sQ[kk][ty + 16];
+            acc[0][0] += p0 * q0; acc[0][1] += p0 * q1;
+            acc[1][0] += p1 * q0; acc[1][1] += p1 * q1;
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 2; ++u)
 #pragma unroll
-        for (int w = 0; w < 4; ++w) {
+        for (int w = 0; w < 2; ++w) {
             const int i = i0 + tx + 16 * u, j = j0 + ty + 16 * w;
             if (i < t.n && j <= i) V.at(i, j) -= acc[u][w];
         }
@@ -325,14 +331,18 @@ __global__ void __launch_bounds__(256) potrf_update_kernel(const hcore_potrf_tas
 // ---------------------------------------------------------------------------
 static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-static int trsm_stride(int maxn) {  // vectors per CTA that fit shared memory
+// vectors per CTA: up to 8 while the CTA's vectors take at most 64 KB of
+// shared memory (two or more CTAs per SM), fewer for longer vectors, 0 if
+// not even one fits
+static int trsm_stride(int maxn) {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const int stat = (kTrRc + kTrBs) * (kTrBs + 1) * (int)sizeof(double);
+    const long long stat = (kTrRc + kTrBs) * (kTrBs + 1) * (long long)sizeof(double);
+    const long long per = (long long)maxn * (long long)sizeof(double);
     for (int S = 8; S >= 1; S >>= 1)
-        if ((long long)maxn * S * (long long)sizeof(double) + stat <= optin) return S;
-    return 0;
+        if (per * S <= 65536 && per * S + stat <= optin) return S;
+    return per + stat <= optin ? 1 : 0;
 }
 
 static bool trsm_valid(const hcore_trsm_task &t) {
@@ -453,8 +463,8 @@ static int run_potrf(int n, const hcore_potrf_task *tasks, int *info, cudaStream
         potrf_diag_kernel<<<nr, 256, 0, s>>>(d_t, d_info, kb);
         const int below = maxn - std::min(maxn, kb + kPb);
         if (below > 0) {
-            const int tiles = (below + kPb - 1) / kPb;
-            potrf_panel_kernel<<<dim3(tiles, nr), 256, 0, s>>>(d_t, d_info, kb);
+            const int panels = (below + kPb - 1) / kPb, tiles = (below + kUt - 1) / kUt;
+            potrf_panel_kernel<<<dim3(panels, nr), 256, 0, s>>>(d_t, d_info, kb);
             potrf_update_kernel<<<dim3(tiles * tiles, nr), 256, 0, s>>>(d_t, d_info, kb, tiles);
         }
         e = cudaGetLastError();
