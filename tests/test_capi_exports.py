@@ -35,10 +35,11 @@ def test_headers_declare_the_reference_entry_points():
     funcs, globs = declared_symbols()
     for f in ("HCORE_dgemm", "HCORE_sgemm", "HCORE_dgemm_fast", "HCORE_dsyrk", "HCORE_dgemmcd",
               "HCORE_dgemm_qr_svd", "HCORE_dgemm_qr_svd_b_dense", "HCORE_dgemm_ormqr",
-              "HCORE_sgemm_qr_svd", "HCORE_sgemm_ormqr", "HCORE_dgemm_dense"):
+              "HCORE_sgemm_qr_svd", "HCORE_sgemm_ormqr", "HCORE_dgemm_dense", "HCORE_dtrsm",
+              "HCORE_dpotrf", "HCORE_duncompress", "HCORE_dgemmbdcd"):
         assert f in funcs
     for g in ("use_trmm", "gemm_print_index", "gemm_print_mat", "hc_nelm_limit",
-              "sgemm_use_trmm", "syrk_print_index", "gemmcd_print_index"):
+              "sgemm_use_trmm", "syrk_print_index", "gemmcd_print_index", "gemmbdcd_print_index"):
         assert g in globs
     assert "use_scratch" not in globs   # the caller's, as in the reference
 
