@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--max-updates", type=int, default=None, help="truncate the update list")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="panel workload: use the built-in launch shapes instead of autotuning")
     p.add_argument("--per-tile-sample", type=int, default=48)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--c5-shape", default=None,
@@ -235,7 +237,10 @@ def run_gb300(args):
     # the plan's launch shapes, picked by the library's autotuner on this batch
     # (set-up, outside the timed region)
     t0 = time.time()
-    tuning, tuned_ms = hc.autotune(tasks, reps=3, stream=stream.cuda_stream)
+    if args.no_autotune:   # the library's built-in launch shapes (profiling runs)
+        tuning, tuned_ms = hc.make_tuning(), None
+    else:
+        tuning, tuned_ms = hc.autotune(tasks, reps=3, stream=stream.cuda_stream)
     tune_s = time.time() - t0
     batch = hc.Batch(tasks, tuning=tuning)
     batch.execute(stream.cuda_stream)
