@@ -15,6 +15,8 @@ interface so tests and benchmarks read like the reference's own:
 * :func:`trsm_batched` / :func:`potrf_batched` — HCORE_dtrsm on many factors
   and HCORE_dpotrf on dense tiles, the steps either side of the update in a
   TLR Cholesky;
+* :func:`compress_batched` — dense tiles to U, V factors (the reference
+  tests' compressor semantics) on the GPU;
 * :class:`RankMLP` — the rank predictor's network, trained and run by the
   library's own CUDA kernels (see :mod:`hcore_gb300.predictor`).
 
@@ -32,7 +34,8 @@ import numpy as np
 from .build import LIB as _LIB_PATH
 
 __all__ = ["lib", "LrTask", "DenseTask", "Batch", "DensePlan", "hcore_dgemm", "hcore_sgemm", "hcore_dgemm_fast",
-           "dense_batched", "TrsmTask", "PotrfTask", "trsm_batched", "potrf_batched", "HcoreError", "STATUS", "FlopCounter", "RankMLP", "Tuning",
+           "dense_batched", "TrsmTask", "PotrfTask", "trsm_batched", "potrf_batched",
+           "CompressTask", "compress_batched", "HcoreError", "STATUS", "FlopCounter", "RankMLP", "Tuning",
            "make_tuning", "autotune"]
 
 F64, F32 = 0, 1
@@ -83,6 +86,14 @@ class PotrfTask(C.Structure):
     """Mirror of hcore_potrf_task (include/hcore_gb300.h); uplo is 'L' or 'U'."""
 
     _fields_ = [("uplo", C.c_int), ("n", C.c_int), ("A", C.c_void_p), ("lda", C.c_int)]
+
+
+class CompressTask(C.Structure):
+    """Mirror of hcore_compress_task (include/hcore_gb300.h)."""
+
+    _fields_ = [("M", C.c_int), ("D", C.c_void_p), ("ldd", C.c_int), ("acc", C.c_double),
+                ("relative", C.c_int), ("maxrank", C.c_int), ("U", C.c_void_p), ("V", C.c_void_p),
+                ("ldo", C.c_int)]
 
 
 class Tuning(C.Structure):
@@ -162,6 +173,8 @@ def lib() -> C.CDLL:
     L.hcore_gpu_dense_plan_execute.argtypes = [vp, vp]
     L.hcore_gpu_dense_plan_destroy.argtypes = [vp]
     L.hcore_gpu_trsm_batched.argtypes = [C.c_int, C.POINTER(TrsmTask), vp]
+    L.hcore_gpu_compress_batched.argtypes = [C.c_int, C.POINTER(CompressTask),
+                                             C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
     L.hcore_gpu_potrf_batched.argtypes = [C.c_int, C.POINTER(PotrfTask), C.POINTER(C.c_int), vp]
     L.hcore_gpu_mlp_create.argtypes = [C.POINTER(vp), C.c_ulonglong]
     L.hcore_gpu_mlp_params.argtypes = [vp, _fp, C.c_int]
@@ -423,6 +436,18 @@ def potrf_batched(tasks, stream=None) -> np.ndarray:
     _check(lib().hcore_gpu_potrf_batched(len(tasks), arr, info, stream or None),
            "hcore_gpu_potrf_batched")
     return np.array(info[:len(tasks)], dtype=np.int32)
+
+
+def compress_batched(tasks, stream=None):
+    """Compress dense tiles (CompressTask list, device or pinned pointers);
+    returns (ranks, status) arrays.  A non-zero status (NOCONV, RANK_MAX) is
+    reported per tile, not raised."""
+    arr = (CompressTask * max(len(tasks), 1))(*tasks)
+    r = (C.c_int * max(len(tasks), 1))()
+    st = (C.c_int * max(len(tasks), 1))()
+    _check(lib().hcore_gpu_compress_batched(len(tasks), arr, r, st, stream or None),
+           "hcore_gpu_compress_batched")
+    return (np.array(r[:len(tasks)], dtype=np.int32), np.array(st[:len(tasks)], dtype=np.int32))
 
 
 class RankMLP:

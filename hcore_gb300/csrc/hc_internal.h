@@ -23,8 +23,11 @@ struct Desc {
     int rank_start;      // rank search starts here (1, or 2 for the fast rules)
     int status0;         // non-zero: rejected on the host, skip
     int idx;             // task index (rank/status slots)
-    int pad_;
+    int rule;            // rank rule bits (kRule*): 0 for HCORE_dgemm's rule
 };
+// rank rule bits of a descriptor: cap the rank at max_rank instead of
+// reporting RANK_MAX; compare with acc * sigma_max instead of acc
+constexpr int kRuleCapRank = 1, kRuleRelative = 2;
 
 // Workspace layout of one update (element offsets from Desc::ws), k = a + c:
 //   UA  M*k   stacked [beta CU | alpha AU], then its QR (R on top, reflectors below)

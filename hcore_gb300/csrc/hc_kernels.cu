@@ -731,18 +731,23 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
     T *sig_out = base + L.sig;
     for (int t = tid; t < k; t += nthr) sig_out[t] = mul_exp2(s_sig[s_perm[t]], sexp);
 
-    // rank rule (hcore_dgemm.c:444-464; the fast rules start at i = 2)
+    // rank rule (hcore_dgemm.c:444-464; the fast rules start at i = 2; the
+    // compressor's starts at 0, may compare with acc * sigma_max and caps
+    // the rank at max_rank)
     int r;
     if (d.rk != 0) {
         r = d.rk < k ? d.rk : k;
     } else {
+        const T thr = (d.rule & kRuleRelative) ? (T)d.acc * mul_exp2(s_sig[s_perm[0]], sexp)
+                                               : (T)d.acc;
         r = k;
         for (int i = d.rank_start; i < k; ++i)
-            if (mul_exp2(s_sig[s_perm[i]], sexp) < (T)d.acc) {
+            if (mul_exp2(s_sig[s_perm[i]], sexp) < thr) {
                 r = i;
                 break;
             }
     }
+    if ((d.rule & kRuleCapRank) && r > d.max_rank) r = d.max_rank;
     int st = HCORE_GPU_S_OK;
     if (!converged || !finite) st = HCORE_GPU_S_NOCONV;
     else if (r > d.max_rank) st = HCORE_GPU_S_RANK_MAX;

@@ -253,6 +253,28 @@ typedef struct hcore_potrf_task {
 } hcore_potrf_task;
 int hcore_gpu_potrf_batched(int n, const hcore_potrf_task *tasks, int *info, void *stream);
 
+/* Tile compression (the reference's compressor semantics, generate_compress
+ * in testing/testing_dgemm.c:119-236): a dense M x M tile D (ld ldd) becomes
+ * U and V (M x r each, ld ldo) with D ~ U V^T, U the first r left singular
+ * vectors, V = (S V^T)^T, r the number of leading singular values >= acc
+ * (relative = 1: >= acc * sigma_max), capped at maxrank; r may be 0.  A
+ * truncated pivoted QR finds the tile's range first, so ranks agree with a
+ * full SVD's except for singular values within 1e-3 * threshold of it.
+ * Status per tile: OK, NOCONV (non-finite input), RANK_MAX (the range needs
+ * more than min(M, 512) columns).  M <= 2048.  Synchronous. */
+typedef struct hcore_compress_task {
+    int M;
+    const double *D;
+    int ldd;
+    double acc;
+    int relative;
+    int maxrank;
+    double *U, *V;
+    int ldo;
+} hcore_compress_task;
+int hcore_gpu_compress_batched(int n, const hcore_compress_task *tasks, int *ranks, int *status,
+                               void *stream);
+
 /* measured FP64 tensor-pipe (DMMA m16n8k16) throughput of this GPU in
  * TFLOP/s, timed on `stream` (about 0.1 s); the roofline denominator of the
  * FP64 phases */

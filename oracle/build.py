@@ -94,13 +94,17 @@ def ref_lib_path() -> str:
     return os.path.join(REF_OUT, "libhcore_ref.so")
 
 
+def ref_test_lib_path() -> str:
+    return os.path.join(REF_OUT, "libhcore_reftest.so")
+
+
 def build_ref(force: bool = False) -> str | None:
     """Compile the reference HCORE from its own sources (only where present)."""
     if not reference_available():
         return None
     os.makedirs(REF_OUT, exist_ok=True)
     out = ref_lib_path()
-    if os.path.exists(out) and not force:
+    if os.path.exists(out) and os.path.exists(ref_test_lib_path()) and not force:
         return out
     inc = ["-I", os.path.join(HERE, "compat"),
            "-I", os.path.join(REFERENCE_ROOT, "src", "include"),
@@ -126,6 +130,12 @@ def build_ref(force: bool = False) -> str | None:
     _run(cflags + ["-c", glob_c, "-o", os.path.join(REF_OUT, "use_scratch.o")])
     _run(["gcc", "-shared", "-o", out] + objs + [os.path.join(REF_OUT, "use_scratch.o")]
          + _link_flags())
+    # testing_dgemm.c as a library (its main renamed) for its compressor,
+    # generate_compress (:119-236), which the reference has nowhere else
+    t_o = os.path.join(REF_OUT, "testing_dgemm_lib.o")
+    _run(cflags + ["-Dmain=hcore_testing_dgemm_main", "-c",
+                   os.path.join(REFERENCE_ROOT, "testing", "testing_dgemm.c"), "-o", t_o])
+    _run(["gcc", "-shared", "-o", ref_test_lib_path(), t_o] + objs + _link_flags())
     # the reference's four known-answer test programs, linked statically
     # against the same objects (each defines its own use_scratch)
     for t in REF_TESTS:

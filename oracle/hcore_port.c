@@ -154,3 +154,36 @@ int port_dpotrf(int uplo, int N, double *A, int LDA, unsigned long *flops_potrf)
     if (flops_potrf) *flops_potrf += port_flop_counts('c', N, 0, 0, 0);
     return info;
 }
+
+/* The reference's tile compressor, generate_compress
+ * (testing/testing_dgemm.c:119-236) after its dlatms step: dgesvd('A','A')
+ * of the M x N tile, rank = the number of leading singular values >= thr
+ * (:194; thr = acc, or acc * sigma_max when relative), capped at maxrank
+ * (:195-197); U = the first r left vectors (:204), V = (S V^T)^T (:173-176,
+ * :209).  sigma (min(M, N)) receives the singular values. */
+int port_dcompress(int M, int N, const double *D, int ldd, double acc, int relative, int maxrank,
+                   double *U, double *V, int ldo, int *rank, double *sigma)
+{
+    const int mn = M < N ? M : N;
+    double *A = malloc((size_t)M * N * sizeof(double));
+    double *tU = malloc((size_t)M * M * sizeof(double));
+    double *tV = malloc((size_t)N * N * sizeof(double));
+    double *sup = malloc((size_t)(mn > 1 ? mn : 1) * sizeof(double));
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < M; ++i) A[(size_t)j * M + i] = D[(size_t)j * ldd + i];
+    const int info = scipy_LAPACKE_dgesvd(LAPACK_COL_MAJOR, 'A', 'A', M, N, A, M, sigma, tU, M,
+                                          tV, N, sup);
+    int r = 0;
+    if (info == 0) {
+        const double thr = relative ? acc * sigma[0] : acc;
+        while (r < mn && sigma[r] >= thr) ++r;
+        if (r > maxrank) r = maxrank;
+        for (int t = 0; t < r; ++t) {
+            for (int i = 0; i < M; ++i) U[(size_t)t * ldo + i] = tU[(size_t)t * M + i];
+            for (int i = 0; i < N; ++i) V[(size_t)t * ldo + i] = sigma[t] * tV[(size_t)i * N + t];
+        }
+    }
+    *rank = r;
+    free(A); free(tU); free(tV); free(sup);
+    return info == 0 ? PORT_OK : PORT_E_LAPACK;
+}

@@ -43,4 +43,6 @@ void port_dgemmbdcd(int transA, int M, int N, double alpha, const double *AU, co
 void port_dtrsm(int side, int uplo, int transA, int diag, int M, int Brank, double alpha,
                 const double *A, int LDA, double *BV, int LDBV, unsigned long *flops_trsm);
 int port_dpotrf(int uplo, int N, double *A, int LDA, unsigned long *flops_potrf);
+int port_dcompress(int M, int N, const double *D, int ldd, double acc, int relative, int maxrank,
+                   double *U, double *V, int ldo, int *rank, double *sigma);
 #endif

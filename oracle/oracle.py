@@ -84,6 +84,9 @@ class Port:
                                        C.c_double, _dp, C.c_int, _dp, C.c_int, _ulp]
             lib.port_dpotrf.restype = C.c_int
             lib.port_dpotrf.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ulp]
+            lib.port_dcompress.restype = C.c_int
+            lib.port_dcompress.argtypes = [C.c_int, C.c_int, _dp, C.c_int, C.c_double, C.c_int,
+                                           C.c_int, _dp, _dp, C.c_int, _ip, _dp]
             lib.port_dlatms.argtypes = [C.c_int, C.c_int, C.c_char, _ip, C.c_char, _dp, C.c_int,
                                         C.c_double, C.c_double, C.c_int, C.c_int, C.c_char, _dp,
                                         C.c_int]
@@ -175,6 +178,21 @@ class Port:
         fl = C.c_ulong(0)
         info = self.lib.port_dpotrf(uplo, N, _ptr(Ao), Ao.shape[0], C.byref(fl))
         return Ao, info, fl.value
+
+    def dcompress(self, D, acc, maxrank, relative=False):
+        """generate_compress's SVD truncation of a dense tile: returns
+        (rank, U, V, sigma) with U, V of shape (M, rank)."""
+        D = fortran(D)
+        M, N = D.shape
+        U = np.zeros((M, max(min(M, N), 1)), order="F")
+        V = np.zeros((M, max(min(M, N), 1)), order="F")
+        sig = np.zeros(max(min(M, N), 1))
+        r = C.c_int(0)
+        st = self.lib.port_dcompress(M, N, _ptr(D), M, acc, int(relative), maxrank, _ptr(U),
+                                     _ptr(V), M, C.byref(r), _ptr(sig))
+        if st != 0:
+            raise RuntimeError(f"dgesvd failed ({st})")
+        return r.value, U[:, :r.value], V[:, :r.value], sig[:min(M, N)]
 
     def dlatms(self, m, n, iseed, d, ld):
         """LAPACKE_dlatms(m, n, 'U', iseed, 'N', d, mode=0, cond=-1, dmax=-1,
@@ -296,6 +314,29 @@ class RefLib:
         self.lib.HCORE_dgemmcd(111, 112, M, -1.0, _ptr(Au), _ptr(Av), Arank, M, _ptr(Bu),
                                _ptr(Bv), Brank, M, 1.0, _ptr(CDo), M, maxrank, None, C.byref(fc))
         return CDo
+
+    _test_lib = None
+
+    def generate_compress(self, M, acc, maxrank, iseed):
+        """The reference tests' generate_compress (testing/testing_dgemm.c:119-236),
+        called as that file's main calls it (ld = M, maxMNK = M): returns the
+        generated tile, its rank and U, V (M x rank), and the advanced iseed."""
+        if RefLib._test_lib is None:
+            lib = C.CDLL(_build.ref_test_lib_path())
+            lib.generate_compress.restype = C.c_int
+            lib.generate_compress.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int,
+                                              C.c_int, C.c_double, _ip, _ip]
+            RefLib._test_lib = lib
+        A = np.zeros((M, M), order="F")
+        U = np.zeros((M, M), order="F")
+        V = np.zeros((M, M), order="F")
+        seed = np.array(iseed, dtype=np.int32)
+        r = C.c_int(0)
+        st = RefLib._test_lib.generate_compress(M, M, M, _ptr(A), _ptr(U), _ptr(V), maxrank, M, acc,
+                                                seed.ctypes.data_as(_ip), C.byref(r))
+        if st != 0:
+            raise RuntimeError("generate_compress failed")
+        return A, r.value, U[:, :r.value].copy(order="F"), V[:, :r.value].copy(order="F"), seed
 
     def duncompress(self, M, N, AU, a, BV, CD):
         AU, BV = fortran(AU), fortran(BV)

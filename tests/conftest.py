@@ -71,6 +71,19 @@ def golden_tlr():
 
 
 @pytest.fixture(scope="session")
+def golden_compress():
+    """Reference outputs of the tests' compressor (generate_compress)."""
+    import json
+
+    import numpy as np
+
+    d = os.path.join(ROOT, "tests", "golden")
+    with open(os.path.join(d, "golden_compress_meta.json")) as f:
+        meta = json.load(f)
+    return meta, dict(np.load(os.path.join(d, "golden_compress.npz")))
+
+
+@pytest.fixture(scope="session")
 def hc():
     """The GPU library, built if absent (the GPU machine builds it via build())."""
     import hcore_gb300

@@ -18,7 +18,10 @@ through ctypes on seeded inputs.  The outputs are committed as
   (every side/uplo/trans/diag) and HCORE_dpotrf (both triangles, a failing
   pivot, an invalid uplo).
 
-Usage:  python tests/golden/make_golden.py [--tlr-only]
+* ``golden_compress.npz`` / ``golden_compress_meta.json`` — the reference
+  tests' compressor (generate_compress) on dlatms tiles.
+
+Usage:  python tests/golden/make_golden.py [--tlr-only | --compress-only]
 """
 from __future__ import annotations
 
@@ -268,7 +271,28 @@ def make_tlr():
           os.path.getsize(os.path.join(OUT, "golden_tlr.npz")))
 
 
+def make_compress():
+    """Fixtures of the reference tests' compressor, generate_compress
+    (testing/testing_dgemm.c:119-236): dlatms tiles with sigma_i = 10^-i from
+    iseed {0,0,0,1}, compressed at thresholds between singular values (no
+    ties), with a rank cap and a rank of 0 (golden_compress.npz / .json)."""
+    ref = O.RefLib()
+    meta, arrs = [], {}
+    for i, (M, acc, maxrank) in enumerate([(64, 3e-8, 64), (100, 3e-13, 10), (48, 2.0, 8),
+                                           (130, 5e-5, 130)]):
+        A, r, U, V, _ = ref.generate_compress(M, acc, maxrank, [0, 0, 0, 1 + 2 * i])
+        name = f"cmp{i}"
+        arrs.update({f"{name}_A": A, f"{name}_U": U, f"{name}_V": V})
+        meta.append(dict(name=name, M=M, acc=acc, maxrank=maxrank, rank=r))
+    np.savez_compressed(os.path.join(OUT, "golden_compress.npz"), **arrs)
+    with open(os.path.join(OUT, "golden_compress_meta.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print("compress cases:", [(c["M"], c["rank"]) for c in meta])
+
+
 if __name__ == "__main__":
-    if "--tlr-only" not in sys.argv:
+    if "--tlr-only" not in sys.argv and "--compress-only" not in sys.argv:
         main()
-    make_tlr()
+    if "--compress-only" not in sys.argv:
+        make_tlr()
+    make_compress()

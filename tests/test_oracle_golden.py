@@ -178,3 +178,16 @@ def test_port_dpotrf_matches_reference(port, golden_tlr):
         _close(out, g[f"{n}_Ao"], 1e-12)
         infos.append(info)
     assert infos == [0, 0, 11, -2]
+
+
+def test_port_compress_matches_reference(port, golden_compress):
+    """The restated compressor against generate_compress: same rank (8, a cap
+    at 10, 0, 5), same product U V^T."""
+    meta, g = golden_compress
+    assert [c["rank"] for c in meta] == [8, 10, 0, 5]
+    for c in meta:
+        n = c["name"]
+        r, U, V, sig = port.dcompress(g[f"{n}_A"], c["acc"], c["maxrank"])
+        assert r == c["rank"]
+        if r:
+            _close(U @ V.T, g[f"{n}_U"] @ g[f"{n}_V"].T, 1e-13)
