@@ -49,11 +49,13 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="panel", choices=["panel", "precision", "dense", "predictor", "tlr"],
+    p.add_argument("--workload", default="panel", choices=["panel", "precision", "dense", "predictor", "tlr",
+                                                         "compress"],
                    help="panel: the headline (config 2); precision: acc sweep (config 3); "
                         "dense: batched dsyrk/dgemmcd tile updates (config 4); predictor: "
                         "learned rank predictor on 3D exponential-kernel sweeps (config 5); "
-                        "tlr: batched POTRF + TRSM, the steps either side of the update")
+                        "tlr: batched POTRF + TRSM, the steps either side of the update; "
+                        "compress: the GPU tile compressor on the panel workload's tiles")
     p.add_argument("--max-updates", type=int, default=None, help="truncate the update list")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -1372,6 +1374,119 @@ def run_tlr(args):
     barrier(world)
 
 
+def run_compress(args):
+    """Tile compression on the GPU (hcore_gpu_compress_batched): all 2016
+    off-diagonal 1024 x 1024 tiles of the panel workload's covariance matrix,
+    relative threshold 1e-8 sigma_max, maxrank 128 (the panel workload's own
+    compression).  A step compresses every tile once, from tiles resident in
+    HBM."""
+    import numpy as np
+    import torch
+
+    import hcore_gb300 as hc
+    from hcore_gb300 import build as hbuild
+    from hcore_gb300 import panel as pnl
+    from oracle import oracle as O
+
+    rank, world, local = dist_init()
+    if not os.path.exists(hbuild.LIB):
+        hbuild.build()
+    hc.lib()
+    dev = torch.device("cuda", local)
+    nb, T, acc, maxrank = 1024, WORKLOAD["points"] // 1024, 1e-8, 128
+    Pt = pnl.morton_points(WORKLOAD["points"], 2, 0)
+    P = torch.from_numpy(Pt).to(dev)
+
+    def ktile(i, j):   # column-major tile (i, j): tensor row c = column c
+        X, Y = P[i * nb:(i + 1) * nb], P[j * nb:(j + 1) * nb]
+        d2 = (X * X).sum(1)[:, None] + (Y * Y).sum(1)[None, :] - 2.0 * X @ Y.T
+        return torch.exp(-torch.clamp(d2, min=0.0) / 0.01).T.contiguous()
+
+    pairs = [(i, j) for i in range(1, T) for j in range(i)]
+    n = len(pairs)
+    D = torch.empty(n, nb, nb, dtype=torch.float64, device=dev)
+    for q, (i, j) in enumerate(pairs):
+        D[q] = ktile(i, j)
+    U = torch.empty(n, maxrank, nb, dtype=torch.float64, device=dev)
+    V = torch.empty_like(U)
+    tasks = [hc.CompressTask(M=nb, D=D[q].data_ptr(), ldd=nb, acc=acc, relative=1,
+                             maxrank=maxrank, U=U[q].data_ptr(), V=V[q].data_ptr(), ldo=nb)
+             for q in range(n)]
+    stream = torch.cuda.current_stream(dev)
+    ranks, status = hc.compress_batched(tasks, stream=stream.cuda_stream)
+    for _ in range(max(args.warmup - 1, 0)):
+        hc.compress_batched(tasks, stream=stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ranks, status = hc.compress_batched(tasks, stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms.append(e0.elapsed_time(e1))
+    ms_step = float(np.mean(ms))
+    # accuracy on a sample against the oracle (full SVD, the reference's rule
+    # with the relative threshold)
+    port = O.Port()
+    samp = list(range(0, n, max(1, n // 12)))[:12]
+    eq, diffs, margins = 0, [], []
+    for q in samp:
+        Dq = np.asfortranarray(D[q].cpu().numpy().T)
+        rr, Ur, Vr, sig = port.dcompress(Dq, acc, maxrank, relative=True)
+        r = int(ranks[q])
+        eq += int(r == rr)
+        margins.append(float(np.min(np.abs(sig - acc * sig[0])) / (acc * sig[0])))
+        if r == rr and r > 0:
+            Ug = U[q, :r].cpu().numpy().T
+            Vg = V[q, :r].cpu().numpy().T
+            diffs.append(float(np.linalg.norm(Ug @ Vg.T - Ur @ Vr.T) / np.linalg.norm(Ur @ Vr.T)))
+    # CPU: the reference's compressor (full dgesvd, restated) on a sample with
+    # every host core through OpenBLAS threads, and the host path the panel
+    # workload uses (randomized range finder, one process per core)
+    cores = os.cpu_count() or 1
+    port.set_threads(cores)
+    t0 = time.time()
+    for q in samp[:4]:
+        port.dcompress(np.asfortranarray(D[q].cpu().numpy().T), acc, maxrank, relative=True)
+    cpu_exact = 4 / (time.time() - t0)
+    port.set_threads(1)
+    host_pairs = pairs[: 4 * cores]
+    t0 = time.time()
+    pnl.compress_tiles(Pt, nb, host_pairs, "sqexp", 0.01, acc, maxrank)
+    cpu_rand = len(host_pairs) / (time.time() - t0)
+    # flops executed by the pivoted QR (dot, update and norm per trailing
+    # element and step: 6 flops) over the ranges it found, which are at least
+    # the ranks; reported on the ranks (a lower bound)
+    flops = float(sum(6.0 * nb * nb * int(r) for r in ranks))
+    peak = fp64_peak(hc.lib(), torch, dev)
+    line = {"metric": "TLR tiles compressed/s (GPU tile compressor, batched)",
+            "value": n / (ms_step / 1e3), "unit": "tiles/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (covariance tiles of the panel workload, generated on the GPU)",
+            "config": {"workload": f"{n} off-diagonal {nb}^2 tiles, sigma >= {acc:g} sigma_max, "
+                                   f"maxrank {maxrank}", "nb": nb, "tiles": n},
+            "ranks": {"mean": float(ranks.mean()), "max": int(ranks.max()),
+                      "status_nonzero": int((status != 0).sum())},
+            "roofline": {"bound": "fp64", "achieved": flops / (ms_step / 1e3) / 1e12, "peak": peak,
+                         "unit": "TFLOP/s", "frac": flops / (ms_step / 1e3) / 1e12 / peak,
+                         "flops_basis": "6 nb^2 flops per tile and pivoted-QR step, counted "
+                                        "over the final ranks (a lower bound: the QR runs "
+                                        "past the rank to 1e-3 of the threshold)"},
+            "accuracy": {"sample": len(samp), "rank_equal_to_oracle": eq,
+                         "max_rel_fro_diff_vs_oracle": max(diffs) if diffs else None,
+                         "min_threshold_margin": min(margins)},
+            "cpu_baseline": {"value": cpu_exact, "unit": "tiles/s", "cores": cores, "kind": "port",
+                             "sample": "4 tiles, the reference tests' compressor (full dgesvd) "
+                                       "restated, OpenBLAS on all cores"},
+            "host_randomized_tiles_per_s": cpu_rand}
+    if rank == 0:
+        print(json.dumps(line))
+        sys.stdout.flush()
+    barrier(world)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1384,6 +1499,8 @@ def main():
         run_predictor(args)
     elif args.workload == "tlr":
         run_tlr(args)
+    elif args.workload == "compress":
+        run_compress(args)
     else:
         run_gb300(args)
 
