@@ -63,6 +63,8 @@ def parse():
                    help="panel workload: use the built-in launch shapes instead of autotuning")
     p.add_argument("--per-tile-sample", type=int, default=48)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--compress-tiles", type=int, default=None,
+                   help="compress workload: only the first N tiles (a small profiling case)")
     p.add_argument("--c5-shape", default=None,
                    help="predictor workload at a reduced shape 'block_tiles,nb,sweeps' (a quick check)")
     return p.parse_args()
@@ -1402,7 +1404,7 @@ def run_compress(args):
         d2 = (X * X).sum(1)[:, None] + (Y * Y).sum(1)[None, :] - 2.0 * X @ Y.T
         return torch.exp(-torch.clamp(d2, min=0.0) / 0.01).T.contiguous()
 
-    pairs = [(i, j) for i in range(1, T) for j in range(i)]
+    pairs = [(i, j) for i in range(1, T) for j in range(i)][:args.compress_tiles]
     n = len(pairs)
     D = torch.empty(n, nb, nb, dtype=torch.float64, device=dev)
     for q, (i, j) in enumerate(pairs):
