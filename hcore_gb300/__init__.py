@@ -17,6 +17,8 @@ interface so tests and benchmarks read like the reference's own:
   TLR Cholesky;
 * :func:`compress_batched` — dense tiles to U, V factors (the reference
   tests' compressor semantics) on the GPU;
+* :func:`hcore_zgemm` — the complex update (HCORE_zgemm) through its drop-in
+  entry point;
 * :class:`RankMLP` — the rank predictor's network, trained and run by the
   library's own CUDA kernels (see :mod:`hcore_gb300.predictor`).
 
@@ -35,7 +37,7 @@ from .build import LIB as _LIB_PATH
 
 __all__ = ["lib", "LrTask", "DenseTask", "Batch", "DensePlan", "hcore_dgemm", "hcore_sgemm", "hcore_dgemm_fast",
            "dense_batched", "TrsmTask", "PotrfTask", "trsm_batched", "potrf_batched",
-           "CompressTask", "compress_batched", "HcoreError", "STATUS", "FlopCounter", "RankMLP", "Tuning",
+           "CompressTask", "compress_batched", "hcore_zgemm", "HcoreError", "STATUS", "FlopCounter", "RankMLP", "Tuning",
            "make_tuning", "autotune"]
 
 F64, F32 = 0, 1
@@ -94,6 +96,12 @@ class CompressTask(C.Structure):
     _fields_ = [("M", C.c_int), ("D", C.c_void_p), ("ldd", C.c_int), ("acc", C.c_double),
                 ("relative", C.c_int), ("maxrank", C.c_int), ("U", C.c_void_p), ("V", C.c_void_p),
                 ("ldo", C.c_int)]
+
+
+class DComplex(C.Structure):
+    """double _Complex by value (hcore_dcomplex in include/hcore_z.h)."""
+
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
 
 
 class Tuning(C.Structure):
@@ -202,6 +210,10 @@ def lib() -> C.CDLL:
     L.HCORE_dgemmcd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_int, C.c_int,
                                 _dp, _dp, C.c_int, C.c_int, C.c_double, _dp, C.c_int, C.c_int, _dp,
                                 C.POINTER(FlopCounter)]
+    L.HCORE_zgemm.restype = None
+    L.HCORE_zgemm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, DComplex, vp, vp, _dp, C.c_int,
+                              vp, vp, _dp, C.c_int, DComplex, vp, vp, _dp, C.c_int, C.c_int,
+                              C.c_int, C.c_double, vp, C.POINTER(FlopCounter)]
     L.HCORE_duncompress.restype = None
     L.HCORE_duncompress.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp,
                                     C.c_int, _dp, _dp, C.c_int, C.c_double, _dp, C.c_int]
@@ -277,6 +289,29 @@ def hcore_sgemm(M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, *, rk=0, maxrk,
     """HCORE_sgemm on host arrays (drop-in path). Returns (rank, CU, CV, flops)."""
     return _lr_update("HCORE_sgemm", M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, rk, maxrk,
                       acc, np.float32)
+
+
+def hcore_zgemm(M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, *, rk=0, maxrk, acc):
+    """HCORE_zgemm (src/compute/hcore_zgemm.c:663) on complex128 arrays
+    through the drop-in entry point; returns (rank, CU, CV, flops)."""
+    z = lambda x: np.asfortranarray(np.asarray(x, dtype=np.complex128))  # noqa: E731
+    AU, AV, BU, BV = (z(x) for x in (AU, AV, BU, BV))
+    ldc = CU.shape[0]
+    ncol = max(a + c, c, 1)
+    CUo = np.zeros((ldc, ncol), dtype=np.complex128, order="F")
+    CVo = np.zeros((ldc, ncol), dtype=np.complex128, order="F")
+    CUo[:, :c] = CU[:, :c]
+    CVo[:, :c] = CV[:, :c]
+    ra, rb, rc = (np.array([v], dtype=np.float64) for v in (a, b, c))
+    fc = FlopCounter()
+    p = lambda x: x.ctypes.data  # noqa: E731
+    lib().HCORE_zgemm(111, 112, M, M, DComplex(complex(alpha).real, complex(alpha).imag), p(AU),
+                      p(AV), ra.ctypes.data_as(_dp), AU.shape[0], p(BU), p(BV),
+                      rb.ctypes.data_as(_dp), BV.shape[0],
+                      DComplex(complex(beta).real, complex(beta).imag), p(CUo), p(CVo),
+                      rc.ctypes.data_as(_dp), ldc, rk, maxrk, acc, None, C.byref(fc))
+    r = int(rc[0])
+    return r, CUo[:, :r], CVo[:, :r], fc.update
 
 
 def hcore_dgemm_fast(M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, *, rk=0, maxrk, acc):

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <complex>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -21,6 +22,7 @@
 #include "hc_host.h"
 #include "hcore_d.h"
 #include "hcore_s.h"
+#include "hcore_z.h"
 
 // ---- the reference's globals -------------------------------------------------
 extern "C" {
@@ -1145,3 +1147,143 @@ int hcore_gpu_dense_plan_destroy(hcore_gpu_dense_plan p) {
 void *hcore_gpu_thread_stream(void) { return (void *)thread_ctx().stream; }
 
 }  // extern "C"
+
+// ---- HCORE_zgemm through the real pipeline ----------------------------------
+// A complex m x n matrix X embeds as the real 2m x 2n matrix
+//     phi(X) = [Re X, -Im X; Im X, Re X],
+// with phi(X Y^T) = phi(X) psi(Y)^T where psi(Y) = phi(conj Y).  So
+//     phi(C) = phi(beta CU) psi(CV)^T,
+//     phi(A B^T) = phi(alpha AU) psi(AV)^T (psi(BU) phi(BV)^T)^T,
+// a real update of order 2M with ranks 2a, 2b, 2c, which the real plan
+// recompresses (maxrk and rk doubled: phi(X) has each singular value of X
+// twice, so the real rank rule keeps whole pairs).  The truncated real
+// product is phi(C_new), whose left block column gives C_new = Z0 R^T with
+// Z0 = CU'_top + i CU'_bottom and R = CV'_top.  The complex factors are an
+// orthonormal basis Z of Z0's columns (modified Gram-Schmidt in column order,
+// keeping a column when at least half of it is new: one column per pair of
+// equal singular values) and CV = C_new^T conj(Z) = R (Z0^T conj(Z)), so
+// CU CV^T = Z Z^H C_new = C_new.  In column order the basis vectors are
+// C_new's left singular vectors and CV carries the singular values, as in
+// the reference (hcore_zgemm.c:380-430).
+namespace hc {
+using zc = std::complex<double>;
+
+// copy a complex block (rows x cols, ld) from host or device memory
+static std::vector<zc> zget(const hcore_dcomplex *p, int rows, int cols, int ld) {
+    std::vector<zc> out((size_t)rows * cols);
+    if (rows > 0 && cols > 0 &&
+        cudaMemcpy2D(out.data(), rows * sizeof(zc), p, (size_t)ld * sizeof(zc), rows * sizeof(zc),
+                     cols, cudaMemcpyDefault) != cudaSuccess)
+        cuda_fatal("HCORE_zgemm");
+    return out;
+}
+
+// phi (conj_ = false) or psi (conj_ = true) of the M x n block X, scaled by s,
+// into E (2M x 2n, ld 2M)
+static void zembed(double *E, const std::vector<zc> &X, int M, int n, zc s, bool conj_) {
+    const size_t M2 = 2 * (size_t)M;
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < M; ++i) {
+            zc x = s * X[(size_t)j * M + i];
+            if (conj_) x = std::conj(x);
+            E[(size_t)j * M2 + i] = x.real();
+            E[(size_t)j * M2 + M + i] = x.imag();
+            E[(size_t)(n + j) * M2 + i] = -x.imag();
+            E[(size_t)(n + j) * M2 + M + i] = x.real();
+        }
+}
+}  // namespace hc
+
+extern "C" void HCORE_zgemm(HCORE_enum transA, int transB, int M, int N, hcore_dcomplex alpha,
+                            hcore_dcomplex *AU, hcore_dcomplex *AV, double *Ark, int LDA,
+                            hcore_dcomplex *BU, hcore_dcomplex *BV, double *Brk, int LDB,
+                            hcore_dcomplex beta, hcore_dcomplex *CU, hcore_dcomplex *CV,
+                            double *Crk, int LDC, int rk, int maxrk, double acc,
+                            hcore_dcomplex *work, flop_counter *flops) {
+    (void)transA; (void)transB; (void)N; (void)work;
+    const char *fn = "HCORE_zgemm";
+    const int a = (int)Ark[0], b = (int)Brk[0], c = (int)Crk[0];
+    // the reference's exits (hcore_zgemm.c:703-706 and __zqra/ld_newV as in
+    // HCORE_dgemm), on the complex ranks
+    if (a == 0 || b == 0 || c == 0)
+        fatal("%s: _Ark=%d _Brk=%d _Crk=%d. These rank values should not be zero.\n", fn, a, b, c);
+    if (a + c > 2 * maxrk)
+        fatal("%s: Sum of ranks (%d) is too big! _Ark:%d _Crk:%d maxrank:%d (x2: %d)\n", fn,
+              a + c, a, c, maxrk, 2 * maxrk);
+    if (maxrk < a + c)
+        fatal("%s: Increase maxrank. %d is not enough ld_newV:%d CU_ncols:%d\n", fn, maxrk,
+              maxrk, a + c);
+    if (2 * M > kMaxRowsPerLane * 32 || 2 * (a + c) > kMaxK)
+        fatal("%s: M=%d, a+c=%d exceed this library's complex limits (M <= %d, a+c <= %d)\n", fn,
+              M, a + c, kMaxRowsPerLane * 16, kMaxK / 2);
+    const std::vector<zc> xAU = zget(AU, M, a, LDA), xAV = zget(AV, M, a, LDA);
+    const std::vector<zc> xBU = zget(BU, M, b, LDB), xBV = zget(BV, M, b, LDB);
+    const std::vector<zc> xCU = zget(CU, M, c, LDC), xCV = zget(CV, M, c, LDC);
+    const int M2 = 2 * M, k2 = 2 * (a + c);
+    const zc al(alpha.re, alpha.im), be(beta.re, beta.im);
+    std::vector<double> eAU((size_t)M2 * 2 * a), eAV(eAU.size()), eBU((size_t)M2 * 2 * b),
+        eBV(eBU.size()), eCU((size_t)M2 * k2), eCV(eCU.size());
+    zembed(eAU.data(), xAU, M, a, al, false);
+    zembed(eAV.data(), xAV, M, a, 1.0, true);
+    zembed(eBU.data(), xBU, M, b, 1.0, true);
+    zembed(eBV.data(), xBV, M, b, 1.0, false);
+    zembed(eCU.data(), xCU, M, c, be, false);
+    zembed(eCV.data(), xCV, M, c, 1.0, true);
+    double ea = 2 * a, eb = 2 * b, ec = 2 * c;
+    lr_update<double>(fn, M2, 1.0, eAU.data(), eAV.data(), &ea, M2, eBU.data(), eBV.data(), &eb,
+                      M2, 1.0, eCU.data(), eCV.data(), &ec, M2, 2 * rk, 2 * maxrk, acc, nullptr,
+                      false);
+    const int r2 = (int)ec;
+    // C_new = Z0 R^T; orthonormal basis Z of Z0's columns
+    std::vector<zc> Z0((size_t)M * r2), Z;
+    for (int j = 0; j < r2; ++j)
+        for (int i = 0; i < M; ++i)
+            Z0[(size_t)j * M + i] = zc(eCU[(size_t)j * M2 + i], eCU[(size_t)j * M2 + M + i]);
+    int r = 0;
+    std::vector<zc> z(M);
+    for (int j = 0; j < r2; ++j) {
+        double n0 = 0;
+        for (int i = 0; i < M; ++i) {
+            z[i] = Z0[(size_t)j * M + i];
+            n0 += std::norm(z[i]);
+        }
+        for (int pass = 0; pass < 2; ++pass)
+            for (int q = 0; q < r; ++q) {
+                zc h = 0;
+                for (int i = 0; i < M; ++i) h += std::conj(Z[(size_t)q * M + i]) * z[i];
+                for (int i = 0; i < M; ++i) z[i] -= h * Z[(size_t)q * M + i];
+            }
+        double n1 = 0;
+        for (int i = 0; i < M; ++i) n1 += std::norm(z[i]);
+        if (n0 > 0 && n1 > 0.25 * n0) {
+            const double inv = 1.0 / std::sqrt(n1);
+            for (int i = 0; i < M; ++i) Z.push_back(z[i] * inv);
+            ++r;
+        }
+    }
+    if (r > maxrk)  // hcore_zgemm.c's r > maxrk exit
+        fatal("%s: Rank after truncation is too big! finalrank:%d maxrank:%d\n", fn, r, maxrk);
+    // CV = R G, G = Z0^T conj(Z) (r2 x r)
+    std::vector<zc> G((size_t)r2 * r), oU((size_t)M * r), oV((size_t)M * r);
+    for (int q = 0; q < r; ++q)
+        for (int j = 0; j < r2; ++j) {
+            zc g = 0;
+            for (int i = 0; i < M; ++i) g += Z0[(size_t)j * M + i] * std::conj(Z[(size_t)q * M + i]);
+            G[(size_t)q * r2 + j] = g;
+        }
+    for (int q = 0; q < r; ++q)
+        for (int i = 0; i < M; ++i) {
+            zc v = 0;
+            for (int j = 0; j < r2; ++j) v += eCV[(size_t)j * M2 + i] * G[(size_t)q * r2 + j];
+            oV[(size_t)q * M + i] = v;
+            oU[(size_t)q * M + i] = Z[(size_t)q * M + i];
+        }
+    if (r > 0 &&
+        (cudaMemcpy2D(CU, (size_t)LDC * sizeof(zc), oU.data(), M * sizeof(zc), M * sizeof(zc), r,
+                      cudaMemcpyDefault) != cudaSuccess ||
+         cudaMemcpy2D(CV, (size_t)LDC * sizeof(zc), oV.data(), M * sizeof(zc), M * sizeof(zc), r,
+                      cudaMemcpyDefault) != cudaSuccess))
+        cuda_fatal(fn);
+    Crk[0] = r;
+    if (flops) flops->update += update_flops(M, a, b, c, r, false);  // hcore_zgemm.c: same model
+}

@@ -1,0 +1,35 @@
+/*
+ * hcore-gb300 — complex (double _Complex) drop-in entry point, replacing
+ * src/include/hcore_z.h:27-48 (src/compute/hcore_zgemm.c:663-976).
+ *
+ * The prototype is the reference's.  C++ sees double _Complex as a struct of
+ * two doubles, real part first: the same layout and the same argument passing
+ * (two floating-point registers on x86-64 and AArch64) as C's type.
+ */
+#ifndef HCORE_GB300_HCORE_Z_H
+#define HCORE_GB300_HCORE_Z_H
+#include "flop_util_structs.h"
+#include "hcore.h"
+#ifdef __cplusplus
+extern "C" {
+typedef struct hcore_dcomplex {
+    double re, im;
+} hcore_dcomplex;
+#else
+typedef double _Complex hcore_dcomplex;
+#endif
+
+/* C = beta*C + alpha*A*B^T (plain transposes: X = XU*XV^T) with A, B, C low
+ * rank and complex, then recompression to the first i >= 1 singular values
+ * with sigma_i >= acc (or rk).  Ranks as double* (value in, new rank of C out
+ * in Crk[0]).  Limits of this library: M <= 1024, Ark + Crk <= 256. */
+void HCORE_zgemm(HCORE_enum transA, int transB, int M, int N, hcore_dcomplex alpha,
+                 hcore_dcomplex *AU, hcore_dcomplex *AV, double *Ark, int LDA, hcore_dcomplex *BU,
+                 hcore_dcomplex *BV, double *Brk, int LDB, hcore_dcomplex beta,
+                 hcore_dcomplex *CU, hcore_dcomplex *CV, double *Crk, int LDC, int rk, int maxrk,
+                 double acc, hcore_dcomplex *work, flop_counter *flops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

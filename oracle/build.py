@@ -38,6 +38,7 @@ REF_SOURCES = [
     "src/compute/hcore_dpotrf.c",
     "src/compute/hcore_dtrsm.c",
     "src/compute/hcore_duncompress.c",
+    "src/compute/hcore_zgemm.c",
     "src/misc/descutil/flop_counts.c",
 ]
 REF_TESTS = ["testing_dgemm", "testing_sgemm", "testing_dsyrk", "testing_dgemmcd"]

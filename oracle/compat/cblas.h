@@ -58,4 +58,17 @@ void cblas_dsyrk(int order, int uplo, int trans, int n, int k, double alpha,
 void cblas_dgemv(int order, int ta, int m, int n, double alpha, const double *a,
                  int lda, const double *x, int incx, double beta, double *y, int incy);
 double cblas_dnrm2(int n, const double *x, int incx);
+
+/* complex (hcore_zgemm.c): scalars by address, as CBLAS specifies */
+#define cblas_zgemm ORACLE_CB(zgemm)
+#define cblas_zcopy ORACLE_CB(zcopy)
+#define cblas_zscal ORACLE_CB(zscal)
+#define cblas_ztrmm ORACLE_CB(ztrmm)
+void cblas_zgemm(int order, int ta, int tb, int m, int n, int k, const void *alpha,
+                 const void *a, int lda, const void *b, int ldb, const void *beta, void *c,
+                 int ldc);
+void cblas_zcopy(int n, const void *x, int incx, void *y, int incy);
+void cblas_zscal(int n, const void *alpha, void *x, int incx);
+void cblas_ztrmm(int order, int side, int uplo, int ta, int diag, int m, int n,
+                 const void *alpha, const void *a, int lda, void *b, int ldb);
 #endif

@@ -76,4 +76,24 @@ float scipy_slange_(const char *, const int *, const int *, const float *,
                     const int *, float *);
 double scipy_dlamch_(const char *);
 float scipy_slamch_(const char *);
+
+/* complex (hcore_zgemm.c) */
+#define LAPACKE_zgeqrf    ORACLE_LE(zgeqrf)
+#define LAPACKE_zgesvd    ORACLE_LE(zgesvd)
+#define LAPACKE_zunmqr    ORACLE_LE(zunmqr)
+#define LAPACKE_zlacpy    ORACLE_LE(zlacpy)
+#define LAPACKE_zge_trans ORACLE_LE(zge_trans)
+#define zlacpy_ scipy_zlacpy_
+#define zlaset_ scipy_zlaset_
+int LAPACKE_zgeqrf(int, int, int, double _Complex *, int, double _Complex *);
+int LAPACKE_zgesvd(int, char, char, int, int, double _Complex *, int, double *,
+                   double _Complex *, int, double _Complex *, int, double *);
+int LAPACKE_zunmqr(int, char, char, int, int, int, const double _Complex *, int,
+                   const double _Complex *, double _Complex *, int);
+int LAPACKE_zlacpy(int, char, int, int, const double _Complex *, int, double _Complex *, int);
+void LAPACKE_zge_trans(int, int, int, const double _Complex *, int, double _Complex *, int);
+void scipy_zlacpy_(const char *, const int *, const int *, const double _Complex *,
+                   const int *, double _Complex *, const int *);
+void scipy_zlaset_(const char *, const int *, const int *, const double _Complex *,
+                   const double _Complex *, double _Complex *, const int *);
 #endif

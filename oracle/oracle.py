@@ -54,6 +54,17 @@ class FlopCounter(C.Structure):
                             ("__pad4", C.c_ulong)]
 
 
+class DComplex(C.Structure):
+    """double _Complex passed by value (two doubles, real first)."""
+
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+    @classmethod
+    def of(cls, z):
+        z = complex(z)
+        return cls(z.real, z.imag)
+
+
 class Port:
     """ctypes wrapper of the C restatement."""
 
@@ -259,6 +270,12 @@ class RefLib:
             lib.HCORE_dpotrf.restype = None
             lib.HCORE_dpotrf.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip,
                                          C.POINTER(FlopCounter)]
+            lib.HCORE_zgemm.restype = None
+            lib.HCORE_zgemm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, DComplex, C.c_void_p,
+                                        C.c_void_p, _dp, C.c_int, C.c_void_p, C.c_void_p, _dp,
+                                        C.c_int, DComplex, C.c_void_p, C.c_void_p, _dp, C.c_int,
+                                        C.c_int, C.c_int, C.c_double, C.c_void_p,
+                                        C.POINTER(FlopCounter)]
             RefLib._lib = lib
         self.lib = RefLib._lib
 
@@ -315,6 +332,27 @@ class RefLib:
                                _ptr(Bv), Brank, M, 1.0, _ptr(CDo), M, maxrank, None, C.byref(fc))
         return CDo
 
+    def zgemm(self, M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, *, rk=0, maxrk, acc):
+        """HCORE_zgemm (src/compute/hcore_zgemm.c:663) on complex128 arrays;
+        returns dict(rank, CU, CV, flops)."""
+        AU, AV, BU, BV = (np.asfortranarray(x, dtype=np.complex128) for x in (AU, AV, BU, BV))
+        ldc = CU.shape[0]
+        ncol = max(a + c, c)
+        CUo = np.zeros((ldc, ncol), dtype=np.complex128, order="F")
+        CVo = np.zeros((ldc, ncol), dtype=np.complex128, order="F")
+        CUo[:, :c] = CU[:, :c]
+        CVo[:, :c] = CV[:, :c]
+        ra, rb, rc = (np.array([v], dtype=np.float64) for v in (a, b, c))
+        fc = FlopCounter()
+        p = lambda x: x.ctypes.data_as(C.c_void_p)  # noqa: E731
+        self.lib.HCORE_zgemm(111, 112, M, M, DComplex.of(alpha), p(AU), p(AV), _ptr(ra),
+                             AU.shape[0], p(BU), p(BV), _ptr(rb), BV.shape[0],
+                             DComplex.of(beta), p(CUo), p(CVo), _ptr(rc), ldc, rk, maxrk, acc,
+                             None, C.byref(fc))
+        r = int(rc[0])
+        return dict(rank=r, CU=CUo[:, :r].copy(order="F"), CV=CVo[:, :r].copy(order="F"),
+                    flops=fc.update)
+
     _test_lib = None
 
     def generate_compress(self, M, acc, maxrank, iseed):
@@ -370,6 +408,26 @@ class RefLib:
         fc = FlopCounter()
         self.lib.HCORE_dpotrf(uplo, N, _ptr(Ao), Ao.shape[0], C.byref(info), C.byref(fc))
         return Ao, info.value, fc.potrf
+
+
+def zgemm_dense_truncation(alpha, AU, AV, BU, BV, beta, CU, CV, *, rk=0, acc):
+    """The complex update's mathematics restated densely (numpy, small cases):
+    C = beta CU CV^T + alpha AU AV^T (BU BV^T)^T with plain transposes
+    (hcore_zgemm.c:138-220), its singular values, and the truncation of
+    hcore_zgemm.c's rank rule (the first i >= 1 with sigma_i < acc, or
+    min(rk, k)).  Returns (rank, truncated product, sigma)."""
+    Cd = beta * (CU @ CV.T) + alpha * (AU @ AV.T) @ (BU @ BV.T).T
+    k = AU.shape[1] + CU.shape[1]
+    U, S, Vh = np.linalg.svd(Cd)
+    if rk:
+        r = min(rk, k)
+    else:
+        r = k
+        for i in range(1, k):
+            if S[i] < acc:
+                r = i
+                break
+    return r, (U[:, :r] * S[:r]) @ Vh[:r], S[:k]
 
 
 # --------------------------------------------------------------------------

@@ -84,6 +84,19 @@ def golden_compress():
 
 
 @pytest.fixture(scope="session")
+def golden_zgemm():
+    """Reference outputs of HCORE_zgemm."""
+    import json
+
+    import numpy as np
+
+    d = os.path.join(ROOT, "tests", "golden")
+    with open(os.path.join(d, "golden_zgemm_meta.json")) as f:
+        meta = json.load(f)
+    return meta, dict(np.load(os.path.join(d, "golden_zgemm.npz")))
+
+
+@pytest.fixture(scope="session")
 def hc():
     """The GPU library, built if absent (the GPU machine builds it via build())."""
     import hcore_gb300

@@ -21,7 +21,10 @@ through ctypes on seeded inputs.  The outputs are committed as
 * ``golden_compress.npz`` / ``golden_compress_meta.json`` — the reference
   tests' compressor (generate_compress) on dlatms tiles.
 
-Usage:  python tests/golden/make_golden.py [--tlr-only | --compress-only]
+* ``golden_zgemm.npz`` / ``golden_zgemm_meta.json`` — the reference's
+  HCORE_zgemm (complex) on seeded complex low-rank inputs.
+
+Usage:  python tests/golden/make_golden.py [--tlr-only | --compress-only | --zgemm-only]
 """
 from __future__ import annotations
 
@@ -290,9 +293,55 @@ def make_compress():
     print("compress cases:", [(c["M"], c["rank"]) for c in meta])
 
 
+def complex_lowrank(rng, M, k, decades):
+    """U diag(sigma) and V with complex orthonormal U, V (QR of complex
+    Gaussians), sigma_i = 10^(-decades*i/k) folded into U."""
+    U, _ = np.linalg.qr(rng.standard_normal((M, k)) + 1j * rng.standard_normal((M, k)))
+    V, _ = np.linalg.qr(rng.standard_normal((M, k)) + 1j * rng.standard_normal((M, k)))
+    s = 10.0 ** (-decades * np.arange(k) / k)
+    return np.asfortranarray(U * s), np.asfortranarray(V)
+
+
+# (name, M, a, b, c, alpha, beta, rk, maxrk, acc)
+ZGEMM_CASES = [
+    ("z_small", 64, 6, 7, 5, 1 + 0.5j, 0.8 - 0.2j, 0, 16, 1e-8),
+    ("z_schur", 96, 12, 10, 14, -1.0, 1.0, 0, 40, 1e-6),
+    ("z_fixed", 80, 10, 9, 11, 1.0, 1.0, 5, 24, 1e-8),
+    ("z_rank1", 48, 1, 1, 1, 0.5j, 1.0, 0, 4, 1e-8),
+]
+
+
+def make_zgemm():
+    """Fixtures of the reference's HCORE_zgemm (golden_zgemm.npz / .json)."""
+    ref = O.RefLib()
+    meta, arrs = [], {}
+    for i, (name, M, a, b, c, alpha, beta, rk, maxrk, acc) in enumerate(ZGEMM_CASES):
+        rng = np.random.default_rng(900 + i)
+        AU, AV = complex_lowrank(rng, M, a, 8)
+        BU, BV = complex_lowrank(rng, M, b, 8)
+        CU, CV = complex_lowrank(rng, M, c, 8)
+        out = ref.zgemm(M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, rk=rk, maxrk=maxrk,
+                        acc=acc)
+        for nm, v in dict(AU=AU, AV=AV, BU=BU, BV=BV, CU=CU, CV=CV, CUo=out["CU"],
+                          CVo=out["CV"]).items():
+            arrs[f"{name}_{nm}"] = v
+        meta.append(dict(name=name, M=M, a=a, b=b, c=c,
+                         alpha=[complex(alpha).real, complex(alpha).imag],
+                         beta=[complex(beta).real, complex(beta).imag], rk=rk, maxrk=maxrk,
+                         acc=acc, rank=out["rank"], flops=out["flops"]))
+    np.savez_compressed(os.path.join(OUT, "golden_zgemm.npz"), **arrs)
+    with open(os.path.join(OUT, "golden_zgemm_meta.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print("zgemm cases:", [(c["name"], c["rank"]) for c in meta])
+
+
 if __name__ == "__main__":
-    if "--tlr-only" not in sys.argv and "--compress-only" not in sys.argv:
+    only = [a for a in sys.argv[1:] if a.endswith("-only")]
+    if not only:
         main()
-    if "--compress-only" not in sys.argv:
+    if not only or "--tlr-only" in only:
         make_tlr()
-    make_compress()
+    if not only or "--compress-only" in only:
+        make_compress()
+    if not only or "--zgemm-only" in only:
+        make_zgemm()

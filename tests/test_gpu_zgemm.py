@@ -1,0 +1,108 @@
+"""HCORE_zgemm (complex update) on the GPU against the reference's fixtures and
+the dense restatement.
+
+The library runs the complex update as a real update of twice the order and
+ranks (X -> [Re X, -Im X; Im X, Re X]) through the FP64 plan, then takes one
+complex vector per pair of equal singular values.  Gates: the rank equals the
+reference's, the product agrees to 1e-11 relative Frobenius, the flop count
+equals the reference's; CU has orthonormal columns and CV carries the singular
+values.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _clr(rng, M, k, decades):
+    U, _ = np.linalg.qr(rng.standard_normal((M, k)) + 1j * rng.standard_normal((M, k)))
+    V, _ = np.linalg.qr(rng.standard_normal((M, k)) + 1j * rng.standard_normal((M, k)))
+    return np.asfortranarray(U * 10.0 ** (-decades * np.arange(k) / k)), np.asfortranarray(V)
+
+
+def _rel(P, Q):
+    return np.linalg.norm(P - Q) / np.linalg.norm(Q)
+
+
+def test_zgemm_matches_reference_fixtures(hc, golden_zgemm):
+    meta, g = golden_zgemm
+    for c in meta:
+        n = c["name"]
+        r, CU, CV, fl = hc.hcore_zgemm(c["M"], complex(*c["alpha"]), g[f"{n}_AU"], g[f"{n}_AV"],
+                                       c["a"], g[f"{n}_BU"], g[f"{n}_BV"], c["b"],
+                                       complex(*c["beta"]), g[f"{n}_CU"], g[f"{n}_CV"], c["c"],
+                                       rk=c["rk"], maxrk=c["maxrk"], acc=c["acc"])
+        assert r == c["rank"], (n, r, c["rank"])
+        assert _rel(CU @ CV.T, g[f"{n}_CUo"] @ g[f"{n}_CVo"].T) < 1e-11, n
+        assert fl == c["flops"]
+        assert np.abs(CU.conj().T @ CU - np.eye(r)).max() < 1e-12
+        sv_ref = np.linalg.norm(g[f"{n}_CVo"], axis=0)
+        assert np.allclose(np.linalg.norm(CV, axis=0), sv_ref, rtol=1e-10, atol=1e-15)
+
+
+@pytest.mark.parametrize("M,a,c", [(512, 32, 32), (1024, 20, 24)])
+def test_zgemm_large_against_dense_truncation(hc, M, a, c):
+    """Orders 512 and 1024 (the largest, a real order of 2048) against the
+    dense restatement; the inputs' singular values are graded, so none lies
+    near the threshold (checked)."""
+    rng = np.random.default_rng(M + a)
+    AU, AV = _clr(rng, M, a, 10)
+    BU, BV = _clr(rng, M, a, 10)
+    CU, CV = _clr(rng, M, c, 10)
+    rr, P, S = O.zgemm_dense_truncation(-1.0, AU, AV, BU, BV, 1.0, CU, CV, acc=1e-8)
+    assert np.all(np.abs(S - 1e-8) > 1e-3 * 1e-8)
+    r, CUo, CVo, _ = hc.hcore_zgemm(M, -1.0, AU, AV, a, BU, BV, a, 1.0, CU, CV, c, maxrk=2 * (a + c),
+                                    acc=1e-8)
+    assert r == rr
+    assert _rel(CUo @ CVo.T, P) < 1e-11
+
+
+def test_zgemm_repeated_singular_values(hc):
+    """C = Q Q2^T with all its singular values equal (one degenerate cluster of
+    multiplicity 6) plus a small A B^T: the rank and the product still match
+    the dense restatement."""
+    rng = np.random.default_rng(91)
+    M, a, c = 128, 3, 6
+    Q, _ = np.linalg.qr(rng.standard_normal((M, c)) + 1j * rng.standard_normal((M, c)))
+    Q2, _ = np.linalg.qr(rng.standard_normal((M, c)) + 1j * rng.standard_normal((M, c)))
+    AU, AV = _clr(rng, M, a, 4)
+    BU, BV = _clr(rng, M, a, 4)
+    AU *= 1e-3
+    rr, P, _ = O.zgemm_dense_truncation(1.0, AU, AV, BU, BV, 1.0, Q, Q2, acc=1e-10)
+    r, CUo, CVo, _ = hc.hcore_zgemm(M, 1.0, AU, AV, a, BU, BV, a, 1.0, np.asfortranarray(Q),
+                                    np.asfortranarray(Q2), c, maxrk=2 * (a + c), acc=1e-10)
+    assert r == rr
+    assert _rel(CUo @ CVo.T, P) < 1e-11
+
+
+def test_zgemm_device_memory_inputs(hc, golden_zgemm):
+    """The same entry point with the factors in device memory."""
+    import ctypes as C
+
+    import torch
+
+    meta, g = golden_zgemm
+    c = meta[1]
+    n = c["name"]
+    M = c["M"]
+    dev = {k: torch.from_numpy(np.ascontiguousarray(g[f"{n}_{k}"].T)).cuda()
+           for k in ("AU", "AV", "BU", "BV")}
+    k = c["a"] + c["c"]
+    CU = torch.zeros((k, M), dtype=torch.complex128, device="cuda")
+    CV = torch.zeros_like(CU)
+    CU[:c["c"]] = torch.from_numpy(np.ascontiguousarray(g[f"{n}_CU"].T)).cuda()
+    CV[:c["c"]] = torch.from_numpy(np.ascontiguousarray(g[f"{n}_CV"].T)).cuda()
+    ra, rb, rc = (np.array([v], dtype=np.float64) for v in (c["a"], c["b"], c["c"]))
+    dp = C.POINTER(C.c_double)
+    fc = hc.FlopCounter()
+    hc.lib().HCORE_zgemm(111, 112, M, M, hc.DComplex(*c["alpha"]), dev["AU"].data_ptr(),
+                         dev["AV"].data_ptr(), ra.ctypes.data_as(dp), M, dev["BU"].data_ptr(),
+                         dev["BV"].data_ptr(), rb.ctypes.data_as(dp), M, hc.DComplex(*c["beta"]),
+                         CU.data_ptr(), CV.data_ptr(), rc.ctypes.data_as(dp), M, c["rk"],
+                         c["maxrk"], c["acc"], None, C.byref(fc))
+    r = int(rc[0])
+    assert r == c["rank"]
+    P = CU[:r].cpu().numpy().T @ CV[:r].cpu().numpy()
+    assert _rel(P, g[f"{n}_CUo"] @ g[f"{n}_CVo"].T) < 1e-11

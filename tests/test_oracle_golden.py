@@ -191,3 +191,22 @@ def test_port_compress_matches_reference(port, golden_compress):
         assert r == c["rank"]
         if r:
             _close(U @ V.T, g[f"{n}_U"] @ g[f"{n}_V"].T, 1e-13)
+
+
+def test_complex_restatement_matches_reference_zgemm(golden_zgemm):
+    """The dense restatement of the complex update (plain transposes, the
+    reference's rank rule) against HCORE_zgemm's fixtures: same rank, same
+    product; the flop model of HCORE_dgemm applies unchanged."""
+    from hcore_gb300.panel import update_flops
+
+    meta, g = golden_zgemm
+    for c in meta:
+        n = c["name"]
+        alpha, beta = complex(*c["alpha"]), complex(*c["beta"])
+        r, P, _ = O.zgemm_dense_truncation(alpha, g[f"{n}_AU"], g[f"{n}_AV"], g[f"{n}_BU"],
+                                           g[f"{n}_BV"], beta, g[f"{n}_CU"], g[f"{n}_CV"],
+                                           rk=c["rk"], acc=c["acc"])
+        assert r == c["rank"]
+        Pref = g[f"{n}_CUo"] @ g[f"{n}_CVo"].T
+        assert np.linalg.norm(P - Pref) <= 1e-12 * np.linalg.norm(Pref)
+        assert update_flops(c["M"], c["a"], c["b"], c["c"], r) == c["flops"]
