@@ -60,17 +60,19 @@ def test_zgemm_large_against_dense_truncation(hc, M, a, c):
 
 
 def test_zgemm_repeated_singular_values(hc):
-    """C = Q Q2^T with all its singular values equal (one degenerate cluster of
-    multiplicity 6) plus a small A B^T: the rank and the product still match
-    the dense restatement."""
+    """C = Q Q2^T with all its singular values equal (a cluster of
+    multiplicity 6, split only by an A B^T of size 1e-13, below acc): in the
+    real embedding the 12 equal values mix freely, and the complex factors
+    still come out with the rank and the product of the dense restatement."""
     rng = np.random.default_rng(91)
     M, a, c = 128, 3, 6
     Q, _ = np.linalg.qr(rng.standard_normal((M, c)) + 1j * rng.standard_normal((M, c)))
     Q2, _ = np.linalg.qr(rng.standard_normal((M, c)) + 1j * rng.standard_normal((M, c)))
     AU, AV = _clr(rng, M, a, 4)
     BU, BV = _clr(rng, M, a, 4)
-    AU *= 1e-3
+    AU *= 1e-13
     rr, P, _ = O.zgemm_dense_truncation(1.0, AU, AV, BU, BV, 1.0, Q, Q2, acc=1e-10)
+    assert rr == c
     r, CUo, CVo, _ = hc.hcore_zgemm(M, 1.0, AU, AV, a, BU, BV, a, 1.0, np.asfortranarray(Q),
                                     np.asfortranarray(Q2), c, maxrk=2 * (a + c), acc=1e-10)
     assert r == rr
