@@ -187,3 +187,107 @@ int port_dcompress(int M, int N, const double *D, int ldd, double acc, int relat
     free(A); free(tU); free(tV); free(sup);
     return info == 0 ? PORT_OK : PORT_E_LAPACK;
 }
+
+/* ---- HCORE_zgemm (src/compute/hcore_zgemm.c:663-976), restated with the
+ * same complex LAPACK/BLAS calls: __zqra stacks [beta*CU | alpha*AU] and
+ * zgeqrf (:65-135); __zqrb F = AV^T BV, G = BU F^T, [CV | G], zgeqrf
+ * (:138-220; plain transposes); __zsvd T = R_A R_B^T, zgesvd('A','A'), the
+ * rank rule, rows of V^H scaled by sigma (:222-430); __znewu zunmqr('L','N')
+ * (:435-560); __znewv conj, zunmqr('R','C'), conj, transpose (:561-640),
+ * i.e. CV = (S_r V^H_r Q_B^T)^T.  ld_newV = maxrk as in HCORE_dgemm. ---- */
+#include <complex.h>
+typedef double _Complex zdouble;
+void scipy_cblas_zgemm(int, int, int, int, int, int, const void *, const void *, int,
+                       const void *, int, const void *, void *, int);
+int scipy_LAPACKE_zgeqrf(int, int, int, zdouble *, int, zdouble *);
+int scipy_LAPACKE_zgesvd(int, char, char, int, int, zdouble *, int, double *, zdouble *, int,
+                         zdouble *, int, double *);
+int scipy_LAPACKE_zunmqr(int, char, char, int, int, int, const zdouble *, int, const zdouble *,
+                         zdouble *, int);
+
+int port_zgemm(int M, zdouble alpha, const zdouble *AU, const zdouble *AV, int a, int lda,
+               const zdouble *BU, const zdouble *BV, int b, int ldb, zdouble beta, zdouble *CU,
+               zdouble *CV, int *c_inout, int ldc, int rk, int maxrk, double acc,
+               unsigned long *flops_update)
+{
+    const int c = *c_inout;
+    if (a == 0 || b == 0 || c == 0) return PORT_E_ZERO_RANK;  /* :703-706 */
+    if (a + c > 2 * maxrk) return PORT_E_RANK_SUM;
+    const int k = a + c;
+    if (k > M) return PORT_E_SHAPE;
+    if (maxrk < k) return PORT_E_LDNEWV;
+    unsigned long fl = 0;
+    const zdouble one = 1.0, zero = 0.0;
+    zdouble *UA = calloc((size_t)M * k, sizeof(zdouble)), *VB = calloc((size_t)M * k, sizeof(zdouble));
+    zdouble *tauA = calloc(k, sizeof(zdouble)), *tauB = calloc(k, sizeof(zdouble));
+    zdouble *T = calloc((size_t)k * k, sizeof(zdouble)), *U = calloc((size_t)k * k, sizeof(zdouble));
+    zdouble *VT = calloc((size_t)k * k, sizeof(zdouble)), *F = calloc((size_t)a * b, sizeof(zdouble));
+    double *s = calloc(k, sizeof(double)), *superb = calloc(k, sizeof(double));
+    int status = PORT_OK, i, j, l, r;
+    for (j = 0; j < c; j++)
+        for (i = 0; i < M; i++) UA[(size_t)j * M + i] = beta * CU[(size_t)j * ldc + i];
+    for (j = 0; j < a; j++)
+        for (i = 0; i < M; i++) UA[(size_t)(c + j) * M + i] = alpha * AU[(size_t)j * lda + i];
+    if (scipy_LAPACKE_zgeqrf(LAPACK_COL_MAJOR, M, k, UA, M, tauA)) { status = PORT_E_LAPACK; goto done; }
+    fl += port_flop_counts('q', M, k, 0, 0);
+    for (j = 0; j < c; j++)
+        for (i = 0; i < M; i++) VB[(size_t)j * M + i] = CV[(size_t)j * ldc + i];
+    scipy_cblas_zgemm(CblasColMajor, CblasTrans, CblasNoTrans, a, b, M, &one, AV, lda, BV, ldb,
+                      &zero, F, a);
+    scipy_cblas_zgemm(CblasColMajor, CblasNoTrans, CblasTrans, M, a, b, &one, BU, ldb, F, a,
+                      &zero, VB + (size_t)c * M, M);
+    fl += port_flop_counts('m', a, b, M, 0) + port_flop_counts('m', M, a, b, 0);
+    if (scipy_LAPACKE_zgeqrf(LAPACK_COL_MAJOR, M, k, VB, M, tauB)) { status = PORT_E_LAPACK; goto done; }
+    fl += port_flop_counts('q', M, k, 0, 0);
+    for (j = 0; j < k; j++)
+        for (i = 0; i < k; i++) {
+            zdouble t = 0;
+            for (l = (i > j ? i : j); l < k; l++) t += UA[(size_t)l * M + i] * VB[(size_t)l * M + j];
+            T[(size_t)j * k + i] = t;
+        }
+    if (scipy_LAPACKE_zgesvd(LAPACK_COL_MAJOR, 'A', 'A', k, k, T, k, s, U, k, VT, k, superb)) {
+        status = PORT_E_LAPACK; goto done;
+    }
+    fl += port_flop_counts('s', k, 0, 0, 0);
+    if (rk != 0) {
+        r = rk > k ? k : rk;
+    } else {
+        r = k;
+        for (i = 1; i < k; i++)
+            if (s[i] < acc) { r = i; break; }
+    }
+    if (r > maxrk) { status = PORT_E_RANK_MAX; goto done; }
+    for (i = 0; i < r; i++)
+        for (j = 0; j < k; j++) VT[(size_t)j * k + i] *= s[i];
+    fl += (unsigned long)r * (unsigned long)k;
+    {   /* CU = Q_A [U_r; 0] */
+        zdouble *X = calloc((size_t)M * r, sizeof(zdouble));
+        for (j = 0; j < r; j++)
+            for (i = 0; i < k; i++) X[(size_t)j * M + i] = U[(size_t)j * k + i];
+        if (scipy_LAPACKE_zunmqr(LAPACK_COL_MAJOR, 'L', 'N', M, r, k, UA, M, tauA, X, M)) {
+            free(X); status = PORT_E_LAPACK; goto done;
+        }
+        fl += port_flop_counts('o', M, r, k, 1);
+        for (j = 0; j < r; j++)
+            for (i = 0; i < M; i++) CU[(size_t)j * ldc + i] = X[(size_t)j * M + i];
+        free(X);
+    }
+    {   /* CV = (S_r V^H_r Q_B^T)^T = conj(conj(S_r V^H_r) Q_B^H)^T */
+        zdouble *X = calloc((size_t)r * M, sizeof(zdouble));
+        for (j = 0; j < k; j++)
+            for (i = 0; i < r; i++) X[(size_t)j * r + i] = conj(VT[(size_t)j * k + i]);
+        if (scipy_LAPACKE_zunmqr(LAPACK_COL_MAJOR, 'R', 'C', r, M, k, VB, M, tauB, X, r)) {
+            free(X); status = PORT_E_LAPACK; goto done;
+        }
+        fl += port_flop_counts('o', r, M, k, 2);
+        for (j = 0; j < r; j++)
+            for (i = 0; i < M; i++) CV[(size_t)j * ldc + i] = conj(X[(size_t)i * r + j]);
+        free(X);
+    }
+    *c_inout = r;
+done:
+    if (flops_update) *flops_update += fl;
+    free(UA); free(VB); free(tauA); free(tauB); free(T); free(U); free(VT); free(F);
+    free(s); free(superb);
+    return status;
+}

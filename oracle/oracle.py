@@ -95,6 +95,11 @@ class Port:
                                        C.c_double, _dp, C.c_int, _dp, C.c_int, _ulp]
             lib.port_dpotrf.restype = C.c_int
             lib.port_dpotrf.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ulp]
+            lib.port_zgemm.restype = C.c_int
+            lib.port_zgemm.argtypes = [C.c_int, DComplex, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_int, C.c_int, DComplex,
+                                       C.c_void_p, C.c_void_p, _ip, C.c_int, C.c_int, C.c_int,
+                                       C.c_double, _ulp]
             lib.port_dcompress.restype = C.c_int
             lib.port_dcompress.argtypes = [C.c_int, C.c_int, _dp, C.c_int, C.c_double, C.c_int,
                                            C.c_int, _dp, _dp, C.c_int, _ip, _dp]
@@ -189,6 +194,25 @@ class Port:
         fl = C.c_ulong(0)
         info = self.lib.port_dpotrf(uplo, N, _ptr(Ao), Ao.shape[0], C.byref(fl))
         return Ao, info, fl.value
+
+    def zgemm(self, M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, *, rk=0, maxrk, acc):
+        """The restated HCORE_zgemm on complex128 arrays: dict(status, rank, CU,
+        CV, flops)."""
+        AU, AV, BU, BV = (np.asfortranarray(x, dtype=np.complex128) for x in (AU, AV, BU, BV))
+        ldc = CU.shape[0]
+        ncol = max(a + c, c, 1)
+        CUo = np.zeros((ldc, ncol), dtype=np.complex128, order="F")
+        CVo = np.zeros((ldc, ncol), dtype=np.complex128, order="F")
+        CUo[:, :c] = CU[:, :c]
+        CVo[:, :c] = CV[:, :c]
+        crk = C.c_int(c)
+        fl = C.c_ulong(0)
+        p = lambda x: x.ctypes.data_as(C.c_void_p)  # noqa: E731
+        st = self.lib.port_zgemm(M, DComplex.of(alpha), p(AU), p(AV), a, AU.shape[0], p(BU),
+                                 p(BV), b, BV.shape[0], DComplex.of(beta), p(CUo), p(CVo),
+                                 C.byref(crk), ldc, rk, maxrk, acc, C.byref(fl))
+        r = crk.value
+        return dict(status=st, rank=r, CU=CUo[:, :r], CV=CVo[:, :r], flops=fl.value)
 
     def dcompress(self, D, acc, maxrank, relative=False):
         """generate_compress's SVD truncation of a dense tile: returns

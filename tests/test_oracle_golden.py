@@ -210,3 +210,17 @@ def test_complex_restatement_matches_reference_zgemm(golden_zgemm):
         Pref = g[f"{n}_CUo"] @ g[f"{n}_CVo"].T
         assert np.linalg.norm(P - Pref) <= 1e-12 * np.linalg.norm(Pref)
         assert update_flops(c["M"], c["a"], c["b"], c["c"], r) == c["flops"]
+
+
+def test_port_zgemm_matches_reference(port, golden_zgemm):
+    """The C restatement of HCORE_zgemm against its fixtures: rank, flops and
+    the product (within 1e-12: the same LAPACK calls)."""
+    meta, g = golden_zgemm
+    for c in meta:
+        n = c["name"]
+        out = port.zgemm(c["M"], complex(*c["alpha"]), g[f"{n}_AU"], g[f"{n}_AV"], c["a"],
+                         g[f"{n}_BU"], g[f"{n}_BV"], c["b"], complex(*c["beta"]), g[f"{n}_CU"],
+                         g[f"{n}_CV"], c["c"], rk=c["rk"], maxrk=c["maxrk"], acc=c["acc"])
+        assert out["status"] == 0 and out["rank"] == c["rank"] and out["flops"] == c["flops"]
+        Pref = g[f"{n}_CUo"] @ g[f"{n}_CVo"].T
+        assert np.linalg.norm(out["CU"] @ out["CV"].T - Pref) <= 1e-12 * np.linalg.norm(Pref)
