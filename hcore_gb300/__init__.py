@@ -214,6 +214,9 @@ def lib() -> C.CDLL:
     L.HCORE_zgemm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, DComplex, vp, vp, _dp, C.c_int,
                               vp, vp, _dp, C.c_int, DComplex, vp, vp, _dp, C.c_int, C.c_int,
                               C.c_int, C.c_double, vp, C.POINTER(FlopCounter)]
+    L.HCORE_zuncompress.restype = None
+    L.HCORE_zuncompress.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, DComplex, vp, _dp, C.c_int,
+                                    vp, _dp, C.c_int, DComplex, vp, C.c_int]
     L.HCORE_duncompress.restype = None
     L.HCORE_duncompress.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp,
                                     C.c_int, _dp, _dp, C.c_int, C.c_double, _dp, C.c_int]

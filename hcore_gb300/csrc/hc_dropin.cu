@@ -1287,3 +1287,63 @@ extern "C" void HCORE_zgemm(HCORE_enum transA, int transB, int M, int N, hcore_d
     Crk[0] = r;
     if (flops) flops->update += update_flops(M, a, b, c, r, false);  // hcore_zgemm.c: same model
 }
+
+// HCORE_zuncompress (src/compute/hcore_zuncompress.c:35-86): CD = AU BV^T
+// in complex arithmetic (alpha and beta unused, Ark == Brk asserted), as two
+// real uncompress tasks of rank 2a on the dense tile kernel:
+//   Re CD = [Re AU, -Im AU] [Re BV, Im BV]^T,  Im CD = [Re AU, Im AU] [Im BV, Re BV]^T.
+extern "C" void HCORE_zuncompress(HCORE_enum transA, HCORE_enum transB, int M, int N,
+                                  hcore_dcomplex alpha, hcore_dcomplex *AU, double *Ark, int LDA,
+                                  hcore_dcomplex *BV, double *Brk, int LDB, hcore_dcomplex beta,
+                                  hcore_dcomplex *CD, int LDC) {
+    (void)transA; (void)transB; (void)alpha; (void)beta;
+    const char *fn = "HCORE_zuncompress";
+    const long long a = (long long)Ark[0], b = (long long)Brk[0];
+    if (a != b) fatal("%s: Ark (%lld) and Brk (%lld) must be equal\n", fn, a, b);
+    if (M <= 0 || N <= 0) return;
+    if (LDA < M || LDB < N || LDC < M)
+        fatal("%s: invalid leading dimension (LDA %d, LDB %d, LDC %d)\n", fn, LDA, LDB, LDC);
+    const int r = (int)a;
+    const std::vector<zc> xU = zget(AU, M, r, LDA), xV = zget(BV, N, r, LDB);
+    // host: [Re U | -Im U], [Re U | Im U] (M x 2r); [Re V | Im V], [Im V | Re V] (N x 2r)
+    std::vector<double> h((size_t)2 * M * 2 * r + (size_t)2 * N * 2 * r);
+    double *Pre = h.data(), *Pim = Pre + (size_t)M * 2 * r, *Qre = Pim + (size_t)M * 2 * r,
+           *Qim = Qre + (size_t)N * 2 * r;
+    for (int j = 0; j < r; ++j) {
+        for (int i = 0; i < M; ++i) {
+            const zc u = xU[(size_t)j * M + i];
+            Pre[(size_t)j * M + i] = u.real(); Pre[(size_t)(r + j) * M + i] = -u.imag();
+            Pim[(size_t)j * M + i] = u.real(); Pim[(size_t)(r + j) * M + i] = u.imag();
+        }
+        for (int i = 0; i < N; ++i) {
+            const zc v = xV[(size_t)j * N + i];
+            Qre[(size_t)j * N + i] = v.real(); Qre[(size_t)(r + j) * N + i] = v.imag();
+            Qim[(size_t)j * N + i] = v.imag(); Qim[(size_t)(r + j) * N + i] = v.real();
+        }
+    }
+    ThreadCtx &tc = thread_ctx();
+    const size_t nin = h.size(), nout = (size_t)2 * M * N;
+    double *buf = stage_buffer(nin + nout, fn);
+    if (nin && cudaMemcpyAsync(buf, h.data(), nin * sizeof(double), cudaMemcpyHostToDevice,
+                               tc.stream) != cudaSuccess)
+        cuda_fatal(fn);
+    double *dP = buf, *dQ = buf + (size_t)2 * M * 2 * r, *dOut = buf + nin;
+    hcore_dense_task t[2] = {};
+    for (int q = 0; q < 2; ++q) {
+        t[q].kind = 2; t[q].M = M; t[q].N = N; t[q].a = 2 * r;
+        t[q].Au = dP + (size_t)q * M * 2 * r; t[q].lda = M;
+        t[q].Bv = dQ + (size_t)q * N * 2 * r; t[q].ldb = N;
+        t[q].CD = dOut + (size_t)q * M * N; t[q].ldcd = M;
+    }
+    if (run_dense(2, t, tc.stream, true)) fatal("%s: %s\n", fn, last_error());
+    std::vector<double> o(nout);
+    if (cudaMemcpyAsync(o.data(), dOut, nout * sizeof(double), cudaMemcpyDeviceToHost,
+                        tc.stream) != cudaSuccess ||
+        cudaStreamSynchronize(tc.stream) != cudaSuccess)
+        cuda_fatal(fn);
+    std::vector<zc> z((size_t)M * N);
+    for (size_t e = 0; e < (size_t)M * N; ++e) z[e] = zc(o[e], o[(size_t)M * N + e]);
+    if (cudaMemcpy2D(CD, (size_t)LDC * sizeof(zc), z.data(), M * sizeof(zc), M * sizeof(zc), N,
+                     cudaMemcpyDefault) != cudaSuccess)
+        cuda_fatal(fn);
+}

@@ -1,6 +1,7 @@
 /*
- * hcore-gb300 — complex (double _Complex) drop-in entry point, replacing
- * src/include/hcore_z.h:27-48 (src/compute/hcore_zgemm.c:663-976).
+ * hcore-gb300 — complex (double _Complex) drop-in entry points, replacing the
+ * declarations of src/include/hcore_z.h that the reference defines
+ * (src/compute/hcore_zgemm.c:663-976, src/compute/hcore_zuncompress.c:35-86).
  *
  * The prototype is the reference's.  C++ sees double _Complex as a struct of
  * two doubles, real part first: the same layout and the same argument passing
@@ -28,6 +29,13 @@ void HCORE_zgemm(HCORE_enum transA, int transB, int M, int N, hcore_dcomplex alp
                  hcore_dcomplex *BV, double *Brk, int LDB, hcore_dcomplex beta,
                  hcore_dcomplex *CU, hcore_dcomplex *CV, double *Crk, int LDC, int rk, int maxrk,
                  double acc, hcore_dcomplex *work, flop_counter *flops);
+
+/* CD = AU*BV^T (M x N, complex, plain transpose) from factors of rank
+ * Ark == Brk; alpha and beta are not used.  Replaces src/include/hcore_z.h:76-88
+ * (src/compute/hcore_zuncompress.c:35-86). */
+void HCORE_zuncompress(HCORE_enum transA, HCORE_enum transB, int M, int N, hcore_dcomplex alpha,
+                       hcore_dcomplex *AU, double *Ark, int LDA, hcore_dcomplex *BV, double *Brk,
+                       int LDB, hcore_dcomplex beta, hcore_dcomplex *CD, int LDC);
 
 #ifdef __cplusplus
 }

@@ -39,6 +39,7 @@ REF_SOURCES = [
     "src/compute/hcore_dtrsm.c",
     "src/compute/hcore_duncompress.c",
     "src/compute/hcore_zgemm.c",
+    "src/compute/hcore_zuncompress.c",
     "src/misc/descutil/flop_counts.c",
 ]
 REF_TESTS = ["testing_dgemm", "testing_sgemm", "testing_dsyrk", "testing_dgemmcd"]
@@ -116,13 +117,8 @@ def build_ref(force: bool = False) -> str | None:
         o = os.path.join(REF_OUT, os.path.basename(s).replace(".c", ".o"))
         _run(cflags + ["-c", os.path.join(REFERENCE_ROOT, s), "-o", o])
         objs.append(o)
-    # hcore_duncompress.c:23-24 declares two globals that nothing in the
-    # reference defines; this one-file definition stands in for its caller
-    frk_c = os.path.join(REF_OUT, "frk_globals.c")
-    with open(frk_c, "w") as f:
-        f.write("int gemmfrk_print_index = 0;\nint gemmfrk_print_mat = 0;\n")
-    _run(cflags + ["-c", frk_c, "-o", os.path.join(REF_OUT, "frk_globals.o")])
-    objs.append(os.path.join(REF_OUT, "frk_globals.o"))
+    # (hcore_duncompress.c:23-24 declares gemmfrk_print_index/_mat extern;
+    # hcore_zuncompress.c defines them)
     # the library leaves use_scratch to its caller (hcore_dgemm.c:38); the
     # ctypes-loaded copy gets it from this one-line definition
     glob_c = os.path.join(REF_OUT, "use_scratch.c")

@@ -300,6 +300,10 @@ class RefLib:
                                         C.c_int, DComplex, C.c_void_p, C.c_void_p, _dp, C.c_int,
                                         C.c_int, C.c_int, C.c_double, C.c_void_p,
                                         C.POINTER(FlopCounter)]
+            lib.HCORE_zuncompress.restype = None
+            lib.HCORE_zuncompress.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, DComplex,
+                                              C.c_void_p, _dp, C.c_int, C.c_void_p, _dp, C.c_int,
+                                              DComplex, C.c_void_p, C.c_int]
             RefLib._lib = lib
         self.lib = RefLib._lib
 
@@ -376,6 +380,16 @@ class RefLib:
         r = int(rc[0])
         return dict(rank=r, CU=CUo[:, :r].copy(order="F"), CV=CVo[:, :r].copy(order="F"),
                     flops=fc.update)
+
+    def zuncompress(self, M, N, AU, a, BV, CD):
+        AU, BV = (np.asfortranarray(x, dtype=np.complex128) for x in (AU, BV))
+        CDo = np.asfortranarray(CD, dtype=np.complex128).copy(order="F")
+        ra = np.array([a], dtype=np.float64)
+        p = lambda x: x.ctypes.data_as(C.c_void_p)  # noqa: E731
+        self.lib.HCORE_zuncompress(111, 112, M, N, DComplex.of(1.0), p(AU), _ptr(ra), AU.shape[0],
+                                   p(BV), _ptr(ra), BV.shape[0], DComplex.of(0.0), p(CDo),
+                                   CDo.shape[0])
+        return CDo
 
     _test_lib = None
 

@@ -329,6 +329,13 @@ def make_zgemm():
                          alpha=[complex(alpha).real, complex(alpha).imag],
                          beta=[complex(beta).real, complex(beta).imag], rk=rk, maxrk=maxrk,
                          acc=acc, rank=out["rank"], flops=out["flops"]))
+    # HCORE_zuncompress: CD = AU BV^T (M x N), plain transpose
+    rng = np.random.default_rng(950)
+    M, N, r = 50, 40, 5
+    AU = np.asfortranarray(rng.standard_normal((M, r)) + 1j * rng.standard_normal((M, r)))
+    BV = np.asfortranarray(rng.standard_normal((N, r)) + 1j * rng.standard_normal((N, r)))
+    CD = np.asfortranarray(rng.standard_normal((M, N)) + 0j)
+    arrs.update(zunc_AU=AU, zunc_BV=BV, zunc_CDo=ref.zuncompress(M, N, AU, r, BV, CD))
     np.savez_compressed(os.path.join(OUT, "golden_zgemm.npz"), **arrs)
     with open(os.path.join(OUT, "golden_zgemm_meta.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)

@@ -108,3 +108,20 @@ def test_zgemm_device_memory_inputs(hc, golden_zgemm):
     assert r == c["rank"]
     P = CU[:r].cpu().numpy().T @ CV[:r].cpu().numpy()
     assert _rel(P, g[f"{n}_CUo"] @ g[f"{n}_CVo"].T) < 1e-11
+
+
+def test_zuncompress_matches_reference(hc, golden_zgemm):
+    """HCORE_zuncompress (CD = AU BV^T, complex) against the reference's output."""
+    import ctypes as C
+
+    _, g = golden_zgemm
+    AU, BV = g["zunc_AU"], g["zunc_BV"]
+    M, r = AU.shape
+    N = BV.shape[0]
+    CD = np.zeros((M, N), dtype=np.complex128, order="F")
+    ra = np.array([r], dtype=np.float64)
+    dp = C.POINTER(C.c_double)
+    hc.lib().HCORE_zuncompress(111, 112, M, N, hc.DComplex(1, 0), AU.ctypes.data,
+                               ra.ctypes.data_as(dp), M, BV.ctypes.data, ra.ctypes.data_as(dp), N,
+                               hc.DComplex(0, 0), CD.ctypes.data, M)
+    assert np.abs(CD - g["zunc_CDo"]).max() <= 1e-13 * np.abs(g["zunc_CDo"]).max()

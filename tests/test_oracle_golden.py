@@ -224,3 +224,9 @@ def test_port_zgemm_matches_reference(port, golden_zgemm):
         assert out["status"] == 0 and out["rank"] == c["rank"] and out["flops"] == c["flops"]
         Pref = g[f"{n}_CUo"] @ g[f"{n}_CVo"].T
         assert np.linalg.norm(out["CU"] @ out["CV"].T - Pref) <= 1e-12 * np.linalg.norm(Pref)
+
+
+def test_zuncompress_fixture_is_the_plain_transpose_product(golden_zgemm):
+    _, g = golden_zgemm
+    P = g["zunc_AU"] @ g["zunc_BV"].T
+    assert np.abs(g["zunc_CDo"] - P).max() <= 1e-13 * np.abs(P).max()
