@@ -37,7 +37,7 @@ from .build import LIB as _LIB_PATH
 
 __all__ = ["lib", "LrTask", "DenseTask", "Batch", "DensePlan", "hcore_dgemm", "hcore_sgemm", "hcore_dgemm_fast",
            "dense_batched", "TrsmTask", "PotrfTask", "trsm_batched", "potrf_batched",
-           "CompressTask", "compress_batched", "hcore_zgemm", "HcoreError", "STATUS", "FlopCounter", "RankMLP", "Tuning",
+           "CompressTask", "compress_batched", "hcore_zgemm", "ZlrTask", "zgemm_batched", "HcoreError", "STATUS", "FlopCounter", "RankMLP", "Tuning",
            "make_tuning", "autotune"]
 
 F64, F32 = 0, 1
@@ -102,6 +102,16 @@ class DComplex(C.Structure):
     """double _Complex by value (hcore_dcomplex in include/hcore_z.h)."""
 
     _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+class ZlrTask(C.Structure):
+    """Mirror of hcore_zlr_task (include/hcore_z.h)."""
+
+    _fields_ = [("M", C.c_int), ("a", C.c_int), ("b", C.c_int), ("c", C.c_int),
+                ("rk", C.c_int), ("maxrk", C.c_int), ("alpha", DComplex), ("beta", DComplex),
+                ("acc", C.c_double), ("AU", C.c_void_p), ("AV", C.c_void_p), ("lda", C.c_int),
+                ("BU", C.c_void_p), ("BV", C.c_void_p), ("ldb", C.c_int), ("CU", C.c_void_p),
+                ("CV", C.c_void_p), ("ldc", C.c_int)]
 
 
 class Tuning(C.Structure):
@@ -214,6 +224,8 @@ def lib() -> C.CDLL:
     L.HCORE_zgemm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, DComplex, vp, vp, _dp, C.c_int,
                               vp, vp, _dp, C.c_int, DComplex, vp, vp, _dp, C.c_int, C.c_int,
                               C.c_int, C.c_double, vp, C.POINTER(FlopCounter)]
+    L.hcore_gpu_zgemm_batched.argtypes = [C.c_int, C.POINTER(ZlrTask), C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int), vp]
     L.HCORE_zuncompress.restype = None
     L.HCORE_zuncompress.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, DComplex, vp, _dp, C.c_int,
                                     vp, _dp, C.c_int, DComplex, vp, C.c_int]
@@ -315,6 +327,17 @@ def hcore_zgemm(M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, *, rk=0, maxrk,
                       rc.ctypes.data_as(_dp), ldc, rk, maxrk, acc, None, C.byref(fc))
     r = int(rc[0])
     return r, CUo[:, :r], CVo[:, :r], fc.update
+
+
+def zgemm_batched(tasks, stream=None):
+    """Run ZlrTask list (complex updates, CU/CV in place); returns (ranks,
+    status) arrays."""
+    arr = (ZlrTask * max(len(tasks), 1))(*tasks)
+    r = (C.c_int * max(len(tasks), 1))()
+    st = (C.c_int * max(len(tasks), 1))()
+    _check(lib().hcore_gpu_zgemm_batched(len(tasks), arr, r, st, stream or None),
+           "hcore_gpu_zgemm_batched")
+    return (np.array(r[:len(tasks)], dtype=np.int32), np.array(st[:len(tasks)], dtype=np.int32))
 
 
 def hcore_dgemm_fast(M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, *, rk=0, maxrk, acc):

@@ -1192,6 +1192,83 @@ static void zembed(double *E, const std::vector<zc> &X, int M, int n, zc s, bool
             E[(size_t)(n + j) * M2 + M + i] = x.real();
         }
 }
+// Complex factors of C_new from the real plan's outputs eU, eV (2M x r2,
+// ld 2M): C_new = Z0 R^T, Z0 = eU_top + i eU_bottom, R = eV_top.  With
+// `mgs` false, one column per pair is taken directly (column 2j; its
+// partner must be J = [0 -I; I 0] times it, which is checked): CU_j =
+// Z0_{2j}, CV_j = eV_top_{2j} - i eV_bottom_{2j}.  Where the check fails
+// (singular values that are equal, so that pairs mix) or with `mgs` true,
+// an orthonormal basis Z of Z0's columns is taken instead (modified
+// Gram-Schmidt in column order, a column kept when more than half of it is
+// new) and CV = R (Z0^T conj Z).  Returns the complex rank.
+static int zextract(const double *eU, const double *eV, int M, int r2, bool mgs,
+                    std::vector<zc> &oU, std::vector<zc> &oV) {
+    const size_t M2 = 2 * (size_t)M;
+    if (!mgs) {
+        for (int j = 0; j + 1 < r2 && !mgs; j += 2) {  // partner == +-J * column
+            const double *u = eU + (size_t)j * M2, *w = eU + (size_t)(j + 1) * M2;
+            double d = 0;
+            for (int i = 0; i < M; ++i) d += w[i] * -u[M + i] + w[M + i] * u[i];
+            if (std::fabs(std::fabs(d) - 1.0) > 1e-6) mgs = true;
+        }
+    }
+    if (!mgs) {
+        const int r = (r2 + 1) / 2;
+        oU.assign((size_t)M * r, zc());
+        oV.assign((size_t)M * r, zc());
+        for (int q = 0; q < r; ++q) {
+            const double *u = eU + (size_t)(2 * q) * M2, *v = eV + (size_t)(2 * q) * M2;
+            for (int i = 0; i < M; ++i) {
+                oU[(size_t)q * M + i] = zc(u[i], u[M + i]);
+                oV[(size_t)q * M + i] = zc(v[i], -v[M + i]);
+            }
+        }
+        return r;
+    }
+    std::vector<zc> Z0((size_t)M * r2), Z;
+    for (int j = 0; j < r2; ++j)
+        for (int i = 0; i < M; ++i)
+            Z0[(size_t)j * M + i] = zc(eU[(size_t)j * M2 + i], eU[(size_t)j * M2 + M + i]);
+    int r = 0;
+    std::vector<zc> z(M);
+    for (int j = 0; j < r2; ++j) {
+        double n0 = 0;
+        for (int i = 0; i < M; ++i) {
+            z[i] = Z0[(size_t)j * M + i];
+            n0 += std::norm(z[i]);
+        }
+        for (int pass = 0; pass < 2; ++pass)
+            for (int q = 0; q < r; ++q) {
+                zc h = 0;
+                for (int i = 0; i < M; ++i) h += std::conj(Z[(size_t)q * M + i]) * z[i];
+                for (int i = 0; i < M; ++i) z[i] -= h * Z[(size_t)q * M + i];
+            }
+        double n1 = 0;
+        for (int i = 0; i < M; ++i) n1 += std::norm(z[i]);
+        if (n0 > 0 && n1 > 0.25 * n0) {
+            const double inv = 1.0 / std::sqrt(n1);
+            for (int i = 0; i < M; ++i) Z.push_back(z[i] * inv);
+            ++r;
+        }
+    }
+    std::vector<zc> G((size_t)r2 * r);
+    for (int q = 0; q < r; ++q)
+        for (int j = 0; j < r2; ++j) {
+            zc g = 0;
+            for (int i = 0; i < M; ++i) g += Z0[(size_t)j * M + i] * std::conj(Z[(size_t)q * M + i]);
+            G[(size_t)q * r2 + j] = g;
+        }
+    oU.assign((size_t)M * r, zc());
+    oV.assign((size_t)M * r, zc());
+    for (int q = 0; q < r; ++q)
+        for (int i = 0; i < M; ++i) {
+            zc v = 0;
+            for (int j = 0; j < r2; ++j) v += eV[(size_t)j * M2 + i] * G[(size_t)q * r2 + j];
+            oV[(size_t)q * M + i] = v;
+            oU[(size_t)q * M + i] = Z[(size_t)q * M + i];
+        }
+    return r;
+}
 }  // namespace hc
 
 extern "C" void HCORE_zgemm(HCORE_enum transA, int transB, int M, int N, hcore_dcomplex alpha,
@@ -1234,50 +1311,10 @@ extern "C" void HCORE_zgemm(HCORE_enum transA, int transB, int M, int N, hcore_d
                       M2, 1.0, eCU.data(), eCV.data(), &ec, M2, 2 * rk, 2 * maxrk, acc, nullptr,
                       false);
     const int r2 = (int)ec;
-    // C_new = Z0 R^T; orthonormal basis Z of Z0's columns
-    std::vector<zc> Z0((size_t)M * r2), Z;
-    for (int j = 0; j < r2; ++j)
-        for (int i = 0; i < M; ++i)
-            Z0[(size_t)j * M + i] = zc(eCU[(size_t)j * M2 + i], eCU[(size_t)j * M2 + M + i]);
-    int r = 0;
-    std::vector<zc> z(M);
-    for (int j = 0; j < r2; ++j) {
-        double n0 = 0;
-        for (int i = 0; i < M; ++i) {
-            z[i] = Z0[(size_t)j * M + i];
-            n0 += std::norm(z[i]);
-        }
-        for (int pass = 0; pass < 2; ++pass)
-            for (int q = 0; q < r; ++q) {
-                zc h = 0;
-                for (int i = 0; i < M; ++i) h += std::conj(Z[(size_t)q * M + i]) * z[i];
-                for (int i = 0; i < M; ++i) z[i] -= h * Z[(size_t)q * M + i];
-            }
-        double n1 = 0;
-        for (int i = 0; i < M; ++i) n1 += std::norm(z[i]);
-        if (n0 > 0 && n1 > 0.25 * n0) {
-            const double inv = 1.0 / std::sqrt(n1);
-            for (int i = 0; i < M; ++i) Z.push_back(z[i] * inv);
-            ++r;
-        }
-    }
+    std::vector<zc> oU, oV;
+    const int r = zextract(eCU.data(), eCV.data(), M, r2, true, oU, oV);
     if (r > maxrk)  // hcore_zgemm.c's r > maxrk exit
         fatal("%s: Rank after truncation is too big! finalrank:%d maxrank:%d\n", fn, r, maxrk);
-    // CV = R G, G = Z0^T conj(Z) (r2 x r)
-    std::vector<zc> G((size_t)r2 * r), oU((size_t)M * r), oV((size_t)M * r);
-    for (int q = 0; q < r; ++q)
-        for (int j = 0; j < r2; ++j) {
-            zc g = 0;
-            for (int i = 0; i < M; ++i) g += Z0[(size_t)j * M + i] * std::conj(Z[(size_t)q * M + i]);
-            G[(size_t)q * r2 + j] = g;
-        }
-    for (int q = 0; q < r; ++q)
-        for (int i = 0; i < M; ++i) {
-            zc v = 0;
-            for (int j = 0; j < r2; ++j) v += eCV[(size_t)j * M2 + i] * G[(size_t)q * r2 + j];
-            oV[(size_t)q * M + i] = v;
-            oU[(size_t)q * M + i] = Z[(size_t)q * M + i];
-        }
     if (r > 0 &&
         (cudaMemcpy2D(CU, (size_t)LDC * sizeof(zc), oU.data(), M * sizeof(zc), M * sizeof(zc), r,
                       cudaMemcpyDefault) != cudaSuccess ||
@@ -1346,4 +1383,122 @@ extern "C" void HCORE_zuncompress(HCORE_enum transA, HCORE_enum transB, int M, i
     if (cudaMemcpy2D(CD, (size_t)LDC * sizeof(zc), z.data(), M * sizeof(zc), M * sizeof(zc), N,
                      cudaMemcpyDefault) != cudaSuccess)
         cuda_fatal(fn);
+}
+
+// Batched complex updates: every task embedded as above, all of them run as
+// one real plan, the complex factors extracted per task (one column per pair
+// of equal singular values, Gram-Schmidt where pairs mix).
+extern "C" int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *ranks,
+                                       int *status, void *stream) {
+    if (n < 0 || (n > 0 && (!tasks || !ranks || !status))) {
+        set_error("hcore_gpu_zgemm_batched: invalid argument");
+        return HCORE_GPU_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    // validation on the complex ranks (the reference's exit conditions)
+    std::vector<int> run;
+    std::vector<size_t> off_in, off_out;
+    size_t n_in = 0, n_out = 0;
+    for (int q = 0; q < n; ++q) {
+        const hcore_zlr_task &t = tasks[q];
+        ranks[q] = 0;
+        int st = HCORE_GPU_S_OK;
+        if (t.a <= 0 || t.b <= 0 || t.c <= 0) st = HCORE_GPU_S_ZERO_RANK;
+        else if (t.a + t.c > 2 * t.maxrk) st = HCORE_GPU_S_RANK_SUM;
+        else if (t.maxrk < t.a + t.c) st = HCORE_GPU_S_LDNEWV;
+        else if (t.M < 1 || 2 * t.M > kMaxRowsPerLane * 32 || 2 * (t.a + t.c) > kMaxK ||
+                 t.a + t.c > t.M || t.lda < t.M || t.ldb < t.M || t.ldc < t.M)
+            st = HCORE_GPU_S_SHAPE;
+        status[q] = st;
+        if (st) continue;
+        run.push_back(q);
+        const size_t M2 = 2 * (size_t)t.M;
+        off_in.push_back(n_in);
+        n_in += M2 * 2 * (2 * (size_t)t.a + 2 * (size_t)t.b + 2 * (size_t)t.c);
+        off_out.push_back(n_out);
+        n_out += 2 * M2 * 2 * (size_t)(t.a + t.c);
+    }
+    const int nr = (int)run.size();
+    if (nr == 0) return n ? HCORE_GPU_ETASK : HCORE_GPU_OK;
+    std::vector<double> h(n_in);
+    std::vector<hcore_lr_task> rt(nr);
+    double *dbuf = nullptr;
+    if (cudaMalloc(&dbuf, (n_in + n_out) * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("hcore_gpu_zgemm_batched: cudaMalloc of %zu bytes failed",
+                  (n_in + n_out) * sizeof(double));
+        return HCORE_GPU_ENOMEM;
+    }
+    for (int x = 0; x < nr; ++x) {
+        const hcore_zlr_task &t = tasks[run[x]];
+        const int M = t.M, a = t.a, b = t.b, c = t.c, M2 = 2 * M;
+        double *p = h.data() + off_in[x];
+        double *eAU = p, *eAV = eAU + (size_t)M2 * 2 * a, *eBU = eAV + (size_t)M2 * 2 * a,
+               *eBV = eBU + (size_t)M2 * 2 * b, *eCU = eBV + (size_t)M2 * 2 * b,
+               *eCV = eCU + (size_t)M2 * 2 * c;
+        const zc al(t.alpha.re, t.alpha.im), be(t.beta.re, t.beta.im);
+        zembed(eAU, zget(t.AU, M, a, t.lda), M, a, al, false);
+        zembed(eAV, zget(t.AV, M, a, t.lda), M, a, 1.0, true);
+        zembed(eBU, zget(t.BU, M, b, t.ldb), M, b, 1.0, true);
+        zembed(eBV, zget(t.BV, M, b, t.ldb), M, b, 1.0, false);
+        zembed(eCU, zget(t.CU, M, c, t.ldc), M, c, be, false);
+        zembed(eCV, zget(t.CV, M, c, t.ldc), M, c, 1.0, true);
+        const double *d = dbuf + off_in[x];
+        double *o = dbuf + n_in + off_out[x];
+        hcore_lr_task &u = rt[x];
+        u = hcore_lr_task{};
+        u.M = M2; u.a = 2 * a; u.b = 2 * b; u.c = 2 * c; u.rk = 2 * t.rk; u.maxrk = 2 * t.maxrk;
+        u.ld_newv = 2 * t.maxrk; u.alpha = 1.0; u.beta = 1.0; u.acc = t.acc;
+        u.AU = d + (eAU - p); u.AV = d + (eAV - p); u.lda = M2;
+        u.BU = d + (eBU - p); u.BV = d + (eBV - p); u.ldb = M2;
+        u.CU = d + (eCU - p); u.CV = d + (eCV - p); u.ldc = M2;
+        u.CUo = o; u.CVo = o + (size_t)M2 * 2 * (a + c); u.ldco = M2;
+    }
+    int rc = HCORE_GPU_OK;
+    hcore_gpu_plan plan = nullptr;
+    std::vector<int> r2(nr), st2(nr);
+    if (cudaMemcpyAsync(dbuf, h.data(), n_in * sizeof(double), cudaMemcpyHostToDevice, s) !=
+        cudaSuccess) {
+        set_error("hcore_gpu_zgemm_batched: upload failed");
+        rc = HCORE_GPU_ECUDA;
+    }
+    if (rc == HCORE_GPU_OK) rc = hcore_gpu_plan_create(&plan, HCORE_GPU_F64, nr, rt.data(), 0);
+    if (rc == HCORE_GPU_OK) rc = hcore_gpu_plan_execute(plan, stream);
+    if (rc == HCORE_GPU_OK) rc = hcore_gpu_plan_results(plan, r2.data(), st2.data(), stream);
+    if (plan) hcore_gpu_plan_destroy(plan);
+    std::vector<double> out;
+    if (rc == HCORE_GPU_OK) {
+        out.resize(n_out);
+        if (cudaMemcpy(out.data(), dbuf + n_in, n_out * sizeof(double), cudaMemcpyDeviceToHost) !=
+            cudaSuccess) {
+            set_error("hcore_gpu_zgemm_batched: download failed");
+            rc = HCORE_GPU_ECUDA;
+        }
+    }
+    cudaFree(dbuf);
+    if (rc) return rc;
+    bool any = false;
+    for (int x = 0; x < nr; ++x) {
+        const hcore_zlr_task &t = tasks[run[x]];
+        const int q = run[x];
+        status[q] = st2[x];
+        if (st2[x]) { any = true; continue; }
+        const int M = t.M, M2 = 2 * M;
+        const double *eU = out.data() + off_out[x];
+        const double *eV = eU + (size_t)M2 * 2 * (t.a + t.c);
+        std::vector<zc> oU, oV;
+        const int r = zextract(eU, eV, M, r2[x], false, oU, oV);
+        if (r > t.maxrk) { status[q] = HCORE_GPU_S_RANK_MAX; any = true; continue; }
+        if (r > 0 &&
+            (cudaMemcpy2D(t.CU, (size_t)t.ldc * sizeof(zc), oU.data(), M * sizeof(zc),
+                          M * sizeof(zc), r, cudaMemcpyDefault) != cudaSuccess ||
+             cudaMemcpy2D(t.CV, (size_t)t.ldc * sizeof(zc), oV.data(), M * sizeof(zc),
+                          M * sizeof(zc), r, cudaMemcpyDefault) != cudaSuccess)) {
+            set_error("hcore_gpu_zgemm_batched: output copy failed");
+            return HCORE_GPU_ECUDA;
+        }
+        ranks[q] = r;
+    }
+    for (int q = 0; q < n && !any; ++q) any = status[q] != 0;
+    return any ? HCORE_GPU_ETASK : HCORE_GPU_OK;
 }

@@ -37,6 +37,26 @@ void HCORE_zuncompress(HCORE_enum transA, HCORE_enum transB, int M, int N, hcore
                        hcore_dcomplex *AU, double *Ark, int LDA, hcore_dcomplex *BV, double *Brk,
                        int LDB, hcore_dcomplex beta, hcore_dcomplex *CD, int LDC);
 
+/* Batched complex updates on the GPU (the same semantics per task, statuses
+ * HCORE_GPU_S_* instead of exit): all tasks run as one real plan.  CU/CV are
+ * updated in place (room for max(c, new rank) columns); pointers may be host
+ * or device memory.  Synchronous.  Returns HCORE_GPU_OK, HCORE_GPU_ETASK (a
+ * task's status is set) or a negative error. */
+typedef struct hcore_zlr_task {
+    int M, a, b, c;
+    int rk, maxrk;
+    hcore_dcomplex alpha, beta;
+    double acc;
+    const hcore_dcomplex *AU, *AV;
+    int lda;
+    const hcore_dcomplex *BU, *BV;
+    int ldb;
+    hcore_dcomplex *CU, *CV;
+    int ldc;
+} hcore_zlr_task;
+int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *ranks, int *status,
+                            void *stream);
+
 #ifdef __cplusplus
 }
 #endif

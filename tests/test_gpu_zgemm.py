@@ -125,3 +125,45 @@ def test_zuncompress_matches_reference(hc, golden_zgemm):
                                ra.ctypes.data_as(dp), M, BV.ctypes.data, ra.ctypes.data_as(dp), N,
                                hc.DComplex(0, 0), CD.ctypes.data, M)
     assert np.abs(CD - g["zunc_CDo"]).max() <= 1e-13 * np.abs(g["zunc_CDo"]).max()
+
+
+def test_zgemm_batched_against_port(hc, port):
+    """40 complex updates of mixed ranks in one batch (one real plan), one of
+    them with a degenerate singular-value cluster (extraction falls back to
+    Gram-Schmidt), and one with a zero rank (status, the rest unaffected):
+    every rank and product equals the restated reference's."""
+    rng = np.random.default_rng(92)
+    M, maxrk = 256, 64
+    tasks, keep, refs = [], [], []
+    for q in range(40):
+        a, b, c = (int(x) for x in rng.integers(1, 16, 3))
+        AU, AV = _clr(rng, M, a, 8)
+        BU, BV = _clr(rng, M, b, 8)
+        if q == 7:   # all of C's singular values equal, A B^T far below acc
+            CU, _ = np.linalg.qr(rng.standard_normal((M, c)) + 1j * rng.standard_normal((M, c)))
+            CV, _ = np.linalg.qr(rng.standard_normal((M, c)) + 1j * rng.standard_normal((M, c)))
+            CU, CV = np.asfortranarray(CU), np.asfortranarray(CV)
+            AU = np.asfortranarray(AU * 1e-13)
+        else:
+            CU, CV = _clr(rng, M, c, 8)
+        alpha, beta = complex(rng.standard_normal(), rng.standard_normal()), 1.0
+        ref = port.zgemm(M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, maxrk=maxrk, acc=1e-8)
+        oU = np.zeros((M, maxrk), dtype=np.complex128, order="F")
+        oV = np.zeros_like(oU)
+        oU[:, :c], oV[:, :c] = CU, CV
+        if q == 11:
+            c = 0  # zero rank: status 1
+        keep += [AU, AV, BU, BV, oU, oV]
+        tasks.append(hc.ZlrTask(M=M, a=a, b=b, c=c, rk=0, maxrk=maxrk,
+                                alpha=hc.DComplex(alpha.real, alpha.imag), beta=hc.DComplex(1, 0),
+                                acc=1e-8, AU=AU.ctypes.data, AV=AV.ctypes.data, lda=M,
+                                BU=BU.ctypes.data, BV=BV.ctypes.data, ldb=M, CU=oU.ctypes.data,
+                                CV=oV.ctypes.data, ldc=M))
+        refs.append((ref, oU, oV))
+    ranks, status = hc.zgemm_batched(tasks)
+    for q, ((ref, oU, oV), r, st) in enumerate(zip(refs, ranks, status)):
+        if q == 11:
+            assert st == 1
+            continue
+        assert st == 0 and r == ref["rank"], (q, st, r, ref["rank"])
+        assert _rel(oU[:, :r] @ oV[:, :r].T, ref["CU"] @ ref["CV"].T) < 1e-11, q
