@@ -51,9 +51,10 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="panel", choices=["panel", "precision", "dense", "predictor", "tlr",
                                                          "compress", "zgemm"],
-                   help="panel: the headline (config 2); precision: acc sweep (config 3); "
-                        "dense: batched dsyrk/dgemmcd tile updates (config 4); predictor: "
-                        "learned rank predictor on 3D exponential-kernel sweeps (config 5); "
+                   help="panel: the headline (1953 Schur updates of a 65,536-point TLR panel); "
+                        "precision: acc sweep on the same updates; "
+                        "dense: batched dsyrk/dgemmcd tile updates; predictor: "
+                        "learned rank predictor on 3D exponential-kernel Cholesky sweeps; "
                         "tlr: batched POTRF + TRSM, the steps either side of the update; "
                         "compress: the GPU tile compressor on the panel workload's tiles; "
                         "zgemm: the complex update through HCORE_zgemm")
@@ -66,7 +67,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--compress-tiles", type=int, default=None,
                    help="compress workload: only the first N tiles (a small profiling case)")
-    p.add_argument("--c5-shape", default=None,
+    p.add_argument("--sweep-shape", default=None,
                    help="predictor workload at a reduced shape 'block_tiles,nb,sweeps' (a quick check)")
     return p.parse_args()
 
@@ -815,7 +816,7 @@ def run_dense(args):
     barrier(world)
 
 
-C5 = dict(workload="learned rank predictor: 16 panel sweeps of a TLR Cholesky factorization",
+SWEEPS = dict(workload="learned rank predictor: 16 panel sweeps of a TLR Cholesky factorization",
           points=262144, dim=3, nb=2048, tiles_per_dim=128, block_tiles=64,
           kernel="exp(-|x-y|/0.1) (Matern 1/2)", nugget=1e-2, acc=1e-7, maxrank=256, maxrk=512,
           sweeps=16,
@@ -943,11 +944,11 @@ def run_predictor(args):
     F2, R2 = _panel_logs(hc, torch, dev, pnl, P)
     t_logs = time.time() - t0
 
-    nb, B, S = C5["nb"], C5["block_tiles"], C5["sweeps"]
-    if args.c5_shape:
-        B, nb, S = (int(x) for x in args.c5_shape.split(","))
-    MAXR, MAXRK, ACC = C5["maxrank"], C5["maxrk"], C5["acc"]
-    pts = pnl.morton_points(C5["points"], C5["dim"], 0)[:B * nb]
+    nb, B, S = SWEEPS["nb"], SWEEPS["block_tiles"], SWEEPS["sweeps"]
+    if args.sweep_shape:
+        B, nb, S = (int(x) for x in args.sweep_shape.split(","))
+    MAXR, MAXRK, ACC = SWEEPS["maxrank"], SWEEPS["maxrk"], SWEEPS["acc"]
+    pts = pnl.morton_points(SWEEPS["points"], SWEEPS["dim"], 0)[:B * nb]
     t0 = time.time()
     tiles = [(i, j) for i in range(B) for j in range(i)]
     store0 = pnl.TileStore.build(pts, nb, tiles, "exp", 0.1, 1e-7, MAXR, seed=0, device=str(dev))
@@ -957,7 +958,7 @@ def run_predictor(args):
         X = Pd[i * nb:(i + 1) * nb]
         d2 = (X * X).sum(1)[:, None] + (X * X).sum(1)[None, :] - 2.0 * X @ X.T
         K = torch.exp(-torch.sqrt(torch.clamp(d2, min=0.0)) / 0.1)
-        return (K + C5["nugget"] * torch.eye(nb, dtype=K.dtype, device=K.device)).contiguous()
+        return (K + SWEEPS["nugget"] * torch.eye(nb, dtype=K.dtype, device=K.device)).contiguous()
 
     D0 = [dense_tile(i) for i in range(B)]
     t_tiles = time.time() - t0
@@ -1207,12 +1208,12 @@ def run_predictor(args):
         return t["ok"] / ((t["ms_gemm"] + t["ms_rebuild"] + t["ms_predict"]) / 1e3)
 
     pad, prd = arms["pad"], arms["predictor"]
-    line = {"metric": "config-5 TLR Schur updates/s: predictor-sized vs pad-to-maxrank vs per-tile",
+    line = {"metric": "TLR Cholesky sweep Schur updates/s (3D kernel, nb 2048): predictor-sized vs pad-to-maxrank vs per-tile",
             "value": gemm_ups(prd), "unit": "updates/s", "n_gpus": world, "steps": 1,
             "warmup": 1, "ms_per_step": prd["ms_gemm"] + prd["ms_rebuild"] + prd["ms_predict"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded 3D points, tiles compressed on the host cores)",
-            "config": dict(C5, block_tiles=B, nb=nb, sweeps=S),
+            "config": dict(SWEEPS, block_tiles=B, nb=nb, sweeps=S),
             "pad_to_maxrank": {"updates_per_s": gemm_ups(pad),
                                **{k: v for k, v in pad.items() if k != "per_sweep"}},
             "predictor": {k: v for k, v in prd.items() if k != "per_sweep"},

@@ -116,7 +116,8 @@ def test_port_error_statuses(port):
 
 
 def test_flop_model_matches_reference_formula(port):
-    """flop_counts.c:3-70 restated; the survey's config-1 total 2.7635e7."""
+    """flop_counts.c:3-70 restated; the total of one nb=512, ranks-32 update
+    (new rank 47) is 2.7635e7."""
     M, a, b, c, r = 512, 32, 32, 32, 47
     k = a + c
     tot = (2 * port.flop_counts("q", M, k) + port.flop_counts("m", a, b, M) +
