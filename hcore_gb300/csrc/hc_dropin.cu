@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <thread>
 #include <vector>
 
 #include "hc_host.h"
@@ -1385,9 +1386,26 @@ extern "C" void HCORE_zuncompress(HCORE_enum transA, HCORE_enum transB, int M, i
         cuda_fatal(fn);
 }
 
+// run body(i) for i in [0, n) on up to 16 host threads
+template <typename F>
+static void parallel_for(int n, F body) {
+    const int nt = std::max(1, std::min<int>({n, 16, (int)std::thread::hardware_concurrency()}));
+    if (nt <= 1) {
+        for (int i = 0; i < n; ++i) body(i);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back([=, &body] {
+            for (int i = t; i < n; i += nt) body(i);
+        });
+    for (auto &th : pool) th.join();
+}
+
 // Batched complex updates: every task embedded as above, all of them run as
 // one real plan, the complex factors extracted per task (one column per pair
-// of equal singular values, Gram-Schmidt where pairs mix).
+// of equal singular values, Gram-Schmidt where pairs mix).  The host work
+// runs on up to 16 threads.
 extern "C" int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *ranks,
                                        int *status, void *stream) {
     if (n < 0 || (n > 0 && (!tasks || !ranks || !status))) {
@@ -1429,7 +1447,7 @@ extern "C" int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *
                   (n_in + n_out) * sizeof(double));
         return HCORE_GPU_ENOMEM;
     }
-    for (int x = 0; x < nr; ++x) {
+    parallel_for(nr, [&](int x) {
         const hcore_zlr_task &t = tasks[run[x]];
         const int M = t.M, a = t.a, b = t.b, c = t.c, M2 = 2 * M;
         double *p = h.data() + off_in[x];
@@ -1453,7 +1471,7 @@ extern "C" int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *
         u.BU = d + (eBU - p); u.BV = d + (eBV - p); u.ldb = M2;
         u.CU = d + (eCU - p); u.CV = d + (eCV - p); u.ldc = M2;
         u.CUo = o; u.CVo = o + (size_t)M2 * 2 * (a + c); u.ldco = M2;
-    }
+    });
     int rc = HCORE_GPU_OK;
     hcore_gpu_plan plan = nullptr;
     std::vector<int> r2(nr), st2(nr);
@@ -1477,28 +1495,35 @@ extern "C" int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *
     }
     cudaFree(dbuf);
     if (rc) return rc;
-    bool any = false;
-    for (int x = 0; x < nr; ++x) {
+    std::vector<int> copy_failed(nr, 0);
+    parallel_for(nr, [&](int x) {
         const hcore_zlr_task &t = tasks[run[x]];
         const int q = run[x];
         status[q] = st2[x];
-        if (st2[x]) { any = true; continue; }
+        if (st2[x]) return;
         const int M = t.M, M2 = 2 * M;
         const double *eU = out.data() + off_out[x];
         const double *eV = eU + (size_t)M2 * 2 * (t.a + t.c);
         std::vector<zc> oU, oV;
         const int r = zextract(eU, eV, M, r2[x], false, oU, oV);
-        if (r > t.maxrk) { status[q] = HCORE_GPU_S_RANK_MAX; any = true; continue; }
+        if (r > t.maxrk) {
+            status[q] = HCORE_GPU_S_RANK_MAX;
+            return;
+        }
         if (r > 0 &&
             (cudaMemcpy2D(t.CU, (size_t)t.ldc * sizeof(zc), oU.data(), M * sizeof(zc),
                           M * sizeof(zc), r, cudaMemcpyDefault) != cudaSuccess ||
              cudaMemcpy2D(t.CV, (size_t)t.ldc * sizeof(zc), oV.data(), M * sizeof(zc),
-                          M * sizeof(zc), r, cudaMemcpyDefault) != cudaSuccess)) {
+                          M * sizeof(zc), r, cudaMemcpyDefault) != cudaSuccess))
+            copy_failed[x] = 1;
+        ranks[q] = r;
+    });
+    for (int x = 0; x < nr; ++x)
+        if (copy_failed[x]) {
             set_error("hcore_gpu_zgemm_batched: output copy failed");
             return HCORE_GPU_ECUDA;
         }
-        ranks[q] = r;
-    }
+    bool any = false;
     for (int q = 0; q < n && !any; ++q) any = status[q] != 0;
     return any ? HCORE_GPU_ETASK : HCORE_GPU_OK;
 }
