@@ -360,7 +360,7 @@ static int run_compress(int n, const hcore_compress_task *tasks, int *ranks, int
                 compress_form_kernel<<<nd, 256, 0, s>>>(d_fw);
                 e = cudaGetLastError();
             }
-            if (e == cudaSuccess) e = configure_recompress<double>(maxK, &shape.svd_smem_kmax);
+            if (e == cudaSuccess) e = configure_recompress<double>(maxK, &shape.svd_smem_kmax, &shape.svd_half_kmax);
             if (e == cudaSuccess)
                 e = launch_recompress<double>(d_desc, nd, pws, d_rank, d_status, nullptr, shape, s,
                                               kPhaseQR | kPhaseSVD | kPhaseApply);

@@ -255,7 +255,7 @@ struct Single {
         shape.maxK = k;
         shape.nbuckets = 1;
         shape.buckets[0] = Bucket{0, 1, k};
-        cudaError_t e = configure_recompress<T>(k, &shape.svd_smem_kmax);
+        cudaError_t e = configure_recompress<T>(k, &shape.svd_smem_kmax, &shape.svd_half_kmax);
         if (e == cudaSuccess)
             e = launch_recompress<T>(d_desc, 1, ws, d_rs, d_rs + 1, nullptr, shape, tc.stream,
                                      phases);

@@ -86,6 +86,9 @@ struct Bucket {
 };
 struct LaunchShape {
     int maxM = 1, maxK = 1, svd_smem_kmax = 0;
+    // largest k whose R^T alone fits shared memory (the SVD's mode with V_J
+    // in the workspace); 0: that mode is not used
+    int svd_half_kmax = 0;
     // most output columns an accepted update may have, max of
     // min(k, storage_rank): the rebuild's grid (0: maxK)
     int maxR = 0;
@@ -110,7 +113,7 @@ int bucket_edge(int k, int width);
 // (not capturable) and returns the largest k whose Jacobi matrices fit in
 // shared memory; launch_recompress only launches (capturable).
 template <typename T>
-cudaError_t configure_recompress(int maxK, int *svd_smem_kmax);
+cudaError_t configure_recompress(int maxK, int *svd_smem_kmax, int *svd_half_kmax = nullptr);
 template <typename T>
 cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int *d_status,
                               int *d_info, const LaunchShape &shape, cudaStream_t s,

@@ -384,12 +384,12 @@ __host__ __device__ inline int svd_threads(int K, bool smem, const int *lanes) {
 }
 __host__ __device__ inline int svd_ld(int k) { return k | 1; }
 
-// Dynamic shared memory of the SVD kernel: two K x ld matrices (when they
-// fit), then the column scales, squared norms, singular values, Householder
-// scalars, and two index arrays.
+// Dynamic shared memory of the SVD kernel: `mats` K x ld matrices (2, 1 or 0:
+// the launch mode), then the column scales, squared norms, singular values,
+// Householder scalars, and two index arrays.
 template <typename T>
-__host__ __device__ inline size_t svd_smem_bytes(int K, bool in_smem) {
-    return (in_smem ? (size_t)2 * K * svd_ld(K) * sizeof(T) : 0) + (size_t)4 * (K + 1) * sizeof(T) +
+__host__ __device__ inline size_t svd_smem_bytes(int K, int mats) {
+    return (size_t)mats * K * svd_ld(K) * sizeof(T) + (size_t)4 * (K + 1) * sizeof(T) +
            (size_t)2 * (K + 1) * sizeof(int) + 64;
 }
 
@@ -413,7 +413,7 @@ __host__ __device__ inline size_t svd_smem_bytes(int K, bool in_smem) {
 // norm is below safmin is negligible (< 2^-485 relative in FP64, 2^-51 in
 // FP32) and not rotated.  A non-finite singular value marks the update
 // NOCONV; the sort below is a total order even then.
-template <typename T, bool SMEM>
+template <typename T, int MODE>
 __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__restrict__ descs,
                                                                T *__restrict__ ws,
                                                                int *__restrict__ rank,
@@ -440,15 +440,24 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
     // the k x k working matrices: column-major in shared memory (odd ld: a
     // lane walking its own column is free of bank conflicts), row-major in
     // the workspace (the lanes of a warp own consecutive columns in the
-    // tournament and in every lane-per-column loop: coalesced)
-    const int ld = SMEM ? svd_ld(k) : k;
-    const size_t rs = SMEM ? 1 : (size_t)ld;   // distance of rows i and i + 1 in a column
-    auto ix = [ld](int i, int j) -> size_t {
-        return SMEM ? (size_t)j * ld + i : (size_t)i * ld + j;
+    // tournament and in every lane-per-column loop: coalesced).  MODE 1: both
+    // in shared memory; 2: B (R^T) in shared memory, A (V_J) in the
+    // workspace; 0: both in the workspace.
+    constexpr bool A_SM = MODE == 1, B_SM = MODE >= 1;
+    const int ldA = A_SM ? svd_ld(k) : k, ldB = B_SM ? svd_ld(k) : k;
+    // distance of rows i and i + 1 in a column
+    const size_t rsA = A_SM ? 1 : (size_t)ldA, rsB = B_SM ? 1 : (size_t)ldB;
+    auto ixA = [ldA](int i, int j) -> size_t {
+        return A_SM ? (size_t)j * ldA + i : (size_t)i * ldA + j;
     };
-    T *A = SMEM ? reinterpret_cast<T *>(smem_raw) : base + L.W;   // T, then QR, then V_J
-    T *B = SMEM ? A + (size_t)maxK * svd_ld(maxK) : base + L.V;   // R^T, rotated
-    T *aux = reinterpret_cast<T *>(smem_raw + (SMEM ? (size_t)2 * maxK * svd_ld(maxK) * sizeof(T) : 0));
+    auto ixB = [ldB](int i, int j) -> size_t {
+        return B_SM ? (size_t)j * ldB + i : (size_t)i * ldB + j;
+    };
+    T *A = A_SM ? reinterpret_cast<T *>(smem_raw) : base + L.W;   // T, then QR, then V_J
+    T *B = B_SM ? reinterpret_cast<T *>(smem_raw) + (A_SM ? (size_t)maxK * svd_ld(maxK) : 0)
+                : base + L.V;                                       // R^T, rotated
+    const int nsm = (A_SM ? 1 : 0) + (B_SM ? 1 : 0);
+    T *aux = reinterpret_cast<T *>(smem_raw + (size_t)nsm * maxK * svd_ld(maxK) * sizeof(T));
     T *s_d = aux, *s_nrm = aux + (maxK + 1), *s_sig = aux + 2 * (maxK + 1);
     T *s_tau = aux + 3 * (maxK + 1);
     int *s_perm = reinterpret_cast<int *>(aux + 4 * (maxK + 1));   // Jacobi sort
@@ -459,10 +468,10 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
     T amax = 0;
     for (int o = 0; o < k; ++o)
         for (int t = tid; t < k; t += nthr) {   // the lanes walk the contiguous index
-            const int i = SMEM ? t : o, j = SMEM ? o : t;
+            const int i = A_SM ? t : o, j = A_SM ? o : t;
             T s = 0;
             for (int l = max(i, j); l < k; ++l) s += UA[(size_t)l * M + i] * VB[(size_t)l * M + j];
-            A[ix(i, j)] = s;
+            A[ixA(i, j)] = s;
             amax = max(amax, abs(s));
         }
     // scale T by 2^-e, e = exponent of its largest entry (nthr is a multiple of 32)
@@ -478,13 +487,13 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
     const int sexp = s_exp;
     if (sexp != 0)
         for (int o = 0; o < k; ++o)
-            for (int t = tid; t < k; t += nthr) A[(size_t)o * ld + t] = mul_exp2(A[(size_t)o * ld + t], -sexp);
+            for (int t = tid; t < k; t += nthr) A[(size_t)o * ldA + t] = mul_exp2(A[(size_t)o * ldA + t], -sexp);
     __syncthreads();
 
     // ---- QR with column pivoting, T P = Q R (lane per column) ----
     for (int c = tid; c < k; c += nthr) {
         T s = 0;
-        for (int i = 0; i < k; ++i) s += A[ix(i, c)] * A[ix(i, c)];
+        for (int i = 0; i < k; ++i) s += A[ixA(i, c)] * A[ixA(i, c)];
         s_nrm[c] = s;   // partial column norms (rows j..k-1), squared
         s_d[c] = s;     // norms at the last exact computation
         s_pcol[c] = c;
@@ -515,9 +524,9 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
         const int pv = s_piv;
         if (pv != j) {
             for (int i = tid; i < k; i += nthr) {
-                const T x = A[ix(i, j)];
-                A[ix(i, j)] = A[ix(i, pv)];
-                A[ix(i, pv)] = x;
+                const T x = A[ixA(i, j)];
+                A[ixA(i, j)] = A[ixA(i, pv)];
+                A[ixA(i, pv)] = x;
             }
             if (tid == 0) {
                 T x = s_nrm[j]; s_nrm[j] = s_nrm[pv]; s_nrm[pv] = x;
@@ -528,17 +537,17 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
         __syncthreads();
         // reflector of column j, rows j..k-1 (dlarfg), by thread 0
         if (tid == 0) {
-            T *aj = A + ix(0, j);
-            const T alpha = aj[j * rs];
+            T *aj = A + ixA(0, j);
+            const T alpha = aj[j * rsA];
             T ss = 0;
-            for (int i = j + 1; i < k; ++i) ss += aj[i * rs] * aj[i * rs];
+            for (int i = j + 1; i < k; ++i) ss += aj[i * rsA] * aj[i * rsA];
             T tj = 0;
             if (ss > T(0)) {
                 const T beta = -copysign(sqrt(alpha * alpha + ss), alpha);
                 tj = (beta - alpha) / beta;
                 const T scal = T(1) / (alpha - beta);
-                for (int i = j + 1; i < k; ++i) aj[i * rs] *= scal;
-                aj[j * rs] = beta;
+                for (int i = j + 1; i < k; ++i) aj[i * rsA] *= scal;
+                aj[j * rsA] = beta;
             }
             s_tau[j] = tj;
         }
@@ -546,21 +555,21 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
         // apply to the trailing columns and downdate their norms (lane per column)
         const T tj = s_tau[j];
         for (int c = j + 1 + tid; c < k; c += nthr) {
-            T *ac = A + ix(0, c);
-            const T *aj = A + ix(0, j);
+            T *ac = A + ixA(0, c);
+            const T *aj = A + ixA(0, j);
             if (tj != T(0)) {
-                T dot = ac[j * rs];
-                for (int i = j + 1; i < k; ++i) dot += aj[i * rs] * ac[i * rs];
+                T dot = ac[j * rsA];
+                for (int i = j + 1; i < k; ++i) dot += aj[i * rsA] * ac[i * rsA];
                 const T s = tj * dot;
-                ac[j * rs] -= s;
-                for (int i = j + 1; i < k; ++i) ac[i * rs] -= s * aj[i * rs];
+                ac[j * rsA] -= s;
+                for (int i = j + 1; i < k; ++i) ac[i * rsA] -= s * aj[i * rsA];
             }
             // partial norm of rows j+1..k-1 (dlaqp2's downdate with recomputation)
-            const T rjc = ac[j * rs];
+            const T rjc = ac[j * rsA];
             T nn = s_nrm[c] - rjc * rjc;
             if (nn <= s_d[c] * T(1.0 / 1024) || nn <= T(0)) {
                 T s = 0;
-                for (int i = j + 1; i < k; ++i) s += ac[i * rs] * ac[i * rs];
+                for (int i = j + 1; i < k; ++i) s += ac[i * rsA] * ac[i * rsA];
                 nn = s;
                 s_d[c] = s;
             }
@@ -572,16 +581,16 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
     // A = I (V_J)
     for (int j = 0; j < k; ++j)
         for (int i = tid; i < k; i += nthr) {
-            const T x = A[ix(i, j)];
+            const T x = A[ixA(i, j)];
             Yg[(size_t)j * k + i] = i > j ? x : T(0);
-            B[ix(j, i)] = i <= j ? x : T(0);   // B(j, i) = R(i, j)
+            B[ixB(j, i)] = i <= j ? x : T(0);   // B(j, i) = R(i, j)
         }
     __syncthreads();
     for (int o = 0; o < k; ++o)
-        for (int t = tid; t < k; t += nthr) A[(size_t)o * ld + t] = o == t ? T(1) : T(0);
+        for (int t = tid; t < k; t += nthr) A[(size_t)o * ldA + t] = o == t ? T(1) : T(0);
     for (int c = tid; c < k; c += nthr) {
         T s = 0;
-        for (int i = 0; i < k; ++i) s += B[ix(i, c)] * B[ix(i, c)];
+        for (int i = 0; i < k; ++i) s += B[ixB(i, c)] * B[ixB(i, c)];
         s_nrm[c] = s;
         s_d[c] = T(1);
     }
@@ -613,10 +622,10 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                 int p = 0, q = 0;
                 if (pi < np) rr_pair(round, pi, n, p, q);
                 const bool valid = pi < np && p < k && q < k;
-                T *xp = B + ix(0, p), *xq = B + ix(0, q);
+                T *xp = B + ixB(0, p), *xq = B + ixB(0, q);
                 T dot = 0;
                 if (valid)
-                    for (int i = lig; i < k; i += G) dot += xp[i * rs] * xq[i * rs];
+                    for (int i = lig; i < k; i += G) dot += xp[i * rsB] * xq[i * rsB];
                 for (int o = G / 2; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
                 T dp = 1, dq = 1, app = 0, aqq = 0, apq = 0;
                 if (valid) {
@@ -638,14 +647,14 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                     cs = T(1) / sqrt(T(1) + t * t);
                     // true columns p' = c (p - t q), q' = c (q + t p), in B and V_J
                     const T f1 = t * dq / dp, f2 = t * dp / dq;
-                    T *vp = A + ix(0, p), *vq = A + ix(0, q);
+                    T *vp = A + ixA(0, p), *vq = A + ixA(0, q);
                     for (int i = lig; i < k; i += G) {
-                        const T a = xp[i * rs], b = xq[i * rs];
-                        xp[i * rs] = a - f1 * b;
-                        xq[i * rs] = b + f2 * a;
-                        const T u = vp[i * rs], v = vq[i * rs];
-                        vp[i * rs] = u - f1 * v;
-                        vq[i * rs] = v + f2 * u;
+                        const T a = xp[i * rsB], b = xq[i * rsB];
+                        xp[i * rsB] = a - f1 * b;
+                        xq[i * rsB] = b + f2 * a;
+                        const T u = vp[i * rsA], v = vq[i * rsA];
+                        vp[i * rsA] = u - f1 * v;
+                        vq[i * rsA] = v + f2 * u;
                     }
                 }
                 T np_ = app - t * apq, nq_ = aqq + t * apq;
@@ -657,8 +666,8 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                     T sp = 0, sq = 0;
                     if (redo_p || redo_q)
                         for (int i = lig; i < k; i += G) {
-                            sp += xp[i * rs] * xp[i * rs];
-                            sq += xq[i * rs] * xq[i * rs];
+                            sp += xp[i * rsB] * xp[i * rsB];
+                            sq += xq[i * rsB] * xq[i * rsB];
                         }
                     for (int o = G / 2; o > 0; o >>= 1) {
                         sp += __shfl_xor_sync(0xffffffffu, sp, o);
@@ -679,19 +688,19 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
         }
         // exact norms once per sweep; fold scales before they underflow
         for (int j = tid; j < k; j += nthr) {
-            T *xj = B + ix(0, j);
+            T *xj = B + ixB(0, j);
             T dj = s_d[j];
             if (dj < JacobiLim<T>::tiny_scale) {
-                T *vj = A + ix(0, j);
+                T *vj = A + ixA(0, j);
                 for (int i = 0; i < k; ++i) {
-                    xj[i * rs] *= dj;
-                    vj[i * rs] *= dj;
+                    xj[i * rsB] *= dj;
+                    vj[i * rsA] *= dj;
                 }
                 dj = T(1);
                 s_d[j] = dj;
             }
             T s2 = 0;
-            for (int i = 0; i < k; ++i) s2 += xj[i * rs] * xj[i * rs];
+            for (int i = 0; i < k; ++i) s2 += xj[i * rsB] * xj[i * rsB];
             s_nrm[j] = dj * dj * s2;
         }
         ++sweeps;
@@ -762,18 +771,18 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
         // last to first.
         for (int t = tid; t < r; t += nthr) {
             const int j = s_perm[t];
-            T *x = A + ix(0, j);   // each lane owns the column of its own j
+            T *x = A + ixA(0, j);   // each lane owns the column of its own j
             const T dj = s_d[j];
-            for (int i = 0; i < k; ++i) x[i * rs] *= dj;
+            for (int i = 0; i < k; ++i) x[i * rsA] *= dj;
             for (int h = k - 1; h >= 0; --h) {
                 const T th = s_tau[h];
                 if (th == T(0)) continue;
                 const T *y = Yg + (size_t)h * k;
-                T dot = x[h * rs];
-                for (int i = h + 1; i < k; ++i) dot += y[i] * x[i * rs];
+                T dot = x[h * rsA];
+                for (int i = h + 1; i < k; ++i) dot += y[i] * x[i * rsA];
                 const T s = th * dot;
-                x[h * rs] -= s;
-                for (int i = h + 1; i < k; ++i) x[i * rs] -= s * y[i];
+                x[h * rsA] -= s;
+                for (int i = h + 1; i < k; ++i) x[i * rsA] -= s * y[i];
             }
         }
         __syncthreads();   // the reflectors are dead from here on
@@ -783,8 +792,8 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
         for (int e = tid; e < k * r; e += nthr) {
             const int i = e % k, t = e / k;
             const int j = s_perm[t];
-            Vo[(size_t)t * k + s_pcol[i]] = mul_exp2(s_d[j] * B[ix(i, j)], sexp);
-            Uo[(size_t)t * k + i] = A[ix(i, j)];
+            Vo[(size_t)t * k + s_pcol[i]] = mul_exp2(s_d[j] * B[ixB(i, j)], sexp);
+            Uo[(size_t)t * k + i] = A[ixA(i, j)];
         }
     }
     if (tid == 0) {
@@ -918,9 +927,9 @@ static void launch_geqrf(const Desc *d_desc, int n, T *ws, int warps, cudaStream
 }
 
 template <typename T>
-cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
+cudaError_t configure_recompress(int maxK, int *svd_smem_kmax, int *svd_half_kmax) {
     // the Jacobi matrices live in shared memory when they fit (k <= 119 in FP64,
-    // 168 in FP32, with 227 KB per CTA)
+    // 168 in FP32, with 227 KB per CTA); R^T alone up to k = 167 in FP64
     (void)maxK;
     int dev = 0, optin = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -929,19 +938,26 @@ cudaError_t configure_recompress(int maxK, int *svd_smem_kmax) {
     if (e != cudaSuccess) return e;
     // dynamic shared memory the SVD kernel may take next to its static arrays
     cudaFuncAttributes fa;
-    e = cudaFuncGetAttributes(&fa, gesvd_kernel<T, true>);
+    e = cudaFuncGetAttributes(&fa, gesvd_kernel<T, 1>);
     if (e != cudaSuccess) return e;
     const int dyn_max = optin - (int)fa.sharedSizeBytes;
     int kmax = 0;
-    while (kmax < kMaxK && svd_smem_bytes<T>(kmax + 1, true) <= (size_t)dyn_max) ++kmax;
+    while (kmax < kMaxK && svd_smem_bytes<T>(kmax + 1, 2) <= (size_t)dyn_max) ++kmax;
     *svd_smem_kmax = kmax;
+    int khalf = kmax;
+    while (khalf < kMaxK && svd_smem_bytes<T>(khalf + 1, 1) <= (size_t)dyn_max) ++khalf;
+    if (svd_half_kmax) *svd_half_kmax = khalf;
     e = set_apply_smem<T, T>();
     if (e == cudaSuccess) e = set_apply_smem<T, float>();
     if (e != cudaSuccess) return e;
     // the attribute is per kernel, not per plan: allow the largest size any
     // plan may launch with, so plans of different k coexist
-    return cudaFuncSetAttribute(gesvd_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                dyn_max);
+    e = cudaFuncSetAttribute(gesvd_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             dyn_max);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(gesvd_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 dyn_max);
+    return e;
 }
 
 int bucket_edge(int k, int width) {
@@ -988,16 +1004,21 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
             const Bucket &bk = shape.buckets[b];
             if (bk.count <= 0) continue;
             const int K = bk.K;
-            const bool w_smem = K <= shape.svd_smem_kmax;
+            // both Jacobi matrices in shared memory, only R^T there (V_J in
+            // the workspace), or both in the workspace
+            const int mode = K <= shape.svd_smem_kmax ? 1 : (K <= shape.svd_half_kmax ? 2 : 0);
             cudaStream_t sb = forked ? shape.side[b] : s;
             if (forked) cudaStreamWaitEvent(sb, shape.fork, 0);
-            const int G = svd_group(K, w_smem, shape.svd_lanes);
-            const int nt = svd_threads(K, w_smem, shape.svd_lanes);
-            if (w_smem)
-                gesvd_kernel<T, true><<<bk.count, nt, svd_smem_bytes<T>(K, true), sb>>>(
+            const int G = svd_group(K, mode == 1, shape.svd_lanes);
+            const int nt = svd_threads(K, mode == 1, shape.svd_lanes);
+            if (mode == 1)
+                gesvd_kernel<T, 1><<<bk.count, nt, svd_smem_bytes<T>(K, 2), sb>>>(
+                    d_desc + bk.start, ws, d_rank, d_status, d_info, K, G);
+            else if (mode == 2)
+                gesvd_kernel<T, 2><<<bk.count, nt, svd_smem_bytes<T>(K, 1), sb>>>(
                     d_desc + bk.start, ws, d_rank, d_status, d_info, K, G);
             else
-                gesvd_kernel<T, false><<<bk.count, nt, svd_smem_bytes<T>(K, false), sb>>>(
+                gesvd_kernel<T, 0><<<bk.count, nt, svd_smem_bytes<T>(K, 0), sb>>>(
                     d_desc + bk.start, ws, d_rank, d_status, d_info, K, G);
             if (forked) {
                 cudaEventRecord(shape.join[b], sb);
@@ -1045,8 +1066,8 @@ template cudaError_t launch_rebuild<double>(const Desc *, const int *, const int
 template cudaError_t launch_rebuild<float>(const Desc *, const int *, const int *, int, float *,
                                            int *, int *, int, int, bool, cudaStream_t);
 
-template cudaError_t configure_recompress<double>(int, int *);
-template cudaError_t configure_recompress<float>(int, int *);
+template cudaError_t configure_recompress<double>(int, int *, int *);
+template cudaError_t configure_recompress<float>(int, int *, int *);
 template cudaError_t launch_recompress<double>(const Desc *, int, double *, int *, int *, int *,
                                                const LaunchShape &, cudaStream_t, unsigned);
 template cudaError_t launch_recompress<float>(const Desc *, int, float *, int *, int *, int *,

@@ -129,7 +129,7 @@ extern "C" int hcore_gpu_dgemm_noalloc(int M, double alpha, const double *AU, co
     shape.maxK = k;
     shape.nbuckets = 1;
     shape.buckets[0] = Bucket{0, 1, k};
-    e = configure_recompress<double>(k, &shape.svd_smem_kmax);
+    e = configure_recompress<double>(k, &shape.svd_smem_kmax, &shape.svd_half_kmax);
     if (e == cudaSuccess) {
         noalloc_setup_kernel<<<1, 32, 0, s>>>(d);
         e = cudaGetLastError();

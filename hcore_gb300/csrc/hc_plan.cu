@@ -588,9 +588,14 @@ extern "C" int hcore_gpu_plan_create_tuned(hcore_gpu_plan *plan, int precision, 
     p->h_desc = descs;
     {
         const cudaError_t ce = precision == HCORE_GPU_F64
-                                   ? configure_recompress<double>(p->maxK, &p->shape.svd_smem_kmax)
-                                   : configure_recompress<float>(p->maxK, &p->shape.svd_smem_kmax);
-        for (auto &g : p->groups) g.shape.svd_smem_kmax = p->shape.svd_smem_kmax;
+                                   ? configure_recompress<double>(p->maxK, &p->shape.svd_smem_kmax,
+                                                                  &p->shape.svd_half_kmax)
+                                   : configure_recompress<float>(p->maxK, &p->shape.svd_smem_kmax,
+                                                                 &p->shape.svd_half_kmax);
+        for (auto &g : p->groups) {
+            g.shape.svd_smem_kmax = p->shape.svd_smem_kmax;
+            g.shape.svd_half_kmax = p->shape.svd_half_kmax;
+        }
         const bool mixed = (flags & HCORE_GPU_MIXED_FACTORS) && precision == HCORE_GPU_F64;
         p->shape.mixed = mixed;
         for (auto &g : p->groups) g.shape.mixed = mixed;

@@ -441,7 +441,10 @@ def test_nonfinite_input_marks_update_noconv(hc, port, precision):
 @pytest.mark.parametrize("M,a,b,c,maxrk,acc", [
     (2048, 256, 200, 256, 512, 1e-7),    # k = 512: Jacobi matrices in global memory, 64 rows/lane
     (1024, 150, 100, 130, 300, 1e-8),    # k = 280
-    (2048, 40, 30, 50, 128, 1e-7)])      # M = 2048 with a small k (shared-memory Jacobi)
+    (2048, 40, 30, 50, 128, 1e-7),       # M = 2048 with a small k (shared-memory Jacobi)
+    (512, 60, 50, 70, 160, 1e-8),        # k = 130: R^T in shared memory, V_J in global memory
+    (1024, 80, 70, 80, 200, 1e-8),       # k = 160: the same mode near its limit
+    (1024, 90, 60, 90, 200, 1e-8)])      # k = 180: both in global memory again
 def test_large_rank_updates_vs_oracle(hc, port, M, a, b, c, maxrk, acc):
     """The largest shapes a plan takes (a + c up to 512, M up to 2048), as in
     a 3D covariance matrix with nb = 2048 and tiles of rank up to 256."""
