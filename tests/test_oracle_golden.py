@@ -231,3 +231,24 @@ def test_zuncompress_fixture_is_the_plain_transpose_product(golden_zgemm):
     _, g = golden_zgemm
     P = g["zunc_AU"] @ g["zunc_BV"].T
     assert np.abs(g["zunc_CDo"] - P).max() <= 1e-13 * np.abs(P).max()
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_complex_restatements_agree(port, seed):
+    """The C restatement of HCORE_zgemm and the dense restatement on seeded
+    complex updates with complex alpha and beta (rank and product)."""
+    rng = np.random.default_rng(4000 + seed)
+    M, a, b, c = 80, int(rng.integers(2, 12)), int(rng.integers(2, 12)), int(rng.integers(2, 12))
+
+    def clr(k):
+        U, _ = np.linalg.qr(rng.standard_normal((M, k)) + 1j * rng.standard_normal((M, k)))
+        V, _ = np.linalg.qr(rng.standard_normal((M, k)) + 1j * rng.standard_normal((M, k)))
+        return U * 10.0 ** (-6 * np.arange(k) / k), V
+
+    (AU, AV), (BU, BV), (CU, CV) = clr(a), clr(b), clr(c)
+    alpha = complex(rng.standard_normal(), rng.standard_normal())
+    beta = complex(rng.standard_normal(), rng.standard_normal())
+    out = port.zgemm(M, alpha, AU, AV, a, BU, BV, b, beta, CU, CV, c, maxrk=32, acc=1e-7)
+    r, P, S = O.zgemm_dense_truncation(alpha, AU, AV, BU, BV, beta, CU, CV, acc=1e-7)
+    assert out["status"] == 0 and out["rank"] == r
+    assert np.linalg.norm(out["CU"] @ out["CV"].T - P) <= 1e-12 * np.linalg.norm(P)
