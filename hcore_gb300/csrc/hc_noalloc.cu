@@ -1,18 +1,20 @@
 // hcore-gb300 — one low-rank update that allocates no memory.
 //
-// Some callers cannot call cudaMalloc: a task runtime worker that must not
-// stall the other streams of the device (cudaMalloc/cudaFree synchronise
-// implicitly), code that runs while another stream of the process is being
-// captured in global mode (where allocation calls are refused), or a caller
-// held to a fixed device-memory budget that it reserved up front.  For them,
-// hcore_gpu_dgemm_noalloc runs the same four phases as the batched plans
-// with all of its workspace in one file-scope device array of fixed size.
+// Some callers cannot call cudaMalloc.  A worker thread of a task runtime
+// (StarPU, PaRSEC) that runs tile updates next to other workers' streams
+// must not allocate: cudaMalloc and cudaFree may synchronise the whole
+// device and stall every other worker.  A runtime that reserved all of the
+// device memory it may use up front (its own pool allocator) cannot let a
+// library take more.  For such callers hcore_gpu_dgemm_noalloc runs the same
+// four phases as the batched plans with all of its workspace in one
+// file-scope device array of fixed size.
 //
 // The array is reserved on every GPU that loads the library, until the
 // process exits.  Host code must not hand the array's name to a kernel (in
 // host code it is only a stand-in for the symbol): the device address comes
 // from cudaGetSymbolAddress, once per device, on the first call made with
-// that device current.  That first call should therefore come before any
+// that device current; the same set-up also sets the SVD kernel's shared
+// memory attributes.  That first call should therefore come before any
 // stream capture.  Every call uses the same array, so calls that may overlap
 // on the GPU (different streams, or different host threads) race on it and
 // must be serialised by the caller.
@@ -47,23 +49,36 @@ __global__ void noalloc_setup_kernel(Desc d) {
 }
 
 constexpr int kNoAllocMaxDevices = 64;
+struct NoAllocDevice {
+    unsigned char *addr = nullptr;  // device address of g_noalloc_scratch
+    int svd_smem_kmax = 0;          // SVD shared-memory limits on this device
+    int svd_half_kmax = 0;
+};
 static std::mutex g_noalloc_mu;
-static unsigned char *g_noalloc_addr[kNoAllocMaxDevices];
+static NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
 
-// device address of the scratch array on the current device (set-up once)
-static cudaError_t noalloc_scratch(unsigned char **out) {
+// once per device, with that device current: the scratch array's device
+// address and the SVD kernel's shared-memory attributes (neither changes
+// afterwards, so later calls make no set-up call at all)
+static cudaError_t noalloc_device(NoAllocDevice *out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
+    NoAllocDevice &d = g_noalloc_dev[dev];
+    if (!d.addr) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
-        g_noalloc_addr[dev] = static_cast<unsigned char *>(p);
+        int kmax = 0, khalf = 0;
+        e = configure_recompress<double>(kMaxK, &kmax, &khalf);
+        if (e != cudaSuccess) return e;
+        d.svd_smem_kmax = kmax;
+        d.svd_half_kmax = khalf;
+        d.addr = static_cast<unsigned char *>(p);
     }
-    *out = g_noalloc_addr[dev];
+    *out = d;
     return cudaSuccess;
 }
 
@@ -114,12 +129,22 @@ extern "C" int hcore_gpu_dgemm_noalloc(int M, double alpha, const double *AU, co
                   M, k, a * b, need, kNoAllocWsElems);
         return HCORE_GPU_EINVAL;
     }
-    unsigned char *base = nullptr;
-    cudaError_t e = noalloc_scratch(&base);
+    // an error left pending by the caller's own earlier work stays the
+    // caller's: report it as such and leave it pending
+    cudaError_t e = cudaPeekAtLastError();
     if (e != cudaSuccess) {
-        set_error("hcore_gpu_dgemm_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+        set_error("hcore_gpu_dgemm_noalloc: an earlier CUDA error is pending (%s); nothing "
+                  "was launched", cudaGetErrorString(e));
         return HCORE_GPU_ECUDA;
     }
+    NoAllocDevice nd;
+    e = noalloc_device(&nd);
+    if (e != cudaSuccess) {
+        set_error("hcore_gpu_dgemm_noalloc: device set-up (cudaGetSymbolAddress, kernel "
+                  "attributes) failed: %s", cudaGetErrorString(e));
+        return HCORE_GPU_ECUDA;
+    }
+    unsigned char *base = nd.addr;
     d.ws = 0;
     d.idx = 0;
     d.status0 = 0;
@@ -129,11 +154,10 @@ extern "C" int hcore_gpu_dgemm_noalloc(int M, double alpha, const double *AU, co
     shape.maxK = k;
     shape.nbuckets = 1;
     shape.buckets[0] = Bucket{0, 1, k};
-    e = configure_recompress<double>(k, &shape.svd_smem_kmax, &shape.svd_half_kmax);
-    if (e == cudaSuccess) {
-        noalloc_setup_kernel<<<1, 32, 0, s>>>(d);
-        e = cudaGetLastError();
-    }
+    shape.svd_smem_kmax = nd.svd_smem_kmax;
+    shape.svd_half_kmax = nd.svd_half_kmax;
+    noalloc_setup_kernel<<<1, 32, 0, s>>>(d);
+    e = cudaGetLastError();
     int *rs = reinterpret_cast<int *>(base + kNoAllocRankOff);
     if (e == cudaSuccess)
         e = launch_recompress<double>(reinterpret_cast<const Desc *>(base + kNoAllocDescOff), 1,

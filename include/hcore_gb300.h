@@ -282,18 +282,22 @@ double hcore_gpu_fp64_peak(void *stream);
 
 /* One update with HCORE_dgemm's semantics that allocates no memory (no
  * counterpart in the reference).  For callers that cannot call cudaMalloc:
- * runtime workers that must not stall other streams (allocation synchronises
- * the device), code running while a stream is captured in global mode, or a
- * caller held to a fixed device-memory budget.  The workspace is one
+ * a task-runtime worker that must not stall the other workers' streams
+ * (cudaMalloc/cudaFree may synchronise the device), or a runtime that
+ * reserved all the device memory it may use up front.  The workspace is one
  * fixed-size device array of the library (3 MiB, reserved on every GPU that
  * loads the library until exit), enough for M = 1024 with a + c <= 128 and
  * a*b <= 16384; larger updates are rejected with HCORE_GPU_EINVAL and a
- * message.  Factors are device (or pinned host) memory; CU/CV are updated in
- * place (first new_rank columns; storage must hold max(c, new rank)
- * columns).  The first call on a device looks up the array's device address,
- * so make it before any stream capture.  All calls share the array: calls
- * that can overlap on the GPU race and must be serialised by the caller.
- * Returns HCORE_GPU_OK, HCORE_GPU_ETASK (status set), EINVAL or ECUDA. */
+ * message before anything is launched.  Factors are device (or pinned host)
+ * memory; CU/CV are updated in place (first new_rank columns; storage must
+ * hold max(c, new rank) columns).  The first call on a device sets up that
+ * device (the array's device address, the SVD kernel's shared-memory
+ * attributes), so make it before any stream capture.  All calls share the
+ * array: calls that can overlap on the GPU race and must be serialised by
+ * the caller.  The call waits for its stream to finish the update.  A CUDA
+ * error already pending when it is called is left pending and reported as
+ * HCORE_GPU_ECUDA without launching anything.  Returns HCORE_GPU_OK,
+ * HCORE_GPU_ETASK (status set), EINVAL or ECUDA. */
 int hcore_gpu_dgemm_noalloc(int M, double alpha, const double *AU, const double *AV, int a,
                             int lda, const double *BU, const double *BV, int b, int ldb,
                             double beta, double *CU, double *CV, int c, int ldc, int rk,

@@ -1,7 +1,7 @@
 """hcore_gpu_dgemm_noalloc: the update entry point for callers that cannot
-allocate device memory (runtime workers that must not stall other streams,
-code running while a stream is captured, fixed memory budgets).  Its
-workspace is a fixed device array inside the library.
+allocate device memory (task-runtime workers that must not stall the other
+workers' streams, runtimes that reserved all their device memory up front).
+Its workspace is a fixed device array inside the library.
 
 Checked through the C ABI against the existing plan entry point
 (hcore_gpu_plan_*) on the same inputs, two calls in a row (the second call
@@ -57,26 +57,71 @@ def _via_plan(hc, devmem, M, arrays, a, b, c, maxrk, acc):
     return r, devmem.to_host(dCU, r), devmem.to_host(dCV, r)
 
 
-def test_noalloc_matches_plan_entry_point_twice(hc):
+# capacity of the fixed array in doubles, and the workspace one update needs
+# (the library's per-update layout: two M x k stacks, three k-vectors, a x b,
+# four k x k blocks, each region rounded up to 32 doubles)
+NOALLOC_WS_ELEMS = 393216
+
+
+def _ws_need(M, a, b, k):
+    o = 0
+    for size in (M * k, M * k, k, k, k, a * b, k * k, k * k, k * k, k * k):
+        o = (o + size + 31) & ~31
+    return o
+
+
+def _call(f, hc, M, a, b, c, maxrk, arrays):
     from hcore_gb300 import devmem
 
+    AU, AV, BU, BV, CU, CV = arrays
+    d = [devmem.to_device(x) for x in (AU, AV, BU, BV)]
+    dCU, dCV = devmem.to_device(CU, a + c), devmem.to_device(CV, a + c)
+    r, st = C.c_int(-1), C.c_int(-1)
+    rc = f(M, -1.0, d[0].data_ptr(), d[1].data_ptr(), a, M, d[2].data_ptr(),
+           d[3].data_ptr(), b, M, 1.0, dCU.data_ptr(), dCV.data_ptr(), c, M, 0, maxrk, 1e-8,
+           C.byref(r), C.byref(st), None)
+    assert rc == 0, hc.last_error()
+    assert st.value == 0
+    return r.value, devmem.to_host(dCU, r.value), devmem.to_host(dCV, r.value)
+
+
+def _check_against_plan(f, hc, seed, M, a, b, c, maxrk):
+    from hcore_gb300 import devmem
+
+    arrays = _case(seed, M, a, b, c)
+    r, gU, gV = _call(f, hc, M, a, b, c, maxrk, arrays)
+    r_ref, CU_ref, CV_ref = _via_plan(hc, devmem, M, arrays, a, b, c, maxrk, 1e-8)
+    assert r == r_ref
+    assert O.rel_fro(gU @ gV.T, CU_ref @ CV_ref.T) < FP64_TOL
+
+
+def test_noalloc_matches_plan_entry_point_twice(hc):
     f = _bind(hc.lib())
-    cases = [(41, 512, 20, 18, 24, 64), (42, 1024, 30, 26, 34, 128)]
-    for seed, M, a, b, c, maxrk in cases:     # two calls in a row on the shared array
-        arrays = _case(seed, M, a, b, c)
-        AU, AV, BU, BV, CU, CV = arrays
-        d = [devmem.to_device(x) for x in (AU, AV, BU, BV)]
-        dCU, dCV = devmem.to_device(CU, a + c), devmem.to_device(CV, a + c)
-        r, st = C.c_int(-1), C.c_int(-1)
-        rc = f(M, -1.0, d[0].data_ptr(), d[1].data_ptr(), a, M, d[2].data_ptr(),
-               d[3].data_ptr(), b, M, 1.0, dCU.data_ptr(), dCV.data_ptr(), c, M, 0, maxrk, 1e-8,
-               C.byref(r), C.byref(st), None)
-        assert rc == 0, hc.last_error()
-        assert st.value == 0
-        r_ref, CU_ref, CV_ref = _via_plan(hc, devmem, M, arrays, a, b, c, maxrk, 1e-8)
-        assert r.value == r_ref
-        P = devmem.to_host(dCU, r.value) @ devmem.to_host(dCV, r.value).T
-        assert O.rel_fro(P, CU_ref @ CV_ref.T) < FP64_TOL
+    # two calls in a row on the shared array (the second finds the first's
+    # contents there)
+    for seed, M, a, b, c, maxrk in [(41, 512, 20, 18, 24, 64), (42, 1024, 30, 26, 34, 128)]:
+        _check_against_plan(f, hc, seed, M, a, b, c, maxrk)
+
+
+def test_noalloc_at_its_documented_and_exact_limits(hc):
+    """M = 1024 with a + c = 128 (the documented capacity), then the largest
+    rank sum whose workspace still fits the array (a + c = 146, where the SVD
+    keeps only R^T in shared memory); one more column is refused."""
+    f = _bind(hc.lib())
+    assert _ws_need(1024, 64, 64, 128) <= NOALLOC_WS_ELEMS
+    _check_against_plan(f, hc, 43, 1024, 64, 64, 64, 128)
+    assert _ws_need(1024, 73, 73, 146) <= NOALLOC_WS_ELEMS < _ws_need(1024, 73, 73, 147)
+    _check_against_plan(f, hc, 44, 1024, 73, 73, 73, 146)
+    arrays = _case(45, 1024, 73, 73, 74)
+    from hcore_gb300 import devmem
+
+    d = [devmem.to_device(x) for x in arrays]
+    r, st = C.c_int(-1), C.c_int(-1)
+    rc = f(1024, -1.0, d[0].data_ptr(), d[1].data_ptr(), 73, 1024, d[2].data_ptr(),
+           d[3].data_ptr(), 73, 1024, 1.0, d[4].data_ptr(), d[5].data_ptr(), 74, 1024, 0, 147,
+           1e-8, C.byref(r), C.byref(st), None)
+    assert rc == -1
+    assert "scratch" in hc.last_error()
 
 
 def test_noalloc_rejects_updates_beyond_its_scratch(hc):
