@@ -13,8 +13,10 @@ Arms:
                     restatement, oracle/) on all host cores, same workload
 
 Output: one JSON line (see the keys below).  Multi-GPU: launched under
-torchrun, each rank takes an equal share of the update list (independent
-updates, no collective: weak scaling); value = all ranks' updates / max time.
+torchrun, each rank takes a rank-balanced share of the update list
+(longest processing time first on a per-update cost model; independent
+updates, no collective on the data path: weak scaling) and builds only the
+tiles its share reads; value = all ranks' updates / max time.
 """
 from __future__ import annotations
 
@@ -119,12 +121,35 @@ def sum_over_ranks(x: float, world: int) -> float:
     return float(t.item())
 
 
-def shard(updates, rank, world):
-    """Contiguous equal shares of the update list (independent updates)."""
-    n = len(updates)
-    lo = rank * n // world
-    hi = (rank + 1) * n // world
-    return updates[lo:hi]
+def all_sum_ints(vec, world: int):
+    """Set-up reduction of an integer vector over ranks (tile ranks before
+    the partition); not on the timed path."""
+    import numpy as np
+    import torch
+
+    if world == 1:
+        return np.asarray(vec)
+    import torch.distributed as dist
+
+    on_gpu = torch.cuda.is_available() and dist.get_backend() == "nccl"
+    t = torch.as_tensor(np.asarray(vec, dtype=np.int64), device="cuda" if on_gpu else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return t.cpu().numpy()
+
+
+def panel_for_rank(args, rank, world, dev):
+    """The panel workload of this rank: the whole panel at N=1; at N>1 a
+    rank-balanced share (longest processing time first on the per-update
+    cost model) holding only the tiles the share reads.  Returns (panel,
+    cost imbalance of the partition or None)."""
+    from hcore_gb300 import panel as pnl
+
+    if world > 1:
+        panel, _, imbalance = pnl.build_panel_share(
+            rank, world, lambda v: all_sum_ints(v, world), device=str(dev),
+            max_updates=args.max_updates, workers=max(1, (os.cpu_count() or 1) // world))
+        return panel, imbalance
+    return pnl.build_panel(device=str(dev), max_updates=args.max_updates), None
 
 
 class Clocks:
@@ -228,9 +253,9 @@ def run_gb300(args):
     L = hc.lib()
     dev = torch.device("cuda", local)
     t0 = time.time()
-    panel = pnl.build_panel(device=str(dev), max_updates=args.max_updates)
+    panel, imbalance = panel_for_rank(args, rank, world, dev)
     gen_s = time.time() - t0
-    updates = shard(panel.updates, rank, world)
+    updates = panel.updates
     n = len(updates)
     nb, maxrank = panel.nb, panel.maxrank
     # out-of-place outputs: maxrank columns per update, so steps repeat on
@@ -301,6 +326,9 @@ def run_gb300(args):
               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
               "data": "synthetic (seeded points, covariance tiles compressed on the host cores)",
               "config": dict(WORKLOAD, updates_per_step=int(total_updates), parallelism=f"dp{world}",
+                             **({"shard": "longest processing time first on the per-update "
+                                          "cost model", "shard_cost_imbalance": imbalance}
+                                if world > 1 else {}),
                              l2="inputs+outputs+workspace larger than L2 (no flush needed)",
                              graph=f"{batch.launches} kernel launches ({tuning.stream_groups} stream "
                                    f"groups: stack, QR, one SVD launch per rank bucket, rebuild) "
@@ -664,8 +692,8 @@ def run_precision(args):
         hbuild.build()
     hc.lib()
     dev = torch.device("cuda", local)
-    panel = pnl.build_panel(device=str(dev), max_updates=args.max_updates)
-    updates = shard(panel.updates, rank, world)
+    panel, _ = panel_for_rank(args, rank, world, dev)
+    updates = panel.updates
     n, nb, maxrank = len(updates), panel.nb, panel.maxrank
     out_off = np.arange(n + 1, dtype=np.int64) * nb * maxrank
     stream = torch.cuda.current_stream(dev)

@@ -109,21 +109,12 @@ def _compress_job(args):
     return out
 
 
-def build_panel(n_points: int = 65536, dim: int = 2, nb: int = 1024, kernel: str = "sqexp",
-                ell: float = 0.01, acc: float = 1e-8, maxrank: int = 128, seed: int = 0,
-                device: str = "cuda", max_updates: int | None = None,
-                workers: int | None = None) -> Panel:
-    """Generate and compress the tiles that panel 0's Schur updates touch.
-
-    Compression runs on the host cores (one single-threaded LAPACK process
-    per core, spawn start method so a CUDA context in the parent is safe);
-    the factors are then uploaded to ``device`` (or kept on the host when
-    device is "cpu")."""
-    import multiprocessing as mp
-    import tempfile
-
-    import torch
-
+def panel_layout(n_points: int = 65536, dim: int = 2, nb: int = 1024, seed: int = 0,
+                 max_updates: int | None = None):
+    """Points, tile count per dimension, the tiles panel 0 touches and its
+    update list.  Tile slot s (its index in the returned list) seeds that
+    tile's compression, so any subset of tiles compresses to the same factors
+    as the full panel."""
     T = n_points // nb
     P = morton_points(n_points, dim, seed)
     tiles = [(i, 0) for i in range(1, T)]
@@ -131,10 +122,24 @@ def build_panel(n_points: int = 65536, dim: int = 2, nb: int = 1024, kernel: str
     if max_updates is not None:
         updates = updates[:max_updates]
     tiles += sorted(set(updates))
-    index = {t: s for s, t in enumerate(tiles)}
-    workers = workers or os.cpu_count() or 1
-    jobs = [(s, i, j) for s, (i, j) in enumerate(tiles)]
-    results = [None] * len(tiles)
+    return P, T, tiles, updates
+
+
+def compress_slots(P: np.ndarray, nb: int, tiles: list, slots, kernel: str = "sqexp",
+                   ell: float = 0.01, acc: float = 1e-8, maxrank: int = 128, seed: int = 0,
+                   workers: int | None = None) -> dict:
+    """Compress the tiles at the given slots of `tiles` on the host cores (one
+    single-threaded LAPACK process per core, spawn start method so a CUDA
+    context in the parent is safe).  Returns slot -> (U^T, V^T, rank)."""
+    import multiprocessing as mp
+    import tempfile
+
+    slots = list(slots)
+    workers = max(1, min(workers or os.cpu_count() or 1, len(slots) or 1))
+    jobs = [(s, tiles[s][0], tiles[s][1]) for s in slots]
+    out = {}
+    if not jobs:
+        return out
     with tempfile.TemporaryDirectory() as folder:
         np.save(os.path.join(folder, "points.npy"), P)
         chunks = [jobs[w::workers] for w in range(workers)]
@@ -157,18 +162,84 @@ def build_panel(n_points: int = 65536, dim: int = 2, nb: int = 1024, kernel: str
                         os.environ[v] = old
     for part in parts:
         for s, Ut, Vt, r in part:
-            results[s] = (Ut, Vt, r)
-    ranks = np.array([r for _, _, r in results], dtype=np.int32)
+            out[s] = (Ut, Vt, r)
+    return out
+
+
+def assemble_panel(nb: int, T: int, acc: float, maxrank: int, tiles: list, updates: list,
+                   factors: dict, device: str = "cuda") -> Panel:
+    """A Panel over the given tiles (in that order) from tile -> (U^T, V^T,
+    rank); factors are uploaded to ``device`` (kept on the host for "cpu")."""
+    import torch
+
+    ranks = np.array([factors[t][2] for t in tiles], dtype=np.int32)
     offset = np.zeros(len(tiles) + 1, dtype=np.int64)
     offset[1:] = np.cumsum(ranks.astype(np.int64) * nb)
-    Uflat = np.concatenate([u.reshape(-1) for u, _, _ in results])
-    Vflat = np.concatenate([v.reshape(-1) for _, v, _ in results])
+    Uflat = np.concatenate([factors[t][0].reshape(-1) for t in tiles])
+    Vflat = np.concatenate([factors[t][1].reshape(-1) for t in tiles])
     Ut = torch.from_numpy(Uflat)
     Vt = torch.from_numpy(Vflat)
     if device != "cpu":
         Ut, Vt = Ut.to(device), Vt.to(device)
-    return Panel(nb=nb, ntiles=T, acc=acc, maxrank=maxrank, tiles=tiles, rank=ranks,
-                 offset=offset, U=Ut, V=Vt, updates=updates, index=index)
+    index = {t: s for s, t in enumerate(tiles)}
+    return Panel(nb=nb, ntiles=T, acc=acc, maxrank=maxrank, tiles=list(tiles), rank=ranks,
+                 offset=offset, U=Ut, V=Vt, updates=list(updates), index=index)
+
+
+def build_panel(n_points: int = 65536, dim: int = 2, nb: int = 1024, kernel: str = "sqexp",
+                ell: float = 0.01, acc: float = 1e-8, maxrank: int = 128, seed: int = 0,
+                device: str = "cuda", max_updates: int | None = None,
+                workers: int | None = None) -> Panel:
+    """Generate and compress the tiles that panel 0's Schur updates touch.
+
+    Compression runs on the host cores (compress_slots); the factors are then
+    uploaded to ``device`` (or kept on the host when device is "cpu")."""
+    P, T, tiles, updates = panel_layout(n_points, dim, nb, seed, max_updates)
+    comp = compress_slots(P, nb, tiles, range(len(tiles)), kernel, ell, acc, maxrank, seed,
+                          workers)
+    factors = {tiles[s]: v for s, v in comp.items()}
+    return assemble_panel(nb, T, acc, maxrank, tiles, updates, factors, device)
+
+
+def build_panel_share(rank: int, world: int, all_sum, n_points: int = 65536, dim: int = 2,
+                      nb: int = 1024, kernel: str = "sqexp", ell: float = 0.01,
+                      acc: float = 1e-8, maxrank: int = 128, seed: int = 0,
+                      device: str = "cuda", max_updates: int | None = None,
+                      workers: int | None = None):
+    """One rank's share of panel 0 for a multi-GPU run, holding only the tiles
+    its updates read.
+
+    1. Tile ranks: this rank compresses every world-th tile; `all_sum` (a
+       set-up reduction over ranks of an integer numpy vector, e.g. an
+       all_reduce) gives every rank all tile ranks.
+    2. The updates are partitioned by longest processing time first on the
+       per-update cost model (hcore_gb300.shard), the same on every rank.
+    3. This rank compresses the tiles its share reads that step 1 did not
+       already give it, and keeps only those.
+    Returns (Panel of the share, the partition as update-index lists, the
+    share's imbalance)."""
+    from . import shard as sh
+
+    P, T, tiles, updates = panel_layout(n_points, dim, nb, seed, max_updates)
+    own = compress_slots(P, nb, tiles, range(rank, len(tiles), world), kernel, ell, acc,
+                         maxrank, seed, workers)
+    rk = np.zeros(len(tiles), dtype=np.int64)
+    for s, (_, _, r) in own.items():
+        rk[s] = r
+    rk = np.asarray(all_sum(rk), dtype=np.int64)
+    slot = {t: s for s, t in enumerate(tiles)}
+    costs = [sh.update_cost(nb, int(rk[slot[(i, 0)]]), int(rk[slot[(j, 0)]]),
+                            int(rk[slot[(i, j)]])) for i, j in updates]
+    parts = sh.lpt_partition(costs, world)
+    mine = [updates[u] for u in parts[rank]]
+    need = sh.tiles_read(mine)
+    mine_tiles = [t for t in tiles if t in need]
+    more = compress_slots(P, nb, tiles, [slot[t] for t in mine_tiles if slot[t] not in own],
+                          kernel, ell, acc, maxrank, seed, workers)
+    factors = {tiles[s]: v for s, v in own.items() if tiles[s] in need}
+    factors.update({tiles[s]: v for s, v in more.items()})
+    pnl = assemble_panel(nb, T, acc, maxrank, mine_tiles, mine, factors, device)
+    return pnl, parts, sh.imbalance(costs, parts)
 
 
 def compress_tiles(points: np.ndarray, nb: int, tiles: list, kernel: str, ell: float, acc: float,
