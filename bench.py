@@ -52,14 +52,15 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="panel", choices=["panel", "precision", "dense", "predictor", "tlr",
-                                                         "compress", "zgemm"],
+                                                         "compress", "zgemm", "fp64peak"],
                    help="panel: the headline (1953 Schur updates of a 65,536-point TLR panel); "
                         "precision: acc sweep on the same updates; "
                         "dense: batched dsyrk/dgemmcd tile updates; predictor: "
                         "learned rank predictor on 3D exponential-kernel Cholesky sweeps; "
                         "tlr: batched POTRF + TRSM, the steps either side of the update; "
                         "compress: the GPU tile compressor on the panel workload's tiles; "
-                        "zgemm: the complex update through HCORE_zgemm")
+                        "zgemm: the complex update through HCORE_zgemm; "
+                        "fp64peak: the FP64 probe forms with sampled clocks")
     p.add_argument("--max-updates", type=int, default=None, help="truncate the update list")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -67,6 +68,10 @@ def parse():
                    help="panel workload: use the built-in launch shapes instead of autotuning")
     p.add_argument("--per-tile-sample", type=int, default=48)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--probe-seconds", type=float, default=2.0,
+                   help="fp64peak workload: seconds per probe form")
+    p.add_argument("--probe-forms", default=None,
+                   help="fp64peak workload: only these forms, 'name:chains,...'")
     p.add_argument("--compress-tiles", type=int, default=None,
                    help="compress workload: only the first N tiles (a small profiling case)")
     p.add_argument("--sweep-shape", default=None,
@@ -358,7 +363,8 @@ def run_gb300(args):
             ph_ms[nm] += evs[q].elapsed_time(evs[q + 1]) / reps
     dom = max(ph_ms, key=ph_ms.get)
     result["phase_tflops_model"] = {nm: phase_model[nm] / (ph_ms[nm] / 1e3) / 1e12 for nm in ph_ms}
-    peak = fp64_peak(L, torch, dev)
+    ceiling = fp64_ceiling(L, torch, dev, local)
+    peak = ceiling["tflops"]
     # algorithmic bytes of each phase (see DRAM_PER_ALG_BYTE)
     alg_bytes = {"stack": 0, "qr": 0, "svd": 0, "rebuild": 0}
     for u, (i, j) in enumerate(updates):
@@ -382,13 +388,15 @@ def run_gb300(args):
                           "traffic_basis": "ncu DRAM bytes per algorithmic byte of this kernel in "
                                            "one 300-update launch (working set beyond L2), times "
                                            f"this phase's algorithmic bytes ({alg_bytes[dom]:.3e})",
-                          "peak_source": "fp64 DMMA m16n8k16 issue-rate probe timed live "
-                                         "(MEASURED_PEAKS.json has no FP64 figure)",
+                          "peak_source": "FP64 issue-rate probe timed live (DMMA and DFMA "
+                                         "share the FP64 pipe at 1.06-1.10 TFLOP/s on GB300; "
+                                         "MEASURED_PEAKS.json has no FP64 figure)",
+                          "peak_probe": ceiling,
                           "flops_basis": "reference flop model (flop_counts.c) of that phase"}
 
     # ---- accuracy on a sample of the timed updates vs the oracle and the
     # exact dense update (rel err <= acc is the metric's condition) ----
-    result["accuracy"] = accuracy_sample(panel, updates, ranks, out_U, out_V, out_off, 16)
+    result["accuracy"] = accuracy_all(panel, updates, ranks, out_U, out_V, out_off)
 
     # ---- plain per-tile loop: one plan per update, device pointers ----
     k = min(args.per_tile_sample, n)
@@ -479,6 +487,124 @@ def accuracy_sample(panel, updates, ranks, out_U, out_V, out_off, count, acc=Non
             "max_tile_rel_fro_err_vs_dense": worst_tile,
             "oracle_max_tile_rel_fro_err_vs_dense": worst_tile_ref,
             "max_rel_fro_diff_vs_oracle": worst_oracle,
+            "note": "per-tile errors above acc come from the reference's absolute threshold on "
+                    "tiles whose entries are themselves near acc; the oracle shows the same"}
+
+
+def _lr_norm(X, Y) -> float:
+    """||X Y^T||_F without forming the product: QR of both factors, then the
+    small core (backward stable, so a difference far below the terms'
+    magnitude is still resolved to about eps times that magnitude)."""
+    import numpy as np
+
+    if X.shape[1] == 0:
+        return 0.0
+    rx = np.linalg.qr(X, mode="r")
+    ry = np.linalg.qr(Y, mode="r")
+    return float(np.linalg.norm(rx @ ry.T))
+
+
+def _accuracy_worker(args):
+    """Oracle check of a chunk of updates (spawned process, one BLAS thread):
+    the oracle's LAPACK restatement of the reference on the same inputs, and
+    the exact update D = C - A B^T in low-rank form.  Returns per update
+    (index, oracle rank, ||P - P_oracle||, ||P_oracle||, ||P - D||,
+    ||P_oracle - D||, ||D||), P being the GPU's product."""
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    sys.path.insert(0, ROOT)
+    import numpy as np
+
+    from oracle import oracle as O
+
+    folder, items, nb, acc, maxrk = args
+    U = np.load(os.path.join(folder, "U.npy"), mmap_mode="r")
+    V = np.load(os.path.join(folder, "V.npy"), mmap_mode="r")
+    off = np.load(os.path.join(folder, "off.npy"))
+    gU_all = np.load(os.path.join(folder, "gU.npy"), mmap_mode="r")
+    gV_all = np.load(os.path.join(folder, "gV.npy"), mmap_mode="r")
+    goff = np.load(os.path.join(folder, "goff.npy"))
+    port = O.Port()
+    port.set_threads(1)
+
+    def fac(s_):
+        o0, o1 = int(off[s_]), int(off[s_ + 1])
+        r = (o1 - o0) // nb
+        return (np.asfortranarray(U[o0:o1].reshape(r, nb).T),
+                np.asfortranarray(V[o0:o1].reshape(r, nb).T), r)
+
+    out = []
+    for u, sa, sb, sc in items:
+        AU, AV, a = fac(sa)
+        BU, BV, b = fac(sb)
+        CU, CV, c = fac(sc)
+        o0, o1 = int(goff[u]), int(goff[u + 1])
+        r = (o1 - o0) // nb
+        gU = np.asarray(gU_all[o0:o1]).reshape(r, nb).T
+        gV = np.asarray(gV_all[o0:o1]).reshape(r, nb).T
+        ref = port.gemm(nb, -1.0, AU, AV, a, BU, BV, b, 1.0, CU, CV, c, maxrk=maxrk, acc=acc,
+                        variant=2)
+        rU, rV = ref["CU"], ref["CV"]
+        AF = AU @ (AV.T @ BV)                          # D = [CU | AF] [CV | -BU]^T
+        d_or = _lr_norm(np.hstack([gU, rU]), np.hstack([gV, -rV]))
+        n_or = _lr_norm(rU, rV)
+        eg = _lr_norm(np.hstack([gU, CU, AF]), np.hstack([gV, -CV, BU]))
+        er = _lr_norm(np.hstack([rU, CU, AF]), np.hstack([rV, -CV, BU]))
+        nd = _lr_norm(np.hstack([CU, AF]), np.hstack([CV, -BU]))
+        out.append((u, int(ref["rank"]), d_or, n_or, eg, er, nd))
+    return out
+
+
+def accuracy_all(panel, updates, ranks, out_U, out_V, out_off, acc=None, slack=1e-14):
+    """Every update of the step against the oracle (rank, product) and against
+    the exact dense update, on all host cores.  The gate per update is the
+    reference's own truncation error: ||P - D|| <= 1.01 ||P_oracle - D|| +
+    slack ||D|| (`slack` 1e-14 for FP64 paths)."""
+    import multiprocessing as mp
+
+    import numpy as np
+    import torch
+
+    nb = panel.nb
+    acc = panel.acc if acc is None else acc
+    n = len(updates)
+    goff = np.zeros(n + 1, dtype=np.int64)
+    goff[1:] = np.cumsum(np.asarray(ranks, dtype=np.int64) * nb)
+    segs_U = [out_U[int(out_off[u]):int(out_off[u]) + nb * int(ranks[u])] for u in range(n)]
+    segs_V = [out_V[int(out_off[u]):int(out_off[u]) + nb * int(ranks[u])] for u in range(n)]
+    gU = torch.cat(segs_U).double().cpu().numpy()
+    gV = torch.cat(segs_V).double().cpu().numpy()
+    items = [(u, panel.index[(i, 0)], panel.index[(j, 0)], panel.index[(i, j)])
+             for u, (i, j) in enumerate(updates)]
+    cores = os.cpu_count() or 1
+    t0 = time.time()
+    with tempfile.TemporaryDirectory() as folder:
+        np.save(os.path.join(folder, "U.npy"), panel.U.double().cpu().numpy())
+        np.save(os.path.join(folder, "V.npy"), panel.V.double().cpu().numpy())
+        np.save(os.path.join(folder, "off.npy"), panel.offset)
+        np.save(os.path.join(folder, "gU.npy"), gU)
+        np.save(os.path.join(folder, "gV.npy"), gV)
+        np.save(os.path.join(folder, "goff.npy"), goff)
+        os.environ.update(OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+        chunks = [c for c in (items[w::cores] for w in range(cores)) if c]
+        with mp.get_context("spawn").Pool(len(chunks)) as pool:
+            res = pool.map(_accuracy_worker, [(folder, ch, nb, acc, panel.maxrank)
+                                              for ch in chunks])
+    rows = sorted(r for part in res for r in part)
+    rk_ref = np.array([r[1] for r in rows])
+    d_or, n_or, eg, er, nd = (np.array([r[q] for r in rows]) for q in range(2, 7))
+    rank_ok = int((rk_ref == np.asarray(ranks)).sum())
+    gate = eg <= 1.01 * er + slack * nd
+    rel_or = d_or / np.maximum(n_or, 1e-300)
+    return {"checked": n, "rank_equal_to_oracle": rank_ok, "within_oracle_error": int(gate.sum()),
+            "panel_rel_fro_err_vs_dense": float(np.sqrt((eg ** 2).sum() / (nd ** 2).sum())),
+            "oracle_panel_rel_fro_err_vs_dense": float(np.sqrt((er ** 2).sum() / (nd ** 2).sum())),
+            "max_tile_rel_fro_err_vs_dense": float((eg / nd).max()),
+            "oracle_max_tile_rel_fro_err_vs_dense": float((er / nd).max()),
+            "max_rel_fro_diff_vs_oracle": float(rel_or.max()),
+            "check_s": round(time.time() - t0, 1), "cores": cores,
+            "how": "every update of the step: the oracle (LAPACK restatement of the reference) "
+                   "on the same inputs, and the exact update C - A B^T, norms of the low-rank "
+                   "differences by QR of the stacked factors (no dense product formed)",
             "note": "per-tile errors above acc come from the reference's absolute threshold on "
                     "tiles whose entries are themselves near acc; the oracle shows the same"}
 
@@ -1268,8 +1394,30 @@ def run_predictor(args):
 
 
 def fp64_peak(L, torch, dev) -> float:
-    """FP64 tensor-pipe (DMMA m16n8k16) throughput in TFLOP/s, measured now."""
+    """FP64 ceiling in TFLOP/s, measured now (hcore_gpu_fp64_peak: the DMMA
+    m16n8k16 probe; DMMA and DFMA share the FP64 pipe on this GPU)."""
     return float(L.hcore_gpu_fp64_peak(torch.cuda.current_stream(dev).cuda_stream))
+
+
+def fp64_ceiling(L, torch, dev, index, seconds=1.5) -> dict:
+    """The best FP64 probe form (DMMA m16n8k4, 2 chains: 1.10 TFLOP/s at
+    2070 MHz, the same pipe and rate as DFMA) timed for about `seconds` with
+    nvidia-smi sampling SM clock, power and throttle reasons meanwhile."""
+    import ctypes as C
+
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    tf, ms = C.c_double(), C.c_double()
+    L.hcore_gpu_fp64_probe(2, 2, 8, 256, stream, C.byref(tf), C.byref(ms))
+    iters = max(256, int(256 * seconds * 1e3 / max(ms.value, 1e-3)))
+    clocks = Clocks(index)
+    clocks.start()
+    time.sleep(0.3)
+    rc = L.hcore_gpu_fp64_probe(2, 2, 8, iters, stream, C.byref(tf), C.byref(ms))
+    clk = clocks.stop()
+    if rc != 0:
+        raise SystemExit(f"FP64 probe failed: {rc}")
+    return {"tflops": tf.value, "form": "DMMA m16n8k4 f64, 2 chains, 8 CTAs x 128 threads per SM",
+            "ms": ms.value, "clocks": clk}
 
 
 def run_tlr(args):
@@ -1623,6 +1771,65 @@ def run_zgemm(args):
     barrier(world)
 
 
+FP64_PROBES = [("dfma", 0), ("dmma_m8n8k4", 1), ("dmma_m16n8k4", 2), ("dmma_m16n8k8", 3),
+               ("dmma_m16n8k16", 4), ("dmma_m16n8k16_b_one_register", 5),
+               ("dmma_m16n8k16_b_equal_values", 6)]
+
+
+def run_fp64peak(args):
+    """The FP64 ceiling, clock-stamped: every probe form of the library
+    (hcore_gpu_fp64_probe: DFMA, DMMA shapes, and the m16n8k16 form with its
+    B operands in one register or as equal values in distinct registers), at
+    2, 4 and 8 accumulator chains, each timed for about `--probe-seconds`
+    with nvidia-smi sampling SM clock, power and throttle reasons meanwhile."""
+    import ctypes as C
+
+    import torch
+
+    import hcore_gb300 as hc
+    from hcore_gb300 import build as hbuild
+
+    rank, world, local = dist_init()
+    if not os.path.exists(hbuild.LIB):
+        hbuild.build()
+    L = hc.lib()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    forms = [(nm, kd, ch) for nm, kd in FP64_PROBES for ch in (2, 4, 8)]
+    if args.probe_forms:
+        want = [f.split(":") for f in args.probe_forms.split(",")]
+        kinds = dict(FP64_PROBES)
+        forms = [(nm, kinds[nm], int(ch)) for nm, ch in want]
+    rows = []
+    for name, kind, chains in forms:
+        tf, ms = C.c_double(), C.c_double()
+        rc = L.hcore_gpu_fp64_probe(kind, chains, 8, 256, stream, C.byref(tf), C.byref(ms))
+        if rc != 0:
+            raise SystemExit(f"probe {name} failed: {rc}")
+        iters = max(256, int(256 * args.probe_seconds * 1e3 / max(ms.value, 1e-3)))
+        clocks = Clocks(local)
+        clocks.start()
+        time.sleep(0.3)
+        rc = L.hcore_gpu_fp64_probe(kind, chains, 8, iters, stream, C.byref(tf), C.byref(ms))
+        clk = clocks.stop()
+        if rc != 0:
+            raise SystemExit(f"probe {name} failed: {rc}")
+        mhz = clk.get("sm_mhz")
+        rows.append({"form": name, "chains": chains, "tflops": tf.value, "ms": ms.value,
+                     "iters": iters, "sm_mhz": mhz, "power_w_max": clk.get("power_w_max"),
+                     "reasons": clk.get("reasons"),
+                     "flop_per_clk_per_sm": (tf.value * 1e12 / (mhz * 1e6) /
+                                             torch.cuda.get_device_properties(dev).multi_processor_count)
+                     if mhz else None})
+    best = max(rows, key=lambda r: r["tflops"])
+    line = {"metric": "FP64 issue rate (probe kernels, no memory traffic)", "value": best["tflops"],
+            "unit": "TFLOP/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
+            "config": {"workload": "fp64 probes", "ctas_per_sm": 8, "threads_per_cta": 128},
+            "best": best["form"], "probes": rows}
+    print(json.dumps(line))
+    sys.stdout.flush()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1639,6 +1846,8 @@ def main():
         run_compress(args)
     elif args.workload == "zgemm":
         run_zgemm(args)
+    elif args.workload == "fp64peak":
+        run_fp64peak(args)
     else:
         run_gb300(args)
 

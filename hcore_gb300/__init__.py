@@ -173,6 +173,7 @@ def lib() -> C.CDLL:
                                          vp]
     L.hcore_gpu_fp64_peak.argtypes = [vp]
     L.hcore_gpu_fp64_peak.restype = C.c_double
+    L.hcore_gpu_fp64_probe.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, vp, _dp, _dp]
     L.hcore_gpu_plan_device_ranks.argtypes = [vp]
     L.hcore_gpu_plan_device_ranks.restype = vp
     L.hcore_gpu_plan_device_status.argtypes = [vp]

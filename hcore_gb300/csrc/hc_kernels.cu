@@ -1074,61 +1074,3 @@ template cudaError_t launch_recompress<float>(const Desc *, int, float *, int *,
                                               const LaunchShape &, cudaStream_t, unsigned);
 
 }  // namespace hc
-
-// ---------------------------------------------------------------------------
-// FP64 tensor-pipe calibration: sustained DMMA m16n8k16 throughput, used as
-// the roofline denominator of the FP64 phases (the driver's measured peaks
-// cover HBM and bf16 only).  Fixed trip count, no memory traffic.
-// ---------------------------------------------------------------------------
-namespace hc {
-__global__ void __launch_bounds__(256) fp64_peak_kernel(double *out, int iters) {
-    double a[8], b[4], c[4][4];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) a[i] = 1e-3 * (threadIdx.x + i);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) b[i] = 0.999 - 1e-4 * i;
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int i = 0; i < 4; ++i) c[j][i] = 0.0;
-    for (int it = 0; it < iters; ++it) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            asm volatile(
-                "mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, "
-                "{%4,%5,%6,%7,%8,%9,%10,%11}, {%12,%13,%14,%15}, {%0,%1,%2,%3};"
-                : "+d"(c[j][0]), "+d"(c[j][1]), "+d"(c[j][2]), "+d"(c[j][3])
-                : "d"(a[0]), "d"(a[1]), "d"(a[2]), "d"(a[3]), "d"(a[4]), "d"(a[5]), "d"(a[6]),
-                  "d"(a[7]), "d"(b[0]), "d"(b[1]), "d"(b[2]), "d"(b[3]));
-    }
-    double s = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) s += c[j][0] + c[j][1] + c[j][2] + c[j][3];
-    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
-}
-}  // namespace hc
-
-extern "C" double hcore_gpu_fp64_peak(void *stream) {
-    cudaStream_t s = (cudaStream_t)stream;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int blocks = sms * 8, threads = 256, iters = 2048;
-    double *out = nullptr;
-    if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return -1.0;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    hc::fp64_peak_kernel<<<blocks, threads, 0, s>>>(out, 64);
-    cudaEventRecord(e0, s);
-    hc::fp64_peak_kernel<<<blocks, threads, 0, s>>>(out, iters);
-    cudaEventRecord(e1, s);
-    cudaEventSynchronize(e1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFree(out);
-    const double flops = 2.0 * 16 * 8 * 16 * 4 * (double)iters * ((double)blocks * threads / 32);
-    return ms > 0 ? flops / (ms * 1e-3) / 1e12 : -1.0;
-}

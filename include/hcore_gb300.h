@@ -275,9 +275,23 @@ typedef struct hcore_compress_task {
 int hcore_gpu_compress_batched(int n, const hcore_compress_task *tasks, int *ranks, int *status,
                                void *stream);
 
-/* measured FP64 tensor-pipe (DMMA m16n8k16) throughput of this GPU in
- * TFLOP/s, timed on `stream` (about 0.1 s); the roofline denominator of the
- * FP64 phases */
+/* FP64 issue-rate probes (no counterpart in the reference): the measured
+ * ceiling that the FP64 phases are compared with.  Each form runs `chains`
+ * independent accumulator chains per thread (2, 4 or 8) in
+ * blocks_per_sm x SM-count CTAs of 128 threads for `iters` iterations, with
+ * no memory traffic; one warm-up launch, then one launch timed with CUDA
+ * events on `stream`.  Returns TFLOP/s and the timed launch's milliseconds. */
+#define HCORE_PROBE_DFMA 0                 /* fma.rn.f64 */
+#define HCORE_PROBE_DMMA_8x8x4 1           /* mma.sync m8n8k4 f64 */
+#define HCORE_PROBE_DMMA_16x8x4 2          /* mma.sync m16n8k4 f64 */
+#define HCORE_PROBE_DMMA_16x8x8 3          /* mma.sync m16n8k8 f64 */
+#define HCORE_PROBE_DMMA_16x8x16 4         /* mma.sync m16n8k16 f64, distinct B */
+#define HCORE_PROBE_DMMA_16x8x16_B_ONE_REG 5 /* the four B operands one register */
+#define HCORE_PROBE_DMMA_16x8x16_B_EQUAL 6 /* four B registers holding one value */
+int hcore_gpu_fp64_probe(int kind, int chains, int blocks_per_sm, int iters, void *stream,
+                         double *tflops, double *ms);
+/* the m16n8k16 DMMA form with distinct operands, 4 chains, 8 CTAs per SM
+ * (about 0.3 s), in TFLOP/s; -1 on error */
 double hcore_gpu_fp64_peak(void *stream);
 
 /* One update with HCORE_dgemm's semantics that allocates no memory (no
