@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="panel", choices=["panel", "precision", "dense", "predictor", "tlr",
-                                                         "compress", "zgemm", "fp64peak"],
+                                                         "compress", "zgemm", "fp64peak", "panelstep"],
                    help="panel: the headline (1953 Schur updates of a 65,536-point TLR panel); "
                         "precision: acc sweep on the same updates; "
                         "dense: batched dsyrk/dgemmcd tile updates; predictor: "
@@ -60,10 +60,13 @@ def parse():
                         "tlr: batched POTRF + TRSM, the steps either side of the update; "
                         "compress: the GPU tile compressor on the panel workload's tiles; "
                         "zgemm: the complex update through HCORE_zgemm; "
-                        "fp64peak: the FP64 probe forms with sampled clocks")
+                        "fp64peak: the FP64 probe forms with sampled clocks; "
+                        "panelstep: a whole TLR Cholesky panel step through the panel API")
     p.add_argument("--max-updates", type=int, default=None, help="truncate the update list")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-sub", action="store_true",
+                   help="panel workload: skip the precision and dense sub-runs")
     p.add_argument("--no-autotune", action="store_true",
                    help="panel workload: use the built-in launch shapes instead of autotuning")
     p.add_argument("--per-tile-sample", type=int, default=48)
@@ -417,6 +420,28 @@ def run_gb300(args):
     for s in singles:
         s.close()
 
+    # ---- one plain drop-in call (the single-update configuration) ----
+    result["config1"] = config1_call(hc)
+
+    # ---- the precision sweep and the dense-C step, each oracle-checked ----
+    sub_steps = max(3, args.steps // 4)
+    if not args.no_sub:
+        runs = precision_runs(hc, torch, panel, updates, dev, stream, args.warmup, sub_steps)
+        result["precision"] = [
+            {"acc": r["acc"], "arithmetic": r["arithmetic"], "updates_per_s": r["updates_per_s"],
+             "ms_per_step": r["ms_per_step"], "mean_rank": r["mean_rank"], "all_ok": r["all_ok"],
+             **{k: r["accuracy"][k] for k in ("checked", "rank_equal_to_oracle",
+                                               "within_oracle_error", "max_rel_fro_diff_vs_oracle",
+                                               "panel_rel_fro_err_vs_dense")}}
+            for r in runs]
+    if not args.no_sub and world == 1:     # the dense step reads all 63 panel tiles
+        d = dense_run(hc, torch, panel, dev, stream, args.warmup, sub_steps, world)
+        result["dense"] = {"value": d["value"], "unit": d["unit"], "ms_per_step": d["ms_per_step"],
+                           "workload": d["config"]["workload"], "tflops": d["roofline"]["achieved"],
+                           "frac_of_fp64_peak": d["roofline"]["frac"],
+                           "max_rel_err_vs_oracle": d["accuracy"]["max_rel_err_vs_oracle_sequential_dsyrk"],
+                           "tiles_checked": d["accuracy"]["tiles_checked"]}
+
     # ---- e2e: the same plan over pinned host buffers (zero-copy C2C) ----
     if not args.no_e2e:
         result["e2e"] = e2e_pinned(hc, panel, updates, stream, dev, args, tuning=tuning)
@@ -607,6 +632,72 @@ def accuracy_all(panel, updates, ranks, out_U, out_V, out_off, acc=None, slack=1
                    "differences by QR of the stacked factors (no dense product formed)",
             "note": "per-tile errors above acc come from the reference's absolute threshold on "
                     "tiles whose entries are themselves near acc; the oracle shows the same"}
+
+
+def config1_call(hc, reps=40, warmup=5):
+    """One plain HCORE_dgemm call on host arrays, as a HiCMA tile codelet makes
+    it (src/compute/hcore_dgemm.c:703; call pattern of the reference's test,
+    testing/testing_dgemm.c:347-359): nb = 512, A, B, C each U diag(sigma) V^T
+    with Haar 512 x 32 factors and sigma_i = 10^(-8i/32), ranks 32, acc 1e-8,
+    maxrk 64, C += A B^T.  Each call is timed on the host clock around the C
+    call: host->device copies, the four phases, the copy back and the sync.
+    The same call of the oracle (the reference's LAPACK sequence restated) is
+    timed on one host core beside it, and its rank and product are the
+    check."""
+    import ctypes as C
+
+    import numpy as np
+
+    from oracle import oracle as O
+
+    L = hc.lib()
+    rng = np.random.default_rng(512)
+    M, k0, maxrk, acc = 512, 32, 64, 1e-8
+    AU, AV = O.graded_lowrank(rng, M, k0)
+    BU, BV = O.graded_lowrank(rng, M, k0)
+    CU, CV = O.graded_lowrank(rng, M, k0)
+    CU0 = np.zeros((M, maxrk), order="F")
+    CV0 = np.zeros((M, maxrk), order="F")
+    CU0[:, :k0], CV0[:, :k0] = CU, CV
+    CUw, CVw = CU0.copy(order="F"), CV0.copy(order="F")
+    ra, rb, rc = (np.array([float(k0)]) for _ in range(3))
+    fc = hc.FlopCounter()
+    dp = C.POINTER(C.c_double)
+    pt = lambda x: x.ctypes.data_as(dp)  # noqa: E731
+    times = []
+    for it in range(warmup + reps):
+        np.copyto(CUw, CU0)
+        np.copyto(CVw, CV0)
+        rc[0] = float(k0)
+        t0 = time.perf_counter()
+        L.HCORE_dgemm(111, 112, M, M, 1.0, pt(AU), pt(AV), pt(ra), M, pt(BU), pt(BV), pt(rb), M,
+                      1.0, pt(CUw), pt(CVw), pt(rc), M, 0, maxrk, acc, None, C.byref(fc))
+        t1 = time.perf_counter()
+        if it >= warmup:
+            times.append((t1 - t0) * 1e3)
+    r = int(rc[0])
+    port = O.Port()
+    port.set_threads(1)
+    ptimes = []
+    for it in range(3 + 10):
+        t0 = time.perf_counter()
+        ref = port.gemm(M, 1.0, AU, AV, k0, BU, BV, k0, 1.0, CU, CV, k0, maxrk=maxrk, acc=acc)
+        if it >= 3:
+            ptimes.append((time.perf_counter() - t0) * 1e3)
+    diff = O.rel_fro(CUw[:, :r] @ CVw[:, :r].T, ref["CU"] @ ref["CV"].T)
+    med = statistics.median(times)
+    return {"ms_per_call": med, "ms_min": min(times), "calls_per_s": 1e3 / med, "calls": reps,
+            "rank": r, "oracle_rank": int(ref["rank"]), "rel_fro_diff_vs_oracle": diff,
+            "cpu_1core_ms_per_call": statistics.median(ptimes),
+            "cpu_1core_kind": "port (the oracle's LAPACK restatement of the reference, one "
+                              "host core, one OpenBLAS thread)",
+            "reference_1core_ms_per_call_x86": 2.51,
+            "reference_1core_note": "the reference library itself on one x86 core (Xeon, "
+                                    "2.7 GHz, OpenBLAS, one thread), measured when the "
+                                    "workload was specified; not re-timed on this host",
+            "how": "HCORE_dgemm drop-in on host arrays, median over calls after warm-up, "
+                   "host clock around the call (copies, kernels and the sync included)",
+            "config": "nb 512, ranks 32/32/32, sigma_i = 10^(-8i/32), acc 1e-8, maxrk 64"}
 
 
 def e2e_pinned(hc, panel, updates, stream, dev, args, tuning=None):
@@ -801,17 +892,49 @@ def timed_plan(hc, batch, torch, dev, stream, warmup, steps):
     return e0.elapsed_time(e1) / steps
 
 
-def run_precision(args):
-    """Precision sweep on the panel's tiles: acc 1e-4 / 1e-6 with FP32 factor
-    products and rebuild (QR, SVD, truncation FP64), acc 1e-8 all FP64, and
-    HCORE_sgemm semantics (FP32 end to end) at 1e-4.  Each run: updates/s and
-    its error against the FP64 oracle at the same acc."""
+PRECISION_RUNS = ((1e-4, "F64", "MIXED_FACTORS", "fp64 QR/SVD, fp32 factors+rebuild"),
+                  (1e-6, "F64", "MIXED_FACTORS", "fp64 QR/SVD, fp32 factors+rebuild"),
+                  (1e-8, "F64", None, "fp64"),
+                  (1e-4, "F32", None, "fp32 end to end (HCORE_sgemm)"))
+
+
+def precision_runs(hc, torch, panel, updates, dev, stream, warmup, steps):
+    """The panel's updates at each accuracy of the sweep: FP32 factor products
+    and rebuild at 1e-4 / 1e-6 (QR, SVD, truncation FP64), FP64 at 1e-8, and
+    HCORE_sgemm semantics (FP32 end to end) at 1e-4.  Each run is graph-timed
+    and every update is checked against the FP64 oracle at the same acc."""
     import numpy as np
+
+    n, nb, maxrank = len(updates), panel.nb, panel.maxrank
+    out_off = np.arange(n + 1, dtype=np.int64) * nb * maxrank
+    runs = []
+    for acc, prec_name, flag_name, label in PRECISION_RUNS:
+        precision = getattr(hc, prec_name)
+        flags = getattr(hc, flag_name) if flag_name else 0
+        dt = torch.float64 if precision == hc.F64 else torch.float32
+        src = (panel.U, panel.V) if dt == torch.float64 else (panel.U.float(), panel.V.float())
+        oU = torch.empty(int(out_off[-1]) + 1, dtype=dt, device=dev)
+        oV = torch.empty_like(oU)
+        tasks = build_tasks(hc, panel, updates, oU, oV, out_off, acc=acc, src=src)
+        batch = hc.Batch(tasks, precision=precision, flags=flags)
+        ms = timed_plan(hc, batch, torch, dev, stream, warmup, steps)
+        ranks, status = batch.results(stream.cuda_stream)
+        accs = accuracy_all(panel, updates, ranks, oU, oV, out_off, acc=acc,
+                            slack=1e-14 if (precision == hc.F64 and not flags) else 2e-6)
+        runs.append({"acc": acc, "arithmetic": label, "updates_per_s": n / (ms / 1e3),
+                     "ms_per_step": ms, "mean_rank": float(np.mean(ranks)),
+                     "all_ok": bool((status == 0).all()), "accuracy": accs})
+        batch.close()
+        del oU, oV, src
+    return runs
+
+
+def run_precision(args):
+    """Precision sweep on the panel's tiles (precision_runs), one JSON line."""
     import torch
 
     import hcore_gb300 as hc
     from hcore_gb300 import build as hbuild
-    from hcore_gb300 import panel as pnl
 
     rank, world, local = dist_init()
     if not os.path.exists(hbuild.LIB):
@@ -820,36 +943,15 @@ def run_precision(args):
     dev = torch.device("cuda", local)
     panel, _ = panel_for_rank(args, rank, world, dev)
     updates = panel.updates
-    n, nb, maxrank = len(updates), panel.nb, panel.maxrank
-    out_off = np.arange(n + 1, dtype=np.int64) * nb * maxrank
     stream = torch.cuda.current_stream(dev)
-    runs = []
-    for acc, precision, flags, label in ((1e-4, hc.F64, hc.MIXED_FACTORS, "fp64 QR/SVD, fp32 factors+rebuild"),
-                                         (1e-6, hc.F64, hc.MIXED_FACTORS, "fp64 QR/SVD, fp32 factors+rebuild"),
-                                         (1e-8, hc.F64, 0, "fp64"),
-                                         (1e-4, hc.F32, 0, "fp32 end to end (HCORE_sgemm)")):
-        dt = torch.float64 if precision == hc.F64 else torch.float32
-        src = (panel.U, panel.V) if dt == torch.float64 else (panel.U.float(), panel.V.float())
-        oU = torch.empty(int(out_off[-1]) + 1, dtype=dt, device=dev)
-        oV = torch.empty_like(oU)
-        tasks = build_tasks(hc, panel, updates, oU, oV, out_off, acc=acc, src=src)
-        batch = hc.Batch(tasks, precision=precision, flags=flags)
-        ms = timed_plan(hc, batch, torch, dev, stream, args.warmup, args.steps)
-        ranks, status = batch.results(stream.cuda_stream)
-        accs = accuracy_sample(panel, updates, ranks, oU, oV, out_off, 12, acc=acc,
-                               slack=1e-14 if (precision == hc.F64 and not flags) else 2e-6)
-        runs.append({"acc": acc, "arithmetic": label, "updates_per_s": n / (ms / 1e3),
-                     "ms_per_step": ms, "mean_rank": float(np.mean(ranks)),
-                     "all_ok": bool((status == 0).all()), "accuracy": accs})
-        batch.close()
-        del oU, oV
+    runs = precision_runs(hc, torch, panel, updates, dev, stream, args.warmup, args.steps)
     if rank == 0:
         line = {"metric": "TLR-GEMM updates/s per accuracy (precision sweep)", "value": runs[0]["updates_per_s"],
                 "unit": "updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32",
                 "data": "synthetic (the panel workload's tiles)",
                 "config": dict(WORKLOAD, workload="precision sweep on the panel-0 Schur updates",
-                               updates_per_step=n), "runs": runs}
+                               updates_per_step=len(updates)), "runs": runs}
         print(json.dumps(line))
         sys.stdout.flush()
     barrier(world)
@@ -876,6 +978,22 @@ def run_dense(args):
     hc.lib()
     dev = torch.device("cuda", local)
     panel = pnl.build_panel(device=str(dev), max_updates=1)   # the 63 panel tiles
+    stream = torch.cuda.current_stream(dev)
+    line = dense_run(hc, torch, panel, dev, stream, args.warmup, args.steps, world)
+    if rank == 0:
+        print(json.dumps(line))
+        sys.stdout.flush()
+    barrier(world)
+
+
+def dense_run(hc, torch, panel, dev, stream, warmup, steps, world=1):
+    """The dense-C step on the panel's 63 low-rank tiles (see run_dense);
+    returns its JSON line."""
+    import numpy as np
+
+    from hcore_gb300 import panel as pnl
+    from oracle import oracle as O
+
     nb, T = panel.nb, panel.ntiles
     P = torch.from_numpy(pnl.morton_points(WORKLOAD["points"], 2, 0)).to(dev)
 
@@ -917,7 +1035,6 @@ def run_dense(args):
         flops += f
         flops_exec += f
     plan = hc.DensePlan(tasks)
-    stream = torch.cuda.current_stream(dev)
     # correctness on a sample: tiles 0 and 63 and one off-diagonal tile after one step
     plan.execute(stream.cuda_stream)
     torch.cuda.synchronize(dev)
@@ -935,21 +1052,21 @@ def run_dense(args):
         got = diag[i].cpu().numpy().T
         errs.append(float(np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300)))
     # timed steps
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         plan.execute(stream.cuda_stream)
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         plan.execute(stream.cuda_stream)
     e1.record(stream)
     torch.cuda.synchronize(dev)
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = e0.elapsed_time(e1) / steps
     peak = fp64_peak(hc.lib(), torch, dev)
     tiles_bytes = (len(diag) + len(offd)) * nb * nb * 8 * 2
     line = {"metric": "dense-C tile updates/s (HCORE_dsyrk + HCORE_dgemmcd batched)",
             "value": len(tasks) / (ms / 1e3), "unit": "tile-updates/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "steps": steps, "warmup": warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (covariance tiles of the panel workload)",
             "config": {"workload": "64 diagonal 1024^2 tiles x 63 syrk updates + 62 gemmcd updates",
@@ -963,11 +1080,9 @@ def run_dense(args):
                          "tile_bytes_per_step": tiles_bytes},
             "accuracy": {"max_rel_err_vs_oracle_sequential_dsyrk": max(errs),
                          "tiles_checked": [0, T - 1]}}
-    if rank == 0:
-        print(json.dumps(line))
-        sys.stdout.flush()
     plan.close()
-    barrier(world)
+    del diag, offd, diag0, offd0
+    return line
 
 
 SWEEPS = dict(workload="learned rank predictor: 16 panel sweeps of a TLR Cholesky factorization",
@@ -1554,6 +1669,138 @@ def run_tlr(args):
     barrier(world)
 
 
+def run_panelstep(args):
+    """One whole panel step of the TLR Cholesky of the headline matrix through
+    the library's panel API (hcore_gpu_tlr_panel_step): POTRF of the 1024^2
+    diagonal tile 0 (kernel + nugget 1, as the tile-steps workload), TRSM of
+    the 63 panel V factors, SYRK of the 63 later diagonal tiles and the 1953
+    recompressed Schur updates (acc 1e-8, maxrk 128), tiles stored with 128
+    columns each.  Every timed step restores the matrix first (device copies,
+    outside the timed region) and times the API call on the host clock (plan
+    creation and its workspace allocation included)."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import hcore_gb300 as hc
+    from hcore_gb300 import build as hbuild
+    from hcore_gb300 import panel as pnl
+    from oracle import oracle as O
+
+    rank, world, local = dist_init()
+    if not os.path.exists(hbuild.LIB):
+        hbuild.build()
+    L = hc.lib()
+    dev = torch.device("cuda", local)
+    panel = pnl.build_panel(device=str(dev))          # every tile of the lower triangle
+    nb, T, store = panel.nb, panel.ntiles, panel.maxrank
+    P = torch.from_numpy(pnl.morton_points(WORKLOAD["points"], 2, 0)).to(dev)
+
+    def ktile(i):
+        X = P[i * nb:(i + 1) * nb]
+        d2 = (X * X).sum(1)[:, None] + (X * X).sum(1)[None, :] - 2.0 * X @ X.T
+        return torch.exp(-torch.clamp(d2, min=0.0) / 0.01) + torch.eye(nb, dtype=torch.float64,
+                                                                         device=dev)
+
+    D0 = torch.stack([ktile(i) for i in range(T)])
+    D = D0.clone()
+    tiles = [t for t in panel.tiles]
+    slot = {t: q for q, t in enumerate(tiles)}
+    S0U = torch.zeros((len(tiles), store, nb), dtype=torch.float64, device=dev)
+    S0V = torch.zeros_like(S0U)
+    rank0 = np.zeros(T * T, dtype=np.int32)
+    for t in tiles:
+        s_ = panel.index[t]
+        o0, o1 = int(panel.offset[s_]), int(panel.offset[s_ + 1])
+        r = int(panel.rank[s_])
+        S0U[slot[t], :r] = panel.U[o0:o1].view(r, nb)
+        S0V[slot[t], :r] = panel.V[o0:o1].view(r, nb)
+        rank0[t[0] + t[1] * T] = r
+    SU, SV = S0U.clone(), S0V.clone()
+    Dp = (C.c_void_p * T)(*[D[i].data_ptr() for i in range(T)])
+    Up = (C.c_void_p * (T * T))()
+    Vp = (C.c_void_p * (T * T))()
+    for t in tiles:
+        Up[t[0] + t[1] * T] = SU[slot[t]].data_ptr()
+        Vp[t[0] + t[1] * T] = SV[slot[t]].data_ptr()
+    rk = (C.c_int * (T * T))()
+    mat = hc.TlrMatrix(nt=T, nb=nb, D=C.cast(Dp, C.c_void_p), ldd=nb, U=C.cast(Up, C.c_void_p),
+                       V=C.cast(Vp, C.c_void_p), rank=C.cast(rk, C.c_void_p), maxrank=store)
+    status = (C.c_int * (T * T))()
+
+    def restore():
+        D.copy_(D0)
+        SU.copy_(S0U)
+        SV.copy_(S0V)
+        C.memmove(rk, rank0.ctypes.data, rank0.nbytes)
+        torch.cuda.synchronize(dev)
+
+    def call():
+        info = C.c_int(-1)
+        t0 = time.perf_counter()
+        rc = L.hcore_gpu_tlr_panel_step(C.byref(mat), 0, panel.acc, store, C.byref(info), status,
+                                        None)
+        dt = (time.perf_counter() - t0) * 1e3
+        if rc != 0:
+            raise SystemExit(f"panel step failed ({rc}): {hc.last_error()}")
+        return dt
+
+    times = []
+    for it in range(args.warmup + args.steps):
+        restore()
+        dt = call()
+        if it >= args.warmup:
+            times.append(dt)
+    ms = statistics.median(times)
+    # oracle: the same panel step on host copies of the initial state
+    port = O.Port()
+    hD = [np.asfortranarray(D0[i].cpu().numpy().T) for i in range(T)]
+    hU, hV, hr = {}, {}, {}
+    for t in tiles:
+        r = int(rank0[t[0] + t[1] * T])
+        hr[t] = r
+        hU[t] = np.asfortranarray(S0U[slot[t], :r].cpu().numpy().T)
+        hV[t] = np.asfortranarray(S0V[slot[t], :r].cpu().numpy().T)
+    t0 = time.time()
+    info_ref, st_ref = O.tlr_panel_step(port, hD, hU, hV, hr, 0, panel.acc, store, store)
+    cpu_s = time.time() - t0
+    ups = [t for t in tiles if t[1] > 0]
+    rank_eq = sum(int(rk[i + j * T]) == hr[(i, j)] for (i, j) in ups)
+    picks = [ups[q] for q in np.unique(np.linspace(0, len(ups) - 1, 48).astype(int))]
+    worst = 0.0
+    for (i, j) in picks:
+        r = int(rk[i + j * T])
+        gU = SU[slot[(i, j)], :r].cpu().numpy().T
+        gV = SV[slot[(i, j)], :r].cpu().numpy().T
+        d = _lr_norm(np.hstack([gU, hU[(i, j)]]), np.hstack([gV, -hV[(i, j)]]))
+        worst = max(worst, d / max(_lr_norm(hU[(i, j)], hV[(i, j)]), 1e-300))
+    dmax = max(float(np.abs(D[i].cpu().numpy().T - hD[i]).max() / np.abs(hD[i]).max())
+               for i in (1, T - 1))
+    l0 = float(np.abs(np.tril(D[0].cpu().numpy().T) - np.tril(hD[0])).max() /
+               np.abs(np.tril(hD[0])).max())
+    line = {"metric": "TLR Cholesky panel steps/s through hcore_gpu_tlr_panel_step",
+            "value": 1e3 / ms, "unit": "panel-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (the panel workload's tiles; diagonal tiles with a nugget of 1)",
+            "config": {"workload": "panel 0 of the 64 x 64-tile TLR Cholesky: POTRF + 63 TRSM + "
+                                   "63 SYRK + 1953 recompressed Schur updates",
+                       "nb": nb, "tiles": T, "storage_columns": store, "acc": panel.acc},
+            "ms_min": min(times),
+            "accuracy": {"schur_updates": len(ups), "rank_equal_to_oracle": int(rank_eq),
+                         "sample_products": len(picks),
+                         "max_rel_fro_diff_vs_oracle": worst,
+                         "potrf_rel_err": l0, "syrk_tiles_rel_err": dmax},
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "panel-steps/s", "cores": 1,
+                             "kind": "port", "sample": "the same panel step through the "
+                                                       "oracle's restatement, one host core"}}
+    if rank == 0:
+        print(json.dumps(line))
+        sys.stdout.flush()
+    barrier(world)
+
+
 def run_compress(args):
     """Tile compression on the GPU (hcore_gpu_compress_batched): all 2016
     off-diagonal 1024 x 1024 tiles of the panel workload's covariance matrix,
@@ -1848,6 +2095,8 @@ def main():
         run_zgemm(args)
     elif args.workload == "fp64peak":
         run_fp64peak(args)
+    elif args.workload == "panelstep":
+        run_panelstep(args)
     else:
         run_gb300(args)
 

@@ -90,6 +90,15 @@ class PotrfTask(C.Structure):
     _fields_ = [("uplo", C.c_int), ("n", C.c_int), ("A", C.c_void_p), ("lda", C.c_int)]
 
 
+class TlrMatrix(C.Structure):
+    """Mirror of hcore_tlr_matrix (include/hcore_gb300.h): D, U, V are
+    addresses of pointer arrays (nt and nt*nt entries), rank the address of
+    an nt*nt int array."""
+
+    _fields_ = [("nt", C.c_int), ("nb", C.c_int), ("D", C.c_void_p), ("ldd", C.c_int),
+                ("U", C.c_void_p), ("V", C.c_void_p), ("rank", C.c_void_p), ("maxrank", C.c_int)]
+
+
 class CompressTask(C.Structure):
     """Mirror of hcore_compress_task (include/hcore_gb300.h)."""
 
@@ -195,6 +204,8 @@ def lib() -> C.CDLL:
     L.hcore_gpu_compress_batched.argtypes = [C.c_int, C.POINTER(CompressTask),
                                              C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
     L.hcore_gpu_potrf_batched.argtypes = [C.c_int, C.POINTER(PotrfTask), C.POINTER(C.c_int), vp]
+    L.hcore_gpu_tlr_panel_step.argtypes = [C.POINTER(TlrMatrix), C.c_int, C.c_double, C.c_int,
+                                           C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
     L.hcore_gpu_mlp_create.argtypes = [C.POINTER(vp), C.c_ulonglong]
     L.hcore_gpu_mlp_params.argtypes = [vp, _fp, C.c_int]
     L.hcore_gpu_mlp_gradient.argtypes = [vp, vp, vp, C.c_int, _fp, _fp, vp]

@@ -275,6 +275,40 @@ typedef struct hcore_compress_task {
 int hcore_gpu_compress_batched(int n, const hcore_compress_task *tasks, int *ranks, int *status,
                                void *stream);
 
+/* A tile low-rank (TLR) symmetric matrix, lower triangle, as HiCMA holds it
+ * for its Cholesky: nt x nt tiles of order nb, dense diagonal tiles D[i]
+ * (column-major, ld ldd) and low-rank tiles A_ij = U_ij V_ij^T for i > j,
+ * whose factors (nb x maxrank storage each, ld nb) are U[i + j*nt] and
+ * V[i + j*nt] with rank rank[i + j*nt] (host array; entries with i <= j are
+ * not used).  Device (or pinned host) pointers. */
+typedef struct hcore_tlr_matrix {
+    int nt, nb;
+    double *const *D;
+    int ldd;
+    double *const *U, *const *V;
+    int *rank;
+    int maxrank;
+} hcore_tlr_matrix;
+
+/* Panel step k of the TLR Cholesky A = L L^T (no single counterpart in the
+ * reference: it chains HiCMA's per-tile calls of HCORE_dpotrf
+ * (src/compute/hcore_dpotrf.c:23-34), HCORE_dtrsm (hcore_dtrsm.c:24-48),
+ * HCORE_dsyrk (hcore_dsyrk.c:47-189) and HCORE_dgemm (hcore_dgemm.c:703)):
+ *   D_kk = L_kk L_kk^T (lower triangle overwritten; info = LAPACK's info),
+ *   V_ik <- L_kk^-1 V_ik for every panel tile i > k,
+ *   D_ii <- D_ii - U_ik (V_ik^T V_ik) U_ik^T for i > k (strict upper set to 0),
+ *   A_ij <- A_ij - A_ik A_jk^T for k < j < i, recompressed in place with the
+ *   reference's absolute rule at acc, a + c <= 2 maxrk, new rank <= maxrk and
+ *   <= the tile storage (maxrank); rank[] is updated.
+ * Tiles of rank 0 contribute nothing (no call is made for them).  The SYRK
+ * batch and the recompression plan run concurrently.  status (nt*nt host
+ * array, may be NULL) receives each Schur update's status at [i + j*nt]; a
+ * failed update leaves its tile unchanged.  Synchronous.  Returns
+ * HCORE_GPU_OK, HCORE_GPU_ETASK (POTRF info != 0, or an update failed),
+ * EINVAL, ENOMEM or ECUDA. */
+int hcore_gpu_tlr_panel_step(const hcore_tlr_matrix *A, int k, double acc, int maxrk, int *info,
+                             int *status, void *stream);
+
 /* FP64 issue-rate probes (no counterpart in the reference): the measured
  * ceiling that the FP64 phases are compared with.  Each form runs `chains`
  * independent accumulator chains per thread (2, 4 or 8) in

@@ -468,6 +468,45 @@ def zgemm_dense_truncation(alpha, AU, AV, BU, BV, beta, CU, CV, *, rk=0, acc):
     return r, (U[:, :r] * S[:r]) @ Vh[:r], S[:k]
 
 
+def tlr_panel_step(port: Port, D, U, V, rank, k, acc, maxrk, maxrank):
+    """Panel step k of a TLR Cholesky on the CPU, the sequence of HiCMA's
+    per-tile calls restated with the reference's kernels as the oracle has
+    them: HCORE_dpotrf of D[k] (src/compute/hcore_dpotrf.c:23-34, lower),
+    HCORE_dtrsm of every panel V factor (hcore_dtrsm.c:24-48: Left, Lower,
+    NoTrans, NonUnit), HCORE_dsyrk of every later diagonal tile
+    (hcore_dsyrk.c:47-189, alpha = -1) and the recompressed Schur updates
+    A_ij -= A_ik A_jk^T (hcore_dgemm.c:703, the split API's rank rules:
+    a + c <= 2 maxrk, new rank <= maxrk and <= maxrank).  Tiles of rank 0 take
+    no call.  D (list of nb x nb), U, V (dicts (i, j) -> nb x rank) and rank
+    (dict) are updated in place.  Returns (potrf info, {(i, j): status})."""
+    nt = len(D)
+    nb = D[0].shape[0]
+    Lk, info, _ = port.dpotrf(ord("L"), nb, D[k])
+    D[k] = Lk
+    if info != 0:
+        return info, {}
+    for i in range(k + 1, nt):
+        if rank[(i, k)] > 0:
+            V[(i, k)], _ = port.dtrsm(141, 122, 111, 131, nb, rank[(i, k)], 1.0, Lk, V[(i, k)])
+    for i in range(k + 1, nt):
+        if rank[(i, k)] > 0:
+            D[i], _ = port.dsyrk(nb, rank[(i, k)], -1.0, U[(i, k)], V[(i, k)], D[i])
+    status = {}
+    for j in range(k + 1, nt):
+        for i in range(j + 1, nt):
+            a, b, c = rank[(i, k)], rank[(j, k)], rank[(i, j)]
+            if a == 0 or b == 0:
+                continue
+            CU = U[(i, j)] if c > 0 else np.zeros((nb, 0))
+            CV = V[(i, j)] if c > 0 else np.zeros((nb, 0))
+            ref = port.gemm(nb, -1.0, U[(i, k)], V[(i, k)], a, U[(j, k)], V[(j, k)], b, 1.0,
+                            CU, CV, c, maxrk=maxrk, acc=acc, variant=2, storage_maxrank=maxrank)
+            status[(i, j)] = ref["status"]
+            if ref["status"] == 0:
+                U[(i, j)], V[(i, j)], rank[(i, j)] = ref["CU"], ref["CV"], ref["rank"]
+    return 0, status
+
+
 # --------------------------------------------------------------------------
 # seeded generators
 # --------------------------------------------------------------------------

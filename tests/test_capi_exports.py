@@ -54,3 +54,24 @@ def test_globals_have_reference_defaults(so):
     assert ctypes.c_int.in_dll(so, "use_trmm").value == 0
     assert ctypes.c_int.in_dll(so, "hc_nelm_limit").value == 512
     assert ctypes.c_int.in_dll(so, "gemm_print_index").value == 0
+
+
+def test_c_caller_compiles_and_links_against_the_headers(so, tmp_path):
+    """tests/capi_caller.c (the compiled caller the GPU test runs) builds with
+    -Wall -Werror against include/*.h and links -lhcore_gb300 with no
+    unresolved symbol: the prototypes agree with a C compiler and linker."""
+    import shutil
+    import subprocess
+
+    from hcore_gb300 import build
+
+    gcc = shutil.which("gcc") or shutil.which("cc")
+    if not gcc:
+        pytest.skip("no C compiler")
+    libdir = os.path.dirname(build.LIB)
+    exe = str(tmp_path / "capi_caller")
+    r = subprocess.run([gcc, "-std=c99", "-O2", "-Wall", "-Werror", "-I",
+                        os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "capi_caller.c"),
+                        "-o", exe, f"-L{libdir}", "-lhcore_gb300", f"-Wl,-rpath,{libdir}",
+                        "-Wl,--no-undefined", "-lm"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
