@@ -430,7 +430,7 @@ def run_gb300(args):
         result["precision"] = [
             {"acc": r["acc"], "arithmetic": r["arithmetic"], "updates_per_s": r["updates_per_s"],
              "ms_per_step": r["ms_per_step"], "mean_rank": r["mean_rank"], "all_ok": r["all_ok"],
-             **{k: r["accuracy"][k] for k in ("checked", "rank_equal_to_oracle",
+             **{k: r["accuracy"][k] for k in ("checked", "rank_equal_to_oracle", "gate",
                                                "within_oracle_error", "max_rel_fro_diff_vs_oracle",
                                                "panel_rel_fro_err_vs_dense")}}
             for r in runs]
@@ -575,15 +575,19 @@ def _accuracy_worker(args):
         eg = _lr_norm(np.hstack([gU, CU, AF]), np.hstack([gV, -CV, BU]))
         er = _lr_norm(np.hstack([rU, CU, AF]), np.hstack([rV, -CV, BU]))
         nd = _lr_norm(np.hstack([CU, AF]), np.hstack([CV, -BU]))
-        out.append((u, int(ref["rank"]), d_or, n_or, eg, er, nd))
+        nin = _lr_norm(CU, CV) + _lr_norm(AF, BU)     # ||C|| + ||A B^T||
+        out.append((u, int(ref["rank"]), d_or, n_or, eg, er, nd, nin))
     return out
 
 
-def accuracy_all(panel, updates, ranks, out_U, out_V, out_off, acc=None, slack=1e-14):
+def accuracy_all(panel, updates, ranks, out_U, out_V, out_off, acc=None, slack=1e-14,
+                 slack_of_inputs=False):
     """Every update of the step against the oracle (rank, product) and against
     the exact dense update, on all host cores.  The gate per update is the
     reference's own truncation error: ||P - D|| <= 1.01 ||P_oracle - D|| +
-    slack ||D|| (`slack` 1e-14 for FP64 paths)."""
+    slack ||D|| (`slack` 1e-14 for FP64 paths).  With FP32 arithmetic the
+    rounding scales with the inputs, not with a result that cancels, so
+    `slack_of_inputs` takes slack (||C|| + ||A B^T||) instead."""
     import multiprocessing as mp
 
     import numpy as np
@@ -616,11 +620,13 @@ def accuracy_all(panel, updates, ranks, out_U, out_V, out_off, acc=None, slack=1
                                               for ch in chunks])
     rows = sorted(r for part in res for r in part)
     rk_ref = np.array([r[1] for r in rows])
-    d_or, n_or, eg, er, nd = (np.array([r[q] for r in rows]) for q in range(2, 7))
+    d_or, n_or, eg, er, nd, nin = (np.array([r[q] for r in rows]) for q in range(2, 8))
     rank_ok = int((rk_ref == np.asarray(ranks)).sum())
-    gate = eg <= 1.01 * er + slack * nd
+    gate = eg <= 1.01 * er + slack * (nin if slack_of_inputs else nd)
     rel_or = d_or / np.maximum(n_or, 1e-300)
     return {"checked": n, "rank_equal_to_oracle": rank_ok, "within_oracle_error": int(gate.sum()),
+            "gate": f"||P - D|| <= 1.01 ||P_oracle - D|| + {slack:g} "
+                    + ("(||C|| + ||A B^T||)" if slack_of_inputs else "||D||"),
             "panel_rel_fro_err_vs_dense": float(np.sqrt((eg ** 2).sum() / (nd ** 2).sum())),
             "oracle_panel_rel_fro_err_vs_dense": float(np.sqrt((er ** 2).sum() / (nd ** 2).sum())),
             "max_tile_rel_fro_err_vs_dense": float((eg / nd).max()),
@@ -919,8 +925,9 @@ def precision_runs(hc, torch, panel, updates, dev, stream, warmup, steps):
         batch = hc.Batch(tasks, precision=precision, flags=flags)
         ms = timed_plan(hc, batch, torch, dev, stream, warmup, steps)
         ranks, status = batch.results(stream.cuda_stream)
+        fp64 = precision == hc.F64 and not flags
         accs = accuracy_all(panel, updates, ranks, oU, oV, out_off, acc=acc,
-                            slack=1e-14 if (precision == hc.F64 and not flags) else 2e-6)
+                            slack=1e-14 if fp64 else 2e-6, slack_of_inputs=not fp64)
         runs.append({"acc": acc, "arithmetic": label, "updates_per_s": n / (ms / 1e3),
                      "ms_per_step": ms, "mean_rank": float(np.mean(ranks)),
                      "all_ok": bool((status == 0).all()), "accuracy": accs})

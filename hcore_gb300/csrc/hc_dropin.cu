@@ -255,6 +255,11 @@ struct Single {
         shape.maxK = k;
         shape.nbuckets = 1;
         shape.buckets[0] = Bucket{0, 1, k};
+        // one update alone: its latency is the call's, so the Jacobi takes
+        // four lanes per column pair (spread over four sub-partitions) and
+        // the QR CTAs eight warps
+        shape.svd_lanes[0] = shape.svd_lanes[1] = shape.svd_lanes[2] = 4;
+        shape.qr_warps = 8;
         cudaError_t e = configure_recompress<T>(k, &shape.svd_smem_kmax, &shape.svd_half_kmax);
         if (e == cudaSuccess)
             e = launch_recompress<T>(d_desc, 1, ws, d_rs, d_rs + 1, nullptr, shape, tc.stream,

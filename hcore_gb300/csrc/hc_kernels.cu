@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <climits>
+#include <mutex>
 
 #include "hc_internal.h"
 
@@ -31,12 +32,10 @@ struct Lim;
 template <>
 struct Lim<double> {
     static constexpr double eps = DBL_EPSILON;
-    static constexpr double big_zeta = 1e150;
 };
 template <>
 struct Lim<float> {
     static constexpr float eps = FLT_EPSILON;
-    static constexpr float big_zeta = 1e18f;
 };
 
 template <typename T>
@@ -370,9 +369,23 @@ struct JacobiLim<float> {
 // shared-memory limit): four lanes per pair, up to 1024 threads, to keep
 // enough loads in flight on the L2-resident matrices.
 constexpr int kSvdMaxThreads = 1024;
+// A tuning value of 0 fills the warps: one lane per pair needs ceil(np/32)
+// warps, and the pairs take as many lanes each (a power of two) as still fit
+// in them.  On this GPU one FP64 warp instruction holds a sub-partition's
+// pipe for about 64 cycles whatever its active lanes, so lanes left idle in a
+// warp are free to share a pair's rows, while an extra warp would repeat the
+// rotation-parameter arithmetic.
 __host__ __device__ inline int svd_group(int K, bool smem, const int *lanes) {
     const int np = (K + 1) / 2;
-    if (smem) return np <= 24 ? lanes[0] : (np <= 64 ? lanes[1] : lanes[2]);
+    if (smem) {
+        int g = np <= 24 ? lanes[0] : (np <= 64 ? lanes[1] : lanes[2]);
+        if (g == 0) {
+            const int w = (np + 31) / 32;
+            g = 1;
+            while (g < 32 && 2 * g * np <= 32 * w) g *= 2;
+        }
+        return g;
+    }
     return np <= kSvdMaxThreads / 4 ? 4 : (np <= kSvdMaxThreads / 2 ? 2 : 1);
 }
 // Threads per CTA of the SVD kernel: G lanes for each of the K/2 pairs.
@@ -535,21 +548,24 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
             }
         }
         __syncthreads();
-        // reflector of column j, rows j..k-1 (dlarfg), by thread 0
-        if (tid == 0) {
+        // reflector of column j, rows j..k-1 (dlarfg), by warp 0: the lanes
+        // split the sum of squares and the scaling
+        if (tid < 32) {
             T *aj = A + ixA(0, j);
             const T alpha = aj[j * rsA];
             T ss = 0;
-            for (int i = j + 1; i < k; ++i) ss += aj[i * rsA] * aj[i * rsA];
+            for (int i = j + 1 + lane; i < k; i += 32) ss += aj[i * rsA] * aj[i * rsA];
+            ss = warp_sum(ss);
             T tj = 0;
             if (ss > T(0)) {
                 const T beta = -copysign(sqrt(alpha * alpha + ss), alpha);
                 tj = (beta - alpha) / beta;
                 const T scal = T(1) / (alpha - beta);
-                for (int i = j + 1; i < k; ++i) aj[i * rsA] *= scal;
-                aj[j * rsA] = beta;
+                for (int i = j + 1 + lane; i < k; i += 32) aj[i * rsA] *= scal;
+                __syncwarp();
+                if (lane == 0) aj[j * rsA] = beta;
             }
-            s_tau[j] = tj;
+            if (lane == 0) s_tau[j] = tj;
         }
         __syncthreads();
         // apply to the trailing columns and downdate their norms (lane per column)
@@ -608,13 +624,16 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
     // off-diagonal |a_pq| / sqrt(a_pp a_qq) was at most sqrt(tol): cyclic
     // Jacobi converges quadratically, so the next sweep would only rotate by
     // angles near tol, moving the singular values at second order (the
-    // product U S V^T is exact after every sweep; only orthogonality remains)
-    const T stop_rel = sqrt(tol);
+    // product U S V^T is exact after every sweep; only orthogonality remains).
+    // Both tests compare squares (a_pq^2 against tol^2 a_pp a_qq), so they
+    // take no square root or division.
+    const T tol2 = tol * tol;
+    const T stop2 = tol;   // (sqrt(tol))^2
     bool converged = (k == 1);
     int sweeps = 0;
     for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
         if (tid == 0) s_rot = 0;
-        T sweep_rel = 0;   // this thread's largest relative off-diagonal rotated
+        bool sweep_big = false;   // this thread rotated a pair above sqrt(tol)
         __syncthreads();
         for (int round = 0; round < n - 1; ++round) {
             for (int base = 0; base < np; base += ngrp) {
@@ -635,18 +654,27 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                     aqq = s_nrm[q];
                     apq = dp * dq * dot;
                 }
+                // the squared norms are at most 4k (T is scaled to entries
+                // below 2), so the products below cannot overflow
+                const T apq2 = apq * apq, pq = app * aqq;
                 const bool rot = valid && app > NormLim<T>::safmin && aqq > NormLim<T>::safmin &&
-                                 apq != T(0) && abs(apq) > tol * sqrt(app) * sqrt(aqq);
+                                 apq != T(0) && apq2 > tol2 * pq;
                 T t = 0, cs = 1;
                 if (rot) {
-                    sweep_rel = max(sweep_rel, abs(apq) / (sqrt(app) * sqrt(aqq)));
-                    const T zeta = (aqq - app) / (T(2) * apq);
-                    const T az = abs(zeta);
-                    t = az > Lim<T>::big_zeta ? T(0.5) / zeta
-                                              : copysign(T(1), zeta) / (az + sqrt(T(1) + az * az));
-                    cs = T(1) / sqrt(T(1) + t * t);
-                    // true columns p' = c (p - t q), q' = c (q + t p), in B and V_J
-                    const T f1 = t * dq / dp, f2 = t * dp / dq;
+                    sweep_big |= apq2 > stop2 * pq;
+                    // t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)), zeta = w / v with
+                    // w = a_qq - a_pp, v = 2 a_pq, taken as |v| / (|w| + sqrt(w^2 + v^2))
+                    // with the sign of w v (w = 0 gives t = sign(v)): one square
+                    // root and one division, and no overflow for tiny a_pq
+                    const T w = aqq - app, v = T(2) * apq;
+                    const T h = sqrt(fma(w, w, v * v));
+                    t = abs(v) / (abs(w) + h);
+                    if ((w < T(0)) != (v < T(0))) t = -t;
+                    cs = rsqrt(fma(t, t, T(1)));
+                    // true columns p' = c (p - t q), q' = c (q + t p), in B and V_J;
+                    // with scales d: f1 = t dq / dp, f2 = t dp / dq from one reciprocal
+                    const T inv = T(1) / (dp * dq);
+                    const T f1 = t * (dq * dq) * inv, f2 = t * (dp * dp) * inv;
                     T *vp = A + ixA(0, p), *vq = A + ixA(0, q);
                     for (int i = lig; i < k; i += G) {
                         const T a = xp[i * rsB], b = xq[i * rsB];
@@ -704,13 +732,13 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
             s_nrm[j] = dj * dj * s2;
         }
         ++sweeps;
-        sweep_rel = warp_max(sweep_rel);
-        if (lane == 0) s_wmax[tid >> 5] = sweep_rel;
+        const bool big = __any_sync(0xffffffffu, sweep_big);
+        if (lane == 0) s_wmax[tid >> 5] = big ? T(1) : T(0);
         __syncthreads();
         if (tid == 0) {
             T m = 0;
             for (int w = 0; w < nthr / 32; ++w) m = max(m, s_wmax[w]);
-            s_conv = (s_rot == 0 || m <= stop_rel) ? 1 : 0;
+            s_conv = (s_rot == 0 || m == T(0)) ? 1 : 0;
         }
         __syncthreads();
         converged = s_conv != 0;
@@ -927,14 +955,38 @@ static void launch_geqrf(const Desc *d_desc, int n, T *ws, int warps, cudaStream
 }
 
 template <typename T>
+static cudaError_t configure_recompress_once(int dev, int *svd_smem_kmax, int *svd_half_kmax);
+
+// The kernel attributes are per device and do not depend on the plan, so
+// they are set once per device and scalar type; later calls (every drop-in
+// call, every plan) only read the cached limits.
+template <typename T>
 cudaError_t configure_recompress(int maxK, int *svd_smem_kmax, int *svd_half_kmax) {
+    (void)maxK;
+    constexpr int kDevices = 64;
+    static std::mutex mu;
+    static int done[kDevices], kmax_c[kDevices], khalf_c[kDevices];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kDevices) return configure_recompress_once<T>(dev, svd_smem_kmax, svd_half_kmax);
+    std::lock_guard<std::mutex> lk(mu);
+    if (!done[dev]) {
+        e = configure_recompress_once<T>(dev, &kmax_c[dev], &khalf_c[dev]);
+        if (e != cudaSuccess) return e;
+        done[dev] = 1;
+    }
+    *svd_smem_kmax = kmax_c[dev];
+    if (svd_half_kmax) *svd_half_kmax = khalf_c[dev];
+    return cudaSuccess;
+}
+
+template <typename T>
+static cudaError_t configure_recompress_once(int dev, int *svd_smem_kmax, int *svd_half_kmax) {
     // the Jacobi matrices live in shared memory when they fit (k <= 119 in FP64,
     // 168 in FP32, with 227 KB per CTA); R^T alone up to k = 167 in FP64
-    (void)maxK;
-    int dev = 0, optin = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess)
-        e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    int optin = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return e;
     // dynamic shared memory the SVD kernel may take next to its static arrays
     cudaFuncAttributes fa;

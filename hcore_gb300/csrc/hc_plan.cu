@@ -449,9 +449,9 @@ extern "C" int hcore_gpu_tuning_default(hcore_gpu_tuning *t) {
     t->stream_groups = 16;
     if (const char *env = getenv("HCORE_GPU_STREAMS")) t->stream_groups = atoi(env);
     t->stream_groups = std::max(1, std::min(t->stream_groups, 64));
-    t->svd_lanes[0] = 2;
-    t->svd_lanes[1] = 2;
-    t->svd_lanes[2] = 2;
+    t->svd_lanes[0] = 0;   // fill the warps (see svd_group)
+    t->svd_lanes[1] = 0;
+    t->svd_lanes[2] = 0;
     t->bucket_width = 8;
     t->phase_sync = 0;
     t->qr_warps = 4;
@@ -459,9 +459,9 @@ extern "C" int hcore_gpu_tuning_default(hcore_gpu_tuning *t) {
 }
 
 static bool valid_tuning(const hcore_gpu_tuning &t) {
-    auto pow2 = [](int x) { return x >= 1 && x <= 32 && (x & (x - 1)) == 0; };
-    return t.stream_groups >= 1 && t.stream_groups <= 64 && pow2(t.svd_lanes[0]) &&
-           pow2(t.svd_lanes[1]) && pow2(t.svd_lanes[2]) &&
+    auto lanes = [](int x) { return x == 0 || (x >= 1 && x <= 32 && (x & (x - 1)) == 0); };
+    return t.stream_groups >= 1 && t.stream_groups <= 64 && lanes(t.svd_lanes[0]) &&
+           lanes(t.svd_lanes[1]) && lanes(t.svd_lanes[2]) &&
            (t.bucket_width == 8 || t.bucket_width == 16) && (t.phase_sync == 0 || t.phase_sync == 1) &&
            (t.qr_warps == 2 || t.qr_warps == 4 || t.qr_warps == 8);
 }
@@ -1003,7 +1003,8 @@ extern "C" int hcore_gpu_autotune(int precision, int n, const hcore_lr_task *tas
     int rc = time_cfg(cur, cur_ms);
     // one parameter at a time, keeping a change only if it gains 0.5 %
     const int groups[] = {4, 8, 16, 24, 32};
-    const int lanes0[] = {1, 2}, lanes1[] = {2, 4, 8}, lanes2[] = {1, 2, 4}, widths[] = {8, 16};
+    const int lanes0[] = {0, 1, 2}, lanes1[] = {0, 1, 2, 4, 8}, lanes2[] = {0, 1, 2, 4};
+    const int widths[] = {8, 16};
     // field(t) is the parameter being searched, as a reference into t
     auto try_values = [&](auto field, const int *vals, int nv) {
         for (int v = 0; v < nv && !rc; ++v) {
@@ -1023,9 +1024,9 @@ extern "C" int hcore_gpu_autotune(int precision, int n, const hcore_lr_task *tas
     try_values([](hcore_gpu_tuning &t) -> int & { return t.stream_groups; }, groups, 5);
     const int qrw[] = {8, 4, 2};
     try_values([](hcore_gpu_tuning &t) -> int & { return t.qr_warps; }, qrw, 3);
-    try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[1]; }, lanes1, 3);
-    try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[2]; }, lanes2, 3);
-    try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[0]; }, lanes0, 2);
+    try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[1]; }, lanes1, 5);
+    try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[2]; }, lanes2, 4);
+    try_values([](hcore_gpu_tuning &t) -> int & { return t.svd_lanes[0]; }, lanes0, 3);
     try_values([](hcore_gpu_tuning &t) -> int & { return t.bucket_width; }, widths, 2);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -145,16 +145,18 @@ int hcore_gpu_plan_destroy(hcore_gpu_plan plan);
 /* Launch-shape tuning of a plan (no counterpart in the reference).
  *   stream_groups      updates are dealt into this many concurrent groups
  *   svd_lanes[3]       lanes per column pair of the shared-memory SVD buckets
- *                      with <= 24, <= 64 and more column pairs
+ *                      with <= 24, <= 64 and more column pairs (1..32, a
+ *                      power of two; 0: as many as fit in the warps that one
+ *                      lane per pair needs)
  *   bucket_width       rank-bucket edges every 8 (fine) or 16 (coarse)
  *   phase_sync         0: each group runs its four phases as soon as it can
  *                      (phases of different groups overlap); 1: every group
  *                      finishes a phase before any group starts the next
  *   qr_warps           warps per Householder-QR CTA: 8 (shortest path per
  *                      update), 4 or 2 (two or four times the CTAs per SM)
- * hcore_gpu_tuning_default fills the built-in choice (16 groups, 2 lanes per
- * pair, width 8, no phase sync, 4 QR warps: the best measured on a TLR
- * panel of 1953 updates; HCORE_GPU_STREAMS overrides the groups).  hcore_gpu_autotune
+ * hcore_gpu_tuning_default fills the built-in choice (16 groups, lanes per
+ * pair filling the warps (0), width 8, no phase sync, 4 QR warps;
+ * HCORE_GPU_STREAMS overrides the groups).  hcore_gpu_autotune
  * times plans of the given tasks over a search of these parameters
  * (coordinate descent; each candidate's execute captured in a CUDA graph on
  * a private stream and replayed `reps` times) and returns the fastest; the

@@ -86,7 +86,7 @@ def _batch_case(rng, M, a, b, c, decades=8.0):
     return AU, AV, BU, BV, CU, CV
 
 
-def _run_batch(hc, cases, dtype=np.float64, flags=0, precision=0, in_place=False):
+def _run_batch(hc, cases, dtype=np.float64, flags=0, precision=0, in_place=False, tuning=None):
     """cases: list of dict(M, a, b, c, alpha, beta, rk, maxrk, acc, arrays)."""
     import torch
     from hcore_gb300 import devmem
@@ -112,7 +112,7 @@ def _run_batch(hc, cases, dtype=np.float64, flags=0, precision=0, in_place=False
                       CU=dCU.data_ptr(), CV=dCV.data_ptr(), ldc=M, CUo=oCU.data_ptr(),
                       CVo=oCV.data_ptr(), ldco=M)
         tasks.append(t)
-    batch = hc.Batch(tasks, precision=precision, flags=flags)
+    batch = hc.Batch(tasks, precision=precision, flags=flags, tuning=tuning)
     batch.execute()
     ranks, status = batch.results()
     outs = []
@@ -143,11 +143,15 @@ def test_batched_uneven_ranks_vs_oracle(hc, port):
 
 
 def test_batched_equals_single_calls(hc):
-    """The batched plan and the drop-in call run the same kernels: identical bits."""
+    """The batched plan and the drop-in call run the same kernels: identical
+    bits when the plan takes the single call's launch shape (four lanes per
+    Jacobi column pair, eight-warp QR CTAs; the lanes set the SVD's
+    reduction order)."""
     rng = np.random.default_rng(3)
     cases = [dict(M=192, a=12, b=9, c=15, alpha=-1.0, beta=1.0, maxrk=40, acc=1e-8,
                   arrays=_batch_case(rng, 192, 12, 9, 15)) for _ in range(4)]
-    _, ranks, status, outs = _run_batch(hc, cases)
+    _, ranks, status, outs = _run_batch(hc, cases,
+                                        tuning=hc.make_tuning(svd_lanes=[4, 4, 4], qr_warps=8))
     for cs, r, (CUo, CVo) in zip(cases, ranks, outs):
         AU, AV, BU, BV, CU, CV = cs["arrays"]
         r1, CU1, CV1, _ = hc.hcore_dgemm(192, -1.0, AU, AV, 12, BU, BV, 9, 1.0, CU, CV, 15,
