@@ -692,8 +692,41 @@ def config1_call(hc, reps=40, warmup=5):
             ptimes.append((time.perf_counter() - t0) * 1e3)
     diff = O.rel_fro(CUw[:, :r] @ CVw[:, :r].T, ref["CU"] @ ref["CV"].T)
     med = statistics.median(times)
+    # where the call's time goes: the same update as a one-task plan with the
+    # drop-in's launch shape, its four phases timed with CUDA events
+    import torch
+
+    from hcore_gb300 import devmem
+
+    dv = [devmem.to_device(x) for x in (AU, AV, BU, BV, CU, CV)]
+    oU, oV = (torch.zeros((maxrk, M), dtype=torch.float64, device="cuda") for _ in range(2))
+    task = hc.LrTask(M=M, a=k0, b=k0, c=k0, rk=0, maxrk=maxrk, ld_newv=maxrk, storage_maxrank=0,
+                     alpha=1.0, beta=1.0, acc=acc, AU=dv[0].data_ptr(), AV=dv[1].data_ptr(),
+                     lda=M, BU=dv[2].data_ptr(), BV=dv[3].data_ptr(), ldb=M, Bdense=None,
+                     CU=dv[4].data_ptr(), CV=dv[5].data_ptr(), ldc=M, CUo=oU.data_ptr(),
+                     CVo=oV.data_ptr(), ldco=M)
+    one = hc.Batch([task], tuning=hc.make_tuning(stream_groups=1, svd_lanes=[4, 4, 4], qr_warps=8))
+    st = torch.cuda.current_stream()
+    ph = {"stack": 1, "qr": 2, "svd": 4, "rebuild": 8}
+    acc_ms = {nm: [] for nm in ph}
+    for it in range(8):
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        torch.cuda.synchronize()
+        evs[0].record(st)
+        for q, bit in enumerate(ph.values()):
+            one.execute_phases(bit, st.cuda_stream)
+            evs[q + 1].record(st)
+        torch.cuda.synchronize()
+        if it >= 3:
+            for q, nm in enumerate(ph):
+                acc_ms[nm].append(evs[q].elapsed_time(evs[q + 1]))
+    one.close()
+    phases = {nm: round(statistics.median(v), 4) for nm, v in acc_ms.items()}
     return {"ms_per_call": med, "ms_min": min(times), "calls_per_s": 1e3 / med, "calls": reps,
             "rank": r, "oracle_rank": int(ref["rank"]), "rel_fro_diff_vs_oracle": diff,
+            "phases_ms": phases,
+            "phases_how": "the same update as a one-task plan (device pointers, the drop-in's "
+                          "launch shape), phases timed back to back with CUDA events",
             "cpu_1core_ms_per_call": statistics.median(ptimes),
             "cpu_1core_kind": "port (the oracle's LAPACK restatement of the reference, one "
                               "host core, one OpenBLAS thread)",
@@ -1392,7 +1425,9 @@ def run_predictor(args):
                 # the plans' launch shapes: the library autotuner on sweep 0's batch
                 # (set-up, outside the timed region; used by both arms and all sweeps)
                 make_t = maker(store, ups, k)
-                sub = list(range(n))
+                # at most 2000 evenly spread updates of the batch (the whole
+                # 64-tile sweep; a sample of the 8001 of the full-size one)
+                sub = sorted(set(np.linspace(0, n - 1, min(n, 2000)).astype(int).tolist()))
                 tU = torch.empty(len(sub) * nb * MAXR + 1, dtype=torch.float64, device=dev)
                 tV = torch.empty_like(tU)
                 t0 = time.time()
@@ -1489,7 +1524,12 @@ def run_predictor(args):
             "warmup": 1, "ms_per_step": prd["ms_gemm"] + prd["ms_rebuild"] + prd["ms_predict"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded 3D points, tiles compressed on the host cores)",
-            "config": dict(SWEEPS, block_tiles=B, nb=nb, sweeps=S),
+            "config": dict(SWEEPS, block_tiles=B, nb=nb, sweeps=S,
+                           region=(f"the whole matrix: {B} x {B} tiles, all {B * nb} points"
+                                   if B * nb >= SWEEPS["points"] else
+                                   f"leading {B} x {B} tiles (the first {B * nb} of the "
+                                   f"{SWEEPS['points']} Morton-sorted points); their "
+                                   "factorization does not depend on the rest of the matrix")),
             "pad_to_maxrank": {"updates_per_s": gemm_ups(pad),
                                **{k: v for k, v in pad.items() if k != "per_sweep"}},
             "predictor": {k: v for k, v in prd.items() if k != "per_sweep"},

@@ -72,6 +72,14 @@ __device__ __forceinline__ T mul_exp2(T x, int n) {
     return (x * exp2i<T>(n / 2)) * exp2i<T>(n - n / 2);
 }
 
+// -x by its sign bit (integer pipe; exact, NaN payloads kept)
+__device__ __forceinline__ double flip_sign(double x) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+}
+__device__ __forceinline__ float flip_sign(float x) {
+    return __int_as_float(__float_as_int(x) ^ (int)0x80000000u);
+}
+
 // ---------------------------------------------------------------------------
 // phase 1: stack the factors
 // ---------------------------------------------------------------------------
@@ -90,15 +98,20 @@ __global__ void __launch_bounds__(kThreads) stack_kernel(const Desc *__restrict_
     const T *AU = (const T *)d.AU, *AV = (const T *)d.AV;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-    // [beta*CU | alpha*AU] and [CV | .] (hcore_dgemm.c:106-114, :199-205)
+    // [beta*CU | alpha*AU] and [CV | .] (hcore_dgemm.c:106-114, :199-205).
+    // The Schur update's coefficients 1 and -1 are applied without an FP64
+    // instruction (a copy, a sign-bit flip on the integer pipe): same bits.
+    const bool beta_one = beta == T(1), alpha_minus_one = alpha == T(-1);
     for (long long e = tid; e < (long long)M * c; e += kThreads) {
         const int i = (int)(e % M), j = (int)(e / M);
-        UA[(size_t)j * M + i] = beta * CU[(size_t)j * d.ldc + i];
+        const T x = CU[(size_t)j * d.ldc + i];
+        UA[(size_t)j * M + i] = beta_one ? x : beta * x;
         VB[(size_t)j * M + i] = CV[(size_t)j * d.ldc + i];
     }
     for (long long e = tid; e < (long long)M * a; e += kThreads) {
         const int i = (int)(e % M), j = (int)(e / M);
-        UA[(size_t)(c + j) * M + i] = alpha * AU[(size_t)j * d.lda + i];
+        const T x = AU[(size_t)j * d.lda + i];
+        UA[(size_t)(c + j) * M + i] = alpha_minus_one ? flip_sign(x) : alpha * x;
     }
     if (a == 0) return;
     T *G = VB + (size_t)c * M;

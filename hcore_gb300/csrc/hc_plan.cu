@@ -449,9 +449,9 @@ extern "C" int hcore_gpu_tuning_default(hcore_gpu_tuning *t) {
     t->stream_groups = 16;
     if (const char *env = getenv("HCORE_GPU_STREAMS")) t->stream_groups = atoi(env);
     t->stream_groups = std::max(1, std::min(t->stream_groups, 64));
-    t->svd_lanes[0] = 0;   // fill the warps (see svd_group)
-    t->svd_lanes[1] = 0;
-    t->svd_lanes[2] = 0;
+    t->svd_lanes[0] = 2;   // the autotuner's pick on a TLR panel of 1953 updates
+    t->svd_lanes[1] = 2;
+    t->svd_lanes[2] = 2;
     t->bucket_width = 8;
     t->phase_sync = 0;
     t->qr_warps = 4;

@@ -154,9 +154,9 @@ int hcore_gpu_plan_destroy(hcore_gpu_plan plan);
  *                      finishes a phase before any group starts the next
  *   qr_warps           warps per Householder-QR CTA: 8 (shortest path per
  *                      update), 4 or 2 (two or four times the CTAs per SM)
- * hcore_gpu_tuning_default fills the built-in choice (16 groups, lanes per
- * pair filling the warps (0), width 8, no phase sync, 4 QR warps;
- * HCORE_GPU_STREAMS overrides the groups).  hcore_gpu_autotune
+ * hcore_gpu_tuning_default fills the built-in choice (16 groups, 2 lanes per
+ * pair, width 8, no phase sync, 4 QR warps: the autotuner's pick on a TLR
+ * panel of 1953 updates; HCORE_GPU_STREAMS overrides the groups).  hcore_gpu_autotune
  * times plans of the given tasks over a search of these parameters
  * (coordinate descent; each candidate's execute captured in a CUDA graph on
  * a private stream and replayed `reps` times) and returns the fastest; the

@@ -50,6 +50,7 @@ def test_tunings_give_the_same_results(hc):
     assert (s0 == 0).all()
     for tun in ({"stream_groups": 1}, {"stream_groups": 3, "bucket_width": 16},
                 {"svd_lanes": (2, 8, 4)}, {"stream_groups": 64, "svd_lanes": (1, 2, 1)},
+                {"svd_lanes": (2, 2, 2)}, {"svd_lanes": (4, 4, 4), "qr_warps": 8},
                 {"stream_groups": 8, "phase_sync": 1}, {"qr_warps": 4}, {"qr_warps": 2}):
         r, st, p = _run(hc, tasks, keep, tun)
         assert np.array_equal(r, r0) and np.array_equal(st, s0), tun
@@ -65,7 +66,7 @@ def test_autotune_returns_a_valid_tuning(hc):
     assert ms > 0
     assert 1 <= t["stream_groups"] <= 64 and t["bucket_width"] in (8, 16)
     assert t["phase_sync"] in (0, 1) and t["qr_warps"] in (2, 4, 8)
-    assert all(x in (1, 2, 4, 8, 16, 32) for x in t["svd_lanes"])
+    assert all(x in (0, 1, 2, 4, 8, 16, 32) for x in t["svd_lanes"])   # 0: fill the warps
     r, st, _ = _run(hc, tasks, keep, best)
     assert (st == 0).all()
 
@@ -73,7 +74,8 @@ def test_autotune_returns_a_valid_tuning(hc):
 def test_invalid_tuning_is_refused(hc):
     rng = np.random.default_rng(73)
     keep, tasks = _tasks(hc, rng, n=4)
-    for bad in ({"stream_groups": 0}, {"svd_lanes": (3, 4, 2)}, {"bucket_width": 12},
+    for bad in ({"stream_groups": 0}, {"svd_lanes": (3, 4, 2)}, {"svd_lanes": (-1, 2, 2)},
+                {"bucket_width": 12},
                 {"phase_sync": 2}, {"qr_warps": 6}):
         with pytest.raises(hc.HcoreError):
             hc.Batch(tasks, tuning=bad)
