@@ -104,6 +104,48 @@ int port_dlatms(int m, int n, char dist, int *iseed, char sym, double *d, int mo
 
 /* ---- the tile steps either side of the update (FP64 only, as in the
  * reference): the same BLAS/LAPACK calls in the same order ---- */
+/* A list of Schur-type updates over two factor arenas, as a benchmark's CPU
+ * baseline runs them: update u reads tiles sa[u], sb[u] and sc[u], whose
+ * factors are column-major nb x rank blocks at U + off[t], V + off[t] (rank
+ * = (off[t+1] - off[t]) / nb), and runs port_dgemm on a copy of C (so the
+ * list can be repeated on the same inputs).  The loop is in C so that the
+ * timed work is the reference's sequence of calls and not interpreter
+ * overhead.  Returns the number of updates whose status was not PORT_OK,
+ * or -1 if the scratch could not be allocated. */
+int port_dgemm_list(int nb, const double *U, const double *V, const long long *off, int n,
+                    const int *sa, const int *sb, const int *sc, double alpha, double beta,
+                    int maxrk, double acc, int variant)
+{
+    int kmax = 1, bad = 0;
+    for (int u = 0; u < n; ++u) {
+        const int a = (int)((off[sa[u] + 1] - off[sa[u]]) / nb);
+        const int c = (int)((off[sc[u] + 1] - off[sc[u]]) / nb);
+        if (a + c > kmax) kmax = a + c;
+    }
+    double *CU = (double *)malloc(sizeof(double) * (size_t)nb * kmax);
+    double *CV = (double *)malloc(sizeof(double) * (size_t)nb * kmax);
+    if (!CU || !CV) {
+        free(CU);
+        free(CV);
+        return -1;
+    }
+    for (int u = 0; u < n; ++u) {
+        const long long oa = off[sa[u]], ob = off[sb[u]], oc = off[sc[u]];
+        const int a = (int)((off[sa[u] + 1] - oa) / nb);
+        const int b = (int)((off[sb[u] + 1] - ob) / nb);
+        int c = (int)((off[sc[u] + 1] - oc) / nb);
+        memcpy(CU, U + oc, sizeof(double) * (size_t)nb * c);
+        memcpy(CV, V + oc, sizeof(double) * (size_t)nb * c);
+        unsigned long fl = 0;
+        const int st = port_dgemm(nb, alpha, U + oa, V + oa, a, nb, U + ob, V + ob, b, nb, NULL,
+                                  beta, CU, CV, &c, nb, 0, maxrk, maxrk, acc, variant, NULL, &fl);
+        if (st != PORT_OK) ++bad;
+    }
+    free(CU);
+    free(CV);
+    return bad;
+}
+
 void scipy_cblas_dtrsm(int, int, int, int, int, int, int, double, const double *, int,
                        double *, int);
 int scipy_LAPACKE_dpotrf_work(int, char, int, double *, int);

@@ -31,6 +31,9 @@ int port_sgemm(int M, float alpha, const float *AU, const float *AV, int a, int 
                float beta, float *CU, float *CV, int *c_inout, int ldc, int rk, int maxrk,
                int storage_maxrank, float acc, int variant, float *sigma_out,
                unsigned long *flops_update);
+int port_dgemm_list(int nb, const double *U, const double *V, const long long *off, int n,
+                    const int *sa, const int *sb, const int *sc, double alpha, double beta,
+                    int maxrk, double acc, int variant);
 int port_dsyrk(int M, int K, double alpha, const double *AU, int LDAU, const double *AV,
                double *CD, int LDCD, unsigned long *flops_syrk);
 int port_dgemmcd(int M, const double *Au, const double *Av, int Arank, const double *Bu,

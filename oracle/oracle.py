@@ -107,11 +107,26 @@ class Port:
                                         C.c_double, C.c_double, C.c_int, C.c_int, C.c_char, _dp,
                                         C.c_int]
             lib.port_set_threads.argtypes = [C.c_int]
+            lib.port_dgemm_list.restype = C.c_int
+            lib.port_dgemm_list.argtypes = [C.c_int, _dp, _dp, C.c_void_p, C.c_int, _ip, _ip, _ip,
+                                            C.c_double, C.c_double, C.c_int, C.c_double, C.c_int]
             Port._lib = lib
         self.lib = Port._lib
 
     def set_threads(self, n: int) -> None:
         self.lib.port_set_threads(n)
+
+    def gemm_list(self, nb, U, V, off, sa, sb, sc, *, alpha, beta, maxrk, acc, variant=0):
+        """port_dgemm over a list of updates whose factors live in two flat
+        FP64 arenas U, V (tile t: column-major nb x rank block at off[t]);
+        the loop runs in C.  Returns the count of updates that failed."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        off = np.ascontiguousarray(off, dtype=np.int64)
+        sa, sb, sc = (np.ascontiguousarray(x, dtype=np.int32) for x in (sa, sb, sc))
+        return int(self.lib.port_dgemm_list(nb, _ptr(U), _ptr(V), off.ctypes.data, len(sa),
+                                            _ptr(sa, _ip), _ptr(sb, _ip), _ptr(sc, _ip), alpha,
+                                            beta, maxrk, acc, variant))
 
     def flop_counts(self, op: str, a: int, b: int = 0, c: int = 0, d: int = 0) -> int:
         return int(self.lib.port_flop_counts(op.encode(), a, b, c, d))

@@ -252,3 +252,21 @@ def test_complex_restatements_agree(port, seed):
     r, P, S = O.zgemm_dense_truncation(alpha, AU, AV, BU, BV, beta, CU, CV, acc=1e-7)
     assert out["status"] == 0 and out["rank"] == r
     assert np.linalg.norm(out["CU"] @ out["CV"].T - P) <= 1e-12 * np.linalg.norm(P)
+
+
+def test_gemm_list_runs_the_same_calls(port):
+    """The CPU baseline's C loop (port_dgemm_list) over a small panel: every
+    update succeeds with the benchmark's limits, and every one is refused when
+    maxrk is below the rank sums (the reference's exit condition as a status),
+    so the loop really calls port_dgemm per update."""
+    from hcore_gb300 import panel as pnl
+
+    p = pnl.build_panel(n_points=4096, nb=256, device="cpu", workers=2)
+    sa = [p.index[(i, 0)] for i, j in p.updates]
+    sb = [p.index[(j, 0)] for i, j in p.updates]
+    sc = [p.index[(i, j)] for i, j in p.updates]
+    U, V = p.U.numpy(), p.V.numpy()
+    assert port.gemm_list(p.nb, U, V, p.offset, sa, sb, sc, alpha=-1.0, beta=1.0,
+                          maxrk=p.maxrank, acc=p.acc, variant=2) == 0
+    assert port.gemm_list(p.nb, U, V, p.offset, sa, sb, sc, alpha=-1.0, beta=1.0, maxrk=1,
+                          acc=p.acc, variant=2) == len(sa)
