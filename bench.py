@@ -590,7 +590,9 @@ def accuracy_all(panel, updates, ranks, out_U, out_V, out_off, acc=None, slack=1
     reference's own truncation error: ||P - D|| <= 1.01 ||P_oracle - D|| +
     slack ||D|| (`slack` 1e-14 for FP64 paths).  With FP32 arithmetic the
     rounding scales with the inputs, not with a result that cancels, so
-    `slack_of_inputs` takes slack (||C|| + ||A B^T||) instead."""
+    `slack_of_inputs` takes slack (||C|| + ||A B^T||) instead, plus FP32's
+    absolute floor nb * FLT_MIN (far-field tiles of the panel have norms near
+    1e-42, where FP32 values are subnormal)."""
     import multiprocessing as mp
 
     import numpy as np
@@ -625,11 +627,14 @@ def accuracy_all(panel, updates, ranks, out_U, out_V, out_off, acc=None, slack=1
     rk_ref = np.array([r[1] for r in rows])
     d_or, n_or, eg, er, nd, nin = (np.array([r[q] for r in rows]) for q in range(2, 8))
     rank_ok = int((rk_ref == np.asarray(ranks)).sum())
-    gate = eg <= 1.01 * er + slack * (nin if slack_of_inputs else nd)
+    # FP32 arithmetic also has an absolute floor: below its smallest normal
+    # number (1.2e-38) values are subnormal and lose relative precision
+    floor = np.finfo(np.float32).tiny * nb if slack_of_inputs else 0.0
+    gate = eg <= 1.01 * er + slack * (nin if slack_of_inputs else nd) + floor
     rel_or = d_or / np.maximum(n_or, 1e-300)
     return {"checked": n, "rank_equal_to_oracle": rank_ok, "within_oracle_error": int(gate.sum()),
             "gate": f"||P - D|| <= 1.01 ||P_oracle - D|| + {slack:g} "
-                    + ("(||C|| + ||A B^T||)" if slack_of_inputs else "||D||"),
+                    + ("(||C|| + ||A B^T||) + nb * FLT_MIN" if slack_of_inputs else "||D||"),
             "panel_rel_fro_err_vs_dense": float(np.sqrt((eg ** 2).sum() / (nd ** 2).sum())),
             "oracle_panel_rel_fro_err_vs_dense": float(np.sqrt((er ** 2).sum() / (nd ** 2).sum())),
             "max_tile_rel_fro_err_vs_dense": float((eg / nd).max()),
@@ -1297,6 +1302,9 @@ def run_predictor(args):
         warm execute, timed execute, rebuild of capacity overflows (timed)."""
         n = len(ups)
         make = maker(store, ups, k)
+        # memory torch no longer uses goes back to the driver before the
+        # plan allocates its own workspace (large sweeps of the full matrix)
+        torch.cuda.empty_cache()
         off = P.slot_offsets(caps, nb)
         oU = torch.empty(int(off[-1]) + 1, dtype=torch.float64, device=dev)
         oV = torch.empty_like(oU)
@@ -1963,10 +1971,11 @@ def run_zgemm(args):
     independent updates of the "nb=512, ranks 32" shape in complex
     arithmetic (seeded complex factors, sigma_i = 10^(-8i/32) folded into U,
     acc 1e-8, maxrk 64, alpha = beta = 1), host arrays in and out.  A step is
-    one hcore_gpu_zgemm_batched call over all of them: the host embeds each
-    as a real update of order 1024 (ranks 64), one real plan runs them all,
-    the host extracts the complex factors.  The single-call drop-in
-    (HCORE_zgemm) is timed beside it."""
+    one hcore_gpu_zgemm_batched call over all of them: each is embedded on
+    the GPU as a real update of order 1024 (ranks 64), one real plan runs
+    them all, and the complex factors are extracted on the GPU; only complex
+    factors cross the host link.  The single-call drop-in (HCORE_zgemm) is
+    timed beside it."""
     import numpy as np
     import torch
 
@@ -2050,8 +2059,8 @@ def run_zgemm(args):
             "e2e": {"value": n / (ms / 1e3), "unit": "updates/s",
                     "h2d_bytes_per_step": n * 6 * M * a * 16,
                     "d2h_bytes_per_step": int(2 * M * 16 * np.sum(ranks)),
-                    "how": "host complex arrays through hcore_gpu_zgemm_batched: host embedding, "
-                           "one real plan of order 1024 on the GPU, host extraction"},
+                    "how": "host complex arrays through hcore_gpu_zgemm_batched: embedding, "
+                           "one real plan of order 1024 and extraction on the GPU"},
             "single_call_ms": single_ms,
             "cpu_baseline": {"value": cpu1 * cores, "unit": "updates/s", "cores": cores,
                              "kind": "port", "sample": f"{nc} calls of the restated HCORE_zgemm "

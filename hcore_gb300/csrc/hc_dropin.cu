@@ -1184,20 +1184,6 @@ static std::vector<zc> zget(const hcore_dcomplex *p, int rows, int cols, int ld)
     return out;
 }
 
-// phi (conj_ = false) or psi (conj_ = true) of the M x n block X, scaled by s,
-// into E (2M x 2n, ld 2M)
-static void zembed(double *E, const std::vector<zc> &X, int M, int n, zc s, bool conj_) {
-    const size_t M2 = 2 * (size_t)M;
-    for (int j = 0; j < n; ++j)
-        for (int i = 0; i < M; ++i) {
-            zc x = s * X[(size_t)j * M + i];
-            if (conj_) x = std::conj(x);
-            E[(size_t)j * M2 + i] = x.real();
-            E[(size_t)j * M2 + M + i] = x.imag();
-            E[(size_t)(n + j) * M2 + i] = -x.imag();
-            E[(size_t)(n + j) * M2 + M + i] = x.real();
-        }
-}
 // Complex factors of C_new from the real plan's outputs eU, eV (2M x r2,
 // ld 2M): C_new = Z0 R^T, Z0 = eU_top + i eU_bottom, R = eV_top.  With
 // `mgs` false, one column per pair is taken directly (column 2j; its
@@ -1299,34 +1285,20 @@ extern "C" void HCORE_zgemm(HCORE_enum transA, int transB, int M, int N, hcore_d
     if (2 * M > kMaxRowsPerLane * 32 || 2 * (a + c) > kMaxK)
         fatal("%s: M=%d, a+c=%d exceed this library's complex limits (M <= %d, a+c <= %d)\n", fn,
               M, a + c, kMaxRowsPerLane * 16, kMaxK / 2);
-    const std::vector<zc> xAU = zget(AU, M, a, LDA), xAV = zget(AV, M, a, LDA);
-    const std::vector<zc> xBU = zget(BU, M, b, LDB), xBV = zget(BV, M, b, LDB);
-    const std::vector<zc> xCU = zget(CU, M, c, LDC), xCV = zget(CV, M, c, LDC);
-    const int M2 = 2 * M, k2 = 2 * (a + c);
-    const zc al(alpha.re, alpha.im), be(beta.re, beta.im);
-    std::vector<double> eAU((size_t)M2 * 2 * a), eAV(eAU.size()), eBU((size_t)M2 * 2 * b),
-        eBV(eBU.size()), eCU((size_t)M2 * k2), eCV(eCU.size());
-    zembed(eAU.data(), xAU, M, a, al, false);
-    zembed(eAV.data(), xAV, M, a, 1.0, true);
-    zembed(eBU.data(), xBU, M, b, 1.0, true);
-    zembed(eBV.data(), xBV, M, b, 1.0, false);
-    zembed(eCU.data(), xCU, M, c, be, false);
-    zembed(eCV.data(), xCV, M, c, 1.0, true);
-    double ea = 2 * a, eb = 2 * b, ec = 2 * c;
-    lr_update<double>(fn, M2, 1.0, eAU.data(), eAV.data(), &ea, M2, eBU.data(), eBV.data(), &eb,
-                      M2, 1.0, eCU.data(), eCV.data(), &ec, M2, 2 * rk, 2 * maxrk, acc, nullptr,
-                      false);
-    const int r2 = (int)ec;
-    std::vector<zc> oU, oV;
-    const int r = zextract(eCU.data(), eCV.data(), M, r2, true, oU, oV);
-    if (r > maxrk)  // hcore_zgemm.c's r > maxrk exit
+    // one task of the batched complex path: embedding, the real plan and the
+    // pair extraction on the GPU, CU/CV written in place
+    hcore_zlr_task t{};
+    t.M = M; t.a = a; t.b = b; t.c = c; t.rk = rk; t.maxrk = maxrk;
+    t.alpha = alpha; t.beta = beta; t.acc = acc;
+    t.AU = AU; t.AV = AV; t.lda = LDA; t.BU = BU; t.BV = BV; t.ldb = LDB;
+    t.CU = CU; t.CV = CV; t.ldc = LDC;
+    int r = 0, st = 0;
+    const int rc = hcore_gpu_zgemm_batched(1, &t, &r, &st, thread_ctx().stream);
+    if (st == HCORE_GPU_S_RANK_MAX)  // hcore_zgemm.c's r > maxrk exit
         fatal("%s: Rank after truncation is too big! finalrank:%d maxrank:%d\n", fn, r, maxrk);
-    if (r > 0 &&
-        (cudaMemcpy2D(CU, (size_t)LDC * sizeof(zc), oU.data(), M * sizeof(zc), M * sizeof(zc), r,
-                      cudaMemcpyDefault) != cudaSuccess ||
-         cudaMemcpy2D(CV, (size_t)LDC * sizeof(zc), oV.data(), M * sizeof(zc), M * sizeof(zc), r,
-                      cudaMemcpyDefault) != cudaSuccess))
-        cuda_fatal(fn);
+    if (rc == HCORE_GPU_ECUDA || rc == HCORE_GPU_ENOMEM) cuda_fatal(fn);
+    if (rc != HCORE_GPU_OK || st != HCORE_GPU_S_OK)
+        fatal("%s: recompression failed (status %d): %s\n", fn, st, last_error());
     Crk[0] = r;
     if (flops) flops->update += update_flops(M, a, b, c, r, false);  // hcore_zgemm.c: same model
 }
@@ -1409,8 +1381,86 @@ static void parallel_for(int n, F body) {
 
 // Batched complex updates: every task embedded as above, all of them run as
 // one real plan, the complex factors extracted per task (one column per pair
-// of equal singular values, Gram-Schmidt where pairs mix).  The host work
-// runs on up to 16 threads.
+// of equal singular values, Gram-Schmidt where pairs mix).  The embedding
+// and the pair extraction run on the GPU (zembed_kernel, zextract_kernel):
+// only the complex factors cross the host link, and host inputs in pageable
+// memory are packed on up to 16 threads into pinned memory that the kernel
+// reads in place.
+namespace hc {
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+// one complex factor block (M x n, ld in complex elements, device-accessible)
+// into its real embedding (2M x 2n, ld 2M), scaled by s, conjugated (psi) or
+// not (phi)
+struct ZEmbedBlock {
+    const double *src;
+    int ld;
+    double *dst;
+    int M, n;
+    double sre, sim;
+    int conj;
+};
+__global__ void __launch_bounds__(256) zembed_kernel(const ZEmbedBlock *__restrict__ blocks) {
+    const ZEmbedBlock b = blocks[blockIdx.x];
+    const size_t M = b.M, M2 = 2 * M, n = b.n;
+    for (size_t e = threadIdx.x; e < M * n; e += blockDim.x) {
+        const size_t i = e % M, j = e / M;
+        const double xr = b.src[2 * (j * b.ld + i)], xi = b.src[2 * (j * b.ld + i) + 1];
+        double re = b.sre * xr - b.sim * xi, im = b.sre * xi + b.sim * xr;
+        if (b.conj) im = -im;
+        b.dst[j * M2 + i] = re;
+        b.dst[j * M2 + M + i] = im;
+        b.dst[(n + j) * M2 + i] = -im;
+        b.dst[(n + j) * M2 + M + i] = re;
+    }
+}
+// the complex factors of one task from the real plan's outputs (eU, eV:
+// 2M x r2, ld 2M): column 2q of each pair (CU_q = top + i bottom of eU,
+// CV_q = top - i bottom of eV) into oU, oV (complex M x r, ld M); mixed = 1
+// when some pair's partner is not +-J times its first column (singular
+// values that are equal), which the host then resolves by Gram-Schmidt
+struct ZExtractTask {
+    const double *eU, *eV;
+    int M, r2;
+    double *oU, *oV;
+};
+__global__ void __launch_bounds__(256) zextract_kernel(const ZExtractTask *__restrict__ tasks,
+                                                       int *__restrict__ mixed) {
+    const ZExtractTask t = tasks[blockIdx.x];
+    const size_t M = t.M, M2 = 2 * M;
+    __shared__ double red[8];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int mix = 0;
+    for (int j = 0; j + 1 < t.r2; j += 2) {
+        const double *u = t.eU + j * M2, *w = t.eU + (j + 1) * M2;
+        double d = 0;
+        for (size_t i = tid; i < M; i += blockDim.x) d += w[i] * -u[M + i] + w[M + i] * u[i];
+        d = warp_sum_d(d);
+        if (lane == 0) red[warp] = d;
+        __syncthreads();
+        if (tid == 0) {
+            double s = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+            if (fabs(fabs(s) - 1.0) > 1e-6) mix = 1;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) mixed[blockIdx.x] = mix;
+    const int r = (t.r2 + 1) / 2;
+    for (size_t e = tid; e < M * (size_t)r; e += blockDim.x) {
+        const size_t i = e % M, q = e / M;
+        const double *u = t.eU + 2 * q * M2, *v = t.eV + 2 * q * M2;
+        t.oU[2 * (q * M + i)] = u[i];
+        t.oU[2 * (q * M + i) + 1] = u[M + i];
+        t.oV[2 * (q * M + i)] = v[i];
+        t.oV[2 * (q * M + i) + 1] = -v[M + i];
+    }
+}
+}  // namespace hc
+
 extern "C" int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *ranks,
                                        int *status, void *stream) {
     if (n < 0 || (n > 0 && (!tasks || !ranks || !status))) {
@@ -1420,8 +1470,8 @@ extern "C" int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *
     cudaStream_t s = (cudaStream_t)stream;
     // validation on the complex ranks (the reference's exit conditions)
     std::vector<int> run;
-    std::vector<size_t> off_in, off_out;
-    size_t n_in = 0, n_out = 0;
+    std::vector<size_t> off_in, off_out, off_z;
+    size_t n_in = 0, n_out = 0, n_z = 0;
     for (int q = 0; q < n; ++q) {
         const hcore_zlr_task &t = tasks[q];
         ranks[q] = 0;
@@ -1440,66 +1490,177 @@ extern "C" int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *
         n_in += M2 * 2 * (2 * (size_t)t.a + 2 * (size_t)t.b + 2 * (size_t)t.c);
         off_out.push_back(n_out);
         n_out += 2 * M2 * 2 * (size_t)(t.a + t.c);
+        off_z.push_back(n_z);
+        n_z += 2 * 2 * (size_t)t.M * (size_t)(t.a + t.c);   // complex CU, CV (a + c columns)
     }
     const int nr = (int)run.size();
     if (nr == 0) return n ? HCORE_GPU_ETASK : HCORE_GPU_OK;
-    std::vector<double> h(n_in);
-    std::vector<hcore_lr_task> rt(nr);
-    double *dbuf = nullptr;
-    if (cudaMalloc(&dbuf, (n_in + n_out) * sizeof(double)) != cudaSuccess) {
+
+    // complex inputs the kernel cannot read in place (pageable host memory)
+    // are packed into pinned staging; the rest are read where they are
+    struct Src {
+        const hcore_dcomplex *p;
+        int rows, cols, ld;
+    };
+    std::vector<Src> src;
+    std::vector<const double *> src_dev;   // device-accessible address per block
+    std::vector<size_t> pack_off;          // offset in the staging (doubles), or SIZE_MAX
+    size_t n_pack = 0;
+    for (int x = 0; x < nr; ++x) {
+        const hcore_zlr_task &t = tasks[run[x]];
+        const Src f[6] = {{t.AU, t.M, t.a, t.lda}, {t.AV, t.M, t.a, t.lda},
+                          {t.BU, t.M, t.b, t.ldb}, {t.BV, t.M, t.b, t.ldb},
+                          {t.CU, t.M, t.c, t.ldc}, {t.CV, t.M, t.c, t.ldc}};
+        for (const Src &b : f) {
+            src.push_back(b);
+            const void *alias = device_alias(b.p);
+            src_dev.push_back((const double *)alias);
+            if (alias) {
+                pack_off.push_back(SIZE_MAX);
+            } else {
+                pack_off.push_back(n_pack);
+                n_pack += 2 * (size_t)b.rows * b.cols;
+            }
+        }
+    }
+    ThreadCtx &tc = thread_ctx();
+    const size_t n_blocks = src.size();
+    const size_t stage_doubles = std::max(n_pack, n_z);
+    double *pin = (double *)tc.pin_ensure(std::max<size_t>(stage_doubles * sizeof(double), 1024));
+    const size_t b_in = al256(n_in * sizeof(double)), b_out = al256(n_out * sizeof(double));
+    const size_t b_z = al256(n_z * sizeof(double));
+    const size_t b_blk = al256(n_blocks * sizeof(ZEmbedBlock));
+    const size_t b_ex = al256((size_t)nr * sizeof(ZExtractTask)), b_mix = al256(nr * sizeof(int));
+    char *arena = nullptr;
+    if (!pin || cudaMalloc(&arena, b_in + b_out + b_z + b_blk + b_ex + b_mix) != cudaSuccess) {
         cudaGetLastError();
-        set_error("hcore_gpu_zgemm_batched: cudaMalloc of %zu bytes failed",
-                  (n_in + n_out) * sizeof(double));
+        set_error("hcore_gpu_zgemm_batched: allocation of %zu bytes failed",
+                  b_in + b_out + b_z + b_blk + b_ex + b_mix);
         return HCORE_GPU_ENOMEM;
     }
-    parallel_for(nr, [&](int x) {
+    double *din = (double *)arena, *dout = (double *)(arena + b_in);
+    double *dz = (double *)(arena + b_in + b_out);
+    ZEmbedBlock *dblk = (ZEmbedBlock *)(arena + b_in + b_out + b_z);
+    ZExtractTask *dex = (ZExtractTask *)(arena + b_in + b_out + b_z + b_blk);
+    int *dmix = (int *)(arena + b_in + b_out + b_z + b_blk + b_ex);
+    // the pinned staging may have been used by an earlier call's copies
+    cudaStreamSynchronize(tc.stream);
+    parallel_for((int)n_blocks, [&](int bi) {
+        if (pack_off[bi] == SIZE_MAX) return;
+        const Src &b = src[bi];
+        double *dst = pin + pack_off[bi];
+        for (int j = 0; j < b.cols; ++j)
+            std::memcpy(dst + 2 * (size_t)j * b.rows, b.p + (size_t)j * b.ld,
+                        2 * sizeof(double) * b.rows);
+    });
+    const double *pin_dev = (const double *)device_alias(pin);
+    std::vector<ZEmbedBlock> blk(n_blocks);
+    std::vector<hcore_lr_task> rt(nr);
+    for (int x = 0; x < nr; ++x) {
         const hcore_zlr_task &t = tasks[run[x]];
         const int M = t.M, a = t.a, b = t.b, c = t.c, M2 = 2 * M;
-        double *p = h.data() + off_in[x];
-        double *eAU = p, *eAV = eAU + (size_t)M2 * 2 * a, *eBU = eAV + (size_t)M2 * 2 * a,
+        double *e0 = din + off_in[x];
+        double *eAU = e0, *eAV = eAU + (size_t)M2 * 2 * a, *eBU = eAV + (size_t)M2 * 2 * a,
                *eBV = eBU + (size_t)M2 * 2 * b, *eCU = eBV + (size_t)M2 * 2 * b,
                *eCV = eCU + (size_t)M2 * 2 * c;
-        const zc al(t.alpha.re, t.alpha.im), be(t.beta.re, t.beta.im);
-        zembed(eAU, zget(t.AU, M, a, t.lda), M, a, al, false);
-        zembed(eAV, zget(t.AV, M, a, t.lda), M, a, 1.0, true);
-        zembed(eBU, zget(t.BU, M, b, t.ldb), M, b, 1.0, true);
-        zembed(eBV, zget(t.BV, M, b, t.ldb), M, b, 1.0, false);
-        zembed(eCU, zget(t.CU, M, c, t.ldc), M, c, be, false);
-        zembed(eCV, zget(t.CV, M, c, t.ldc), M, c, 1.0, true);
-        const double *d = dbuf + off_in[x];
-        double *o = dbuf + n_in + off_out[x];
+        double *dst[6] = {eAU, eAV, eBU, eBV, eCU, eCV};
+        const double sc[6][2] = {{t.alpha.re, t.alpha.im}, {1, 0}, {1, 0},
+                                 {1, 0}, {t.beta.re, t.beta.im}, {1, 0}};
+        const int cj[6] = {0, 1, 1, 0, 0, 1};   // phi(alpha AU) psi(AV), psi(BU) phi(BV), ...
+        for (int f = 0; f < 6; ++f) {
+            const size_t bi = (size_t)x * 6 + f;
+            const Src &sb = src[bi];
+            ZEmbedBlock &z = blk[bi];
+            if (pack_off[bi] == SIZE_MAX) {
+                z.src = src_dev[bi];
+                z.ld = sb.ld;
+            } else {
+                z.src = pin_dev + pack_off[bi];
+                z.ld = sb.rows;
+            }
+            z.dst = dst[f];
+            z.M = M;
+            z.n = sb.cols;
+            z.sre = sc[f][0];
+            z.sim = sc[f][1];
+            z.conj = cj[f];
+        }
+        double *o = dout + off_out[x];
         hcore_lr_task &u = rt[x];
         u = hcore_lr_task{};
         u.M = M2; u.a = 2 * a; u.b = 2 * b; u.c = 2 * c; u.rk = 2 * t.rk; u.maxrk = 2 * t.maxrk;
         u.ld_newv = 2 * t.maxrk; u.alpha = 1.0; u.beta = 1.0; u.acc = t.acc;
-        u.AU = d + (eAU - p); u.AV = d + (eAV - p); u.lda = M2;
-        u.BU = d + (eBU - p); u.BV = d + (eBV - p); u.ldb = M2;
-        u.CU = d + (eCU - p); u.CV = d + (eCV - p); u.ldc = M2;
+        u.AU = eAU; u.AV = eAV; u.lda = M2;
+        u.BU = eBU; u.BV = eBV; u.ldb = M2;
+        u.CU = eCU; u.CV = eCV; u.ldc = M2;
         u.CUo = o; u.CVo = o + (size_t)M2 * 2 * (a + c); u.ldco = M2;
-    });
+    }
     int rc = HCORE_GPU_OK;
     hcore_gpu_plan plan = nullptr;
-    std::vector<int> r2(nr), st2(nr);
-    if (cudaMemcpyAsync(dbuf, h.data(), n_in * sizeof(double), cudaMemcpyHostToDevice, s) !=
-        cudaSuccess) {
+    std::vector<int> r2(nr), st2(nr), mixed(nr, 0);
+    if (cudaMemcpyAsync(dblk, blk.data(), n_blocks * sizeof(ZEmbedBlock), cudaMemcpyHostToDevice,
+                        s) != cudaSuccess) {
         set_error("hcore_gpu_zgemm_batched: upload failed");
         rc = HCORE_GPU_ECUDA;
+    }
+    if (rc == HCORE_GPU_OK) {
+        zembed_kernel<<<(unsigned)n_blocks, 256, 0, s>>>(dblk);
+        if (cudaGetLastError() != cudaSuccess) {
+            set_error("hcore_gpu_zgemm_batched: embedding kernel failed to launch");
+            rc = HCORE_GPU_ECUDA;
+        }
     }
     if (rc == HCORE_GPU_OK) rc = hcore_gpu_plan_create(&plan, HCORE_GPU_F64, nr, rt.data(), 0);
     if (rc == HCORE_GPU_OK) rc = hcore_gpu_plan_execute(plan, stream);
     if (rc == HCORE_GPU_OK) rc = hcore_gpu_plan_results(plan, r2.data(), st2.data(), stream);
     if (plan) hcore_gpu_plan_destroy(plan);
-    std::vector<double> out;
     if (rc == HCORE_GPU_OK) {
-        out.resize(n_out);
-        if (cudaMemcpy(out.data(), dbuf + n_in, n_out * sizeof(double), cudaMemcpyDeviceToHost) !=
-            cudaSuccess) {
+        std::vector<ZExtractTask> ex(nr);
+        for (int x = 0; x < nr; ++x) {
+            const hcore_zlr_task &t = tasks[run[x]];
+            const int M2 = 2 * t.M;
+            const double *eU = dout + off_out[x];
+            ex[x] = ZExtractTask{eU, eU + (size_t)M2 * 2 * (t.a + t.c), t.M,
+                                 st2[x] == HCORE_GPU_S_OK ? r2[x] : 0, dz + off_z[x],
+                                 dz + off_z[x] + 2 * (size_t)t.M * (t.a + t.c)};
+        }
+        if (cudaMemcpyAsync(dex, ex.data(), nr * sizeof(ZExtractTask), cudaMemcpyHostToDevice,
+                            s) != cudaSuccess) {
+            rc = HCORE_GPU_ECUDA;
+        } else {
+            zextract_kernel<<<nr, 256, 0, s>>>(dex, dmix);
+            if (cudaGetLastError() != cudaSuccess) rc = HCORE_GPU_ECUDA;
+        }
+        // the complex factors and the mixed flags back to the host (pinned)
+        if (rc == HCORE_GPU_OK &&
+            (cudaMemcpyAsync(pin, dz, n_z * sizeof(double), cudaMemcpyDeviceToHost, s) !=
+                 cudaSuccess ||
+             cudaMemcpyAsync(mixed.data(), dmix, nr * sizeof(int), cudaMemcpyDeviceToHost, s) !=
+                 cudaSuccess ||
+             cudaStreamSynchronize(s) != cudaSuccess))
+            rc = HCORE_GPU_ECUDA;
+        if (rc == HCORE_GPU_ECUDA) set_error("hcore_gpu_zgemm_batched: extraction failed");
+    }
+    // tasks whose pairs mixed: their real factors to the host for Gram-Schmidt
+    std::vector<int> need;
+    for (int x = 0; x < nr && rc == HCORE_GPU_OK; ++x)
+        if (st2[x] == HCORE_GPU_S_OK && mixed[x]) need.push_back(x);
+    std::vector<std::vector<double>> eh(need.size());
+    for (size_t m = 0; m < need.size() && rc == HCORE_GPU_OK; ++m) {
+        const int x = need[m];
+        const hcore_zlr_task &t = tasks[run[x]];
+        const size_t cnt = 2 * (2 * (size_t)t.M) * 2 * (t.a + t.c);
+        eh[m].resize(cnt);
+        if (cudaMemcpy(eh[m].data(), dout + off_out[x], cnt * sizeof(double),
+                       cudaMemcpyDeviceToHost) != cudaSuccess) {
             set_error("hcore_gpu_zgemm_batched: download failed");
             rc = HCORE_GPU_ECUDA;
         }
     }
-    cudaFree(dbuf);
+    cudaFree(arena);
     if (rc) return rc;
+    std::vector<int> slot(nr, -1);
+    for (size_t m = 0; m < need.size(); ++m) slot[need[m]] = (int)m;
     std::vector<int> copy_failed(nr, 0);
     parallel_for(nr, [&](int x) {
         const hcore_zlr_task &t = tasks[run[x]];
@@ -1507,20 +1668,37 @@ extern "C" int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *
         status[q] = st2[x];
         if (st2[x]) return;
         const int M = t.M, M2 = 2 * M;
-        const double *eU = out.data() + off_out[x];
-        const double *eV = eU + (size_t)M2 * 2 * (t.a + t.c);
         std::vector<zc> oU, oV;
-        const int r = zextract(eU, eV, M, r2[x], false, oU, oV);
+        const zc *pU, *pV;
+        int r;
+        if (slot[x] >= 0) {
+            const double *eU = eh[slot[x]].data();
+            r = zextract(eU, eU + (size_t)M2 * 2 * (t.a + t.c), M, r2[x], true, oU, oV);
+            pU = oU.data();
+            pV = oV.data();
+        } else {
+            r = (r2[x] + 1) / 2;
+            pU = (const zc *)(pin + off_z[x]);
+            pV = pU + (size_t)M * (t.a + t.c);
+        }
         if (r > t.maxrk) {
             status[q] = HCORE_GPU_S_RANK_MAX;
             return;
         }
-        if (r > 0 &&
-            (cudaMemcpy2D(t.CU, (size_t)t.ldc * sizeof(zc), oU.data(), M * sizeof(zc),
-                          M * sizeof(zc), r, cudaMemcpyDefault) != cudaSuccess ||
-             cudaMemcpy2D(t.CV, (size_t)t.ldc * sizeof(zc), oV.data(), M * sizeof(zc),
-                          M * sizeof(zc), r, cudaMemcpyDefault) != cudaSuccess))
-            copy_failed[x] = 1;
+        if (r > 0) {
+            if (is_device_memory(t.CU) || is_device_memory(t.CV)) {
+                if (cudaMemcpy2D(t.CU, (size_t)t.ldc * sizeof(zc), pU, M * sizeof(zc),
+                                 M * sizeof(zc), r, cudaMemcpyDefault) != cudaSuccess ||
+                    cudaMemcpy2D(t.CV, (size_t)t.ldc * sizeof(zc), pV, M * sizeof(zc),
+                                 M * sizeof(zc), r, cudaMemcpyDefault) != cudaSuccess)
+                    copy_failed[x] = 1;
+            } else {
+                for (int j = 0; j < r; ++j) {
+                    std::memcpy(t.CU + (size_t)j * t.ldc, pU + (size_t)j * M, M * sizeof(zc));
+                    std::memcpy(t.CV + (size_t)j * t.ldc, pV + (size_t)j * M, M * sizeof(zc));
+                }
+            }
+        }
         ranks[q] = r;
     });
     for (int x = 0; x < nr; ++x)

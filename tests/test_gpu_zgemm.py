@@ -167,3 +167,56 @@ def test_zgemm_batched_against_port(hc, port):
             continue
         assert st == 0 and r == ref["rank"], (q, st, r, ref["rank"])
         assert _rel(oU[:, :r] @ oV[:, :r].T, ref["CU"] @ ref["CV"].T) < 1e-11, q
+
+
+def test_zgemm_batched_device_and_pinned_memory(hc):
+    """The batched complex path reads its inputs where they are (device or
+    pinned host memory, through the embedding kernel) and packs pageable ones;
+    outputs go back to device or host memory.  The same tasks with their
+    factors in pageable host, pinned host and device memory give identical
+    ranks and bits."""
+    import torch
+
+    rng = np.random.default_rng(93)
+    M, maxrk, n = 192, 48, 6
+    cases = []
+    for q in range(n):
+        a, b, c = (int(x) for x in rng.integers(2, 14, 3))
+        cases.append((a, b, c) + _clr(rng, M, a, 8) + _clr(rng, M, b, 8) + _clr(rng, M, c, 8))
+
+    def run(where):
+        keep, tasks = [], []
+        for (a, b, c, AU, AV, BU, BV, CU, CV) in cases:
+            oU = np.zeros((M, maxrk), dtype=np.complex128, order="F")
+            oV = np.zeros_like(oU)
+            oU[:, :c], oV[:, :c] = CU, CV
+            arrs = [AU, AV, BU, BV, oU, oV]
+            if where == "device":
+                arrs = [torch.from_numpy(np.ascontiguousarray(x.T)).cuda() for x in arrs]
+                ptr = [x.data_ptr() for x in arrs]
+            elif where == "pinned":
+                arrs = [torch.from_numpy(np.ascontiguousarray(x.T)).pin_memory() for x in arrs]
+                ptr = [x.data_ptr() for x in arrs]
+            else:
+                ptr = [x.ctypes.data for x in arrs]
+            keep.append(arrs)
+            tasks.append(hc.ZlrTask(M=M, a=a, b=b, c=c, rk=0, maxrk=maxrk,
+                                    alpha=hc.DComplex(-1, 0), beta=hc.DComplex(1, 0), acc=1e-8,
+                                    AU=ptr[0], AV=ptr[1], lda=M, BU=ptr[2], BV=ptr[3], ldb=M,
+                                    CU=ptr[4], CV=ptr[5], ldc=M))
+        ranks, status = hc.zgemm_batched(tasks)
+        outs = []
+        for arrs, r in zip(keep, ranks):
+            oU, oV = arrs[4], arrs[5]
+            if where in ("device", "pinned"):
+                oU, oV = oU.cpu().numpy().T, oV.cpu().numpy().T
+            outs.append((oU[:, :r].copy(), oV[:, :r].copy()))
+        return ranks.copy(), status.copy(), outs
+
+    r0, s0, o0 = run("pageable")
+    assert (s0 == 0).all()
+    for where in ("pinned", "device"):
+        r1, s1, o1 = run(where)
+        assert np.array_equal(r0, r1) and np.array_equal(s0, s1), where
+        for (u0, v0), (u1, v1) in zip(o0, o1):
+            assert np.array_equal(u0, u1) and np.array_equal(v0, v1), where
