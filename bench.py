@@ -730,9 +730,27 @@ def config1_call(hc, reps=40, warmup=5):
                 acc_ms[nm].append(evs[q].elapsed_time(evs[q + 1]))
     one.close()
     phases = {nm: round(statistics.median(v), 4) for nm, v in acc_ms.items()}
+    # the SVD phase of this one update against the lanes per column pair
+    svd_by_lanes = {}
+    for g in (2, 4, 8, 16):
+        one = hc.Batch([task], tuning=hc.make_tuning(stream_groups=1, svd_lanes=[g, g, g],
+                                                     qr_warps=8))
+        ts = []
+        for it in range(6):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            one.execute_phases(3, st.cuda_stream)
+            e0.record(st)
+            one.execute_phases(4, st.cuda_stream)
+            e1.record(st)
+            torch.cuda.synchronize()
+            if it >= 2:
+                ts.append(e0.elapsed_time(e1))
+        one.close()
+        svd_by_lanes[g] = round(statistics.median(ts), 4)
     return {"ms_per_call": med, "ms_min": min(times), "calls_per_s": 1e3 / med, "calls": reps,
             "rank": r, "oracle_rank": int(ref["rank"]), "rel_fro_diff_vs_oracle": diff,
             "phases_ms": phases,
+            "svd_ms_by_lanes_per_pair": svd_by_lanes,
             "phases_how": "the same update as a one-task plan (device pointers, the drop-in's "
                           "launch shape), phases timed back to back with CUDA events",
             "cpu_1core_ms_per_call": statistics.median(ptimes),

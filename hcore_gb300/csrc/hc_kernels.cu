@@ -321,13 +321,15 @@ __global__ void __launch_bounds__(NW * 32, (RPL <= 32 ? 2 : 1) * (8 / NW))
                 x[t] = i < M ? Ac[i] : T(0);
             }
             if (tj != T(0)) {
-                T d0 = 0, d1 = 0;
+                T d0 = 0, d1 = 0, d2 = 0, d3 = 0;   // four chains (RPL is a multiple of 4)
 #pragma unroll
-                for (int t = 0; t < RPL; t += 2) {
+                for (int t = 0; t < RPL; t += 4) {
                     d0 += v[lane + 32 * t] * x[t];
-                    if (t + 1 < RPL) d1 += v[lane + 32 * (t + 1)] * x[t + 1];
+                    d1 += v[lane + 32 * (t + 1)] * x[t + 1];
+                    d2 += v[lane + 32 * (t + 2)] * x[t + 2];
+                    d3 += v[lane + 32 * (t + 3)] * x[t + 3];
                 }
-                const T sc = tj * warp_sum(d0 + d1);
+                const T sc = tj * warp_sum((d0 + d1) + (d2 + d3));
                 // re-read v from shared memory instead of holding RPL values in registers
                 const volatile T *vv = v;
 #pragma unroll
@@ -656,8 +658,20 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                 const bool valid = pi < np && p < k && q < k;
                 T *xp = B + ixB(0, p), *xq = B + ixB(0, q);
                 T dot = 0;
-                if (valid)
-                    for (int i = lig; i < k; i += G) dot += xp[i * rsB] * xq[i * rsB];
+                if (valid) {
+                    // four partial sums: the chain of dependent FMAs is a quarter
+                    // as long (one update's Jacobi round is latency-bound)
+                    T d1 = 0, d2 = 0, d3 = 0;
+                    int i = lig;
+                    for (; i + 3 * G < k; i += 4 * G) {
+                        dot += xp[i * rsB] * xq[i * rsB];
+                        d1 += xp[(i + G) * rsB] * xq[(i + G) * rsB];
+                        d2 += xp[(i + 2 * G) * rsB] * xq[(i + 2 * G) * rsB];
+                        d3 += xp[(i + 3 * G) * rsB] * xq[(i + 3 * G) * rsB];
+                    }
+                    for (; i < k; i += G) dot += xp[i * rsB] * xq[i * rsB];
+                    dot = (dot + d1) + (d2 + d3);
+                }
                 for (int o = G / 2; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
                 T dp = 1, dq = 1, app = 0, aqq = 0, apq = 0;
                 if (valid) {
@@ -689,7 +703,29 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                     const T inv = T(1) / (dp * dq);
                     const T f1 = t * (dq * dq) * inv, f2 = t * (dp * dp) * inv;
                     T *vp = A + ixA(0, p), *vq = A + ixA(0, q);
-                    for (int i = lig; i < k; i += G) {
+                    // two rows per iteration, all loads before the stores: the rows
+                    // are distinct, so the loads of the second row need not wait
+                    // for the stores of the first
+                    // (shared-memory modes only: the workspace mode has no registers
+                    // to spare at 1024 threads)
+                    int i = lig;
+                    if (MODE != 0)
+                    for (; i + G < k; i += 2 * G) {
+                        const size_t r0 = (size_t)i, r1 = (size_t)(i + G);
+                        const T a0 = xp[r0 * rsB], b0 = xq[r0 * rsB];
+                        const T a1 = xp[r1 * rsB], b1 = xq[r1 * rsB];
+                        const T u0 = vp[r0 * rsA], v0 = vq[r0 * rsA];
+                        const T u1 = vp[r1 * rsA], v1 = vq[r1 * rsA];
+                        xp[r0 * rsB] = a0 - f1 * b0;
+                        xq[r0 * rsB] = b0 + f2 * a0;
+                        xp[r1 * rsB] = a1 - f1 * b1;
+                        xq[r1 * rsB] = b1 + f2 * a1;
+                        vp[r0 * rsA] = u0 - f1 * v0;
+                        vq[r0 * rsA] = v0 + f2 * u0;
+                        vp[r1 * rsA] = u1 - f1 * v1;
+                        vq[r1 * rsA] = v1 + f2 * u1;
+                    }
+                    for (; i < k; i += G) {
                         const T a = xp[i * rsB], b = xq[i * rsB];
                         xp[i * rsB] = a - f1 * b;
                         xq[i * rsB] = b + f2 * a;
@@ -740,9 +776,14 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                 dj = T(1);
                 s_d[j] = dj;
             }
-            T s2 = 0;
-            for (int i = 0; i < k; ++i) s2 += xj[i * rsB] * xj[i * rsB];
-            s_nrm[j] = dj * dj * s2;
+            T s2 = 0, s3 = 0;
+            int i = 0;
+            for (; i + 1 < k; i += 2) {
+                s2 += xj[i * rsB] * xj[i * rsB];
+                s3 += xj[(i + 1) * rsB] * xj[(i + 1) * rsB];
+            }
+            if (i < k) s2 += xj[i * rsB] * xj[i * rsB];
+            s_nrm[j] = dj * dj * (s2 + s3);
         }
         ++sweeps;
         const bool big = __any_sync(0xffffffffu, sweep_big);
@@ -908,13 +949,15 @@ __global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) apply_kernel(cons
             const Tc tj = s_tau[c];
             if (tj == Tc(0)) continue;
             const Tc *v = sv + c * ROWS;
-            Tc d0 = 0, d1 = 0;
+            Tc d0 = 0, d1 = 0, d2 = 0, d3 = 0;   // four chains (RPL is a multiple of 4)
 #pragma unroll
-            for (int t = 0; t < RPL; t += 2) {
+            for (int t = 0; t < RPL; t += 4) {
                 d0 += v[lane + 32 * t] * x[t];
-                if (t + 1 < RPL) d1 += v[lane + 32 * (t + 1)] * x[t + 1];
+                d1 += v[lane + 32 * (t + 1)] * x[t + 1];
+                d2 += v[lane + 32 * (t + 2)] * x[t + 2];
+                d3 += v[lane + 32 * (t + 3)] * x[t + 3];
             }
-            const Tc s = tj * warp_sum(d0 + d1);
+            const Tc s = tj * warp_sum((d0 + d1) + (d2 + d3));
             const volatile Tc *vv = v;  // re-read rather than hold RPL values in registers
 #pragma unroll
             for (int t = 0; t < RPL; ++t) x[t] -= s * vv[lane + 32 * t];
