@@ -589,9 +589,14 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
             T *ac = A + ixA(0, c);
             const T *aj = A + ixA(0, j);
             if (tj != T(0)) {
-                T dot = ac[j * rsA];
-                for (int i = j + 1; i < k; ++i) dot += aj[i * rsA] * ac[i * rsA];
-                const T s = tj * dot;
+                T dot = ac[j * rsA], dot2 = 0;
+                int i = j + 1;
+                for (; i + 1 < k; i += 2) {
+                    dot += aj[i * rsA] * ac[i * rsA];
+                    dot2 += aj[(i + 1) * rsA] * ac[(i + 1) * rsA];
+                }
+                if (i < k) dot += aj[i * rsA] * ac[i * rsA];
+                const T s = tj * (dot + dot2);
                 ac[j * rsA] -= s;
                 for (int i = j + 1; i < k; ++i) ac[i * rsA] -= s * aj[i * rsA];
             }
