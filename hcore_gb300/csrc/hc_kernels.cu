@@ -321,15 +321,15 @@ __global__ void __launch_bounds__(NW * 32, (RPL <= 32 ? 2 : 1) * (8 / NW))
                 x[t] = i < M ? Ac[i] : T(0);
             }
             if (tj != T(0)) {
-                T d0 = 0, d1 = 0, d2 = 0, d3 = 0;   // four chains (RPL is a multiple of 4)
+                // two chains: four measured slower here (register pressure at
+                // four CTAs per SM; other CTAs already hide the chain's latency)
+                T d0 = 0, d1 = 0;
 #pragma unroll
-                for (int t = 0; t < RPL; t += 4) {
+                for (int t = 0; t < RPL; t += 2) {
                     d0 += v[lane + 32 * t] * x[t];
-                    d1 += v[lane + 32 * (t + 1)] * x[t + 1];
-                    d2 += v[lane + 32 * (t + 2)] * x[t + 2];
-                    d3 += v[lane + 32 * (t + 3)] * x[t + 3];
+                    if (t + 1 < RPL) d1 += v[lane + 32 * (t + 1)] * x[t + 1];
                 }
-                const T sc = tj * warp_sum((d0 + d1) + (d2 + d3));
+                const T sc = tj * warp_sum(d0 + d1);
                 // re-read v from shared memory instead of holding RPL values in registers
                 const volatile T *vv = v;
 #pragma unroll
@@ -954,15 +954,13 @@ __global__ void __launch_bounds__(kThreads, RPL <= 32 ? 2 : 1) apply_kernel(cons
             const Tc tj = s_tau[c];
             if (tj == Tc(0)) continue;
             const Tc *v = sv + c * ROWS;
-            Tc d0 = 0, d1 = 0, d2 = 0, d3 = 0;   // four chains (RPL is a multiple of 4)
+            Tc d0 = 0, d1 = 0;
 #pragma unroll
-            for (int t = 0; t < RPL; t += 4) {
+            for (int t = 0; t < RPL; t += 2) {
                 d0 += v[lane + 32 * t] * x[t];
-                d1 += v[lane + 32 * (t + 1)] * x[t + 1];
-                d2 += v[lane + 32 * (t + 2)] * x[t + 2];
-                d3 += v[lane + 32 * (t + 3)] * x[t + 3];
+                if (t + 1 < RPL) d1 += v[lane + 32 * (t + 1)] * x[t + 1];
             }
-            const Tc s = tj * warp_sum((d0 + d1) + (d2 + d3));
+            const Tc s = tj * warp_sum(d0 + d1);
             const volatile Tc *vv = v;  // re-read rather than hold RPL values in registers
 #pragma unroll
             for (int t = 0; t < RPL; ++t) x[t] -= s * vv[lane + 32 * t];
