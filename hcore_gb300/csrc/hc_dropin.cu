@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "hc_host.h"
+#include "hc_zinternal.h"
 #include "hcore_d.h"
 #include "hcore_s.h"
 #include "hcore_z.h"
@@ -1461,6 +1462,145 @@ __global__ void __launch_bounds__(256) zextract_kernel(const ZExtractTask *__res
 }
 }  // namespace hc
 
+// Native complex path (hc_zkernels.cu): the tasks in `run` (validated) with
+// M <= 1024 and a + c within the complex SVD's shared-memory limit.  Inputs
+// are read where they are (device or pinned memory) or packed into pinned
+// staging (pageable memory); the new factors are written to a device buffer
+// and copied to the tasks' CU/CV.
+static int zgemm_batched_native(const hcore_zlr_task *tasks, const std::vector<int> &run,
+                                int *ranks, int *status, cudaStream_t s) {
+    const int nr = (int)run.size();
+    struct Src {
+        const hcore_dcomplex *p;
+        int rows, cols, ld;
+    };
+    std::vector<Src> src;
+    std::vector<const zd *> where;     // device-accessible address, or null: packed
+    std::vector<size_t> pack_off;
+    std::vector<long long> ws_off(nr);
+    std::vector<size_t> out_off(nr);
+    size_t n_pack = 0, n_out = 0;
+    long long n_ws = 0;
+    int maxM = 1, maxK = 1;
+    for (int x = 0; x < nr; ++x) {
+        const hcore_zlr_task &t = tasks[run[x]];
+        const Src f[6] = {{t.AU, t.M, t.a, t.lda}, {t.AV, t.M, t.a, t.lda},
+                          {t.BU, t.M, t.b, t.ldb}, {t.BV, t.M, t.b, t.ldb},
+                          {t.CU, t.M, t.c, t.ldc}, {t.CV, t.M, t.c, t.ldc}};
+        for (const Src &b : f) {
+            src.push_back(b);
+            const zd *alias = (const zd *)device_alias(b.p);
+            where.push_back(alias);
+            pack_off.push_back(alias ? SIZE_MAX : n_pack);
+            if (!alias) n_pack += (size_t)b.rows * b.cols;
+        }
+        const int k = t.a + t.c;
+        ws_off[x] = n_ws;
+        n_ws += zlayout(t.M, t.a, t.b, k).total;
+        out_off[x] = n_out;
+        n_out += 2 * (size_t)t.M * k;
+        maxM = std::max(maxM, t.M);
+        maxK = std::max(maxK, k);
+    }
+    ThreadCtx &tc = thread_ctx();
+    const size_t stage = std::max(n_pack, n_out) * sizeof(zd);
+    zd *pin = (zd *)tc.pin_ensure(std::max<size_t>(stage, 1024));
+    const size_t b_ws = al256((size_t)n_ws * sizeof(zd)), b_out = al256(n_out * sizeof(zd));
+    const size_t b_desc = al256((size_t)nr * sizeof(ZDesc)), b_rs = al256(2 * (size_t)nr * sizeof(int));
+    char *arena = nullptr;
+    if (!pin || cudaMalloc(&arena, b_ws + b_out + b_desc + b_rs) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("hcore_gpu_zgemm_batched: allocation of %zu bytes failed",
+                  b_ws + b_out + b_desc + b_rs);
+        return HCORE_GPU_ENOMEM;
+    }
+    zd *dws = (zd *)arena, *dout = (zd *)(arena + b_ws);
+    ZDesc *ddesc = (ZDesc *)(arena + b_ws + b_out);
+    int *drank = (int *)(arena + b_ws + b_out + b_desc), *dstat = drank + nr;
+    cudaStreamSynchronize(tc.stream);   // the staging may still feed an earlier copy
+    parallel_for((int)src.size(), [&](int bi) {
+        if (pack_off[bi] == SIZE_MAX) return;
+        const Src &b = src[bi];
+        zd *dst = pin + pack_off[bi];
+        for (int j = 0; j < b.cols; ++j)
+            std::memcpy(dst + (size_t)j * b.rows, b.p + (size_t)j * b.ld, sizeof(zd) * b.rows);
+    });
+    const zd *pin_dev = (const zd *)device_alias(pin);
+    std::vector<ZDesc> desc(nr);
+    for (int x = 0; x < nr; ++x) {
+        const hcore_zlr_task &t = tasks[run[x]];
+        const zd *pt[6];
+        int ldv[6];
+        for (int f = 0; f < 6; ++f) {
+            const size_t bi = (size_t)x * 6 + f;
+            pt[f] = pack_off[bi] == SIZE_MAX ? where[bi] : pin_dev + pack_off[bi];
+            ldv[f] = pack_off[bi] == SIZE_MAX ? src[bi].ld : src[bi].rows;
+        }
+        ZDesc &d = desc[x];
+        d = ZDesc{};
+        d.AU = pt[0]; d.AV = pt[1]; d.BU = pt[2]; d.BV = pt[3]; d.CU = pt[4]; d.CV = pt[5];
+        d.ldau = ldv[0]; d.ldav = ldv[1]; d.ldbu = ldv[2];
+        d.ldbv = ldv[3]; d.ldcu = ldv[4]; d.ldcv = ldv[5];
+        const int k = t.a + t.c;
+        d.CUo = dout + out_off[x];
+        d.CVo = d.CUo + (size_t)t.M * k;
+        d.ldco = t.M;
+        d.ws = ws_off[x];
+        d.alpha = zd{t.alpha.re, t.alpha.im};
+        d.beta = zd{t.beta.re, t.beta.im};
+        d.acc = t.acc;
+        d.M = t.M; d.a = t.a; d.b = t.b; d.c = t.c; d.k = k;
+        d.rk = t.rk;
+        d.max_rank = t.maxrk;
+        d.idx = x;
+        d.status0 = 0;
+    }
+    int rc = HCORE_GPU_OK;
+    std::vector<int> rs(2 * nr);
+    if (cudaMemcpyAsync(ddesc, desc.data(), nr * sizeof(ZDesc), cudaMemcpyHostToDevice, s) !=
+            cudaSuccess ||
+        launch_zrecompress(ddesc, nr, dws, drank, dstat, maxM, maxK, s) != cudaSuccess ||
+        cudaMemcpyAsync(rs.data(), drank, 2 * nr * sizeof(int), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(pin, dout, n_out * sizeof(zd), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        set_error("hcore_gpu_zgemm_batched: %s", cudaGetErrorString(cudaGetLastError()));
+        rc = HCORE_GPU_ECUDA;
+    }
+    cudaFree(arena);
+    if (rc) return rc;
+    std::vector<int> copy_failed(nr, 0);
+    parallel_for(nr, [&](int x) {
+        const hcore_zlr_task &t = tasks[run[x]];
+        const int q = run[x], r = rs[x], st = rs[nr + x];
+        status[q] = st;
+        if (st) return;
+        const int M = t.M, k = t.a + t.c;
+        const zd *pU = pin + out_off[x], *pV = pU + (size_t)M * k;
+        if (r > 0) {
+            if (is_device_memory(t.CU) || is_device_memory(t.CV)) {
+                if (cudaMemcpy2D(t.CU, (size_t)t.ldc * sizeof(zd), pU, M * sizeof(zd),
+                                 M * sizeof(zd), r, cudaMemcpyDefault) != cudaSuccess ||
+                    cudaMemcpy2D(t.CV, (size_t)t.ldc * sizeof(zd), pV, M * sizeof(zd),
+                                 M * sizeof(zd), r, cudaMemcpyDefault) != cudaSuccess)
+                    copy_failed[x] = 1;
+            } else {
+                for (int j = 0; j < r; ++j) {
+                    std::memcpy(t.CU + (size_t)j * t.ldc, pU + (size_t)j * M, M * sizeof(zd));
+                    std::memcpy(t.CV + (size_t)j * t.ldc, pV + (size_t)j * M, M * sizeof(zd));
+                }
+            }
+        }
+        ranks[q] = r;
+    });
+    for (int x = 0; x < nr; ++x)
+        if (copy_failed[x]) {
+            set_error("hcore_gpu_zgemm_batched: output copy failed");
+            return HCORE_GPU_ECUDA;
+        }
+    return HCORE_GPU_OK;
+}
+
 extern "C" int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *ranks,
                                        int *status, void *stream) {
     if (n < 0 || (n > 0 && (!tasks || !ranks || !status))) {
@@ -1495,6 +1635,24 @@ extern "C" int hcore_gpu_zgemm_batched(int n, const hcore_zlr_task *tasks, int *
     }
     const int nr = (int)run.size();
     if (nr == 0) return n ? HCORE_GPU_ETASK : HCORE_GPU_OK;
+
+    // native complex kernels where every task fits them (M <= 1024, both
+    // Jacobi matrices in shared memory); the real embedding otherwise
+    {
+        const int zk = zsvd_kmax();
+        bool native = zk > 0 && !getenv("HCORE_GPU_ZGEMM_EMBED");
+        for (int x = 0; x < nr && native; ++x) {
+            const hcore_zlr_task &t = tasks[run[x]];
+            native = t.M <= 1024 && t.a + t.c <= zk;
+        }
+        if (native) {
+            const int rcn = zgemm_batched_native(tasks, run, ranks, status, s);
+            if (rcn) return rcn;
+            bool any = false;
+            for (int q = 0; q < n && !any; ++q) any = status[q] != 0;
+            return any ? HCORE_GPU_ETASK : HCORE_GPU_OK;
+        }
+    }
 
     // complex inputs the kernel cannot read in place (pageable host memory)
     // are packed into pinned staging; the rest are read where they are

@@ -220,3 +220,52 @@ def test_zgemm_batched_device_and_pinned_memory(hc):
         assert np.array_equal(r0, r1) and np.array_equal(s0, s1), where
         for (u0, v0), (u1, v1) in zip(o0, o1):
             assert np.array_equal(u0, u1) and np.array_equal(v0, v1), where
+
+
+def test_zgemm_native_kernels_match_the_embedding(hc, port):
+    """The native complex kernels (rank sums up to the shared-memory limit)
+    and the order-2M real embedding (HCORE_GPU_ZGEMM_EMBED=1 forces it) give
+    the same ranks and products (1e-11), both equal to the restated
+    reference's; the native factors are orthonormal in CU."""
+    import os
+
+    rng = np.random.default_rng(94)
+    M, maxrk = 320, 80
+    cases = []
+    for q in range(12):
+        a, b, c = (int(x) for x in rng.integers(1, 40, 3))
+        cases.append((a, b, c, complex(rng.standard_normal(), rng.standard_normal()))
+                     + _clr(rng, M, a, 8) + _clr(rng, M, b, 8) + _clr(rng, M, c, 8))
+
+    def run():
+        keep, tasks = [], []
+        for (a, b, c, al, AU, AV, BU, BV, CU, CV) in cases:
+            oU = np.zeros((M, maxrk), dtype=np.complex128, order="F")
+            oV = np.zeros_like(oU)
+            oU[:, :c], oV[:, :c] = CU, CV
+            keep.append((oU, oV))
+            tasks.append(hc.ZlrTask(M=M, a=a, b=b, c=c, rk=0, maxrk=maxrk,
+                                    alpha=hc.DComplex(al.real, al.imag), beta=hc.DComplex(1, 0),
+                                    acc=1e-8, AU=AU.ctypes.data, AV=AV.ctypes.data, lda=M,
+                                    BU=BU.ctypes.data, BV=BV.ctypes.data, ldb=M, CU=oU.ctypes.data,
+                                    CV=oV.ctypes.data, ldc=M))
+        ranks, status = hc.zgemm_batched(tasks)
+        return ranks.copy(), status.copy(), [(u[:, :r].copy(), v[:, :r].copy())
+                                             for (u, v), r in zip(keep, ranks)]
+
+    rn, sn, on = run()
+    os.environ["HCORE_GPU_ZGEMM_EMBED"] = "1"
+    try:
+        re_, se, oe = run()
+    finally:
+        del os.environ["HCORE_GPU_ZGEMM_EMBED"]
+    assert (sn == 0).all() and (se == 0).all()
+    assert np.array_equal(rn, re_)
+    for q, ((a, b, c, al, AU, AV, BU, BV, CU, CV), (un, vn), (ue, ve)) in enumerate(zip(cases, on, oe)):
+        ref = port.zgemm(M, al, AU, AV, a, BU, BV, b, 1.0, CU, CV, c, maxrk=maxrk, acc=1e-8)
+        assert rn[q] == ref["rank"], q
+        Pr = ref["CU"] @ ref["CV"].T
+        assert _rel(un @ vn.T, Pr) < 1e-11, q
+        assert _rel(ue @ ve.T, Pr) < 1e-11, q
+        r = int(rn[q])
+        assert np.abs(un.conj().T @ un - np.eye(r)).max() < 1e-12, q
