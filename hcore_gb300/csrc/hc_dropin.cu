@@ -1464,9 +1464,12 @@ __global__ void __launch_bounds__(256) zextract_kernel(const ZExtractTask *__res
 
 // Native complex path (hc_zkernels.cu): the tasks in `run` (validated) with
 // M <= 1024 and a + c within the complex SVD's shared-memory limit.  Inputs
-// are read where they are (device or pinned memory) or packed into pinned
-// staging (pageable memory); the new factors are written to a device buffer
-// and copied to the tasks' CU/CV.
+// in device memory are read in place; host inputs (pageable or pinned) are
+// packed on the host into pinned staging and copied to the device in one
+// transfer, because the stack kernel reads every factor column many times
+// (F = AV^T BV, G = BU F^T), which over the host link would cost each read
+// again.  The new factors are written to a device buffer and copied to the
+// tasks' CU/CV.
 static int zgemm_batched_native(const hcore_zlr_task *tasks, const std::vector<int> &run,
                                 int *ranks, int *status, cudaStream_t s) {
     const int nr = (int)run.size();
@@ -1489,10 +1492,10 @@ static int zgemm_batched_native(const hcore_zlr_task *tasks, const std::vector<i
                           {t.CU, t.M, t.c, t.ldc}, {t.CV, t.M, t.c, t.ldc}};
         for (const Src &b : f) {
             src.push_back(b);
-            const zd *alias = (const zd *)device_alias(b.p);
-            where.push_back(alias);
-            pack_off.push_back(alias ? SIZE_MAX : n_pack);
-            if (!alias) n_pack += (size_t)b.rows * b.cols;
+            const bool dev = is_device_memory(b.p);
+            where.push_back(dev ? (const zd *)b.p : nullptr);
+            pack_off.push_back(dev ? SIZE_MAX : n_pack);
+            if (!dev) n_pack += (size_t)b.rows * b.cols;
         }
         const int k = t.a + t.c;
         ws_off[x] = n_ws;
@@ -1506,17 +1509,18 @@ static int zgemm_batched_native(const hcore_zlr_task *tasks, const std::vector<i
     const size_t stage = std::max(n_pack, n_out) * sizeof(zd);
     zd *pin = (zd *)tc.pin_ensure(std::max<size_t>(stage, 1024));
     const size_t b_ws = al256((size_t)n_ws * sizeof(zd)), b_out = al256(n_out * sizeof(zd));
+    const size_t b_in = al256(n_pack * sizeof(zd));
     const size_t b_desc = al256((size_t)nr * sizeof(ZDesc)), b_rs = al256(2 * (size_t)nr * sizeof(int));
     char *arena = nullptr;
-    if (!pin || cudaMalloc(&arena, b_ws + b_out + b_desc + b_rs) != cudaSuccess) {
+    if (!pin || cudaMalloc(&arena, b_ws + b_out + b_in + b_desc + b_rs) != cudaSuccess) {
         cudaGetLastError();
         set_error("hcore_gpu_zgemm_batched: allocation of %zu bytes failed",
-                  b_ws + b_out + b_desc + b_rs);
+                  b_ws + b_out + b_in + b_desc + b_rs);
         return HCORE_GPU_ENOMEM;
     }
-    zd *dws = (zd *)arena, *dout = (zd *)(arena + b_ws);
-    ZDesc *ddesc = (ZDesc *)(arena + b_ws + b_out);
-    int *drank = (int *)(arena + b_ws + b_out + b_desc), *dstat = drank + nr;
+    zd *dws = (zd *)arena, *dout = (zd *)(arena + b_ws), *din = (zd *)(arena + b_ws + b_out);
+    ZDesc *ddesc = (ZDesc *)(arena + b_ws + b_out + b_in);
+    int *drank = (int *)(arena + b_ws + b_out + b_in + b_desc), *dstat = drank + nr;
     cudaStreamSynchronize(tc.stream);   // the staging may still feed an earlier copy
     parallel_for((int)src.size(), [&](int bi) {
         if (pack_off[bi] == SIZE_MAX) return;
@@ -1525,7 +1529,6 @@ static int zgemm_batched_native(const hcore_zlr_task *tasks, const std::vector<i
         for (int j = 0; j < b.cols; ++j)
             std::memcpy(dst + (size_t)j * b.rows, b.p + (size_t)j * b.ld, sizeof(zd) * b.rows);
     });
-    const zd *pin_dev = (const zd *)device_alias(pin);
     std::vector<ZDesc> desc(nr);
     for (int x = 0; x < nr; ++x) {
         const hcore_zlr_task &t = tasks[run[x]];
@@ -1533,7 +1536,7 @@ static int zgemm_batched_native(const hcore_zlr_task *tasks, const std::vector<i
         int ldv[6];
         for (int f = 0; f < 6; ++f) {
             const size_t bi = (size_t)x * 6 + f;
-            pt[f] = pack_off[bi] == SIZE_MAX ? where[bi] : pin_dev + pack_off[bi];
+            pt[f] = pack_off[bi] == SIZE_MAX ? where[bi] : din + pack_off[bi];
             ldv[f] = pack_off[bi] == SIZE_MAX ? src[bi].ld : src[bi].rows;
         }
         ZDesc &d = desc[x];
@@ -1557,7 +1560,10 @@ static int zgemm_batched_native(const hcore_zlr_task *tasks, const std::vector<i
     }
     int rc = HCORE_GPU_OK;
     std::vector<int> rs(2 * nr);
-    if (cudaMemcpyAsync(ddesc, desc.data(), nr * sizeof(ZDesc), cudaMemcpyHostToDevice, s) !=
+    if ((n_pack > 0 &&
+         cudaMemcpyAsync(din, pin, n_pack * sizeof(zd), cudaMemcpyHostToDevice, s) !=
+             cudaSuccess) ||
+        cudaMemcpyAsync(ddesc, desc.data(), nr * sizeof(ZDesc), cudaMemcpyHostToDevice, s) !=
             cudaSuccess ||
         launch_zrecompress(ddesc, nr, dws, drank, dstat, maxM, maxK, s) != cudaSuccess ||
         cudaMemcpyAsync(rs.data(), drank, 2 * nr * sizeof(int), cudaMemcpyDeviceToHost, s) !=

@@ -31,9 +31,10 @@ struct ZDesc {
 
 // Workspace of one update (complex elements, each region rounded up to 16):
 //   UA M*k | VB M*k | tauA k | tauB k | sig k | F a*b | Y k*k (the SVD's QR
-//   reflectors) | Uo k*k (U_r) | Vo k*k (conj(W_r S_r))
+//   reflectors) | Uo k*k (U_r) | Vo k*k (conj(W_r S_r)) | W k*k (the SVD's
+//   V_J when it does not stay in shared memory)
 struct ZLayout {
-    long long UA, VB, tauA, tauB, sig, F, Y, Uo, Vo, total;
+    long long UA, VB, tauA, tauB, sig, F, Y, Uo, Vo, W, total;
 };
 __host__ __device__ inline long long zalign16(long long x) { return (x + 15) & ~15LL; }
 __host__ __device__ inline ZLayout zlayout(int M, int a, int b, int k) {
@@ -48,6 +49,7 @@ __host__ __device__ inline ZLayout zlayout(int M, int a, int b, int k) {
     L.Y = o; o = zalign16(o + (long long)k * k);
     L.Uo = o; o = zalign16(o + (long long)k * k);
     L.Vo = o; o = zalign16(o + (long long)k * k);
+    L.W = o; o = zalign16(o + (long long)k * k);
     L.total = o;
     return L;
 }
@@ -58,6 +60,10 @@ __host__ __device__ inline int zsvd_ld(int K) { return K | 1; }
 __host__ __device__ inline size_t zsvd_smem_bytes(int K) {
     return (size_t)2 * K * zsvd_ld(K) * sizeof(zd) + (size_t)2 * (K + 1) * sizeof(zd) +
            (size_t)2 * (K + 1) * sizeof(double) + (size_t)2 * (K + 1) * sizeof(int) + 64;
+}
+// the same with V_J in the workspace: one matrix in shared memory
+__host__ __device__ inline size_t zsvd_smem_bytes_half(int K) {
+    return zsvd_smem_bytes(K) - (size_t)K * zsvd_ld(K) * sizeof(zd);
 }
 constexpr int kZApplyChunk = 4;   // reflectors staged per pass of the complex rebuild
 

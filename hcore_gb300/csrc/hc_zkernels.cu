@@ -49,6 +49,10 @@ __device__ __forceinline__ zd zfma(zd a, zd b, zd acc) {
 __device__ __forceinline__ zd zcfma(zd a, zd b, zd acc) {
     return zd{fma(a.re, b.re, fma(a.im, b.im, acc.re)), fma(a.re, b.im, fma(-a.im, b.re, acc.im))};
 }
+// acc - a * b (four FMAs)
+__device__ __forceinline__ zd zfms(zd a, zd b, zd acc) {
+    return zd{fma(-a.re, b.re, fma(a.im, b.im, acc.re)), fma(-a.re, b.im, fma(-a.im, b.re, acc.im))};
+}
 // 1 / a
 __device__ __forceinline__ zd zinv(zd a) {
     const double d = 1.0 / zabs2(a);
@@ -175,7 +179,7 @@ __global__ void __launch_bounds__(256) zgeqrf_kernel(const ZDesc *__restrict__ d
                 zd s = zmk(0, 0);
                 for (int i = j + lane; i < M; i += 32) s = zcfma(sv[i], y[i], s);
                 s = zmul(tc, zwarp_sum(s));
-                for (int i = j + lane; i < M; i += 32) y[i] = zsub(y[i], zmul(s, sv[i]));
+                for (int i = j + lane; i < M; i += 32) y[i] = zfms(s, sv[i], y[i]);
             }
         __syncthreads();
     }
@@ -197,7 +201,10 @@ __device__ __forceinline__ void zrr_pair(int round, int pi, int n, int &p, int &
 // Shared memory: A (V_J, then the QRCP's working matrix) and B (R^H), each
 // K x ld column-major (ld = K | 1), then per-column complex scales d,
 // squared norms, complex QRCP taus, and two index arrays.
-__global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ descs,
+// (one CTA per SM at k near 64: its shared memory is the limit, so the
+// registers need not be)
+template <bool AGLOBAL>
+__global__ void __launch_bounds__(256, 1) zgesvd_kernel(const ZDesc *__restrict__ descs,
                                                      zd *__restrict__ ws, int *__restrict__ rank,
                                                      int *__restrict__ status, int maxK, int G) {
     extern __shared__ unsigned char zsm[];
@@ -217,8 +224,11 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
     zd *base = ws + d.ws;
     const zd *UA = base + L.UA, *VB = base + L.VB;
     const int ld = zsvd_ld(maxK);
-    zd *A = reinterpret_cast<zd *>(zsm);
-    zd *B = A + (size_t)maxK * ld;
+    // AGLOBAL: A (the QRCP's matrix, then V_J) in the workspace, only B in
+    // shared memory, so that three CTAs fit an SM at k near 64
+    zd *B = reinterpret_cast<zd *>(zsm) + (AGLOBAL ? 0 : (size_t)maxK * ld);
+    zd *A = AGLOBAL ? base + L.W : reinterpret_cast<zd *>(zsm);
+    const int ldA = AGLOBAL ? k : ld;
     zd *s_d = B + (size_t)maxK * ld;
     zd *s_tau = s_d + (maxK + 1);
     double *s_nrm = reinterpret_cast<double *>(s_tau + (maxK + 1));
@@ -227,6 +237,7 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
     int *s_pcol = s_perm + (maxK + 1);
     zd *Yg = base + L.Y;   // the QRCP's reflectors (k x k, ld k)
     auto ix = [ld](int i, int j) { return (size_t)j * ld + i; };
+    auto ixA = [ldA](int i, int j) { return (size_t)j * ldA + i; };
 
     // T = triu(R_A) triu(R_B)^T
     double amax = 0;
@@ -235,7 +246,7 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
         zd s = zmk(0, 0);
         for (int l = max(i, j); l < k; ++l)
             s = zfma(UA[(size_t)l * M + i], VB[(size_t)l * M + j], s);
-        A[ix(i, j)] = s;
+        A[ixA(i, j)] = s;
         amax = max(amax, max(fabs(s.re), fabs(s.im)));
     }
     for (int o = 16; o > 0; o >>= 1) amax = max(amax, __shfl_xor_sync(0xffffffffu, amax, o));
@@ -252,15 +263,15 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
     if (sexp != 0)
         for (int e = tid; e < k * k; e += nthr) {
             const int i = e % k, j = e / k;
-            const zd v = A[ix(i, j)];
-            A[ix(i, j)] = zmk(dmul_exp2(v.re, -sexp), dmul_exp2(v.im, -sexp));
+            const zd v = A[ixA(i, j)];
+            A[ixA(i, j)] = zmk(dmul_exp2(v.re, -sexp), dmul_exp2(v.im, -sexp));
         }
     __syncthreads();
 
     // QR with column pivoting, T P = Q R (lane per trailing column)
     for (int c = tid; c < k; c += nthr) {
         double s = 0;
-        for (int i = 0; i < k; ++i) s += zabs2(A[ix(i, c)]);
+        for (int i = 0; i < k; ++i) s += zabs2(A[ixA(i, c)]);
         s_nrm[c] = s;
         s_dn[c] = s;
         s_pcol[c] = c;
@@ -289,9 +300,9 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
         const int pv = s_piv;
         if (pv != j) {
             for (int i = tid; i < k; i += nthr) {
-                const zd x = A[ix(i, j)];
-                A[ix(i, j)] = A[ix(i, pv)];
-                A[ix(i, pv)] = x;
+                const zd x = A[ixA(i, j)];
+                A[ixA(i, j)] = A[ixA(i, pv)];
+                A[ixA(i, pv)] = x;
             }
             if (tid == 0) {
                 double x = s_nrm[j]; s_nrm[j] = s_nrm[pv]; s_nrm[pv] = x;
@@ -302,15 +313,15 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
         __syncthreads();
         if (tid < 32) {   // reflector of column j, rows j..k-1
             double ss = 0;
-            for (int i = j + 1 + lane; i < k; i += 32) ss += zabs2(A[ix(i, j)]);
+            for (int i = j + 1 + lane; i < k; i += 32) ss += zabs2(A[ixA(i, j)]);
             ss = zwarp_sum(ss);
             double beta;
             zd tj, scal;
-            zlarfg(A[ix(j, j)], ss, beta, tj, scal);
-            for (int i = j + 1 + lane; i < k; i += 32) A[ix(i, j)] = zmul(A[ix(i, j)], scal);
+            zlarfg(A[ixA(j, j)], ss, beta, tj, scal);
+            for (int i = j + 1 + lane; i < k; i += 32) A[ixA(i, j)] = zmul(A[ixA(i, j)], scal);
             __syncwarp();
             if (lane == 0) {
-                A[ix(j, j)] = zmk(beta, 0);
+                A[ixA(j, j)] = zmk(beta, 0);
                 s_tau[j] = tj;
             }
         }
@@ -319,16 +330,16 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
         const zd tc = zconj(s_tau[j]);
         for (int c = j + 1 + tid; c < k; c += nthr) {
             if (tc.re != 0.0 || tc.im != 0.0) {
-                zd dot = A[ix(j, c)];
-                for (int i = j + 1; i < k; ++i) dot = zcfma(A[ix(i, j)], A[ix(i, c)], dot);
+                zd dot = A[ixA(j, c)];
+                for (int i = j + 1; i < k; ++i) dot = zcfma(A[ixA(i, j)], A[ixA(i, c)], dot);
                 const zd s = zmul(tc, dot);
-                A[ix(j, c)] = zsub(A[ix(j, c)], s);
-                for (int i = j + 1; i < k; ++i) A[ix(i, c)] = zsub(A[ix(i, c)], zmul(s, A[ix(i, j)]));
+                A[ixA(j, c)] = zsub(A[ixA(j, c)], s);
+                for (int i = j + 1; i < k; ++i) A[ixA(i, c)] = zfms(s, A[ixA(i, j)], A[ixA(i, c)]);
             }
-            double nn = s_nrm[c] - zabs2(A[ix(j, c)]);
+            double nn = s_nrm[c] - zabs2(A[ixA(j, c)]);
             if (nn <= s_dn[c] * (1.0 / 1024) || nn <= 0.0) {
                 double s = 0;
-                for (int i = j + 1; i < k; ++i) s += zabs2(A[ix(i, c)]);
+                for (int i = j + 1; i < k; ++i) s += zabs2(A[ixA(i, c)]);
                 nn = s;
                 s_dn[c] = s;
             }
@@ -339,14 +350,14 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
     // reflectors to the workspace; B = R^H; A = I
     for (int e = tid; e < k * k; e += nthr) {
         const int i = e % k, j = e / k;
-        const zd x = A[ix(i, j)];
+        const zd x = A[ixA(i, j)];
         Yg[(size_t)j * k + i] = i > j ? x : zmk(0, 0);
         B[ix(j, i)] = i <= j ? zconj(x) : zmk(0, 0);   // B(j, i) = conj(R(i, j))
     }
     __syncthreads();
     for (int e = tid; e < k * k; e += nthr) {
         const int i = e % k, j = e / k;
-        A[ix(i, j)] = zmk(i == j ? 1.0 : 0.0, 0);
+        A[ixA(i, j)] = zmk(i == j ? 1.0 : 0.0, 0);
     }
     for (int c = tid; c < k; c += nthr) {
         double s = 0;
@@ -413,13 +424,13 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
                     cs = rsqrt(fma(t, t, 1.0));
                     const zd f1 = zscal(t / zabs2(dp), zmul(zconj(ph), zmul(dq, zconj(dp))));
                     const zd f2 = zscal(t / zabs2(dq), zmul(ph, zmul(dp, zconj(dq))));
-                    zd *vp = A + ix(0, p), *vq = A + ix(0, q);
+                    zd *vp = A + ixA(0, p), *vq = A + ixA(0, q);
                     for (int i = lig; i < k; i += G) {
                         const zd a = xp[i], b = xq[i];
-                        xp[i] = zsub(a, zmul(f1, b));
+                        xp[i] = zfms(f1, b, a);
                         xq[i] = zfma(f2, a, b);
                         const zd u = vp[i], vv = vq[i];
-                        vp[i] = zsub(u, zmul(f1, vv));
+                        vp[i] = zfms(f1, vv, u);
                         vq[i] = zfma(f2, u, vv);
                     }
                 }
@@ -456,7 +467,7 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
             zd *xj = B + ix(0, j);
             zd dj = s_d[j];
             if (zabs2(dj) < 1e-120) {
-                zd *vj = A + ix(0, j);
+                zd *vj = A + ixA(0, j);
                 for (int i = 0; i < k; ++i) {
                     xj[i] = zmul(dj, xj[i]);
                     vj[i] = zmul(dj, vj[i]);
@@ -520,7 +531,7 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
         // column, reflectors from last to first, H_h x = x - tau_h v_h (v_h^H x)
         for (int t = tid; t < r; t += nthr) {
             const int j = s_perm[t];
-            zd *x = A + ix(0, j);
+            zd *x = A + ixA(0, j);
             const zd dj = s_d[j];
             for (int i = 0; i < k; ++i) x[i] = zmul(dj, x[i]);
             for (int h = k - 1; h >= 0; --h) {
@@ -531,7 +542,7 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
                 for (int i = h + 1; i < k; ++i) dot = zcfma(y[i], x[i], dot);
                 const zd s = zmul(th, dot);
                 x[h] = zsub(x[h], s);
-                for (int i = h + 1; i < k; ++i) x[i] = zsub(x[i], zmul(s, y[i]));
+                for (int i = h + 1; i < k; ++i) x[i] = zfms(s, y[i], x[i]);
             }
         }
         __syncthreads();
@@ -542,7 +553,7 @@ __global__ void __launch_bounds__(256) zgesvd_kernel(const ZDesc *__restrict__ d
             const int j = s_perm[t];
             const zd w = zmul(s_d[j], B[ix(i, j)]);
             Vo[(size_t)t * k + s_pcol[i]] = zmk(dmul_exp2(w.re, sexp), -dmul_exp2(w.im, sexp));
-            Uo[(size_t)t * k + i] = A[ix(i, j)];
+            Uo[(size_t)t * k + i] = A[ixA(i, j)];
         }
     }
     if (tid == 0) {
@@ -608,7 +619,7 @@ __global__ void __launch_bounds__(256, 1) zapply_kernel(const ZDesc *__restrict_
             for (int t = 0; t < RPL; ++t) s = zcfma(v[lane + 32 * t], x[t], s);
             s = zmul(tj, zwarp_sum(s));
 #pragma unroll
-            for (int t = 0; t < RPL; ++t) x[t] = zsub(x[t], zmul(s, v[lane + 32 * t]));
+            for (int t = 0; t < RPL; ++t) x[t] = zfms(s, v[lane + 32 * t], x[t]);
         }
     }
     if (active) {
@@ -654,11 +665,27 @@ cudaError_t launch_zrecompress(const ZDesc *d_desc, int n, zd *ws, int *d_rank, 
     int G = 1;
     while (G < 4 && 2 * G * np <= 256) G *= 2;
     const int nt = ((np * G + 31) / 32) * 32;
-    const size_t ssm = zsvd_smem_bytes(maxK);
-    cudaError_t e = cudaFuncSetAttribute(zgesvd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)ssm);
-    if (e != cudaSuccess) return e;
-    zgesvd_kernel<<<n, nt < 32 ? 32 : nt, ssm, s>>>(d_desc, ws, d_rank, d_status, maxK, G);
+    // both Jacobi matrices in shared memory, unless that leaves one CTA per
+    // SM while the batch has more updates than SMs: then V_J moves to the
+    // workspace and three CTAs share an SM
+    int dev = 0, sms = 1, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const bool aglobal = n > sms && 2 * zsvd_smem_bytes(maxK) > (size_t)optin;
+    const size_t ssm = aglobal ? zsvd_smem_bytes_half(maxK) : zsvd_smem_bytes(maxK);
+    cudaError_t e;
+    if (aglobal) {
+        e = cudaFuncSetAttribute(zgesvd_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)ssm);
+        if (e != cudaSuccess) return e;
+        zgesvd_kernel<true><<<n, nt < 32 ? 32 : nt, ssm, s>>>(d_desc, ws, d_rank, d_status, maxK, G);
+    } else {
+        e = cudaFuncSetAttribute(zgesvd_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)ssm);
+        if (e != cudaSuccess) return e;
+        zgesvd_kernel<false><<<n, nt < 32 ? 32 : nt, ssm, s>>>(d_desc, ws, d_rank, d_status, maxK, G);
+    }
     if (rpl <= 4) launch_zapply<4>(d_desc, n, ws, d_rank, d_status, maxK, s);
     else if (rpl <= 8) launch_zapply<8>(d_desc, n, ws, d_rank, d_status, maxK, s);
     else if (rpl <= 16) launch_zapply<16>(d_desc, n, ws, d_rank, d_status, maxK, s);
