@@ -38,10 +38,14 @@ void HCORE_zuncompress(HCORE_enum transA, HCORE_enum transB, int M, int N, hcore
                        int LDB, hcore_dcomplex beta, hcore_dcomplex *CD, int LDC);
 
 /* Batched complex updates on the GPU (the same semantics per task, statuses
- * HCORE_GPU_S_* instead of exit): all tasks run as one real plan.  CU/CV are
- * updated in place (room for max(c, new rank) columns); pointers may be host
- * or device memory.  Synchronous.  Returns HCORE_GPU_OK, HCORE_GPU_ETASK (a
- * task's status is set) or a negative error. */
+ * HCORE_GPU_S_* instead of exit; no counterpart in the reference).  Batches
+ * whose tasks all have M <= 1024 and a + c within the complex SVD's
+ * shared-memory limit (84 on GB300) run on the native complex kernels; other
+ * batches, or any batch with HCORE_GPU_ZGEMM_EMBED=1 in the environment, run
+ * as one real plan of order 2M.  CU/CV are updated in place (room for
+ * max(c, new rank) columns); pointers may be host or device memory.
+ * Synchronous.  Returns HCORE_GPU_OK, HCORE_GPU_ETASK (a task's status is
+ * set) or a negative error. */
 typedef struct hcore_zlr_task {
     int M, a, b, c;
     int rk, maxrk;
