@@ -71,6 +71,9 @@ def parse():
                    help="panel workload: skip the single drop-in call (profiling runs)")
     p.add_argument("--no-autotune", action="store_true",
                    help="panel workload: use the built-in launch shapes instead of autotuning")
+    p.add_argument("--dfma-rebuild", action="store_true",
+                   help="panel workload: the FP64 reflector kernel for every rebuild instead of "
+                        "the tensor-core rebuild (A/B runs)")
     p.add_argument("--per-tile-sample", type=int, default=48)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--probe-seconds", type=float, default=2.0,
@@ -278,12 +281,13 @@ def run_gb300(args):
     # the plan's launch shapes, picked by the library's autotuner on this batch
     # (set-up, outside the timed region)
     t0 = time.time()
+    flags = hc.DFMA_REBUILD if args.dfma_rebuild else 0
     if args.no_autotune:   # the library's built-in launch shapes (profiling runs)
         tuning, tuned_ms = hc.make_tuning(), None
     else:
-        tuning, tuned_ms = hc.autotune(tasks, reps=3, stream=stream.cuda_stream)
+        tuning, tuned_ms = hc.autotune(tasks, flags=flags, reps=3, stream=stream.cuda_stream)
     tune_s = time.time() - t0
-    batch = hc.Batch(tasks, tuning=tuning)
+    batch = hc.Batch(tasks, flags=flags, tuning=tuning)
     batch.execute(stream.cuda_stream)
     ranks, status = batch.results(stream.cuda_stream)
     if (status != 0).any():

@@ -98,6 +98,9 @@ struct LaunchShape {
     int bucket_width = 8;
     int qr_warps = 4;   // warps per QR CTA (2, 4 or 8)
     bool mixed = false;  // FP32 factor products and rebuild (HCORE_GPU_MIXED_FACTORS)
+    // FP64 plans: the rebuild of updates with k <= kTcMaxK on the tensor cores
+    // (hc_rebuild_tc.cu); off: the DFMA reflector kernel for every update
+    bool tc_rebuild = true;
     int nbuckets = 0;
     Bucket buckets[kMaxBuckets];
     // optional fork/join resources so the bucket launches overlap: one stream
@@ -123,7 +126,17 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
 template <typename T>
 cudaError_t launch_rebuild(const Desc *d_desc, const int *d_idx, const int *d_cap, int n, T *ws,
                            int *d_rank, int *d_status, int maxM, int maxK, bool mixed,
-                           cudaStream_t s);
+                           bool tc_rebuild, cudaStream_t s);
+
+// tensor-core rebuild (hc_rebuild_tc.cu): FP64-accurate Q.U products for
+// updates with k <= kTcMaxK.  tc_rebuild_class(k) is the kernel variant
+// (padded k: 16, 32, 48 or 64; 0 above kTcMaxK); configure_rebuild_tc sets
+// the variants' shared-memory attributes (not capturable).
+constexpr int kTcMaxK = 64;
+int tc_rebuild_class(int k);
+cudaError_t configure_rebuild_tc();
+void launch_rebuild_tc(const Desc *d_desc, int n, const double *ws, const int *d_rank,
+                       int *d_status, int kclass, cudaStream_t s);
 
 // dense-C updates (hc_dense.cu): per-task rank-K' form coef * P Q^T
 struct DenseWork {

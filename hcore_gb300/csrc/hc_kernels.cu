@@ -1060,6 +1060,7 @@ static cudaError_t configure_recompress_once(int dev, int *svd_smem_kmax, int *s
     if (svd_half_kmax) *svd_half_kmax = khalf;
     e = set_apply_smem<T, T>();
     if (e == cudaSuccess) e = set_apply_smem<T, float>();
+    if (e == cudaSuccess && sizeof(T) == sizeof(double)) e = configure_rebuild_tc();
     if (e != cudaSuccess) return e;
     // the attribute is per kernel, not per plan: allow the largest size any
     // plan may launch with, so plans of different k coexist
@@ -1139,8 +1140,30 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
     }
     if (phases & kPhaseApply) {
         const int ncols = shape.maxR > 0 ? std::min(shape.maxR, shape.maxK) : shape.maxK;
-        if (mixed) launch_apply_all<T, float>(d_desc, n, ws, d_rank, d_status, ncols, rpl, s);
-        else launch_apply_all<T, T>(d_desc, n, ws, d_rank, d_status, ncols, rpl, s);
+        if (mixed) {
+            launch_apply_all<T, float>(d_desc, n, ws, d_rank, d_status, ncols, rpl, s);
+        } else if (sizeof(T) == sizeof(double) && shape.tc_rebuild && shape.nbuckets > 0) {
+            // descriptors are sorted by decreasing k: the buckets above
+            // kTcMaxK take the DFMA kernel, the rest one tensor-core launch
+            // per padded-k class
+            int b = 0;
+            while (b < shape.nbuckets) {
+                const int cls = tc_rebuild_class(shape.buckets[b].K);
+                const int start = shape.buckets[b].start;
+                int count = 0;
+                while (b < shape.nbuckets && tc_rebuild_class(shape.buckets[b].K) == cls)
+                    count += shape.buckets[b++].count;
+                if (count <= 0) continue;
+                if (cls == 0)
+                    launch_apply_all<T, T>(d_desc + start, count, ws, d_rank, d_status, ncols,
+                                           rpl, s);
+                else
+                    launch_rebuild_tc(d_desc + start, count, (const double *)ws, d_rank,
+                                      d_status, cls, s);
+            }
+        } else {
+            launch_apply_all<T, T>(d_desc, n, ws, d_rank, d_status, ncols, rpl, s);
+        }
     }
     return cudaGetLastError();
 }
@@ -1161,21 +1184,24 @@ __global__ void storage_to_ok_kernel(const int *__restrict__ idx, const int *__r
 template <typename T>
 cudaError_t launch_rebuild(const Desc *d_desc, const int *d_idx, const int *d_cap, int n, T *ws,
                            int *d_rank, int *d_status, int maxM, int maxK, bool mixed,
-                           cudaStream_t s) {
+                           bool tc_rebuild, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     if (maxK > kMaxK || maxM > 32 * kMaxRowsPerLane) return cudaErrorInvalidValue;
     storage_to_ok_kernel<<<(n + 255) / 256, 256, 0, s>>>(d_idx, d_cap, n, d_status, d_rank);
     const int rpl = (maxM + 31) / 32;
     if (mixed && sizeof(T) == sizeof(double))
         launch_apply_all<T, float>(d_desc, n, ws, d_rank, d_status, maxK, rpl, s);
+    else if (sizeof(T) == sizeof(double) && tc_rebuild && tc_rebuild_class(maxK) > 0)
+        launch_rebuild_tc(d_desc, n, (const double *)ws, d_rank, d_status,
+                          tc_rebuild_class(maxK), s);
     else
         launch_apply_all<T, T>(d_desc, n, ws, d_rank, d_status, maxK, rpl, s);
     return cudaGetLastError();
 }
 template cudaError_t launch_rebuild<double>(const Desc *, const int *, const int *, int, double *,
-                                            int *, int *, int, int, bool, cudaStream_t);
+                                            int *, int *, int, int, bool, bool, cudaStream_t);
 template cudaError_t launch_rebuild<float>(const Desc *, const int *, const int *, int, float *,
-                                           int *, int *, int, int, bool, cudaStream_t);
+                                           int *, int *, int, int, bool, bool, cudaStream_t);
 
 template cudaError_t configure_recompress<double>(int, int *, int *);
 template cudaError_t configure_recompress<float>(int, int *, int *);

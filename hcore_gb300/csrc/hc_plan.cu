@@ -597,8 +597,13 @@ extern "C" int hcore_gpu_plan_create_tuned(hcore_gpu_plan *plan, int precision, 
             g.shape.svd_half_kmax = p->shape.svd_half_kmax;
         }
         const bool mixed = (flags & HCORE_GPU_MIXED_FACTORS) && precision == HCORE_GPU_F64;
+        const bool tcr = !(flags & HCORE_GPU_DFMA_REBUILD);
         p->shape.mixed = mixed;
-        for (auto &g : p->groups) g.shape.mixed = mixed;
+        p->shape.tc_rebuild = tcr;
+        for (auto &g : p->groups) {
+            g.shape.mixed = mixed;
+            g.shape.tc_rebuild = tcr;
+        }
         if (ce != cudaSuccess) {
             set_error("hcore_gpu_plan_create: %s", cudaGetErrorString(ce));
             plan_free(p);
@@ -772,11 +777,12 @@ extern "C" int hcore_gpu_plan_rebuild(hcore_gpu_plan p, int n, const int *task_i
     if (e == cudaSuccess) {
         const bool mixed = p->shape.mixed;
         const int *cap = max_rank ? p->d_ridx + n : nullptr;
+        const bool tcr = p->shape.tc_rebuild;
         e = p->prec == HCORE_GPU_F64
                 ? launch_rebuild<double>(p->d_rdesc, p->d_ridx, cap, n, (double *)p->d_ws,
-                                         p->d_rank, p->d_status, maxM, maxK, mixed, s)
+                                         p->d_rank, p->d_status, maxM, maxK, mixed, tcr, s)
                 : launch_rebuild<float>(p->d_rdesc, p->d_ridx, cap, n, (float *)p->d_ws,
-                                        p->d_rank, p->d_status, maxM, maxK, mixed, s);
+                                        p->d_rank, p->d_status, maxM, maxK, mixed, tcr, s);
     }
     if (e != cudaSuccess) {
         set_error("hcore_gpu_plan_rebuild: %s", cudaGetErrorString(e));

@@ -1,0 +1,508 @@
+// hcore-gb300: the rebuild phase (CU = Q_A [U_r; 0], CV = Q_B [V_r S_r; 0])
+// on the tensor cores, FP64-accurate.
+//
+// Reference step: src/compute/hcore_dgemm.c:508-696 (__newu / __newv: dormqr
+// 'L','N' of the k Householder reflectors from dgeqrf onto the k x r core
+// factor).  The DFMA kernel (apply_kernel in hc_kernels.cu) applies the
+// reflectors one by one, 2 M k r FP64 FMAs per side.  Here the same product is
+// formed through the compact WY representation Q = I - Y T Y^T (Schreiber and
+// Van Loan 1989) as
+//
+//     Q X = X - Y Z,   z_j = tau_j (y_j^T X - sum_{i>j} (y_j^T y_i) z_i)
+//
+// (j = k-1 .. 0; X = [X0; 0]), so that the two products with a long dimension,
+// the Gram matrix Y^T Y (inner dimension M) and Y Z (M x r, inner dimension
+// k), run on the tensor cores, and only O(k^2 r) FP64 work stays on the FP64
+// pipe.
+//
+// FP64 accuracy on bf16 tensor cores: the error-free splitting of Ozaki,
+// Ogita, Oishi and Rump (2012), in the fixed-point form of Mukunoki, Ozaki,
+// Ogita and Imamura (2020).  Every value x of a row (or column) with common
+// scale 2^E becomes the integer X = round(x 2^(55-E)), |X| < 2^55, written as
+// seven balanced base-256 digits a_0..a_6 in [-128, 128]; each digit is exact
+// in bf16.  A product of two digits is at most 2^14, so a sum of up to 1024
+// of them is an integer below 2^24 and the tensor core's FP32 accumulator
+// holds it exactly (checked on this GPU up to 1.6e7).  The digit products of
+// equal weight d = i + l accumulate in one tensor-memory accumulator per d.
+// Planes d = 0..7 are kept (34 slice pairs): the dropped terms (d >= 8) are
+// below 2^-61 of the largest product.  Dropping d = 7 as well would leave a
+// systematic error of ~1e-14 in the Gram matrix (measured in a CPU
+// emulation); with it, the rebuilt factors agree with an extended-precision
+// reflector application to about 1e-15, as close as the FP64 path.  Each
+// accumulator is read back with tcgen05.ld and the eight are combined exactly
+// in 64-bit integers, then converted to FP64 once.
+//
+// One CTA (4 warps) per (update, side).  Shared-memory operands use the
+// K-major, no-swizzle core-matrix layout of hc_tc.cuh.
+#include <algorithm>
+#include <mutex>
+
+#include "hc_internal.h"
+#include "hc_tc.cuh"
+
+namespace hc {
+namespace {
+
+constexpr int kTcThreads = 128;
+constexpr int kPlanes = 8;  // digit-product weights d = 0..7
+constexpr long long kTcWaitCycles = 1LL << 30;  // about half a second
+
+constexpr int cmax(int a, int b) { return a > b ? a : b; }
+constexpr int pow2_at_least(int x) {
+    int p = 32;
+    while (p < x) p *= 2;
+    return p;
+}
+
+// Shared-memory plan of the KP variant (KP: padded k, a multiple of 16).
+//   R0: the Gram's seven digit slices (KP rows x 128 rows of Y each; the
+//       last is read as a 128-row operand, so 16 row groups past its start
+//       stay inside R0), later the FP64 matrices G, Y_top, X0 / Z (KP x KP
+//       each), later the seven slices of a 128-row tile of Y (128 x KP).
+//   R1: the seven digit slices of Z^T (up to KP rows x KP).
+template <int KP>
+struct TcCfg {
+    static constexpr int kSliceG = (KP / 8) * 2048;
+    static constexpr int kR0G = 6 * kSliceG + 16 * 2048;
+    static constexpr int kSliceA = 256 * KP;
+    static constexpr int kR0A = 7 * kSliceA;
+    static constexpr int kR0D = 3 * 8 * KP * KP;
+    static constexpr int kR0 = cmax(cmax(kR0G, kR0A), kR0D);
+    static constexpr int kSliceB = 2 * KP * KP;
+    static constexpr int kR1 = 7 * kSliceB;
+    static constexpr int kMisc = 2048;
+    static constexpr int kTmemCols = pow2_at_least(kPlanes * KP);
+    // A CTA holding all 512 tensor-memory columns takes enough shared memory
+    // that no second CTA of this kernel fits beside it on the SM, so no
+    // allocation ever waits for another CTA's columns.
+    static constexpr int kSmem =
+        cmax(kR0 + kR1 + kMisc, kTmemCols == 512 ? 175 * 1024 : 0);
+};
+
+__device__ __forceinline__ int exp_field(double x) {
+    return (int)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FF;
+}
+
+// X = round(x 2^(55 - E)) for |x| < 2^E (|X| < 2^55), from the bits alone.
+__device__ __forceinline__ long long fixed55(double x, int E) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int ef = (int)(b >> 52) & 0x7FF;
+    unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    int e2;
+    if (ef == 0) {
+        e2 = -1074;
+    } else {
+        m |= 1ull << 52;
+        e2 = ef - 1075;
+    }
+    const int sh = e2 + 55 - E;
+    long long X;
+    if (sh >= 0) X = (long long)(m << sh);
+    else if (sh > -64) X = (long long)((m + (1ull << (-sh - 1))) >> (-sh));
+    else X = 0;
+    return (b >> 63) ? -X : X;
+}
+
+// exact float of a small integer (|a| < 2^22) without a conversion instruction
+__device__ __forceinline__ uint32_t small_int_bits(int a) {
+    return __float_as_uint(__int_as_float(0x4B400000 + a) - 12582912.0f);
+}
+
+// the seven digits of X as FP32 bit patterns (bf16 = the upper half, exact)
+__device__ __forceinline__ void digits7(long long X, uint32_t (&f)[7]) {
+#pragma unroll
+    for (int i = 6; i >= 1; --i) {
+        const int lo = (int)((unsigned)X & 0xFFu);
+        const int a = (lo ^ 0x80) - 0x80;
+        f[i] = small_int_bits(a);
+        X = (X - a) >> 8;
+    }
+    f[0] = small_int_bits((int)X);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(uint32_t lo, uint32_t hi) {
+    return __byte_perm(lo, hi, 0x7632);
+}
+
+// Slice eight values (consecutive along K) into seven 16-byte core-matrix
+// rows, one per digit plane; dst[s] = base of slice s + this row's offset.
+__device__ __forceinline__ void slice8_store(const double (&x)[8], int E, unsigned char *dst,
+                                             int slice_stride) {
+    uint32_t w[7][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        uint32_t f0[7], f1[7];
+        digits7(fixed55(x[2 * q], E), f0);
+        digits7(fixed55(x[2 * q + 1], E), f1);
+#pragma unroll
+        for (int s = 0; s < 7; ++s) w[s][q] = pack_bf16(f0[s], f1[s]);
+    }
+#pragma unroll
+    for (int s = 0; s < 7; ++s)
+        *reinterpret_cast<uint4 *>(dst + s * slice_stride) =
+            make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+}
+
+// Two adjacent planes combined exactly, q = acc_2m 2^8 + acc_2m+1 (|q| <
+// 2^33), added as q 2^(88 - 16 m - S); a right shift rounds to nearest, so
+// the few bits dropped below the combined value's last place do not bias it.
+template <int S, int PM>
+__device__ __forceinline__ long long pair_term(float v0, float v1) {
+    constexpr int sh = 88 - 16 * PM - S;
+    const long long q = (long long)__float2int_rn(v0) * 256 + (long long)__float2int_rn(v1);
+    if constexpr (sh >= 0) return q * (1LL << sh);
+    else return (q + (1LL << (-sh - 1))) >> (-sh);
+}
+
+// add the eight planes of 16 columns (taddr: lane base + first column; plane
+// d sits d * KP columns further) into the running sums
+template <int S, int PM, int KP>
+__device__ __forceinline__ void add_pair(long long (&acc)[16], uint32_t taddr) {
+    float v0[16], v1[16];
+    tc::tmem_ld16(taddr + (2 * PM) * KP, v0);
+    tc::tmem_ld16(taddr + (2 * PM + 1) * KP, v1);
+    tc::tmem_ld_wait();
+#pragma unroll
+    for (int e = 0; e < 16; ++e) acc[e] += pair_term<S, PM>(v0[e], v1[e]);
+}
+template <int S, int KP>
+__device__ __forceinline__ void combine_planes(long long (&acc)[16], uint32_t taddr) {
+    add_pair<S, 0, KP>(acc, taddr);
+    add_pair<S, 1, KP>(acc, taddr);
+    add_pair<S, 2, KP>(acc, taddr);
+    add_pair<S, 3, KP>(acc, taddr);
+}
+
+// x 2^p for any p a product of two FP64 values can need (exact unless the
+// result is subnormal)
+__device__ __forceinline__ double scale2(double x, int p) {
+    const int p1 = p / 2, p2 = p - p1;
+    if (p >= -1022 && p <= 1023) return x * __longlong_as_double((long long)(p + 1023) << 52);
+    return (x * __longlong_as_double((long long)(p1 + 1023) << 52)) *
+           __longlong_as_double((long long)(p2 + 1023) << 52);
+}
+
+// Y(i, j) of the reflector block: unit diagonal, zero above it
+__device__ __forceinline__ double yelem(const double *Y, int M, int k, int i, int j) {
+    if (j >= k || i >= M || i < j) return 0.0;
+    return i == j ? 1.0 : Y[(size_t)j * M + i];
+}
+
+// Combine shifts S: the combined sum is T = value 2^(110 - E_x - E_y - S).
+// Gram: |y_j^T y_l| <= ||y_j|| ||y_l|| <= 2 (a Householder vector has
+// ||v||^2 = 2 / tau <= 2), for any partial sum over rows too, and E = 1, so
+// T <= 2^(109 - S) = 2^61 with S = 48; its last place is 2^-60.  Output:
+// |(Y Z)_rc| <= k 2^(E_r + E_c) with k <= 64, so T <= 2^61 with S = 55.
+constexpr int kShiftGram = 48;
+constexpr int kShiftOut = 55;
+
+template <int KP>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    rebuild_tc_kernel(const Desc *__restrict__ descs, const double *__restrict__ ws,
+                      const int *__restrict__ rank, int *__restrict__ status) {
+    using C = TcCfg<KP>;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    unsigned char *R0 = sm, *R1 = sm + C::kR0, *misc = sm + C::kR0 + C::kR1;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(misc);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(misc + 8);
+    int *zE = reinterpret_cast<int *>(misc + 16);              // KP column scales of Z
+    double *s_tau = reinterpret_cast<double *>(misc + 16 + 4 * KP);
+
+    const Desc d = descs[blockIdx.x];
+    if (d.status0 || status[d.idx] != HCORE_GPU_S_OK) return;
+    const int r = rank[d.idx];
+    if (r <= 0) return;
+    const int side = blockIdx.y;
+    const int M = d.M, k = d.k;
+    const WsLayout L = ws_layout(d);
+    const double *Y = ws + d.ws + (side ? L.VB : L.UA);
+    const double *tau = ws + d.ws + (side ? L.tauB : L.tauA);
+    const double *X0 = ws + d.ws + (side ? L.Vo : L.Uo);
+    double *out = (double *)(side ? d.CVo : d.CUo);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int rp = (r + 15) & ~15;
+
+    if (warp == 0) tc::tmem_alloc(tslot, C::kTmemCols);
+    if (tid == 0) tc::mbar_init(mbar, 1);
+    if (tid < KP) s_tau[tid] = tid < k ? tau[tid] : 0.0;
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = *tslot;
+    const uint32_t lane_base = tbase + ((uint32_t)(32 * warp) << 16);
+    const uint32_t r0 = tc::smem_u32(R0), r1 = tc::smem_u32(R1);
+    uint32_t phase = 0;
+    bool failed = false;
+
+    // wait for the MMAs committed last; uniform across the CTA
+    auto wait_mma = [&]() -> bool {
+        const bool ok = tc::mbar_wait(mbar, phase, kTcWaitCycles);
+        phase ^= 1u;
+        return __syncthreads_and(ok) != 0;
+    };
+
+    // ---- 1. Gram G = Y^T Y, 128 rows of Y per pass ---------------------------
+    // Every column of Y has the unit diagonal and |y| <= 1 (dlarfg), so all
+    // columns share the scale 2^1.
+    long long accG[KP];
+#pragma unroll
+    for (int c = 0; c < KP; ++c) accG[c] = 0;
+    {
+        const int jj = tid & 7, g = tid >> 3;  // column within a block of 8, 8-row group
+        const int nchunks = (M + 127) / 128;
+        const uint32_t idG = tc::idesc_bf16_f32(128, KP);
+        for (int ch = 0; ch < nchunks && !failed; ++ch) {
+            const int i0 = ch * 128 + g * 8;
+#pragma unroll 1
+            for (int jb = 0; jb < KP / 8; ++jb) {
+                const int j = jb * 8 + jj;
+                double x[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) x[t] = yelem(Y, M, k, i0 + t, j);
+                slice8_store(x, 1, R0 + jb * 2048 + g * 128 + jj * 16, C::kSliceG);
+            }
+            tc::fence_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (tid == 0) {
+#pragma unroll 1
+                for (int dd = 0; dd < kPlanes; ++dd) {
+                    const int i0 = dd > 6 ? dd - 6 : 0, i1 = dd < 6 ? dd : 6;
+#pragma unroll 1
+                    for (int i = i0; i <= i1; ++i) {
+                        const int l = dd - i;
+                        const uint64_t da = tc::make_desc(r0 + i * C::kSliceG, tc::kLbo, 2048);
+                        const uint64_t db = tc::make_desc(r0 + l * C::kSliceG, tc::kLbo, 2048);
+#pragma unroll
+                        for (int s = 0; s < 8; ++s)
+                            tc::mma_bf16(tbase + dd * KP, da + 16 * s, db + 16 * s, idG,
+                                         i > i0 || s > 0);
+                    }
+                }
+                tc::mma_commit(mbar);
+            }
+            if (!wait_mma()) {
+                failed = true;
+                break;
+            }
+            tc::fence_after_sync();
+#pragma unroll
+            for (int cb = 0; cb < KP / 16; ++cb) {
+                long long a16[16];
+#pragma unroll
+                for (int e = 0; e < 16; ++e) a16[e] = 0;
+                combine_planes<kShiftGram, KP>(a16, lane_base + cb * 16);
+#pragma unroll
+                for (int e = 0; e < 16; ++e) accG[cb * 16 + e] += a16[e];
+            }
+            tc::fence_before_sync();
+            __syncthreads();  // slices and accumulators are free again
+            tc::fence_after_sync();
+        }
+    }
+
+    // ---- 2. Z (FP64, shared memory) -----------------------------------------
+    double *Gs = reinterpret_cast<double *>(R0);  // KP x KP, column-major
+    double *Yt = Gs + KP * KP;                    // top k x k block of Y
+    double *Xs = Yt + KP * KP;                    // X0, then Z
+    if (!failed) {
+        // G = T 2^(S - 110 + 1 + 1)
+        if (tid < k) {
+            const double f = __longlong_as_double((long long)(kShiftGram - 108 + 1023) << 52);
+            static_assert(kShiftGram - 108 >= -1022, "normal scale factor");
+#pragma unroll
+            for (int c = 0; c < KP; ++c)
+                if (c < k) Gs[tid + c * KP] = (double)accG[c] * f;
+        }
+        for (int e = tid; e < k * k; e += kTcThreads) {
+            const int i = e % k, j = e / k;
+            Yt[i + j * KP] = yelem(Y, M, k, i, j);
+        }
+        for (int e = tid; e < k * r; e += kTcThreads) {
+            const int i = e % k, c = e / k;
+            Xs[i + c * KP] = X0[(size_t)c * k + i];
+        }
+        __syncthreads();
+        // W = Y_top^T X0, kept in registers until every thread has read X0
+        double wv[(KP * KP + kTcThreads - 1) / kTcThreads];
+        int nw = 0;
+        for (int e = tid; e < k * r; e += kTcThreads, ++nw) {
+            const int j = e % k, c = e / k;
+            double w0 = Xs[j + c * KP], w1 = 0.0;
+            int i = j + 1;
+            for (; i + 1 < k; i += 2) {
+                w0 += Yt[i + j * KP] * Xs[i + c * KP];
+                w1 += Yt[i + 1 + j * KP] * Xs[i + 1 + c * KP];
+            }
+            if (i < k) w0 += Yt[i + j * KP] * Xs[i + c * KP];
+            wv[nw] = w0 + w1;
+        }
+        __syncthreads();
+        double *Ws = Yt;  // Y_top is no longer read: it holds w', Xs receives z
+        nw = 0;
+        for (int e = tid; e < k * r; e += kTcThreads, ++nw) {
+            const int j = e % k, c = e / k;
+            Ws[j + c * KP] = wv[nw];
+        }
+        __syncthreads();
+        // z_j = tau_j w'_j; w'_i -= G_ij z_j for i < j  (one barrier per j)
+        for (int j = k - 1; j >= 0; --j) {
+            const double tj = s_tau[j];
+            for (int e = tid; e < (j + 1) * r; e += kTcThreads) {
+                const int i = e % (j + 1), c = e / (j + 1);
+                const double zj = tj * Ws[j + c * KP];
+                if (i == j) Xs[j + c * KP] = zj;
+                else Ws[i + c * KP] -= Gs[i + j * KP] * zj;
+            }
+            __syncthreads();
+        }
+        // column scales of Z, then its digit slices (B operand: row c, K = j)
+        if (tid < r) {
+            int ef = 0;
+            for (int j = 0; j < k; ++j) ef = max(ef, exp_field(Xs[j + tid * KP]));
+            zE[tid] = ef - 1022;
+        }
+        __syncthreads();
+        for (int it = tid; it < rp * (KP / 8); it += kTcThreads) {
+            const int cc = it & 7, rest = it >> 3;
+            const int jb = rest % (KP / 8), cb = rest / (KP / 8);
+            const int c = cb * 8 + cc;
+            double x[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int j = jb * 8 + t;
+                x[t] = (c < r && j < k) ? Xs[j + c * KP] : 0.0;
+            }
+            slice8_store(x, c < r ? zE[c] : 0, R1 + cb * (16 * KP) + jb * 128 + cc * 16,
+                         C::kSliceB);
+        }
+        __syncthreads();
+    }
+
+    // ---- 3. out = X - Y Z, 128 rows per tile ----------------------------------
+    if (!failed) {
+        const uint32_t idO = tc::idesc_bf16_f32(128, rp);
+        const int ntiles = (M + 127) / 128;
+        for (int tile = 0; tile < ntiles; ++tile) {
+            const int row = tile * 128 + tid;
+            int ef = 0;
+            for (int j = 0; j < k; ++j) ef = max(ef, exp_field(yelem(Y, M, k, row, j)));
+            const int Erow = ef - 1022;
+#pragma unroll 1
+            for (int jb = 0; jb < KP / 8; ++jb) {
+                double x[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) x[t] = yelem(Y, M, k, row, jb * 8 + t);
+                slice8_store(x, Erow, R0 + (tid >> 3) * (16 * KP) + jb * 128 + (tid & 7) * 16,
+                             C::kSliceA);
+            }
+            tc::fence_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (tid == 0) {
+#pragma unroll 1
+                for (int dd = 0; dd < kPlanes; ++dd) {
+                    const int i0 = dd > 6 ? dd - 6 : 0, i1 = dd < 6 ? dd : 6;
+#pragma unroll 1
+                    for (int i = i0; i <= i1; ++i) {
+                        const int l = dd - i;
+                        const uint64_t da = tc::make_desc(r0 + i * C::kSliceA, tc::kLbo, 16 * KP);
+                        const uint64_t db = tc::make_desc(r1 + l * C::kSliceB, tc::kLbo, 16 * KP);
+#pragma unroll
+                        for (int s = 0; s < KP / 16; ++s)
+                            tc::mma_bf16(tbase + dd * KP, da + 16 * s, db + 16 * s, idO,
+                                         i > i0 || s > 0);
+                    }
+                }
+                tc::mma_commit(mbar);
+            }
+            if (!wait_mma()) {
+                failed = true;
+                break;
+            }
+            tc::fence_after_sync();
+            for (int cb = 0; cb < rp / 16; ++cb) {
+                long long a16[16];
+#pragma unroll
+                for (int e = 0; e < 16; ++e) a16[e] = 0;
+                combine_planes<kShiftOut, KP>(a16, lane_base + cb * 16);
+                if (row < M) {
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) {
+                        const int c = cb * 16 + e;
+                        if (c < r) {
+                            const double v = scale2((double)a16[e], Erow + zE[c] - kShiftOut);
+                            const double x0 = row < k ? X0[(size_t)c * k + row] : 0.0;
+                            out[(size_t)c * d.ldco + row] = x0 - v;
+                        }
+                    }
+                }
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+        }
+    }
+
+    if (failed) {
+        // give up on this update; let MMAs still in flight finish before the
+        // columns are released
+        if (tid == 0) status[d.idx] = HCORE_GPU_S_TIMEOUT;
+        tc::mbar_wait(mbar, phase ^ 1u, kTcWaitCycles);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, C::kTmemCols);
+}
+
+template <int KP>
+cudaError_t set_tc_smem() {
+    return cudaFuncSetAttribute(rebuild_tc_kernel<KP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                TcCfg<KP>::kSmem);
+}
+
+}  // namespace
+
+int tc_rebuild_class(int k) {
+    if (k <= 16) return 16;
+    if (k <= 32) return 32;
+    if (k <= 48) return 48;
+    if (k <= kTcMaxK) return 64;
+    return 0;
+}
+
+cudaError_t configure_rebuild_tc() {
+    cudaError_t e = set_tc_smem<16>();
+    if (e == cudaSuccess) e = set_tc_smem<32>();
+    if (e == cudaSuccess) e = set_tc_smem<48>();
+    if (e == cudaSuccess) e = set_tc_smem<64>();
+    return e;
+}
+
+void launch_rebuild_tc(const Desc *d_desc, int n, const double *ws, const int *d_rank,
+                       int *d_status, int kclass, cudaStream_t s) {
+    if (n <= 0) return;
+    const dim3 grid(n, 2);
+    switch (kclass) {
+        case 16:
+            rebuild_tc_kernel<16><<<grid, kTcThreads, TcCfg<16>::kSmem, s>>>(d_desc, ws, d_rank,
+                                                                            d_status);
+            break;
+        case 32:
+            rebuild_tc_kernel<32><<<grid, kTcThreads, TcCfg<32>::kSmem, s>>>(d_desc, ws, d_rank,
+                                                                            d_status);
+            break;
+        case 48:
+            rebuild_tc_kernel<48><<<grid, kTcThreads, TcCfg<48>::kSmem, s>>>(d_desc, ws, d_rank,
+                                                                            d_status);
+            break;
+        default:
+            rebuild_tc_kernel<64><<<grid, kTcThreads, TcCfg<64>::kSmem, s>>>(d_desc, ws, d_rank,
+                                                                            d_status);
+            break;
+    }
+}
+
+}  // namespace hc

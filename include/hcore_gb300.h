@@ -55,6 +55,7 @@ extern "C" {
 #define HCORE_GPU_S_STORAGE 5   /* new rank > storage maxrank, :1648-1651 */
 #define HCORE_GPU_S_NOCONV 6    /* Jacobi SVD did not converge, or a value was not finite */
 #define HCORE_GPU_S_SHAPE 7     /* a + c > M */
+#define HCORE_GPU_S_TIMEOUT 8   /* a tensor-core wait gave up; the update's output is not written */
 
 /* flags of a plan */
 #define HCORE_GPU_FAST_RULES 0x1 /* HCORE_dgemm_fast: rank search from i=2, no maxrk checks */
@@ -72,6 +73,11 @@ extern "C" {
  * and the truncation stay FP64.  Meant for loose accuracies (1e-4 .. 1e-6);
  * the rebuild's FP32 rounding (~1e-7 relative) is far below such acc. */
 #define HCORE_GPU_MIXED_FACTORS 0x4
+/* FP64 plans run the rebuild (Q.U products) of updates with a + c <= 64 on
+ * the tensor cores, FP64-accurate (exact bf16 digit products, see
+ * hc_rebuild_tc.cu).  This flag keeps the FP64 (DFMA) reflector kernel for
+ * every update instead. */
+#define HCORE_GPU_DFMA_REBUILD 0x8
 
 /* One low-rank update.  Factors are column-major with the given leading
  * dimensions; every factor has M rows.  Ranks are plain ints. */
