@@ -32,7 +32,7 @@
 // accumulator is read back with tcgen05.ld and the eight are combined exactly
 // in 64-bit integers, then converted to FP64 once.
 //
-// One CTA (4 warps) per (update, side).  Shared-memory operands use the
+// One CTA (8 warps) per (update, side).  Shared-memory operands use the
 // K-major, no-swizzle core-matrix layout of hc_tc.cuh.
 #include <algorithm>
 #include <mutex>
@@ -43,7 +43,7 @@
 namespace hc {
 namespace {
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256;
 constexpr int kPlanes = 8;  // digit-product weights d = 0..7
 constexpr long long kTcWaitCycles = 1LL << 30;  // about half a second
 
@@ -103,44 +103,8 @@ __device__ __forceinline__ long long fixed55(double x, int E) {
     return (b >> 63) ? -X : X;
 }
 
-// exact float of a small integer (|a| < 2^22) without a conversion instruction
-__device__ __forceinline__ uint32_t small_int_bits(int a) {
-    return __float_as_uint(__int_as_float(0x4B400000 + a) - 12582912.0f);
-}
-
-// the seven digits of X as FP32 bit patterns (bf16 = the upper half, exact)
-__device__ __forceinline__ void digits7(long long X, uint32_t (&f)[7]) {
-#pragma unroll
-    for (int i = 6; i >= 1; --i) {
-        const int lo = (int)((unsigned)X & 0xFFu);
-        const int a = (lo ^ 0x80) - 0x80;
-        f[i] = small_int_bits(a);
-        X = (X - a) >> 8;
-    }
-    f[0] = small_int_bits((int)X);
-}
-
 __device__ __forceinline__ uint32_t pack_bf16(uint32_t lo, uint32_t hi) {
     return __byte_perm(lo, hi, 0x7632);
-}
-
-// Slice eight values (consecutive along K) into seven 16-byte core-matrix
-// rows, one per digit plane; dst[s] = base of slice s + this row's offset.
-__device__ __forceinline__ void slice8_store(const double (&x)[8], int E, unsigned char *dst,
-                                             int slice_stride) {
-    uint32_t w[7][4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        uint32_t f0[7], f1[7];
-        digits7(fixed55(x[2 * q], E), f0);
-        digits7(fixed55(x[2 * q + 1], E), f1);
-#pragma unroll
-        for (int s = 0; s < 7; ++s) w[s][q] = pack_bf16(f0[s], f1[s]);
-    }
-#pragma unroll
-    for (int s = 0; s < 7; ++s)
-        *reinterpret_cast<uint4 *>(dst + s * slice_stride) =
-            make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
 }
 
 // Two adjacent planes combined exactly, q = acc_2m 2^8 + acc_2m+1 (|q| <
@@ -196,11 +160,57 @@ __device__ __forceinline__ double yelem(const double *Y, int M, int k, int i, in
 constexpr int kShiftGram = 48;
 constexpr int kShiftOut = 55;
 
+// Seven balanced base-256 digits of X (|X| <= 2^55) as FP32 bit patterns,
+// without a data-dependent loop: Z = X + B with B = 128 (256^6 + ... + 1) is
+// non-negative, digit i is byte 6 - i of Z minus 128 (the top one, Z >> 48,
+// may be 256).  One byte permute moves a byte into the mantissa of 2^23 and
+// one FP32 add removes 2^23 + 128, exactly.
+__device__ __forceinline__ void digits7_fast(long long X, uint32_t (&f)[7]) {
+    const unsigned long long z = (unsigned long long)X + 0x0080808080808080ull;
+    const uint32_t lo = (uint32_t)z, hi = (uint32_t)(z >> 32);
+    const float c = 8388736.0f;  // 2^23 + 128
+    f[6] = __float_as_uint(__uint_as_float(__byte_perm(lo, 0x4B000000u, 0x7540)) - c);
+    f[5] = __float_as_uint(__uint_as_float(__byte_perm(lo, 0x4B000000u, 0x7541)) - c);
+    f[4] = __float_as_uint(__uint_as_float(__byte_perm(lo, 0x4B000000u, 0x7542)) - c);
+    f[3] = __float_as_uint(__uint_as_float(__byte_perm(lo, 0x4B000000u, 0x7543)) - c);
+    f[2] = __float_as_uint(__uint_as_float(__byte_perm(hi, 0x4B000000u, 0x7540)) - c);
+    f[1] = __float_as_uint(__uint_as_float(__byte_perm(hi, 0x4B000000u, 0x7541)) - c);
+    f[0] = __float_as_uint(__uint_as_float(0x4B000000u | (hi >> 16)) - c);
+}
+
+// Slice eight values that share the scale 2^E (consecutive along K) into
+// seven 16-byte core-matrix rows, one per digit plane, slice_stride apart.
+__device__ __forceinline__ void slice8(const double (&x)[8], int E, unsigned char *dst,
+                                       int slice_stride) {
+    uint32_t w[7][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        uint32_t f0[7], f1[7];
+        digits7_fast(fixed55(x[2 * q], E), f0);
+        digits7_fast(fixed55(x[2 * q + 1], E), f1);
+#pragma unroll
+        for (int s = 0; s < 7; ++s) w[s][q] = pack_bf16(f0[s], f1[s]);
+    }
+#pragma unroll
+    for (int s = 0; s < 7; ++s)
+        *reinterpret_cast<uint4 *>(dst + s * slice_stride) =
+            make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+}
+
+// Eight warps per CTA: the two warp groups (warps 0-3 and 4-7) see the same
+// 128 tensor-memory lanes and split the accumulator column blocks between
+// them.  Every |y| of a Householder block is at most 1 (dlarfg), so Y takes
+// the one scale 2^1 in both products; the output's error is then absolute,
+// 2^-55 |Z| per term, as a normwise-stable reflector application's is.
 template <int KP>
-__global__ void __launch_bounds__(kTcThreads, 1)
-    rebuild_tc_kernel(const Desc *__restrict__ descs, const double *__restrict__ ws,
-                      const int *__restrict__ rank, int *__restrict__ status) {
+__device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
+                                                const double *__restrict__ ws,
+                                                const int *__restrict__ rank,
+                                                int *__restrict__ status) {
     using C = TcCfg<KP>;
+    constexpr int kItems = KP / 16;            // 8-value slicing items per thread
+    constexpr int kBlocks = KP / 16;           // 16-column accumulator blocks
+    constexpr int kBlk = (kBlocks + 1) / 2;    // blocks per warp group
     extern __shared__ __align__(1024) unsigned char sm[];
     unsigned char *R0 = sm, *R1 = sm + C::kR0, *misc = sm + C::kR0 + C::kR1;
     uint64_t *mbar = reinterpret_cast<uint64_t *>(misc);
@@ -220,6 +230,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const double *X0 = ws + d.ws + (side ? L.Vo : L.Uo);
     double *out = (double *)(side ? d.CVo : d.CUo);
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int lrow = tid & 127;                // tensor-memory lane of this thread
+    const int wg = tid >> 7;                   // warp group
     const int rp = (r + 15) & ~15;
 
     if (warp == 0) tc::tmem_alloc(tslot, C::kTmemCols);
@@ -229,7 +241,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tbase = *tslot;
-    const uint32_t lane_base = tbase + ((uint32_t)(32 * warp) << 16);
+    const uint32_t lane_base = tbase + ((uint32_t)(32 * (warp & 3)) << 16);
     const uint32_t r0 = tc::smem_u32(R0), r1 = tc::smem_u32(R1);
     uint32_t phase = 0;
     bool failed = false;
@@ -240,61 +252,65 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         phase ^= 1u;
         return __syncthreads_and(ok) != 0;
     };
+    // planes d = 0..7, pairs (i, d - i) of the seven digit slices
+    auto issue = [&](uint32_t a0, int a_stride, uint32_t a_sbo, uint32_t b0, int b_stride,
+                     uint32_t b_sbo, int ksteps, uint32_t idesc) {
+#pragma unroll 1
+        for (int dd = 0; dd < kPlanes; ++dd) {
+            const int i0 = dd > 6 ? dd - 6 : 0, i1 = dd < 6 ? dd : 6;
+#pragma unroll 1
+            for (int i = i0; i <= i1; ++i) {
+                const uint64_t da = tc::make_desc(a0 + i * a_stride, tc::kLbo, a_sbo);
+                const uint64_t db = tc::make_desc(b0 + (dd - i) * b_stride, tc::kLbo, b_sbo);
+#pragma unroll 1
+                for (int s = 0; s < ksteps; ++s)
+                    tc::mma_bf16(tbase + dd * KP, da + 16 * s, db + 16 * s, idesc, i > i0 || s > 0);
+            }
+        }
+        tc::mma_commit(mbar);
+    };
 
     // ---- 1. Gram G = Y^T Y, 128 rows of Y per pass ---------------------------
-    // Every column of Y has the unit diagonal and |y| <= 1 (dlarfg), so all
-    // columns share the scale 2^1.
-    long long accG[KP];
+    // Item q of a thread: column j = (jh + 2 q) * 8 + jj, rows g*8 .. g*8+7 of
+    // the chunk; the next chunk's values are loaded while the MMAs run.
+    long long accG[kBlk][16];
 #pragma unroll
-    for (int c = 0; c < KP; ++c) accG[c] = 0;
+    for (int m = 0; m < kBlk; ++m)
+#pragma unroll
+        for (int e = 0; e < 16; ++e) accG[m][e] = 0;
     {
-        const int jj = tid & 7, g = tid >> 3;  // column within a block of 8, 8-row group
+        const int jj = tid & 7, g = (tid >> 3) & 15, jh = tid >> 7;
         const int nchunks = (M + 127) / 128;
-        const uint32_t idG = tc::idesc_bf16_f32(128, KP);
-        for (int ch = 0; ch < nchunks && !failed; ++ch) {
+        double pre[kItems][8];
+        auto load_chunk = [&](int ch) {
             const int i0 = ch * 128 + g * 8;
-#pragma unroll 1
-            for (int jb = 0; jb < KP / 8; ++jb) {
-                const int j = jb * 8 + jj;
-                double x[8];
 #pragma unroll
-                for (int t = 0; t < 8; ++t) x[t] = yelem(Y, M, k, i0 + t, j);
-                slice8_store(x, 1, R0 + jb * 2048 + g * 128 + jj * 16, C::kSliceG);
-            }
+            for (int q = 0; q < kItems; ++q)
+#pragma unroll
+                for (int t = 0; t < 8; ++t) pre[q][t] = yelem(Y, M, k, i0 + t, (jh + 2 * q) * 8 + jj);
+        };
+        load_chunk(0);
+        for (int ch = 0; ch < nchunks; ++ch) {
+#pragma unroll
+            for (int q = 0; q < kItems; ++q)
+                slice8(pre[q], 1, R0 + (jh + 2 * q) * 2048 + g * 128 + jj * 16, C::kSliceG);
             tc::fence_async_smem();
             tc::fence_before_sync();
             __syncthreads();
             tc::fence_after_sync();
-            if (tid == 0) {
-#pragma unroll 1
-                for (int dd = 0; dd < kPlanes; ++dd) {
-                    const int i0 = dd > 6 ? dd - 6 : 0, i1 = dd < 6 ? dd : 6;
-#pragma unroll 1
-                    for (int i = i0; i <= i1; ++i) {
-                        const int l = dd - i;
-                        const uint64_t da = tc::make_desc(r0 + i * C::kSliceG, tc::kLbo, 2048);
-                        const uint64_t db = tc::make_desc(r0 + l * C::kSliceG, tc::kLbo, 2048);
-#pragma unroll
-                        for (int s = 0; s < 8; ++s)
-                            tc::mma_bf16(tbase + dd * KP, da + 16 * s, db + 16 * s, idG,
-                                         i > i0 || s > 0);
-                    }
-                }
-                tc::mma_commit(mbar);
-            }
+            if (tid == 0)
+                issue(r0, C::kSliceG, 2048, r0, C::kSliceG, 2048, 8,
+                      tc::idesc_bf16_f32(128, KP));
+            if (ch + 1 < nchunks) load_chunk(ch + 1);
             if (!wait_mma()) {
                 failed = true;
                 break;
             }
             tc::fence_after_sync();
 #pragma unroll
-            for (int cb = 0; cb < KP / 16; ++cb) {
-                long long a16[16];
-#pragma unroll
-                for (int e = 0; e < 16; ++e) a16[e] = 0;
-                combine_planes<kShiftGram, KP>(a16, lane_base + cb * 16);
-#pragma unroll
-                for (int e = 0; e < 16; ++e) accG[cb * 16 + e] += a16[e];
+            for (int m = 0; m < kBlk; ++m) {
+                const int cb = wg + 2 * m;
+                if (cb < kBlocks) combine_planes<kShiftGram, KP>(accG[m], lane_base + cb * 16);
             }
             tc::fence_before_sync();
             __syncthreads();  // slices and accumulators are free again
@@ -308,12 +324,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     double *Xs = Yt + KP * KP;                    // X0, then Z
     if (!failed) {
         // G = T 2^(S - 110 + 1 + 1)
-        if (tid < k) {
+        if (lrow < k) {
             const double f = __longlong_as_double((long long)(kShiftGram - 108 + 1023) << 52);
             static_assert(kShiftGram - 108 >= -1022, "normal scale factor");
 #pragma unroll
-            for (int c = 0; c < KP; ++c)
-                if (c < k) Gs[tid + c * KP] = (double)accG[c] * f;
+            for (int m = 0; m < kBlk; ++m) {
+                const int cb = wg + 2 * m;
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const int c = cb * 16 + e;
+                    if (cb < kBlocks && c < k) Gs[lrow + c * KP] = (double)accG[m][e] * f;
+                }
+            }
         }
         for (int e = tid; e < k * k; e += kTcThreads) {
             const int i = e % k, j = e / k;
@@ -374,56 +396,48 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 const int j = jb * 8 + t;
                 x[t] = (c < r && j < k) ? Xs[j + c * KP] : 0.0;
             }
-            slice8_store(x, c < r ? zE[c] : 0, R1 + cb * (16 * KP) + jb * 128 + cc * 16,
-                         C::kSliceB);
+            slice8(x, c < r ? zE[c] : 0, R1 + cb * (16 * KP) + jb * 128 + cc * 16, C::kSliceB);
         }
         __syncthreads();
     }
 
     // ---- 3. out = X - Y Z, 128 rows per tile ----------------------------------
     if (!failed) {
-        const uint32_t idO = tc::idesc_bf16_f32(128, rp);
+        const int jh = tid >> 7;
         const int ntiles = (M + 127) / 128;
-        for (int tile = 0; tile < ntiles; ++tile) {
-            const int row = tile * 128 + tid;
-            int ef = 0;
-            for (int j = 0; j < k; ++j) ef = max(ef, exp_field(yelem(Y, M, k, row, j)));
-            const int Erow = ef - 1022;
-#pragma unroll 1
-            for (int jb = 0; jb < KP / 8; ++jb) {
-                double x[8];
+        double pre[kItems][8];
+        auto load_tile = [&](int tile) {
+            const int row = tile * 128 + lrow;
 #pragma unroll
-                for (int t = 0; t < 8; ++t) x[t] = yelem(Y, M, k, row, jb * 8 + t);
-                slice8_store(x, Erow, R0 + (tid >> 3) * (16 * KP) + jb * 128 + (tid & 7) * 16,
-                             C::kSliceA);
-            }
+            for (int q = 0; q < kItems; ++q)
+#pragma unroll
+                for (int t = 0; t < 8; ++t) pre[q][t] = yelem(Y, M, k, row, (jh + 2 * q) * 8 + t);
+        };
+        load_tile(0);
+        for (int tile = 0; tile < ntiles; ++tile) {
+            const int row = tile * 128 + lrow;
+#pragma unroll
+            for (int q = 0; q < kItems; ++q)
+                slice8(pre[q], 1,
+                       R0 + (lrow >> 3) * (16 * KP) + (jh + 2 * q) * 128 + (lrow & 7) * 16,
+                       C::kSliceA);
             tc::fence_async_smem();
             tc::fence_before_sync();
             __syncthreads();
             tc::fence_after_sync();
-            if (tid == 0) {
-#pragma unroll 1
-                for (int dd = 0; dd < kPlanes; ++dd) {
-                    const int i0 = dd > 6 ? dd - 6 : 0, i1 = dd < 6 ? dd : 6;
-#pragma unroll 1
-                    for (int i = i0; i <= i1; ++i) {
-                        const int l = dd - i;
-                        const uint64_t da = tc::make_desc(r0 + i * C::kSliceA, tc::kLbo, 16 * KP);
-                        const uint64_t db = tc::make_desc(r1 + l * C::kSliceB, tc::kLbo, 16 * KP);
-#pragma unroll
-                        for (int s = 0; s < KP / 16; ++s)
-                            tc::mma_bf16(tbase + dd * KP, da + 16 * s, db + 16 * s, idO,
-                                         i > i0 || s > 0);
-                    }
-                }
-                tc::mma_commit(mbar);
-            }
+            if (tid == 0)
+                issue(r0, C::kSliceA, 16 * KP, r1, C::kSliceB, 16 * KP, KP / 16,
+                      tc::idesc_bf16_f32(128, rp));
+            if (tile + 1 < ntiles) load_tile(tile + 1);
             if (!wait_mma()) {
                 failed = true;
                 break;
             }
             tc::fence_after_sync();
-            for (int cb = 0; cb < rp / 16; ++cb) {
+#pragma unroll
+            for (int m = 0; m < kBlk; ++m) {
+                const int cb = wg + 2 * m;
+                if (cb * 16 >= rp) continue;
                 long long a16[16];
 #pragma unroll
                 for (int e = 0; e < 16; ++e) a16[e] = 0;
@@ -433,7 +447,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     for (int e = 0; e < 16; ++e) {
                         const int c = cb * 16 + e;
                         if (c < r) {
-                            const double v = scale2((double)a16[e], Erow + zE[c] - kShiftOut);
+                            const double v = scale2((double)a16[e], 1 + zE[c] - kShiftOut);
                             const double x0 = row < k ? X0[(size_t)c * k + row] : 0.0;
                             out[(size_t)c * d.ldco + row] = x0 - v;
                         }
@@ -457,10 +471,30 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (warp == 0) tc::tmem_dealloc(tbase, C::kTmemCols);
 }
 
+// Two CTAs per SM for KP <= 32 (128 registers a thread); one for the wider
+// variants, whose registers are capped so that other kernels' CTAs (the QR and
+// SVD of other stream groups) still fit beside it on the SM.
+template <int KP>
+__global__ void __launch_bounds__(kTcThreads, 2)
+    rebuild_tc_kernel(const Desc *__restrict__ descs, const double *__restrict__ ws,
+                      const int *__restrict__ rank, int *__restrict__ status) {
+    rebuild_tc_body<KP>(descs, ws, rank, status);
+}
+template <int KP>
+__global__ void __maxnreg__(168)
+    rebuild_tc_wide_kernel(const Desc *__restrict__ descs, const double *__restrict__ ws,
+                           const int *__restrict__ rank, int *__restrict__ status) {
+    rebuild_tc_body<KP>(descs, ws, rank, status);
+}
+
 template <int KP>
 cudaError_t set_tc_smem() {
-    return cudaFuncSetAttribute(rebuild_tc_kernel<KP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                TcCfg<KP>::kSmem);
+    if constexpr (KP <= 32)
+        return cudaFuncSetAttribute(rebuild_tc_kernel<KP>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<KP>::kSmem);
+    else
+        return cudaFuncSetAttribute(rebuild_tc_wide_kernel<KP>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<KP>::kSmem);
 }
 
 }  // namespace
@@ -495,12 +529,12 @@ void launch_rebuild_tc(const Desc *d_desc, int n, const double *ws, const int *d
                                                                             d_status);
             break;
         case 48:
-            rebuild_tc_kernel<48><<<grid, kTcThreads, TcCfg<48>::kSmem, s>>>(d_desc, ws, d_rank,
-                                                                            d_status);
+            rebuild_tc_wide_kernel<48><<<grid, kTcThreads, TcCfg<48>::kSmem, s>>>(
+                d_desc, ws, d_rank, d_status);
             break;
         default:
-            rebuild_tc_kernel<64><<<grid, kTcThreads, TcCfg<64>::kSmem, s>>>(d_desc, ws, d_rank,
-                                                                            d_status);
+            rebuild_tc_wide_kernel<64><<<grid, kTcThreads, TcCfg<64>::kSmem, s>>>(
+                d_desc, ws, d_rank, d_status);
             break;
     }
 }
