@@ -59,7 +59,9 @@ constexpr int pow2_at_least(int x) {
 //       last is read as a 128-row operand, so 16 row groups past its start
 //       stay inside R0), later the FP64 matrices G, Y_top, X0 / Z (KP x KP
 //       each), later the seven slices of a 128-row tile of Y (128 x KP).
-//   R1: the seven digit slices of Z^T (up to KP rows x KP).
+//       The eighth Gram slice position (inside R0) holds zeros.
+//   R1: the seven digit slices of Z^T (r rounded up to 16 rows x KP each,
+//       consecutive), then a zero slice.
 template <int KP>
 struct TcCfg {
     static constexpr int kSliceG = (KP / 8) * 2048;
@@ -68,8 +70,8 @@ struct TcCfg {
     static constexpr int kR0A = 7 * kSliceA;
     static constexpr int kR0D = 3 * 8 * KP * KP;
     static constexpr int kR0 = cmax(cmax(kR0G, kR0A), kR0D);
-    static constexpr int kSliceB = 2 * KP * KP;
-    static constexpr int kR1 = 7 * kSliceB;
+    static constexpr int kSliceB = 2 * KP * KP;  // largest Z slice (r <= KP rows)
+    static constexpr int kR1 = 8 * kSliceB;       // seven slices and a zero one
     static constexpr int kMisc = 2048;
     static constexpr int kTmemCols = pow2_at_least(kPlanes * KP);
     // A CTA holding all 512 tensor-memory columns takes enough shared memory
@@ -119,22 +121,22 @@ __device__ __forceinline__ long long pair_term(float v0, float v1) {
 }
 
 // add the eight planes of 16 columns (taddr: lane base + first column; plane
-// d sits d * KP columns further) into the running sums
-template <int S, int PM, int KP>
-__device__ __forceinline__ void add_pair(long long (&acc)[16], uint32_t taddr) {
+// d sits d * stride columns further) into the running sums
+template <int S, int PM>
+__device__ __forceinline__ void add_pair(long long (&acc)[16], uint32_t taddr, int stride) {
     float v0[16], v1[16];
-    tc::tmem_ld16(taddr + (2 * PM) * KP, v0);
-    tc::tmem_ld16(taddr + (2 * PM + 1) * KP, v1);
+    tc::tmem_ld16(taddr + (2 * PM) * stride, v0);
+    tc::tmem_ld16(taddr + (2 * PM + 1) * stride, v1);
     tc::tmem_ld_wait();
 #pragma unroll
     for (int e = 0; e < 16; ++e) acc[e] += pair_term<S, PM>(v0[e], v1[e]);
 }
-template <int S, int KP>
-__device__ __forceinline__ void combine_planes(long long (&acc)[16], uint32_t taddr) {
-    add_pair<S, 0, KP>(acc, taddr);
-    add_pair<S, 1, KP>(acc, taddr);
-    add_pair<S, 2, KP>(acc, taddr);
-    add_pair<S, 3, KP>(acc, taddr);
+template <int S>
+__device__ __forceinline__ void combine_planes(long long (&acc)[16], uint32_t taddr, int stride) {
+    add_pair<S, 0>(acc, taddr, stride);
+    add_pair<S, 1>(acc, taddr, stride);
+    add_pair<S, 2>(acc, taddr, stride);
+    add_pair<S, 3>(acc, taddr, stride);
 }
 
 // x 2^p for any p a product of two FP64 values can need (exact unless the
@@ -233,6 +235,7 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
     const int lrow = tid & 127;                // tensor-memory lane of this thread
     const int wg = tid >> 7;                   // warp group
     const int rp = (r + 15) & ~15;
+    const int zslice = 2 * rp * KP;            // bytes of one digit slice of Z^T
 
     if (warp == 0) tc::tmem_alloc(tslot, C::kTmemCols);
     if (tid == 0) tc::mbar_init(mbar, 1);
@@ -252,19 +255,27 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
         phase ^= 1u;
         return __syncthreads_and(ok) != 0;
     };
-    // planes d = 0..7, pairs (i, d - i) of the seven digit slices
+    // Planes d = 0..7 (accumulator d at column d * pstride) from the seven
+    // digit slices: one MMA per A slice i, K step and piece of planes, whose
+    // B operand is the run of consecutive B slices d0 - i .. d1 - i (the
+    // slice past the seventh is zero), so each product lands in plane i + l.
+    // A piece spans at most 256 columns.  The first MMAs (i = 0, K step 0)
+    // cover every plane and start the accumulators.
     auto issue = [&](uint32_t a0, int a_stride, uint32_t a_sbo, uint32_t b0, int b_stride,
-                     uint32_t b_sbo, int ksteps, uint32_t idesc) {
+                     uint32_t b_sbo, int ksteps, int pstride) {
+        const int per = 256 / pstride;
 #pragma unroll 1
-        for (int dd = 0; dd < kPlanes; ++dd) {
-            const int i0 = dd > 6 ? dd - 6 : 0, i1 = dd < 6 ? dd : 6;
+        for (int i = 0; i < 7; ++i) {
+            const uint64_t da = tc::make_desc(a0 + i * a_stride, tc::kLbo, a_sbo);
 #pragma unroll 1
-            for (int i = i0; i <= i1; ++i) {
-                const uint64_t da = tc::make_desc(a0 + i * a_stride, tc::kLbo, a_sbo);
-                const uint64_t db = tc::make_desc(b0 + (dd - i) * b_stride, tc::kLbo, b_sbo);
+            for (int d0 = i; d0 < kPlanes; d0 += per) {
+                const int d1 = min(d0 + per, kPlanes);
+                const uint64_t db = tc::make_desc(b0 + (d0 - i) * b_stride, tc::kLbo, b_sbo);
+                const uint32_t id = tc::idesc_bf16_f32(128, (d1 - d0) * pstride);
 #pragma unroll 1
                 for (int s = 0; s < ksteps; ++s)
-                    tc::mma_bf16(tbase + dd * KP, da + 16 * s, db + 16 * s, idesc, i > i0 || s > 0);
+                    tc::mma_bf16(tbase + d0 * pstride, da + 16 * s, db + 16 * s, id,
+                                 i > 0 || s > 0);
             }
         }
         tc::mma_commit(mbar);
@@ -290,6 +301,9 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
                 for (int t = 0; t < 8; ++t) pre[q][t] = yelem(Y, M, k, i0 + t, (jh + 2 * q) * 8 + jj);
         };
         load_chunk(0);
+        // the eighth Gram slice: zeros (the B run of plane 7 with i = 0 ends there)
+        for (int e = tid; e < C::kSliceG / 16; e += kTcThreads)
+            reinterpret_cast<uint4 *>(R0 + 7 * C::kSliceG)[e] = make_uint4(0, 0, 0, 0);
         for (int ch = 0; ch < nchunks; ++ch) {
 #pragma unroll
             for (int q = 0; q < kItems; ++q)
@@ -299,8 +313,7 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
             __syncthreads();
             tc::fence_after_sync();
             if (tid == 0)
-                issue(r0, C::kSliceG, 2048, r0, C::kSliceG, 2048, 8,
-                      tc::idesc_bf16_f32(128, KP));
+                issue(r0, C::kSliceG, 2048, r0, C::kSliceG, 2048, 8, KP);
             if (ch + 1 < nchunks) load_chunk(ch + 1);
             if (!wait_mma()) {
                 failed = true;
@@ -310,7 +323,7 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
 #pragma unroll
             for (int m = 0; m < kBlk; ++m) {
                 const int cb = wg + 2 * m;
-                if (cb < kBlocks) combine_planes<kShiftGram, KP>(accG[m], lane_base + cb * 16);
+                if (cb < kBlocks) combine_planes<kShiftGram>(accG[m], lane_base + cb * 16, KP);
             }
             tc::fence_before_sync();
             __syncthreads();  // slices and accumulators are free again
@@ -368,14 +381,26 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
             Ws[j + c * KP] = wv[nw];
         }
         __syncthreads();
-        // z_j = tau_j w'_j; w'_i -= G_ij z_j for i < j  (one barrier per j)
-        for (int j = k - 1; j >= 0; --j) {
-            const double tj = s_tau[j];
-            for (int e = tid; e < (j + 1) * r; e += kTcThreads) {
-                const int i = e % (j + 1), c = e / (j + 1);
-                const double zj = tj * Ws[j + c * KP];
-                if (i == j) Xs[j + c * KP] = zj;
-                else Ws[i + c * KP] -= Gs[i + j * KP] * zj;
+        // Back substitution (diag(1/tau) + strict upper part of G) Z = W:
+        // z_j = tau_j (w_j - sum_{i>j} G_ji z_i), in blocks of 8 rows from the
+        // bottom.  A block's rows are solved one column per thread, then one
+        // pass takes the block's z out of every row above it.
+        for (int b1 = k; b1 > 0; b1 -= 8) {
+            const int b0 = max(0, b1 - 8);
+            if (tid < r) {
+                const int c = tid;
+                for (int j = b1 - 1; j >= b0; --j) {
+                    double w = Ws[j + c * KP];
+                    for (int i = j + 1; i < b1; ++i) w -= Gs[j + i * KP] * Xs[i + c * KP];
+                    Xs[j + c * KP] = s_tau[j] * w;
+                }
+            }
+            __syncthreads();
+            for (int e = tid; e < b0 * r; e += kTcThreads) {
+                const int i = e % b0, c = e / b0;
+                double w = Ws[i + c * KP];
+                for (int j = b0; j < b1; ++j) w -= Gs[i + j * KP] * Xs[j + c * KP];
+                Ws[i + c * KP] = w;
             }
             __syncthreads();
         }
@@ -396,8 +421,10 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
                 const int j = jb * 8 + t;
                 x[t] = (c < r && j < k) ? Xs[j + c * KP] : 0.0;
             }
-            slice8(x, c < r ? zE[c] : 0, R1 + cb * (16 * KP) + jb * 128 + cc * 16, C::kSliceB);
+            slice8(x, c < r ? zE[c] : 0, R1 + cb * (16 * KP) + jb * 128 + cc * 16, zslice);
         }
+        for (int e = tid; e < zslice / 16; e += kTcThreads)
+            reinterpret_cast<uint4 *>(R1 + 7 * zslice)[e] = make_uint4(0, 0, 0, 0);
         __syncthreads();
     }
 
@@ -426,8 +453,7 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
             __syncthreads();
             tc::fence_after_sync();
             if (tid == 0)
-                issue(r0, C::kSliceA, 16 * KP, r1, C::kSliceB, 16 * KP, KP / 16,
-                      tc::idesc_bf16_f32(128, rp));
+                issue(r0, C::kSliceA, 16 * KP, r1, zslice, 16 * KP, KP / 16, rp);
             if (tile + 1 < ntiles) load_tile(tile + 1);
             if (!wait_mma()) {
                 failed = true;
@@ -441,7 +467,7 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
                 long long a16[16];
 #pragma unroll
                 for (int e = 0; e < 16; ++e) a16[e] = 0;
-                combine_planes<kShiftOut, KP>(a16, lane_base + cb * 16);
+                combine_planes<kShiftOut>(a16, lane_base + cb * 16, rp);
                 if (row < M) {
 #pragma unroll
                     for (int e = 0; e < 16; ++e) {
