@@ -120,23 +120,48 @@ __device__ __forceinline__ long long pair_term(float v0, float v1) {
     else return (q + (1LL << (-sh - 1))) >> (-sh);
 }
 
-// add the eight planes of 16 columns (taddr: lane base + first column; plane
+// add the eight planes of 8 columns (taddr: lane base + first column; plane
 // d sits d * stride columns further) into the running sums
 template <int S, int PM>
-__device__ __forceinline__ void add_pair(long long (&acc)[16], uint32_t taddr, int stride) {
-    float v0[16], v1[16];
-    tc::tmem_ld16(taddr + (2 * PM) * stride, v0);
-    tc::tmem_ld16(taddr + (2 * PM + 1) * stride, v1);
+__device__ __forceinline__ void add_pair(long long (&acc)[8], uint32_t taddr, int stride) {
+    float v0[8], v1[8];
+    tc::tmem_ld8(taddr + (2 * PM) * stride, v0);
+    tc::tmem_ld8(taddr + (2 * PM + 1) * stride, v1);
     tc::tmem_ld_wait();
 #pragma unroll
-    for (int e = 0; e < 16; ++e) acc[e] += pair_term<S, PM>(v0[e], v1[e]);
+    for (int e = 0; e < 8; ++e) acc[e] += pair_term<S, PM>(v0[e], v1[e]);
 }
 template <int S>
-__device__ __forceinline__ void combine_planes(long long (&acc)[16], uint32_t taddr, int stride) {
+__device__ __forceinline__ void combine_planes(long long (&acc)[8], uint32_t taddr, int stride) {
     add_pair<S, 0>(acc, taddr, stride);
     add_pair<S, 1>(acc, taddr, stride);
     add_pair<S, 2>(acc, taddr, stride);
     add_pair<S, 3>(acc, taddr, stride);
+}
+
+// T 2^p as an FP64 value, rounded to nearest even, by integer instructions
+// only (the FP64 pipe is the busy one); ok = false when the result leaves the
+// normal range, and the caller converts with FP64 arithmetic instead.
+__device__ __forceinline__ double i64_times_pow2(long long T, int p, bool &ok) {
+    if (T == 0) {
+        ok = true;
+        return 0.0;
+    }
+    const unsigned long long sgn = (unsigned long long)T & 0x8000000000000000ull;
+    unsigned long long m = T < 0 ? 0ull - (unsigned long long)T : (unsigned long long)T;
+    const int lz = __clzll((long long)m);
+    m <<= lz;                                    // leading one at bit 63
+    int e = 63 - lz + p;
+    unsigned long long mant = m >> 11;           // 53 bits
+    const unsigned rem = (unsigned)(m & 0x7FFu);
+    mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+    if (mant >> 53) {
+        mant >>= 1;
+        ++e;
+    }
+    ok = e >= -1022 && e <= 1023;
+    return __longlong_as_double(
+        (long long)(sgn | ((unsigned long long)(e + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
 // x 2^p for any p a product of two FP64 values can need (exact unless the
@@ -211,8 +236,7 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
                                                 int *__restrict__ status) {
     using C = TcCfg<KP>;
     constexpr int kItems = KP / 16;            // 8-value slicing items per thread
-    constexpr int kBlocks = KP / 16;           // 16-column accumulator blocks
-    constexpr int kBlk = (kBlocks + 1) / 2;    // blocks per warp group
+    constexpr int kBlk = KP / 16;              // 8-column accumulator blocks per warp group
     extern __shared__ __align__(1024) unsigned char sm[];
     unsigned char *R0 = sm, *R1 = sm + C::kR0, *misc = sm + C::kR0 + C::kR1;
     uint64_t *mbar = reinterpret_cast<uint64_t *>(misc);
@@ -284,11 +308,11 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
     // ---- 1. Gram G = Y^T Y, 128 rows of Y per pass ---------------------------
     // Item q of a thread: column j = (jh + 2 q) * 8 + jj, rows g*8 .. g*8+7 of
     // the chunk; the next chunk's values are loaded while the MMAs run.
-    long long accG[kBlk][16];
+    long long accG[kBlk][8];
 #pragma unroll
     for (int m = 0; m < kBlk; ++m)
 #pragma unroll
-        for (int e = 0; e < 16; ++e) accG[m][e] = 0;
+        for (int e = 0; e < 8; ++e) accG[m][e] = 0;
     {
         const int jj = tid & 7, g = (tid >> 3) & 15, jh = tid >> 7;
         const int nchunks = (M + 127) / 128;
@@ -321,10 +345,8 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
             }
             tc::fence_after_sync();
 #pragma unroll
-            for (int m = 0; m < kBlk; ++m) {
-                const int cb = wg + 2 * m;
-                if (cb < kBlocks) combine_planes<kShiftGram>(accG[m], lane_base + cb * 16, KP);
-            }
+            for (int m = 0; m < kBlk; ++m)
+                combine_planes<kShiftGram>(accG[m], lane_base + (wg + 2 * m) * 8, KP);
             tc::fence_before_sync();
             __syncthreads();  // slices and accumulators are free again
             tc::fence_after_sync();
@@ -342,11 +364,10 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
             static_assert(kShiftGram - 108 >= -1022, "normal scale factor");
 #pragma unroll
             for (int m = 0; m < kBlk; ++m) {
-                const int cb = wg + 2 * m;
 #pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    const int c = cb * 16 + e;
-                    if (cb < kBlocks && c < k) Gs[lrow + c * KP] = (double)accG[m][e] * f;
+                for (int e = 0; e < 8; ++e) {
+                    const int c = (wg + 2 * m) * 8 + e;
+                    if (c < k) Gs[lrow + c * KP] = (double)accG[m][e] * f;
                 }
             }
         }
@@ -462,20 +483,24 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
             tc::fence_after_sync();
 #pragma unroll
             for (int m = 0; m < kBlk; ++m) {
-                const int cb = wg + 2 * m;
-                if (cb * 16 >= rp) continue;
-                long long a16[16];
+                const int cb = wg + 2 * m;  // 8-column block
+                if (cb * 8 >= rp) continue;
+                long long a8[8];
 #pragma unroll
-                for (int e = 0; e < 16; ++e) a16[e] = 0;
-                combine_planes<kShiftOut>(a16, lane_base + cb * 16, rp);
+                for (int e = 0; e < 8; ++e) a8[e] = 0;
+                combine_planes<kShiftOut>(a8, lane_base + cb * 8, rp);
                 if (row < M) {
 #pragma unroll
-                    for (int e = 0; e < 16; ++e) {
-                        const int c = cb * 16 + e;
+                    for (int e = 0; e < 8; ++e) {
+                        const int c = cb * 8 + e;
                         if (c < r) {
-                            const double v = scale2((double)a16[e], 1 + zE[c] - kShiftOut);
-                            const double x0 = row < k ? X0[(size_t)c * k + row] : 0.0;
-                            out[(size_t)c * d.ldco + row] = x0 - v;
+                            // rows below k: out = -(Y Z) exactly; above: X0 - (Y Z)
+                            const int p = 1 + zE[c] - kShiftOut;
+                            bool ok;
+                            double v = i64_times_pow2(row < k ? a8[e] : -a8[e], p, ok);
+                            if (!ok) v = scale2((double)(row < k ? a8[e] : -a8[e]), p);
+                            if (row < k) v = X0[(size_t)c * k + row] - v;
+                            out[(size_t)c * d.ldco + row] = v;
                         }
                     }
                 }
