@@ -345,8 +345,11 @@ def run_gb300(args):
                                 if world > 1 else {}),
                              l2="inputs+outputs+workspace larger than L2 (no flush needed)",
                              graph=f"{batch.launches} kernel launches ({tuning.stream_groups} stream "
-                                   f"groups: stack, QR, one SVD launch per rank bucket, rebuild) "
-                                   f"captured in one CUDA graph"),
+                                   f"groups: stack, QR, one SVD launch per rank bucket, one "
+                                   f"rebuild launch per padded-k class) captured in one CUDA "
+                                   f"graph",
+                             rebuild="FP64 reflector kernel" if args.dfma_rebuild else
+                                     "tensor cores (exact bf16 digit products) for a + c <= 64"),
               "gpu_launches": batch.launches * args.steps,
               "tuning": dict(tuning.as_dict(), autotune_ms_per_execute=tuned_ms,
                              autotune_s=round(tune_s, 2)),
@@ -356,16 +359,32 @@ def run_gb300(args):
         barrier(world)
         return
 
-    # ---- per-phase timing: the four phases back to back, events between ----
+    # ---- per-phase timing: each phase's launches captured in a CUDA graph of
+    # their own (as the step runs them: direct launches over dozens of group
+    # and bucket streams are falsely serialised), replayed back to back in
+    # phase order with events between ----
     phases = [("stack", 1), ("qr", 2), ("svd", 4), ("rebuild", 8)]
     reps = 3
+    ph_graphs = []
+    for nm, bit in phases:
+        g = torch.cuda.CUDAGraph()
+        side.wait_stream(stream)
+        with torch.cuda.stream(side):
+            with torch.cuda.graph(g, stream=side):
+                batch.execute_phases(bit, side.cuda_stream)
+        stream.wait_stream(side)
+        ph_graphs.append(g)
+    torch.cuda.synchronize(dev)
+    for g in ph_graphs:   # upload / warm
+        g.replay()
+    torch.cuda.synchronize(dev)
     ph_ms = {nm: 0.0 for nm, _ in phases}
     for _ in range(reps):
         evs = [torch.cuda.Event(enable_timing=True) for _ in range(len(phases) + 1)]
         torch.cuda.synchronize(dev)
         evs[0].record(stream)
-        for q, (nm, bit) in enumerate(phases):
-            batch.execute_phases(bit, stream.cuda_stream)
+        for q, g in enumerate(ph_graphs):
+            g.replay()
             evs[q + 1].record(stream)
         torch.cuda.synchronize(dev)
         for q, (nm, _) in enumerate(phases):
@@ -402,6 +421,26 @@ def run_gb300(args):
                                          "MEASURED_PEAKS.json has no FP64 figure)",
                           "peak_probe": ceiling,
                           "flops_basis": "reference flop model (flop_counts.c) of that phase"}
+
+    # ---- the rebuild on the tensor cores: tensor work executed and the FP64
+    # rate it stands in for ----
+    if not args.dfma_rebuild:
+        ks_r = [(t.a + t.c, int(r)) for t, r in zip(tasks, ranks)]
+        tflop = tc_rebuild_tensor_flops(nb, ks_r)
+        bf16_peak = measured_peak("bf16_tflops")
+        t_s = ph_ms["rebuild"] / 1e3
+        result["rebuild_tensor_cores"] = {
+            "kernel": "rebuild_tc_kernel / rebuild_tc_wide_kernel (tcgen05.mma kind::f16, bf16 "
+                      "digit slices, FP32 accumulators in tensor memory)",
+            "updates_on_tensor_cores": sum(1 for k_, _ in ks_r if k_ <= 64),
+            "tensor_flop_executed": tflop, "tensor_tflops": tflop / t_s / 1e12,
+            "bf16_peak_tflops": bf16_peak,
+            "frac_of_bf16_peak": (tflop / t_s / 1e12 / bf16_peak) if bf16_peak else None,
+            "fp64_equivalent_tflops": phase_model["rebuild"] / t_s / 1e12,
+            "fp64_equivalent_frac_of_fp64_peak": phase_model["rebuild"] / t_s / 1e12 / peak,
+            "note": "the FP64 reflector products (reference flop model) ran as exact digit "
+                    "products on the tensor cores at this FP64-equivalent rate; the tensor work "
+                    "counts every MMA as issued (padding rows and zero slices included)"}
 
     # ---- accuracy on a sample of the timed updates vs the oracle and the
     # exact dense update (rel err <= acc is the metric's condition) ----
@@ -1586,6 +1625,46 @@ def fp64_peak(L, torch, dev) -> float:
     """FP64 ceiling in TFLOP/s, measured now (hcore_gpu_fp64_peak: the DMMA
     m16n8k16 probe; DMMA and DFMA share the FP64 pipe on this GPU)."""
     return float(L.hcore_gpu_fp64_peak(torch.cuda.current_stream(dev).cuda_stream))
+
+
+def measured_peak(key):
+    """A peak from MEASURED_PEAKS.json beside this file (None when absent)."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                               "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)[key])
+    except Exception:
+        return None
+
+
+def tc_rebuild_tensor_flops(nb, ks_r):
+    """Tensor FLOP one execute issues in the tensor-core rebuild, mirroring
+    the kernel's MMA loops (hc_rebuild_tc.cu): per (update, side) with k <=
+    64, padded KP = 16/32/48/64 and rp = r rounded up to 16, the Gram passes
+    (M/128 chunks, 8 K steps) and the output tiles (M/128, KP/16 K steps),
+    each an M=128 MMA per digit slice i and piece of planes i..7 whose N is
+    (planes in the piece) x (plane width)."""
+    def pieces(width):
+        per = 256 // width
+        out = []
+        for i in range(7):
+            d0 = i
+            while d0 < 8:
+                d1 = min(d0 + per, 8)
+                out.append((d1 - d0) * width)
+                d0 = d1
+        return out
+    total = 0
+    nch = (nb + 127) // 128
+    for k, r in ks_r:
+        if k > 64 or r <= 0:
+            continue
+        KP = 16 if k <= 16 else 32 if k <= 32 else 48 if k <= 48 else 64
+        rp = (r + 15) // 16 * 16
+        gram = nch * 8 * sum(2 * 128 * n * 16 for n in pieces(KP))
+        outp = nch * (KP // 16) * sum(2 * 128 * n * 16 for n in pieces(rp))
+        total += 2 * (gram + outp)
+    return float(total)
 
 
 def fp64_ceiling(L, torch, dev, index, seconds=1.5) -> dict:

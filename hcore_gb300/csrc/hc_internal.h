@@ -133,6 +133,8 @@ cudaError_t launch_rebuild(const Desc *d_desc, const int *d_idx, const int *d_ca
 // (padded k: 16, 32, 48 or 64; 0 above kTcMaxK); configure_rebuild_tc sets
 // the variants' shared-memory attributes (not capturable).
 constexpr int kTcMaxK = 64;
+// kernel launches of the rebuild phase of one execute (hc_kernels.cu)
+int rebuild_launches(const LaunchShape &shape, bool fp64);
 int tc_rebuild_class(int k);
 cudaError_t configure_rebuild_tc();
 void launch_rebuild_tc(const Desc *d_desc, int n, const double *ws, const int *d_rank,

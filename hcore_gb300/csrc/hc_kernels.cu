@@ -1168,6 +1168,19 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
     return cudaGetLastError();
 }
 
+int rebuild_launches(const LaunchShape &shape, bool fp64) {
+    if (!fp64 || shape.mixed || !shape.tc_rebuild || shape.nbuckets <= 0) return 1;
+    int launches = 0, b = 0;
+    while (b < shape.nbuckets) {
+        const int cls = tc_rebuild_class(shape.buckets[b].K);
+        int count = 0;
+        while (b < shape.nbuckets && tc_rebuild_class(shape.buckets[b].K) == cls)
+            count += shape.buckets[b++].count;
+        launches += count > 0;
+    }
+    return launches;
+}
+
 // Rebuild of updates that ended with HCORE_GPU_S_STORAGE: their U_r and
 // V_r S_r are still in the workspace, so only the rebuild phase runs again,
 // over descriptors that point at the new output storage.

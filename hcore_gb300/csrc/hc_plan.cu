@@ -819,8 +819,9 @@ extern "C" int hcore_gpu_plan_sweeps(hcore_gpu_plan p, int *sweeps, void *stream
 
 extern "C" int hcore_gpu_plan_launches(hcore_gpu_plan p) {
     if (!p || p->n == 0) return 0;
-    auto count = [](const LaunchShape &sh) {
-        int c = 3;   // stack, QR, rebuild
+    const bool fp64 = p->prec == HCORE_GPU_F64;
+    auto count = [fp64](const LaunchShape &sh) {
+        int c = 2 + rebuild_launches(sh, fp64);   // stack, QR, rebuild
         for (int b = 0; b < sh.nbuckets; ++b) c += sh.buckets[b].count > 0;
         return c;
     };
