@@ -101,6 +101,9 @@ struct LaunchShape {
     // FP64 plans: the rebuild of updates with k <= kTcMaxK on the tensor cores
     // (hc_rebuild_tc.cu); off: the DFMA reflector kernel for every update
     bool tc_rebuild = true;
+    // FP64 plans: the QR of updates with k <= kTcMaxK blocked, with the
+    // trailing updates on the tensor cores; off: the unblocked FP64 kernel
+    bool tc_qr = true;
     int nbuckets = 0;
     Bucket buckets[kMaxBuckets];
     // optional fork/join resources so the bucket launches overlap: one stream
@@ -135,6 +138,27 @@ cudaError_t launch_rebuild(const Desc *d_desc, const int *d_idx, const int *d_ca
 constexpr int kTcMaxK = 64;
 // kernel launches of the rebuild phase of one execute (hc_kernels.cu)
 int rebuild_launches(const LaunchShape &shape, bool fp64);
+
+// Blocked QR (FP64 plans, a + c <= kTcMaxK): 16-column panels factored by the
+// FP64 register kernel, the last panel taking the rest when it is at most 24
+// columns wide; between panels the trailing columns are updated on the tensor
+// cores (hc_qr_tc.cu).  Returns false when panel p does not exist.
+__host__ __device__ inline bool qr_panel_bounds(int k, int p, int &c0, int &c1) {
+    const int q = k > 24 ? (k - 24 + 15) / 16 : 0;   // full panels before the last
+    if (p < 0 || p > q) return false;
+    c0 = 16 * p;
+    c1 = p < q ? c0 + 16 : k;
+    return true;
+}
+constexpr int kQrPanels = 4;  // panels of the widest blocked QR (k = 64)
+// tensor-core trailing update: variant by 16 + (columns right of the panel)
+// rounded up (32, 48 or 64; 0 above 64); launches only
+int qr_update_class(int rows);
+cudaError_t configure_qr_tc();
+void launch_qr_update_tc(const Desc *d_desc, int n, double *ws, int panel, int *d_status,
+                         int rclass, cudaStream_t s);
+// kernel launches of the QR phase of one execute (hc_kernels.cu)
+int qr_launches(const LaunchShape &shape, bool fp64);
 int tc_rebuild_class(int k);
 cudaError_t configure_rebuild_tc();
 void launch_rebuild_tc(const Desc *d_desc, int n, const double *ws, const int *d_rank,

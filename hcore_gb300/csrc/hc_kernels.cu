@@ -285,14 +285,19 @@ __device__ __forceinline__ void make_reflector(T (&x)[RPL], int j, int M, int la
 // NW warps per CTA (a tuning choice): 8 gives the shortest path per update;
 // 4 or 2 keep the same warps per SM in two or four times as many CTAs, so
 // that one CTA's per-column barrier stall is covered by the others.
+// panel < 0: all k columns; panel p >= 0: the columns [c0, c1) of the blocked
+// QR's panel p (qr_panel_bounds), whose earlier columns are already factored
+// and whose own columns already hold the earlier panels' updates.
 template <typename T, int RPL, int NW>
 __global__ void __launch_bounds__(NW * 32, (RPL <= 32 ? 2 : 1) * (8 / NW))
-    geqrf_kernel(const Desc *__restrict__ descs, T *__restrict__ ws) {
+    geqrf_kernel(const Desc *__restrict__ descs, T *__restrict__ ws, int panel) {
     __shared__ T sv[2][32 * RPL];
     __shared__ T s_tau[2];
     const Desc d = descs[blockIdx.x];
     if (d.status0) return;
     const int M = d.M, k = d.k;
+    int c0 = 0, c1 = k;
+    if (panel >= 0 && !qr_panel_bounds(k, panel, c0, c1)) return;
     const WsLayout L = ws_layout(d);
     const int side = blockIdx.y;
     T *A = ws + d.ws + (side ? L.VB : L.UA);
@@ -301,19 +306,20 @@ __global__ void __launch_bounds__(NW * 32, (RPL <= 32 ? 2 : 1) * (8 / NW))
     T x[RPL];
 
     if (warp == 0) {
+        const T *A0 = A + (size_t)c0 * M;
 #pragma unroll
         for (int t = 0; t < RPL; ++t) {
             const int i = lane + 32 * t;
-            x[t] = i < M ? A[i] : T(0);
+            x[t] = i < M ? A0[i] : T(0);
         }
-        make_reflector<T, RPL>(x, 0, M, lane, A, sv[0], &s_tau[0], tau);
+        make_reflector<T, RPL>(x, c0, M, lane, A + (size_t)c0 * M, sv[0], &s_tau[0], tau);
     }
     __syncthreads();
-    for (int j = 0; j + 1 < k; ++j) {
-        const int cur = j & 1;
+    for (int j = c0; j + 1 < c1; ++j) {
+        const int cur = (j - c0) & 1;
         const T *v = sv[cur];
         const T tj = s_tau[cur];
-        for (int col = j + 1 + warp; col < k; col += NW) {
+        for (int col = j + 1 + warp; col < c1; col += NW) {
             T *Ac = A + (size_t)col * M;
 #pragma unroll
             for (int t = 0; t < RPL; ++t) {
@@ -1007,10 +1013,63 @@ static cudaError_t set_apply_smem() {
 }
 
 template <typename T, int RPL>
-static void launch_geqrf(const Desc *d_desc, int n, T *ws, int warps, cudaStream_t s) {
-    if (warps == 2) geqrf_kernel<T, RPL, 2><<<dim3(n, 2), 64, 0, s>>>(d_desc, ws);
-    else if (warps == 4) geqrf_kernel<T, RPL, 4><<<dim3(n, 2), 128, 0, s>>>(d_desc, ws);
-    else geqrf_kernel<T, RPL, 8><<<dim3(n, 2), 256, 0, s>>>(d_desc, ws);
+static void launch_geqrf(const Desc *d_desc, int n, T *ws, int warps, int panel, cudaStream_t s) {
+    if (n <= 0) return;
+    if (warps == 2) geqrf_kernel<T, RPL, 2><<<dim3(n, 2), 64, 0, s>>>(d_desc, ws, panel);
+    else if (warps == 4) geqrf_kernel<T, RPL, 4><<<dim3(n, 2), 128, 0, s>>>(d_desc, ws, panel);
+    else geqrf_kernel<T, RPL, 8><<<dim3(n, 2), 256, 0, s>>>(d_desc, ws, panel);
+}
+
+template <typename T>
+static void launch_geqrf_all(const Desc *d_desc, int n, T *ws, int warps, int rpl, int panel,
+                             cudaStream_t s) {
+    if (rpl <= 4) launch_geqrf<T, 4>(d_desc, n, ws, warps, panel, s);
+    else if (rpl <= 8) launch_geqrf<T, 8>(d_desc, n, ws, warps, panel, s);
+    else if (rpl <= 16) launch_geqrf<T, 16>(d_desc, n, ws, warps, panel, s);
+    else if (rpl <= 32) launch_geqrf<T, 32>(d_desc, n, ws, warps, panel, s);
+    else launch_geqrf<T, 64>(d_desc, n, ws, warps, panel, s);
+}
+
+// Launch plan of the blocked QR over a shape's k-sorted buckets: the
+// descriptors above kTcMaxK (a prefix) take the unblocked kernel; for the
+// rest, panel p runs over every descriptor that has one, and the trailing
+// update after panel p once per update-size class.  fn(kind, start, count,
+// panel, class): kind 0 unblocked QR, 1 panel, 2 trailing update.
+template <typename F>
+static void qr_plan(const LaunchShape &shape, int n, F &&fn) {
+    int split = 0;  // first descriptor with k <= kTcMaxK
+    int b = 0;
+    while (b < shape.nbuckets && shape.buckets[b].K > kTcMaxK) split += shape.buckets[b++].count;
+    if (split > 0) fn(0, 0, split, -1, 0);
+    if (split >= n || b >= shape.nbuckets) return;
+    const int kmax = shape.buckets[b].K;
+    for (int p = 0; p < kQrPanels; ++p) {
+        int c0, c1;
+        if (!qr_panel_bounds(kmax, p, c0, c1)) break;
+        fn(1, split, n - split, p, 0);
+        // trailing updates: descriptors whose panel p is not their last
+        int bb = b, start = split;
+        while (bb < shape.nbuckets) {
+            const int K = shape.buckets[bb].K;
+            if (!qr_panel_bounds(K, p, c0, c1) || c1 >= K) break;  // sorted: none below
+            const int cls = qr_update_class(K - 16 * p);
+            int count = 0;
+            while (bb < shape.nbuckets && qr_panel_bounds(shape.buckets[bb].K, p, c0, c1) &&
+                   c1 < shape.buckets[bb].K && qr_update_class(shape.buckets[bb].K - 16 * p) == cls)
+                count += shape.buckets[bb++].count;
+            if (count > 0) fn(2, start, count, p, cls);
+            start += count;
+        }
+    }
+}
+
+int qr_launches(const LaunchShape &shape, bool fp64) {
+    if (!fp64 || !shape.tc_qr || shape.nbuckets <= 0) return 1;
+    int c = 0;
+    int n = 0;
+    for (int b = 0; b < shape.nbuckets; ++b) n += shape.buckets[b].count;
+    qr_plan(shape, n, [&](int, int, int count, int, int) { c += count > 0; });
+    return c;
 }
 
 template <typename T>
@@ -1061,6 +1120,7 @@ static cudaError_t configure_recompress_once(int dev, int *svd_smem_kmax, int *s
     e = set_apply_smem<T, T>();
     if (e == cudaSuccess) e = set_apply_smem<T, float>();
     if (e == cudaSuccess && sizeof(T) == sizeof(double)) e = configure_rebuild_tc();
+    if (e == cudaSuccess && sizeof(T) == sizeof(double)) e = configure_qr_tc();
     if (e != cudaSuccess) return e;
     // the attribute is per kernel, not per plan: allow the largest size any
     // plan may launch with, so plans of different k coexist
@@ -1101,11 +1161,17 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
     }
     if (phases & kPhaseQR) {
         const int qw = shape.qr_warps;
-        if (rpl <= 4) launch_geqrf<T, 4>(d_desc, n, ws, qw, s);
-        else if (rpl <= 8) launch_geqrf<T, 8>(d_desc, n, ws, qw, s);
-        else if (rpl <= 16) launch_geqrf<T, 16>(d_desc, n, ws, qw, s);
-        else if (rpl <= 32) launch_geqrf<T, 32>(d_desc, n, ws, qw, s);
-        else launch_geqrf<T, 64>(d_desc, n, ws, qw, s);
+        if (sizeof(T) == sizeof(double) && shape.tc_qr && shape.nbuckets > 0) {
+            qr_plan(shape, n, [&](int kind, int start, int count, int p, int cls) {
+                if (count <= 0) return;
+                if (kind == 2)
+                    launch_qr_update_tc(d_desc + start, count, (double *)ws, p, d_status, cls, s);
+                else
+                    launch_geqrf_all<T>(d_desc + start, count, ws, qw, rpl, p, s);
+            });
+        } else {
+            launch_geqrf_all<T>(d_desc, n, ws, qw, rpl, -1, s);
+        }
     }
     if (phases & kPhaseSVD) {
         // buckets run concurrently (largest k first) when the plan provides

@@ -78,6 +78,11 @@ extern "C" {
  * hc_rebuild_tc.cu).  This flag keeps the FP64 (DFMA) reflector kernel for
  * every update instead. */
 #define HCORE_GPU_DFMA_REBUILD 0x8
+/* FP64 plans factor the stacked matrices of updates with a + c <= 64 as a
+ * blocked Householder QR: 16-column panels in FP64, the trailing columns
+ * updated between panels on the tensor cores, FP64-accurate (hc_qr_tc.cu).
+ * This flag keeps the unblocked FP64 QR for every update instead. */
+#define HCORE_GPU_UNBLOCKED_QR 0x10
 
 /* One low-rank update.  Factors are column-major with the given leading
  * dimensions; every factor has M rows.  Ranks are plain ints. */
