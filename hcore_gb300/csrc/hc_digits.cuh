@@ -133,10 +133,19 @@ __device__ __forceinline__ void digits7_fast(long long X, uint32_t (&f)[7]) {
     f[0] = __float_as_uint(__uint_as_float(0x4B000000u | (hi >> 16)) - c);
 }
 
+// Seven 16-byte core-matrix rows of zeros (a padding row of every plane).
+__device__ __forceinline__ void zero8(unsigned char *dst, int slice_stride) {
+#pragma unroll
+    for (int s = 0; s < 7; ++s)
+        *reinterpret_cast<uint4 *>(dst + s * slice_stride) = make_uint4(0, 0, 0, 0);
+}
+
 // Slice eight values that share the scale 2^E (consecutive along K) into
-// seven 16-byte core-matrix rows, one per digit plane, slice_stride apart.
+// seven 16-byte core-matrix rows, one per digit plane, slice_stride apart;
+// with dst2 != nullptr the same rows also go to a second operand buffer.
 __device__ __forceinline__ void slice8(const double (&x)[8], int E, unsigned char *dst,
-                                       int slice_stride) {
+                                       int slice_stride, unsigned char *dst2 = nullptr,
+                                       int slice_stride2 = 0) {
     uint32_t w[7][4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -150,6 +159,12 @@ __device__ __forceinline__ void slice8(const double (&x)[8], int E, unsigned cha
     for (int s = 0; s < 7; ++s)
         *reinterpret_cast<uint4 *>(dst + s * slice_stride) =
             make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+    if (dst2) {
+#pragma unroll
+        for (int s = 0; s < 7; ++s)
+            *reinterpret_cast<uint4 *>(dst2 + s * slice_stride2) =
+                make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+    }
 }
 
 

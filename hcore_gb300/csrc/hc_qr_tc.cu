@@ -165,10 +165,14 @@ __global__ void __maxnreg__(128)
 #pragma unroll
             for (int q = 0; q < kItems; ++q) {
                 const int jb = jh + 2 * q, jr = jb * 8 + jj;
-                const int E = jr < 16 ? 1 : (jr - 16 < nt ? colE[jr - 16] : 0);
-                slice8(pre[q], E, R0 + jb * 2048 + g * 128 + jj * 16, C::kSliceA);
+                unsigned char *dst = R0 + jb * 2048 + g * 128 + jj * 16;
                 if (jr < 16)   // the reflector rows are the B operand too
-                    slice8(pre[q], 1, RB + jb * 2048 + g * 128 + jj * 16, C::kSliceB);
+                    slice8(pre[q], 1, dst, C::kSliceA, RB + jb * 2048 + g * 128 + jj * 16,
+                           C::kSliceB);
+                else if (jr - 16 < nt)
+                    slice8(pre[q], colE[jr - 16], dst, C::kSliceA);
+                else
+                    zero8(dst, C::kSliceA);
             }
             tc::fence_async_smem();
             tc::fence_before_sync();

@@ -181,8 +181,11 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
             reinterpret_cast<uint4 *>(R0 + 7 * C::kSliceG)[e] = make_uint4(0, 0, 0, 0);
         for (int ch = 0; ch < nchunks; ++ch) {
 #pragma unroll
-            for (int q = 0; q < kItems; ++q)
-                slice8(pre[q], 1, R0 + (jh + 2 * q) * 2048 + g * 128 + jj * 16, C::kSliceG);
+            for (int q = 0; q < kItems; ++q) {
+                unsigned char *dst = R0 + (jh + 2 * q) * 2048 + g * 128 + jj * 16;
+                if ((jh + 2 * q) * 8 + jj < k) slice8(pre[q], 1, dst, C::kSliceG);
+                else zero8(dst, C::kSliceG);   // padding column of Y
+            }
             tc::fence_async_smem();
             tc::fence_before_sync();
             __syncthreads();
@@ -316,10 +319,12 @@ __device__ __forceinline__ void rebuild_tc_body(const Desc *__restrict__ descs,
         for (int tile = 0; tile < ntiles; ++tile) {
             const int row = tile * 128 + lrow;
 #pragma unroll
-            for (int q = 0; q < kItems; ++q)
-                slice8(pre[q], 1,
-                       R0 + (lrow >> 3) * (16 * KP) + (jh + 2 * q) * 128 + (lrow & 7) * 16,
-                       C::kSliceA);
+            for (int q = 0; q < kItems; ++q) {
+                unsigned char *dst =
+                    R0 + (lrow >> 3) * (16 * KP) + (jh + 2 * q) * 128 + (lrow & 7) * 16;
+                if ((jh + 2 * q) * 8 < k) slice8(pre[q], 1, dst, C::kSliceA);
+                else zero8(dst, C::kSliceA);   // padding columns of Y
+            }
             tc::fence_async_smem();
             tc::fence_before_sync();
             __syncthreads();
