@@ -33,12 +33,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "TLR-GEMM updates/s batched vs plain per-tile on 1 GB300 at rel err <= acc"
-# DRAM bytes (read + write) per algorithmic byte of each phase's kernel:
-# dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of 300 updates
-# in a single launch (a working set beyond L2, as in each launch of this
-# workload), divided by that launch's algorithmic bytes.  The full phase's
+# DRAM bytes (read + write) per algorithmic byte of each phase's kernels:
+# dram__bytes_read.sum + dram__bytes_write.sum from ncu captures of the
+# 300-update case (a working set beyond L2), divided by the algorithmic bytes.
+# QR: every panel and trailing-update launch of one execute of the blocked QR
+# (406 MB against 353 MB); stack: one 300-update launch.  The full phase's
 # traffic is this ratio times its own algorithmic bytes.
-DRAM_PER_ALG_BYTE = {"stack": 0.46, "qr": 4.44, "svd": None, "rebuild": 0.97}
+DRAM_PER_ALG_BYTE = {"stack": 0.46, "qr": 1.15, "svd": None, "rebuild": None}
 WORKLOAD = dict(workload="TLR Cholesky panel-0 Schur updates (HCORE_dgemm recompression)",
                 points=65536, dim=2, nb=1024, tiles_per_dim=64, kernel="exp(-|x-y|^2/0.01)",
                 acc=1e-8, maxrank=128, tile_compression="relative sigma >= acc*sigma_max",
@@ -413,9 +414,10 @@ def run_gb300(args):
     result["roofline"] = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak,
                           "unit": "TFLOP/s", "frac": achieved / peak,
                           "traffic": (ratio * alg_bytes[dom]) if ratio else None,
-                          "traffic_basis": "ncu DRAM bytes per algorithmic byte of this kernel in "
-                                           "one 300-update launch (working set beyond L2), times "
-                                           f"this phase's algorithmic bytes ({alg_bytes[dom]:.3e})",
+                          "traffic_basis": "ncu DRAM bytes per algorithmic byte of this phase's "
+                                           "kernels in the 300-update case (working set beyond "
+                                           "L2), times this phase's algorithmic bytes "
+                                           f"({alg_bytes[dom]:.3e})",
                           "peak_source": "FP64 issue-rate probe timed live (DMMA and DFMA "
                                          "share the FP64 pipe at 1.06-1.10 TFLOP/s on GB300; "
                                          "MEASURED_PEAKS.json has no FP64 figure)",
