@@ -46,6 +46,7 @@ STAGE_INPUTS = 0x2
 MIXED_FACTORS = 0x4
 DFMA_REBUILD = 0x8
 UNBLOCKED_QR = 0x10
+TC_STACK = 0x20
 STATUS = {0: "ok", 1: "zero rank", 2: "rank sum > 2*maxrk", 3: "rank sum > ld_newV",
           4: "new rank > maxrk", 5: "new rank > storage maxrank", 6: "Jacobi did not converge",
           7: "bad shape", 8: "tensor-core wait timed out"}

@@ -20,7 +20,8 @@ OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libhcore_gb300.so")
 SOURCES = ["hc_kernels.cu", "hc_plan.cu", "hc_dropin.cu", "hc_dense.cu", "hc_noalloc.cu",
            "hc_mlp.cu", "hc_tlr.cu", "hc_compress.cu", "hc_probe.cu",
-           "hc_panel.cu", "hc_zkernels.cu", "hc_rebuild_tc.cu", "hc_qr_tc.cu"]
+           "hc_panel.cu", "hc_zkernels.cu", "hc_rebuild_tc.cu", "hc_qr_tc.cu",
+           "hc_stack_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

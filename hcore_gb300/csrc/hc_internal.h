@@ -104,6 +104,9 @@ struct LaunchShape {
     // FP64 plans: the QR of updates with k <= kTcMaxK blocked, with the
     // trailing updates on the tensor cores; off: the unblocked FP64 kernel
     bool tc_qr = true;
+    // FP64 plans, opt-in (HCORE_GPU_TC_STACK): the stack's products F and G on
+    // the tensor cores for updates that stack_tc_eligible accepts
+    bool tc_stack = false;
     int nbuckets = 0;
     Bucket buckets[kMaxBuckets];
     // optional fork/join resources so the bucket launches overlap: one stream
@@ -159,6 +162,17 @@ void launch_qr_update_tc(const Desc *d_desc, int n, double *ws, int panel, int *
                          int rclass, cudaStream_t s);
 // kernel launches of the QR phase of one execute (hc_kernels.cu)
 int qr_launches(const LaunchShape &shape, bool fp64);
+
+// Stack phase products on the tensor cores (hc_stack_tc.cu): F = AV^T BV and
+// G = BU F^T of updates with a low-rank B, 1 <= a <= 64 and 1 <= b <= 32; the
+// stack kernel then only copies the stacked factors of those updates.
+constexpr int kStackTcMaxA = 64, kStackTcMaxB = 32;
+__host__ __device__ inline bool stack_tc_eligible(const Desc &d) {
+    return !d.status0 && !d.Bd && d.a >= 1 && d.a <= kStackTcMaxA && d.b >= 1 &&
+           d.b <= kStackTcMaxB;
+}
+cudaError_t configure_stack_tc();
+void launch_stack_tc(const Desc *d_desc, int n, double *ws, int *d_status, cudaStream_t s);
 int tc_rebuild_class(int k);
 cudaError_t configure_rebuild_tc();
 void launch_rebuild_tc(const Desc *d_desc, int n, const double *ws, const int *d_rank,

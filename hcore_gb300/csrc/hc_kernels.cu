@@ -83,9 +83,11 @@ __device__ __forceinline__ float flip_sign(float x) {
 // ---------------------------------------------------------------------------
 // phase 1: stack the factors
 // ---------------------------------------------------------------------------
+// tc_products: the products F and G of updates that stack_tc_eligible
+// accepts are left to the tensor-core kernel (hc_stack_tc.cu)
 template <typename T, typename Tc>
 __global__ void __launch_bounds__(kThreads) stack_kernel(const Desc *__restrict__ descs,
-                                                         T *__restrict__ ws) {
+                                                         T *__restrict__ ws, bool tc_products) {
     const Desc d = descs[blockIdx.x];
     if (d.status0) return;
     const int M = d.M, a = d.a, b = d.b, c = d.c;
@@ -113,7 +115,7 @@ __global__ void __launch_bounds__(kThreads) stack_kernel(const Desc *__restrict_
         const T x = AU[(size_t)j * d.lda + i];
         UA[(size_t)(c + j) * M + i] = alpha_minus_one ? flip_sign(x) : alpha * x;
     }
-    if (a == 0) return;
+    if (a == 0 || (tc_products && stack_tc_eligible(d))) return;
     T *G = VB + (size_t)c * M;
     if (d.Bd) {
         // dense B: G = B * AV (hcore_dgemm.c:262-271)
@@ -1121,6 +1123,7 @@ static cudaError_t configure_recompress_once(int dev, int *svd_smem_kmax, int *s
     if (e == cudaSuccess) e = set_apply_smem<T, float>();
     if (e == cudaSuccess && sizeof(T) == sizeof(double)) e = configure_rebuild_tc();
     if (e == cudaSuccess && sizeof(T) == sizeof(double)) e = configure_qr_tc();
+    if (e == cudaSuccess && sizeof(T) == sizeof(double)) e = configure_stack_tc();
     if (e != cudaSuccess) return e;
     // the attribute is per kernel, not per plan: allow the largest size any
     // plan may launch with, so plans of different k coexist
@@ -1156,8 +1159,13 @@ cudaError_t launch_recompress(const Desc *d_desc, int n, T *ws, int *d_rank, int
     const int rpl = (maxM + 31) / 32;
     const bool mixed = shape.mixed && sizeof(T) == sizeof(double);
     if (phases & kPhaseStack) {
-        if (mixed) stack_kernel<T, float><<<n, kThreads, 0, s>>>(d_desc, ws);
-        else stack_kernel<T, T><<<n, kThreads, 0, s>>>(d_desc, ws);
+        if (mixed) {
+            stack_kernel<T, float><<<n, kThreads, 0, s>>>(d_desc, ws, false);
+        } else {
+            const bool tcs = sizeof(T) == sizeof(double) && shape.tc_stack;
+            stack_kernel<T, T><<<n, kThreads, 0, s>>>(d_desc, ws, tcs);
+            if (tcs) launch_stack_tc(d_desc, n, (double *)ws, d_status, s);
+        }
     }
     if (phases & kPhaseQR) {
         const int qw = shape.qr_warps;

@@ -599,13 +599,16 @@ extern "C" int hcore_gpu_plan_create_tuned(hcore_gpu_plan *plan, int precision, 
         const bool mixed = (flags & HCORE_GPU_MIXED_FACTORS) && precision == HCORE_GPU_F64;
         const bool tcr = !(flags & HCORE_GPU_DFMA_REBUILD);
         const bool tcq = !(flags & HCORE_GPU_UNBLOCKED_QR);
+        const bool tcs = (flags & HCORE_GPU_TC_STACK) != 0;
         p->shape.mixed = mixed;
         p->shape.tc_rebuild = tcr;
         p->shape.tc_qr = tcq;
+        p->shape.tc_stack = tcs;
         for (auto &g : p->groups) {
             g.shape.mixed = mixed;
             g.shape.tc_rebuild = tcr;
             g.shape.tc_qr = tcq;
+            g.shape.tc_stack = tcs;
         }
         if (ce != cudaSuccess) {
             set_error("hcore_gpu_plan_create: %s", cudaGetErrorString(ce));
@@ -824,7 +827,9 @@ extern "C" int hcore_gpu_plan_launches(hcore_gpu_plan p) {
     if (!p || p->n == 0) return 0;
     const bool fp64 = p->prec == HCORE_GPU_F64;
     auto count = [fp64](const LaunchShape &sh) {
-        int c = 1 + qr_launches(sh, fp64) + rebuild_launches(sh, fp64);  // stack, QR, rebuild
+        // stack (and its tensor-core products), QR, SVD buckets, rebuild
+        int c = 1 + (fp64 && sh.tc_stack && !sh.mixed) + qr_launches(sh, fp64) +
+                rebuild_launches(sh, fp64);
         for (int b = 0; b < sh.nbuckets; ++b) c += sh.buckets[b].count > 0;
         return c;
     };

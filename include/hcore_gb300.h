@@ -83,6 +83,11 @@ extern "C" {
  * updated between panels on the tensor cores, FP64-accurate (hc_qr_tc.cu).
  * This flag keeps the unblocked FP64 QR for every update instead. */
 #define HCORE_GPU_UNBLOCKED_QR 0x10
+/* FP64 plans: form the stack's products F = AV^T BV and G = BU F^T of updates
+ * with a low-rank B, 1 <= a <= 64 and 1 <= b <= 32 on the tensor cores,
+ * FP64-accurate (hc_stack_tc.cu), instead of in FP64.  Off by default: on the
+ * TLR panel workload (a, b ~ 17) it measured slower than the FP64 products. */
+#define HCORE_GPU_TC_STACK 0x20
 
 /* One low-rank update.  Factors are column-major with the given leading
  * dimensions; every factor has M rows.  Ranks are plain ints. */
