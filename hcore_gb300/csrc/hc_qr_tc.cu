@@ -39,30 +39,39 @@ constexpr int kShiftW = 54;
 constexpr int kShiftU = 53;
 
 // Shared memory of the RP variant (RP = 16 + n_t rounded up to 16):
-//   R0: seven digit slices of [Y_p | A_t]^T (RP rows x 128 rows of A each;
-//       the last is read as a 128-row operand); after the Gram pass: the
-//       FP64 matrices G_p (16 x 16), W (16 x n_t), W', then the output pass's
-//       seven slices of a 128-row tile of Y_p (128 x 16) and the digit
-//       slices of W'^T
-//   RB: the seven digit slices of Y_p^T (16 rows x 128) and a zero slice
+//   R0: two buffers of seven digit slices of [Y_p | A_t]^T (RP rows x 64
+//       rows of A each; a slice is read as a 128-row operand, so the space
+//       after the second buffer covers 16 row groups past its last slice);
+//       after the Gram pass: two buffers of the output pass's seven slices
+//       of a 128-row tile of Y_p (128 x 16), the digit slices of W'^T and
+//       the FP64 matrices G_p (16 x 16), W (16 x n_t), W'
+//   RB: two buffers of the seven digit slices of Y_p^T (16 rows x 64) and a
+//       zero slice
+// While the MMAs of one chunk run, the threads slice the next chunk into the
+// other buffer; the Gram's accumulators (8 planes x 16 columns) are double
+// buffered in tensor memory too, so a chunk's drain overlaps the next
+// chunk's MMAs.
 template <int RP>
 struct QrCfg {
-    static constexpr int kSliceA = (RP / 8) * 2048;
-    static constexpr int kR0 = 6 * kSliceA + 16 * 2048;
-    static constexpr int kSliceB = 2 * 2048;
-    static constexpr int kRB = 8 * kSliceB;
+    static constexpr int kSliceA = (RP / 8) * 1024;
+    static constexpr int kBufA = 7 * kSliceA;
+    static constexpr int kSliceB = 2 * 1024;
+    static constexpr int kBufB = 8 * kSliceB;
+    static constexpr int kRB = 2 * kBufB;
     static constexpr int kMisc = 2048;
+    // output pass layout inside R0
+    static constexpr int kOutA = 0;                    // 2 buffers x 7 x 4096
+    static constexpr int kOutB = 2 * 7 * 4096;         // 8 slices x (32 rows x 32 B), per group
+    static constexpr int kG = kOutB + 8 * 32 * 32;     // G_p, 16 x 16 doubles
+    static constexpr int kW = kG + 16 * 16 * 8;        // W, 16 x 48 doubles
+    static constexpr int kWp = kW + 16 * 48 * 8;       // W', 16 x 48 doubles
+    static constexpr int kOutEnd = kWp + 16 * 48 * 8;
+    static constexpr int kGramEnd = 13 * kSliceA + 16 * 1024;
+    static constexpr int kR0 = kGramEnd > kOutEnd ? kGramEnd : kOutEnd;
     // at least 113 KB with 256 tensor-memory columns (the library's rule, see
     // the rebuild kernel): CTAs on one SM never hold more than 512 columns
     static constexpr int kSmem =
         (kR0 + kRB + kMisc) > 113 * 1024 ? (kR0 + kRB + kMisc) : 113 * 1024;
-    // output pass layout inside R0
-    static constexpr int kOutA = 0;                 // 7 x 4096
-    static constexpr int kOutB = 7 * 4096;          // 8 slices x (32 rows x 32 B), per group
-    static constexpr int kG = kOutB + 8 * 32 * 32;  // G_p, 16 x 16 doubles
-    static constexpr int kW = kG + 16 * 16 * 8;     // W, 16 x 48 doubles
-    static constexpr int kWp = kW + 16 * 48 * 8;    // W', 16 x 48 doubles
-    static_assert(kWp + 16 * 48 * 8 <= kR0, "output pass fits in R0");
 };
 
 // entry (i, l) of the panel's reflector block Y_p (column c0 + l of A):
@@ -106,8 +115,10 @@ __global__ void __maxnreg__(128)
     if (tid == 0) tc::mbar_init(mbar, 1);
     if (tid < 48) colE[tid] = 0;
     if (tid < 16) s_tau[tid] = tau[c0 + tid];
-    for (int e = tid; e < C::kSliceB / 16; e += kQThreads)
+    for (int e = tid; e < C::kSliceB / 16; e += kQThreads) {
         reinterpret_cast<uint4 *>(RB + 7 * C::kSliceB)[e] = make_uint4(0, 0, 0, 0);
+        reinterpret_cast<uint4 *>(RB + C::kBufB + 7 * C::kSliceB)[e] = make_uint4(0, 0, 0, 0);
+    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -137,60 +148,81 @@ __global__ void __maxnreg__(128)
         __syncthreads();
     }
 
-    // ---- 1. [Y_p | A_t]^T Y_p, 128 rows of A per pass ------------------------
-    // Row jr of the A operand: reflector c0 + jr (jr < 16) or trailing column
-    // c1 + jr - 16; item q of a thread: operand rows (jh + 2 q) * 8 + jj, the
-    // eight A rows g*8 .. g*8+7 of the chunk.
+    // ---- 1. [Y_p | A_t]^T Y_p, 64 rows of A per pass, double buffered -------
+    // Item it of a chunk: operand row jr = (it >> 6) * 8 + (it & 7) (a
+    // reflector c0 + jr for jr < 16, else trailing column c1 + jr - 16), the
+    // eight A rows ((it >> 3) & 7) * 8 .. + 7 of the chunk.
     long long accW[8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) accW[e] = 0;
     {
-        const int jj = tid & 7, g = (tid >> 3) & 15, jh = tid >> 7;
-        const int nchunks = (M + 127) / 128;
-        double pre[kItems][8];
+        constexpr int kIt = RP * 8, kMaxIt = (kIt + kQThreads - 1) / kQThreads;
+        const int nchunks = (M + 63) / 64;
+        double pre[kMaxIt][8];
         auto value = [&](int i, int jr) -> double {
             if (jr < 16) return ypanel(A, M, c0, i, jr);
             const int c = jr - 16;
             return (c < nt && i < M) ? A[(size_t)(c1 + c) * M + i] : 0.0;
         };
         auto load_chunk = [&](int ch) {
-            const int i0 = ch * 128 + g * 8;
 #pragma unroll
-            for (int q = 0; q < kItems; ++q)
+            for (int q = 0; q < kMaxIt; ++q) {
+                const int it = tid + q * kQThreads;
+                if (it < kIt) {
+                    const int jr = (it >> 6) * 8 + (it & 7), i0 = ch * 64 + ((it >> 3) & 7) * 8;
 #pragma unroll
-                for (int t = 0; t < 8; ++t) pre[q][t] = value(i0 + t, (jh + 2 * q) * 8 + jj);
+                    for (int t = 0; t < 8; ++t) pre[q][t] = value(i0 + t, jr);
+                }
+            }
+        };
+        auto slice_chunk = [&](int buf) {
+#pragma unroll
+            for (int q = 0; q < kMaxIt; ++q) {
+                const int it = tid + q * kQThreads;
+                if (it < kIt) {
+                    const int jj = it & 7, g = (it >> 3) & 7, jb = it >> 6, jr = jb * 8 + jj;
+                    const int off = jb * 1024 + g * 128 + jj * 16;
+                    unsigned char *dst = R0 + buf * C::kBufA + off;
+                    if (jr < 16)   // the reflector rows are the B operand too
+                        slice8(pre[q], 1, dst, C::kSliceA, RB + buf * C::kBufB + off, C::kSliceB);
+                    else if (jr - 16 < nt)
+                        slice8(pre[q], colE[jr - 16], dst, C::kSliceA);
+                    else
+                        zero8(dst, C::kSliceA);
+                }
+            }
+        };
+        auto issue_chunk = [&](int buf) {
+            issue_planes(tbase + buf * 128, mbar, r0 + buf * C::kBufA, C::kSliceA, 1024,
+                         rb + buf * C::kBufB, C::kSliceB, 1024, 4, 16);
         };
         load_chunk(0);
+        slice_chunk(0);
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (tid == 0) issue_chunk(0);
+        if (nchunks > 1) load_chunk(1);
         for (int ch = 0; ch < nchunks; ++ch) {
-#pragma unroll
-            for (int q = 0; q < kItems; ++q) {
-                const int jb = jh + 2 * q, jr = jb * 8 + jj;
-                unsigned char *dst = R0 + jb * 2048 + g * 128 + jj * 16;
-                if (jr < 16)   // the reflector rows are the B operand too
-                    slice8(pre[q], 1, dst, C::kSliceA, RB + jb * 2048 + g * 128 + jj * 16,
-                           C::kSliceB);
-                else if (jr - 16 < nt)
-                    slice8(pre[q], colE[jr - 16], dst, C::kSliceA);
-                else
-                    zero8(dst, C::kSliceA);
+            const int cur = ch & 1;
+            // slice chunk ch + 1 while the MMAs of chunk ch run (its buffer's
+            // last reader, chunk ch - 1, is done)
+            if (ch + 1 < nchunks) {
+                slice_chunk(cur ^ 1);
+                tc::fence_async_smem();
             }
-            tc::fence_async_smem();
-            tc::fence_before_sync();
-            __syncthreads();
-            tc::fence_after_sync();
-            if (tid == 0)
-                issue_planes(tbase, mbar, r0, C::kSliceA, 2048, rb, C::kSliceB, 2048, 8, 16);
-            if (ch + 1 < nchunks) load_chunk(ch + 1);
-            if (!wait_mma()) {
+            if (!wait_mma()) {   // chunk ch done; every thread's slicing and last drain too
                 failed = true;
                 break;
             }
             tc::fence_after_sync();
-            combine_planes<kShiftW>(accW, lane_base + wg * 8, 16);
+            if (tid == 0 && ch + 1 < nchunks) issue_chunk(cur ^ 1);
+            if (ch + 2 < nchunks) load_chunk(ch + 2);
+            combine_planes<kShiftW>(accW, lane_base + cur * 128 + wg * 8, 16);
             tc::fence_before_sync();
-            __syncthreads();
-            tc::fence_after_sync();
         }
+        __syncthreads();
     }
 
     // ---- 2. G_p, W, and W' by forward substitution (FP64) --------------------
@@ -250,19 +282,32 @@ __global__ void __maxnreg__(128)
 #pragma unroll
                 for (int t = 0; t < 8; ++t) pre[t] = ypanel(A, M, c0, row, jh * 8 + t);
             };
-            load_tile(tile0);
-            for (int tile = tile0; tile < ntiles; ++tile) {
-                const int row = tile * 128 + lrow;
-                slice8(pre, 1, R0 + C::kOutA + (lrow >> 3) * 256 + jh * 128 + (lrow & 7) * 16,
+            auto slice_tile = [&](int buf) {
+                slice8(pre, 1,
+                       R0 + C::kOutA + buf * 7 * 4096 + (lrow >> 3) * 256 + jh * 128 +
+                           (lrow & 7) * 16,
                        4096);
-                tc::fence_async_smem();
-                tc::fence_before_sync();
-                __syncthreads();
-                tc::fence_after_sync();
-                if (tid == 0)
-                    issue_planes(tbase, mbar, r0 + C::kOutA, 4096, 256, r0 + C::kOutB, gw * 32,
-                                 256, 1, gw);
-                if (tile + 1 < ntiles) load_tile(tile + 1);
+            };
+            auto issue_tile = [&](int buf) {
+                issue_planes(tbase, mbar, r0 + C::kOutA + buf * 7 * 4096, 4096, 256,
+                             r0 + C::kOutB, gw * 32, 256, 1, gw);
+            };
+            load_tile(tile0);
+            slice_tile(0);
+            tc::fence_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (tid == 0) issue_tile(0);
+            if (tile0 + 1 < ntiles) load_tile(tile0 + 1);
+            for (int tile = tile0; tile < ntiles; ++tile) {
+                const int cur = (tile - tile0) & 1;
+                const int row = tile * 128 + lrow;
+                // slice the next tile while this tile's MMAs run
+                if (tile + 1 < ntiles) {
+                    slice_tile(cur ^ 1);
+                    tc::fence_async_smem();
+                }
                 if (!wait_mma()) {
                     failed = true;
                     break;
@@ -292,8 +337,10 @@ __global__ void __maxnreg__(128)
                     }
                 }
                 tc::fence_before_sync();
-                __syncthreads();
+                __syncthreads();   // the accumulators are read before the next tile's MMAs
                 tc::fence_after_sync();
+                if (tid == 0 && tile + 1 < ntiles) issue_tile(cur ^ 1);
+                if (tile + 2 < ntiles) load_tile(tile + 2);
             }
         }
     }
