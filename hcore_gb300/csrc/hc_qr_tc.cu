@@ -29,7 +29,8 @@ namespace hc {
 namespace {
 using namespace dg;
 
-constexpr int kQThreads = 256;
+constexpr int kQWorkers = 256;              // warps 0-7: slicing, drains, FP64 work
+constexpr int kQThreads = kQWorkers + 32;   // warp 8: issues the MMAs
 constexpr int kQTmemCols = 256;
 // combine shifts S (T = value 2^(110 - E_x - E_y - S)): Gram pass rows
 // |y_j^T y_l| <= 2 and |y_l^T a_c| <= sqrt(2 M) 2^E_c <= 2^6 2^E_c (M <=
@@ -110,6 +111,7 @@ __global__ void __maxnreg__(128)
     const double *tau = ws + d.ws + (side ? L.tauB : L.tauA);
     const int tid = threadIdx.x, warp = tid >> 5;
     const int lrow = tid & 127, wg = tid >> 7;
+    const bool worker = tid < kQWorkers, issuer = tid == kQWorkers;
 
     if (warp == 0) tc::tmem_alloc(tslot, kQTmemCols);
     if (tid == 0) tc::mbar_init(mbar, 1);
@@ -135,13 +137,27 @@ __global__ void __maxnreg__(128)
 
     // ---- 0. scale of each trailing column (its largest exponent) ------------
     {
-        const int ngroups = (M + 7) / 8;
-        for (int e = tid; e < nt * ngroups; e += kQThreads) {
-            const int c = e % nt, i0 = (e / nt) * 8;
-            const double *col = A + (size_t)(c1 + c) * M;
-            int ef = 0;
-            for (int t = 0; t < 8 && i0 + t < M; ++t) ef = max(ef, exp_field(col[i0 + t]));
-            atomicMax(&colE[c], ef);
+        const int ngroups = (M + 7) / 8, total = nt * ngroups;
+        for (int e0 = tid; e0 < total; e0 += 4 * kQThreads) {
+            double v[4][8];   // four items' loads in flight before any is used
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int e = e0 + u * kQThreads;
+                const int c = e % nt, i0 = (e / nt) * 8;
+#pragma unroll
+                for (int t = 0; t < 8; ++t)
+                    v[u][t] = (e < total && i0 + t < M) ? A[(size_t)(c1 + c) * M + i0 + t] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int e = e0 + u * kQThreads;
+                if (e < total) {
+                    int ef = 0;
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) ef = max(ef, exp_field(v[u][t]));
+                    atomicMax(&colE[e % nt], ef);
+                }
+            }
         }
         __syncthreads();
         if (tid < nt) colE[tid] -= 1022;
@@ -156,7 +172,7 @@ __global__ void __maxnreg__(128)
 #pragma unroll
     for (int e = 0; e < 8; ++e) accW[e] = 0;
     {
-        constexpr int kIt = RP * 8, kMaxIt = (kIt + kQThreads - 1) / kQThreads;
+        constexpr int kIt = RP * 8, kMaxIt = (kIt + kQWorkers - 1) / kQWorkers;
         const int nchunks = (M + 63) / 64;
         double pre[kMaxIt][8];
         auto value = [&](int i, int jr) -> double {
@@ -165,9 +181,10 @@ __global__ void __maxnreg__(128)
             return (c < nt && i < M) ? A[(size_t)(c1 + c) * M + i] : 0.0;
         };
         auto load_chunk = [&](int ch) {
+            if (!worker) return;
 #pragma unroll
             for (int q = 0; q < kMaxIt; ++q) {
-                const int it = tid + q * kQThreads;
+                const int it = tid + q * kQWorkers;
                 if (it < kIt) {
                     const int jr = (it >> 6) * 8 + (it & 7), i0 = ch * 64 + ((it >> 3) & 7) * 8;
 #pragma unroll
@@ -176,9 +193,10 @@ __global__ void __maxnreg__(128)
             }
         };
         auto slice_chunk = [&](int buf) {
+            if (!worker) return;
 #pragma unroll
             for (int q = 0; q < kMaxIt; ++q) {
-                const int it = tid + q * kQThreads;
+                const int it = tid + q * kQWorkers;
                 if (it < kIt) {
                     const int jj = it & 7, g = (it >> 3) & 7, jb = it >> 6, jr = jb * 8 + jj;
                     const int off = jb * 1024 + g * 128 + jj * 16;
@@ -202,7 +220,7 @@ __global__ void __maxnreg__(128)
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
-        if (tid == 0) issue_chunk(0);
+        if (issuer) issue_chunk(0);
         if (nchunks > 1) load_chunk(1);
         for (int ch = 0; ch < nchunks; ++ch) {
             const int cur = ch & 1;
@@ -217,9 +235,9 @@ __global__ void __maxnreg__(128)
                 break;
             }
             tc::fence_after_sync();
-            if (tid == 0 && ch + 1 < nchunks) issue_chunk(cur ^ 1);
+            if (issuer && ch + 1 < nchunks) issue_chunk(cur ^ 1);
             if (ch + 2 < nchunks) load_chunk(ch + 2);
-            combine_planes<kShiftW>(accW, lane_base + cur * 128 + wg * 8, 16);
+            if (worker) combine_planes<kShiftW>(accW, lane_base + cur * 128 + wg * 8, 16);
             tc::fence_before_sync();
         }
         __syncthreads();
@@ -230,7 +248,7 @@ __global__ void __maxnreg__(128)
     double *Wm = reinterpret_cast<double *>(R0 + C::kW);   // (l, c) at l + 16 c
     double *Wp = reinterpret_cast<double *>(R0 + C::kWp);  // W', same layout
     if (!failed) {
-        if (lrow < 16 + nt) {
+        if (worker && lrow < 16 + nt) {
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
                 const int l = wg * 8 + e;
@@ -276,13 +294,28 @@ __global__ void __maxnreg__(128)
             for (int e = tid; e < gw * 2; e += kQThreads)
                 reinterpret_cast<uint4 *>(R0 + C::kOutB + 7 * gw * 32)[e] = make_uint4(0, 0, 0, 0);
             double pre[8];
+            double old[2][8];   // the entries this thread updates, loaded before the wait
             const int jh = tid >> 7;
             auto load_tile = [&](int tile) {
+                if (!worker) return;
                 const int row = tile * 128 + lrow;
 #pragma unroll
                 for (int t = 0; t < 8; ++t) pre[t] = ypanel(A, M, c0, row, jh * 8 + t);
             };
+            auto load_old = [&](int tile) {
+                if (!worker) return;
+                const int row = tile * 128 + lrow;
+#pragma unroll
+                for (int m = 0; m < 2; ++m)
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const int c = cg + (wg + 2 * m) * 8 + e;
+                        old[m][e] = (c < nt && row < M && row >= c0)
+                                        ? A[(size_t)(c1 + c) * M + row] : 0.0;
+                    }
+            };
             auto slice_tile = [&](int buf) {
+                if (!worker) return;
                 slice8(pre, 1,
                        R0 + C::kOutA + buf * 7 * 4096 + (lrow >> 3) * 256 + jh * 128 +
                            (lrow & 7) * 16,
@@ -298,11 +331,12 @@ __global__ void __maxnreg__(128)
             tc::fence_before_sync();
             __syncthreads();
             tc::fence_after_sync();
-            if (tid == 0) issue_tile(0);
+            if (issuer) issue_tile(0);
             if (tile0 + 1 < ntiles) load_tile(tile0 + 1);
             for (int tile = tile0; tile < ntiles; ++tile) {
                 const int cur = (tile - tile0) & 1;
                 const int row = tile * 128 + lrow;
+                load_old(tile);
                 // slice the next tile while this tile's MMAs run
                 if (tile + 1 < ntiles) {
                     slice_tile(cur ^ 1);
@@ -313,25 +347,26 @@ __global__ void __maxnreg__(128)
                     break;
                 }
                 tc::fence_after_sync();
+                if (worker) {
 #pragma unroll
-                for (int m = 0; m < 2; ++m) {
-                    const int cb = wg + 2 * m;  // 8-column block of this pass
-                    if (cb * 8 >= gw) continue;
-                    long long a8[8];
+                    for (int m = 0; m < 2; ++m) {
+                        const int cb = wg + 2 * m;  // 8-column block of this pass
+                        if (cb * 8 >= gw) continue;
+                        long long a8[8];
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) a8[e] = 0;
-                    combine_planes<kShiftU>(a8, lane_base + cb * 8, gw);
-                    if (row < M && row >= c0) {
+                        for (int e = 0; e < 8; ++e) a8[e] = 0;
+                        combine_planes<kShiftU>(a8, lane_base + cb * 8, gw);
+                        if (row < M && row >= c0) {
 #pragma unroll
-                        for (int e = 0; e < 8; ++e) {
-                            const int c = cg + cb * 8 + e;
-                            if (c < nt) {
-                                const int p = kShiftU + 1 + wE[c] - 110;
-                                bool ok;
-                                double v = i64_times_pow2(-a8[e], p, ok);
-                                if (!ok) v = scale2((double)(-a8[e]), p);
-                                double *pa = A + (size_t)(c1 + c) * M + row;
-                                *pa = *pa + v;
+                            for (int e = 0; e < 8; ++e) {
+                                const int c = cg + cb * 8 + e;
+                                if (c < nt) {
+                                    const int p = kShiftU + 1 + wE[c] - 110;
+                                    bool ok;
+                                    double v = i64_times_pow2(-a8[e], p, ok);
+                                    if (!ok) v = scale2((double)(-a8[e]), p);
+                                    A[(size_t)(c1 + c) * M + row] = old[m][e] + v;
+                                }
                             }
                         }
                     }
@@ -339,7 +374,7 @@ __global__ void __maxnreg__(128)
                 tc::fence_before_sync();
                 __syncthreads();   // the accumulators are read before the next tile's MMAs
                 tc::fence_after_sync();
-                if (tid == 0 && tile + 1 < ntiles) issue_tile(cur ^ 1);
+                if (issuer && tile + 1 < ntiles) issue_tile(cur ^ 1);
                 if (tile + 2 < ntiles) load_tile(tile + 2);
             }
         }
