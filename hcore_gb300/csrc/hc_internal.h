@@ -143,11 +143,13 @@ constexpr int kTcMaxK = 64;
 int rebuild_launches(const LaunchShape &shape, bool fp64);
 
 // Blocked QR (FP64 plans, a + c <= kTcMaxK): 16-column panels factored by the
-// FP64 register kernel, the last panel taking the rest when it is at most 24
-// columns wide; between panels the trailing columns are updated on the tensor
-// cores (hc_qr_tc.cu).  Returns false when panel p does not exist.
+// FP64 register kernel, the last panel taking the rest when it is at most 20
+// columns wide (on the TLR panel workload the QR phase took 10.7, 10.1, 9.85
+// and 10.1 ms with limits 32, 24, 20 and 16); between panels the trailing
+// columns are updated on the tensor cores (hc_qr_tc.cu).  Returns false when
+// panel p does not exist.
 __host__ __device__ inline bool qr_panel_bounds(int k, int p, int &c0, int &c1) {
-    const int q = k > 24 ? (k - 24 + 15) / 16 : 0;   // full panels before the last
+    const int q = k > 20 ? (k - 20 + 15) / 16 : 0;   // full panels before the last
     if (p < 0 || p > q) return false;
     c0 = 16 * p;
     c1 = p < q ? c0 + 16 : k;

@@ -5,7 +5,7 @@
 // src/compute/hcore_dgemm.c:123-124 (QR of [beta CU | alpha AU]) and :216-217
 // (QR of [CV | G]).  The QR phase factors 16-column panels with the FP64
 // register kernel (geqrf_kernel with a panel index; the last panel takes up
-// to 24 columns) and, between panels, applies the panel's reflectors
+// to 20 columns) and, between panels, applies the panel's reflectors
 // H_c0 ... H_c1-1 to the columns on its right:
 //
 //     A_t <- Q_p^T A_t = A_t - Y_p W',   W' = T_p^T (Y_p^T A_t),
@@ -104,7 +104,7 @@ __global__ void __maxnreg__(128)
     const int M = d.M, k = d.k;
     int c0, c1;
     if (!qr_panel_bounds(k, panel, c0, c1) || c1 >= k) return;
-    const int nt = k - c1;                      // 9 .. 48 trailing columns
+    const int nt = k - c1;                      // 5 .. 48 trailing columns
     const int side = blockIdx.y;
     const WsLayout L = ws_layout(d);
     double *A = ws + d.ws + (side ? L.VB : L.UA);

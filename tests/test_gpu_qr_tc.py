@@ -9,8 +9,8 @@ cores.  Gates:
 * the rebuilt factors within 1e-13 of the unblocked path's, relative to their
   norm (both FP64-accurate; the panel order changes the rounding only);
 * products within the oracle's 1e-11 gate.
-k covers one panel (24), two (25, 35, 40), three (41, 48, 56) and four (57, 64)
-panels, and k above 64 (unblocked in both plans).
+k covers one panel (20), two (21, 24, 25, 35), three (37, 40, 41, 48) and four
+(53, 56, 57, 64) panels, and k above 64 (unblocked in both plans).
 """
 import numpy as np
 import pytest
@@ -27,7 +27,7 @@ PATH_TOL = 1e-13
 @pytest.mark.parametrize("M", [256, 1000, 2048])
 def test_blocked_qr_matches_unblocked_and_oracle(hc, port, M):
     rng = np.random.default_rng(300 + M)
-    ks = [24, 25, 35, 40, 41, 48, 56, 57, 64, 70]
+    ks = [20, 21, 24, 25, 35, 37, 40, 41, 48, 53, 56, 57, 64, 70]
     cases = _cases(rng, M, ks)
     _, keep_b, r_b, s_b = _run(hc, cases, 0)
     _, keep_u, r_u, s_u = _run(hc, cases, hc.UNBLOCKED_QR)
