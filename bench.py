@@ -422,7 +422,12 @@ def run_gb300(args):
                                          "share the FP64 pipe at 1.06-1.10 TFLOP/s on GB300; "
                                          "MEASURED_PEAKS.json has no FP64 figure)",
                           "peak_probe": ceiling,
-                          "flops_basis": "reference flop model (flop_counts.c) of that phase"}
+                          "flops_basis": "reference flop model (flop_counts.c) of that phase",
+                          "note": "FP64-equivalent: for a + c <= 64 the QR is blocked and its "
+                                  "trailing updates, and the rebuild, run as exact digit "
+                                  "products on the tensor cores; the model counts the "
+                                  "unblocked FP64 flops, so frac can exceed what the FP64 "
+                                  "pipe alone delivers"}
 
     # ---- the rebuild on the tensor cores: tensor work executed and the FP64
     # rate it stands in for ----
