@@ -429,6 +429,23 @@ __host__ __device__ inline size_t svd_smem_bytes(int K, int mats) {
            (size_t)2 * (K + 1) * sizeof(int) + 64;
 }
 
+// Squared deflation bound of the SVD kernel's QR (described there): delta^2
+// for an FP64 update ranked by accuracy, -1 (no deflation) otherwise.  f2 is
+// ||T||_F^2 of T scaled by 2^-sexp.  One thread computes it once per update
+// (a warp-wide sum there cost the Jacobi loops registers).
+template <typename T>
+__device__ __forceinline__ T deflation_bound2(T f2, int k, int rk, int rule, double acc, int sexp) {
+    if constexpr (sizeof(T) != sizeof(double)) {
+        return T(-1);
+    } else {
+        if (rk != 0 || !(acc > 0.0)) return T(-1);
+        const T fro = sqrt(f2);
+        const T thr = (rule & kRuleRelative) ? (T)acc * fro * rsqrt(T(k)) : mul_exp2((T)acc, -sexp);
+        const T dl = min(T(1e-13) * thr, T(1e-16) * fro);
+        return isfinite(dl) ? dl * dl : T(-1);
+    }
+}
+
 // SVD of T = R_A R_B^T (k x k) by QR-preconditioned one-sided Jacobi
 // (Drmac-Veselic): T P = Q R with column pivoting, then one-sided Jacobi on
 // R^T, whose columns are graded by the pivoting, so the sweeps are few.
@@ -459,6 +476,7 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
     extern __shared__ unsigned char smem_raw[];
     __shared__ int s_rot, s_piv, s_exp, s_conv;
     __shared__ T s_wmax[kSvdMaxThreads / 32];
+    __shared__ T s_defl2;
     const Desc d = descs[blockIdx.x];
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
     if (d.status0) {
@@ -535,29 +553,56 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
         s_pcol[c] = c;
     }
     __syncthreads();
+    // Deflation (FP64 rank-by-accuracy updates): the QR stops at the first
+    // step j whose trailing block R22 = R(j:k, j:k) has ||R22||_F <= delta,
+    // and the Jacobi then runs on the first j rows of R only.  Dropping R22
+    // moves every singular value by at most delta (Weyl), with
+    //   delta = min(1e-13 thr, 1e-16 ||T||_F),
+    // thr the truncation threshold (acc, or for the relative rule its lower
+    // bound acc ||T||_F / sqrt(k)): a rank decision can change only for a
+    // singular value within 1e-13 of the threshold, relative, and every
+    // singular value stays within a few eps sigma_max of the full one (the
+    // accuracy of dgesvd's small singular values).  The dropped directions
+    // come out with singular value 0.  On the TLR panel's updates about half
+    // of the columns are below this bound.
+    if (tid == 0) {
+        T f2 = 0;   // ||T||_F^2 of the scaled T
+        for (int c = 0; c < k; ++c) f2 += s_nrm[c];
+        s_defl2 = deflation_bound2(f2, k, d.rk, d.rule, d.acc, sexp);
+    }
+    int kk = k;   // columns of R^T that the Jacobi rotates
+    // (the rank search keeps its first rank_start columns whatever their size)
+    const int kfloor = d.rank_start < k ? (d.rank_start > 0 ? d.rank_start : 0) : k;
     for (int j = 0; j < k; ++j) {
-        // pivot: the largest remaining partial norm (warp 0)
+        // pivot: the largest remaining partial norm (warp 0); deflation test
         if (tid < 32) {
-            T best = -1;
+            T best = -1, tail = 0;
             int bi = j;
-            for (int c = j + lane; c < k; c += 32)
+            for (int c = j + lane; c < k; c += 32) {
+                tail += s_nrm[c];
                 if (s_nrm[c] > best) {
                     best = s_nrm[c];
                     bi = c;
                 }
+            }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 const T ob = __shfl_xor_sync(0xffffffffu, best, o);
                 const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                tail += __shfl_xor_sync(0xffffffffu, tail, o);
                 if (ob > best || (ob == best && oi < bi)) {
                     best = ob;
                     bi = oi;
                 }
             }
-            if (lane == 0) s_piv = bi;
+            if (lane == 0) s_piv = (j >= kfloor && tail <= s_defl2) ? -1 : bi;
         }
         __syncthreads();
         const int pv = s_piv;
+        if (pv < 0) {
+            kk = j;
+            break;
+        }
         if (pv != j) {
             for (int i = tid; i < k; i += nthr) {
                 const T x = A[ixA(i, j)];
@@ -621,20 +666,23 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
         }
         __syncthreads();
     }
-    // Q's reflectors to global (read back when forming U_T = Q V_J); B = R^T;
-    // A = I (V_J)
+    // Q's reflectors to global (read back when forming U_T = Q V_J); B = R^T
+    // (rows kk.. of R dropped: B's columns kk.. are zero); A = I (V_J).
+    // Reflectors kk.. were never formed: tau 0.
+    for (int h = kk + tid; h < k; h += nthr) s_tau[h] = T(0);
     for (int j = 0; j < k; ++j)
         for (int i = tid; i < k; i += nthr) {
             const T x = A[ixA(i, j)];
-            Yg[(size_t)j * k + i] = i > j ? x : T(0);
-            B[ixB(j, i)] = i <= j ? x : T(0);   // B(j, i) = R(i, j)
+            Yg[(size_t)j * k + i] = (i > j && j < kk) ? x : T(0);
+            B[ixB(j, i)] = (i <= j && i < kk) ? x : T(0);   // B(j, i) = R(i, j)
         }
     __syncthreads();
     for (int o = 0; o < k; ++o)
         for (int t = tid; t < k; t += nthr) A[(size_t)o * ldA + t] = o == t ? T(1) : T(0);
     for (int c = tid; c < k; c += nthr) {
         T s = 0;
-        for (int i = 0; i < k; ++i) s += B[ixB(i, c)] * B[ixB(i, c)];
+        if (c < kk)
+            for (int i = 0; i < k; ++i) s += B[ixB(i, c)] * B[ixB(i, c)];
         s_nrm[c] = s;
         s_d[c] = T(1);
     }
@@ -644,7 +692,8 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
     // ---- one-sided Jacobi on B = R^T, rotations accumulated in A ----
     // G lanes per pair (rows i = lig, lig+G, ...); every lane runs the same
     // number of iterations so that the full-warp shuffles stay converged
-    const int n = k + (k & 1);
+    // (columns kk.. of B are zero and take no part; V_J's rows kk.. stay zero)
+    const int n = kk + (kk & 1);
     const int np = n / 2;
     const int grp = tid / G, lig = tid % G, ngrp = nthr / G;
     const T tol = T(k > 8 ? k : 8) * Lim<T>::eps;
@@ -657,7 +706,7 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
     // take no square root or division.
     const T tol2 = tol * tol;
     const T stop2 = tol;   // (sqrt(tol))^2
-    bool converged = (k == 1);
+    bool converged = (kk <= 1);
     int sweeps = 0;
     for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
         if (tid == 0) s_rot = 0;
@@ -668,7 +717,7 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                 const int pi = base + grp;
                 int p = 0, q = 0;
                 if (pi < np) rr_pair(round, pi, n, p, q);
-                const bool valid = pi < np && p < k && q < k;
+                const bool valid = pi < np && p < kk && q < kk;
                 T *xp = B + ixB(0, p), *xq = B + ixB(0, q);
                 T dot = 0;
                 if (valid) {
@@ -721,9 +770,11 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                     // for the stores of the first
                     // (shared-memory modes only: the workspace mode has no registers
                     // to spare at 1024 threads)
+                    // (V_J's rows kk.. are zero in every column the Jacobi
+                    // rotates: rows from kk on update B alone)
                     int i = lig;
                     if (MODE != 0)
-                    for (; i + G < k; i += 2 * G) {
+                    for (; i + G < kk; i += 2 * G) {
                         const size_t r0 = (size_t)i, r1 = (size_t)(i + G);
                         const T a0 = xp[r0 * rsB], b0 = xq[r0 * rsB];
                         const T a1 = xp[r1 * rsB], b1 = xq[r1 * rsB];
@@ -738,13 +789,28 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
                         vp[r1 * rsA] = u1 - f1 * v1;
                         vq[r1 * rsA] = v1 + f2 * u1;
                     }
-                    for (; i < k; i += G) {
+                    for (; i < kk; i += G) {
                         const T a = xp[i * rsB], b = xq[i * rsB];
                         xp[i * rsB] = a - f1 * b;
                         xq[i * rsB] = b + f2 * a;
                         const T u = vp[i * rsA], v = vq[i * rsA];
                         vp[i * rsA] = u - f1 * v;
                         vq[i * rsA] = v + f2 * u;
+                    }
+                    if (MODE != 0)
+                    for (; i + G < k; i += 2 * G) {
+                        const size_t r0 = (size_t)i, r1 = (size_t)(i + G);
+                        const T a0 = xp[r0 * rsB], b0 = xq[r0 * rsB];
+                        const T a1 = xp[r1 * rsB], b1 = xq[r1 * rsB];
+                        xp[r0 * rsB] = a0 - f1 * b0;
+                        xq[r0 * rsB] = b0 + f2 * a0;
+                        xp[r1 * rsB] = a1 - f1 * b1;
+                        xq[r1 * rsB] = b1 + f2 * a1;
+                    }
+                    for (; i < k; i += G) {
+                        const T a = xp[i * rsB], b = xq[i * rsB];
+                        xp[i * rsB] = a - f1 * b;
+                        xq[i * rsB] = b + f2 * a;
                     }
                 }
                 T np_ = app - t * apq, nq_ = aqq + t * apq;
@@ -777,7 +843,7 @@ __global__ void __launch_bounds__(kSvdMaxThreads) gesvd_kernel(const Desc *__res
             __syncthreads();
         }
         // exact norms once per sweep; fold scales before they underflow
-        for (int j = tid; j < k; j += nthr) {
+        for (int j = tid; j < kk; j += nthr) {
             T *xj = B + ixB(0, j);
             T dj = s_d[j];
             if (dj < JacobiLim<T>::tiny_scale) {
