@@ -210,6 +210,7 @@ __global__ void __launch_bounds__(256, 1) zgesvd_kernel(const ZDesc *__restrict_
     extern __shared__ unsigned char zsm[];
     __shared__ int s_piv, s_exp, s_conv, s_rot, s_bad;
     __shared__ double s_wmax[8];
+    __shared__ double s_defl2;
     const ZDesc d = descs[blockIdx.x];
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
     if (d.status0) {
@@ -277,27 +278,47 @@ __global__ void __launch_bounds__(256, 1) zgesvd_kernel(const ZDesc *__restrict_
         s_pcol[c] = c;
     }
     __syncthreads();
+    // Deflation, as in the real kernel (gesvd_kernel): the QR stops at the
+    // first step j >= 1 (the rank search starts at 1) whose trailing block has
+    // ||R(j:k, j:k)||_F <= delta = min(1e-13 acc, 1e-16 ||T||_F) and the
+    // Jacobi works on the first j rows of R.  Every singular value moves by at
+    // most delta (Weyl); the dropped directions come out with singular value 0.
+    if (tid == 0) {
+        double f2 = 0;   // ||T||_F^2 of the scaled T
+        for (int c = 0; c < k; ++c) f2 += s_nrm[c];
+        double dl = -1.0;
+        if (d.rk == 0 && d.acc > 0.0) dl = fmin(1e-13 * dmul_exp2(d.acc, -sexp), 1e-16 * sqrt(f2));
+        s_defl2 = (dl >= 0.0 && isfinite(dl)) ? dl * dl : -1.0;
+    }
+    int kk = k;   // columns of R^H that the Jacobi rotates
     for (int j = 0; j < k; ++j) {
         if (tid < 32) {
-            double best = -1;
+            double best = -1, tail = 0;
             int bi = j;
-            for (int c = j + lane; c < k; c += 32)
+            for (int c = j + lane; c < k; c += 32) {
+                tail += s_nrm[c];
                 if (s_nrm[c] > best) {
                     best = s_nrm[c];
                     bi = c;
                 }
+            }
             for (int o = 16; o > 0; o >>= 1) {
                 const double ob = __shfl_xor_sync(0xffffffffu, best, o);
                 const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                tail += __shfl_xor_sync(0xffffffffu, tail, o);
                 if (ob > best || (ob == best && oi < bi)) {
                     best = ob;
                     bi = oi;
                 }
             }
-            if (lane == 0) s_piv = bi;
+            if (lane == 0) s_piv = (j >= 1 && tail <= s_defl2) ? -1 : bi;
         }
         __syncthreads();
         const int pv = s_piv;
+        if (pv < 0) {
+            kk = j;
+            break;
+        }
         if (pv != j) {
             for (int i = tid; i < k; i += nthr) {
                 const zd x = A[ixA(i, j)];
@@ -347,12 +368,14 @@ __global__ void __launch_bounds__(256, 1) zgesvd_kernel(const ZDesc *__restrict_
         }
         __syncthreads();
     }
-    // reflectors to the workspace; B = R^H; A = I
+    // reflectors to the workspace; B = R^H (rows kk.. of R dropped: B's
+    // columns kk.. are zero; reflectors kk.. were never formed); A = I
+    for (int h = kk + tid; h < k; h += nthr) s_tau[h] = zmk(0, 0);
     for (int e = tid; e < k * k; e += nthr) {
         const int i = e % k, j = e / k;
         const zd x = A[ixA(i, j)];
-        Yg[(size_t)j * k + i] = i > j ? x : zmk(0, 0);
-        B[ix(j, i)] = i <= j ? zconj(x) : zmk(0, 0);   // B(j, i) = conj(R(i, j))
+        Yg[(size_t)j * k + i] = (i > j && j < kk) ? x : zmk(0, 0);
+        B[ix(j, i)] = (i <= j && i < kk) ? zconj(x) : zmk(0, 0);   // B(j, i) = conj(R(i, j))
     }
     __syncthreads();
     for (int e = tid; e < k * k; e += nthr) {
@@ -361,7 +384,8 @@ __global__ void __launch_bounds__(256, 1) zgesvd_kernel(const ZDesc *__restrict_
     }
     for (int c = tid; c < k; c += nthr) {
         double s = 0;
-        for (int i = 0; i < k; ++i) s += zabs2(B[ix(i, c)]);
+        if (c < kk)
+            for (int i = 0; i < k; ++i) s += zabs2(B[ix(i, c)]);
         s_nrm[c] = s;
         s_d[c] = zmk(1, 0);
     }
@@ -373,12 +397,13 @@ __global__ void __launch_bounds__(256, 1) zgesvd_kernel(const ZDesc *__restrict_
     // t the real Jacobi tangent of (a_pp, a_qq, |a_pq|); in scaled form
     // x_p -= f1 x_q, x_q += f2 x_p with f1 = t e^{-i phi} d_q / d_p,
     // f2 = t e^{i phi} d_p / d_q, d_p <- c d_p, d_q <- c e^{-i phi} d_q
-    const int n = k + (k & 1), np = n / 2;
+    // (columns kk.. of B are zero and take no part; V_J's rows kk.. stay zero)
+    const int n = kk + (kk & 1), np = n / 2;
     const int grp = tid / G, lig = tid % G, ngrp = nthr / G;
     const double tol = (double)(k > 8 ? k : 8) * DBL_EPSILON;
     const double tol2 = tol * tol, stop2 = tol;
     const double safmin = DBL_MIN / DBL_EPSILON;
-    bool converged = (k == 1);
+    bool converged = (kk <= 1);
     for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
         if (tid == 0) s_rot = 0;
         bool big = false;
@@ -388,7 +413,7 @@ __global__ void __launch_bounds__(256, 1) zgesvd_kernel(const ZDesc *__restrict_
                 const int pi = bs + grp;
                 int p = 0, q = 0;
                 if (pi < np) zrr_pair(round, pi, n, p, q);
-                const bool valid = pi < np && p < k && q < k;
+                const bool valid = pi < np && p < kk && q < kk;
                 zd *xp = B + ix(0, p), *xq = B + ix(0, q);
                 zd dot = zmk(0, 0);
                 if (valid)
@@ -425,13 +450,19 @@ __global__ void __launch_bounds__(256, 1) zgesvd_kernel(const ZDesc *__restrict_
                     const zd f1 = zscal(t / zabs2(dp), zmul(zconj(ph), zmul(dq, zconj(dp))));
                     const zd f2 = zscal(t / zabs2(dq), zmul(ph, zmul(dp, zconj(dq))));
                     zd *vp = A + ixA(0, p), *vq = A + ixA(0, q);
-                    for (int i = lig; i < k; i += G) {
+                    int i = lig;
+                    for (; i < kk; i += G) {
                         const zd a = xp[i], b = xq[i];
                         xp[i] = zfms(f1, b, a);
                         xq[i] = zfma(f2, a, b);
                         const zd u = vp[i], vv = vq[i];
                         vp[i] = zfms(f1, vv, u);
                         vq[i] = zfma(f2, u, vv);
+                    }
+                    for (; i < k; i += G) {   // V_J's rows kk.. are zero
+                        const zd a = xp[i], b = xq[i];
+                        xp[i] = zfms(f1, b, a);
+                        xq[i] = zfma(f2, a, b);
                     }
                 }
                 double np_ = app - t * sqrt(amag2), nq_ = aqq + t * sqrt(amag2);
@@ -463,7 +494,7 @@ __global__ void __launch_bounds__(256, 1) zgesvd_kernel(const ZDesc *__restrict_
             __syncthreads();
         }
         // exact norms once per sweep; fold scales before they underflow
-        for (int j = tid; j < k; j += nthr) {
+        for (int j = tid; j < kk; j += nthr) {
             zd *xj = B + ix(0, j);
             zd dj = s_d[j];
             if (zabs2(dj) < 1e-120) {

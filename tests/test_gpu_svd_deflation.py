@@ -77,3 +77,40 @@ def test_wide_spectrum_keeps_full_rank_part(hc, port):
                   arrays=_batch_case(rng, 256, a, b, c, decades=8.0))
              for a, b, c in [(16, 16, 16), (30, 28, 34)]]
     _check(cases, *_run_batch(hc, cases), port, expect_zeros=False)
+
+
+def test_deflated_complex_svd_vs_oracle(hc, port):
+    """The complex kernel (zgesvd_kernel, hc_zkernels.cu) deflates the same
+    way.  Complex factors with spectra of 30 decades (part of every core below
+    the bound) and a far-field update with every singular value below acc,
+    through hcore_gpu_zgemm_batched (native complex kernels for a + c <= 84):
+    ranks equal to the restated reference's (zgesvd at hcore_zgemm.c:327),
+    products within 1e-11."""
+    from test_gpu_zgemm import _clr, _rel
+
+    rng = np.random.default_rng(61)
+    M, maxrk = 256, 84
+    tasks, keep, refs = [], [], []
+    for q, (a, b, c) in enumerate([(6, 5, 7), (20, 18, 22), (30, 28, 34), (40, 30, 40),
+                                   (12, 10, 14)]):
+        AU, AV = _clr(rng, M, a, 30)
+        BU, BV = _clr(rng, M, b, 30)
+        CU, CV = _clr(rng, M, c, 30)
+        if q == 4:   # far field: every singular value below acc
+            AU, CU = np.asfortranarray(AU * 1e-7), np.asfortranarray(CU * 1e-12)
+        ref = port.zgemm(M, -1.0, AU, AV, a, BU, BV, b, 1.0, CU, CV, c, maxrk=maxrk, acc=ACC)
+        oU = np.zeros((M, maxrk), dtype=np.complex128, order="F")
+        oV = np.zeros_like(oU)
+        oU[:, :c], oV[:, :c] = CU, CV
+        keep += [AU, AV, BU, BV, oU, oV]
+        tasks.append(hc.ZlrTask(M=M, a=a, b=b, c=c, rk=0, maxrk=maxrk,
+                                alpha=hc.DComplex(-1.0, 0.0), beta=hc.DComplex(1.0, 0.0),
+                                acc=ACC, AU=AU.ctypes.data, AV=AV.ctypes.data, lda=M,
+                                BU=BU.ctypes.data, BV=BV.ctypes.data, ldb=M, CU=oU.ctypes.data,
+                                CV=oV.ctypes.data, ldc=M))
+        refs.append((ref, oU, oV))
+    ranks, status = hc.zgemm_batched(tasks)
+    for q, ((ref, oU, oV), r, st) in enumerate(zip(refs, ranks, status)):
+        assert st == 0 and r == ref["rank"], (q, st, r, ref["rank"])
+        assert _rel(oU[:, :r] @ oV[:, :r].T, ref["CU"] @ ref["CV"].T) < FP64_TOL, q
+    assert ranks[4] == 1
