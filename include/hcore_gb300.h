@@ -8,7 +8,11 @@
  * semantics of HCORE_dgemm (src/compute/hcore_dgemm.c:703-1012): stack,
  * Householder QR of both stacked factors, SVD of R_A R_B^T, truncation with the
  * absolute threshold acc (first i >= min_rank_start with sigma_i < acc), and
- * rebuild CU = Q_A U_r, CV = Q_B V_r S_r.
+ * rebuild CU = Q_A U_r, CV = Q_B V_r S_r.  In FP64 the SVD drops the part of
+ * R_A R_B^T below delta = min(1e-13 acc, 1e-16 ||R_A R_B^T||_F) after its
+ * pivoted QR: every singular value moves by at most delta, so a rank differs
+ * from the full SVD's only for a singular value within 1e-13 of acc,
+ * relative, and the dropped singular values are reported as 0.
  *
  * Pointers in a task may be device memory or pinned (page-locked) host
  * memory; both are read and written directly by the kernels.  Outputs may
@@ -142,7 +146,8 @@ int hcore_gpu_plan_results(hcore_gpu_plan plan, int *ranks, int *status, void *s
  * first call (or one with more tasks than any before) allocates. */
 int hcore_gpu_plan_rebuild(hcore_gpu_plan plan, int n, const int *task_idx, void *const *CUo,
                            void *const *CVo, const int *ldco, const int *max_rank, void *stream);
-/* copy the k singular values of task i (descending) to host (diagnostics) */
+/* copy the k singular values of task i (descending) to host (diagnostics;
+ * in FP64 the values below the SVD's deflation bound are 0) */
 int hcore_gpu_plan_sigma(hcore_gpu_plan plan, int i, double *sigma, int *k, void *stream);
 /* Jacobi sweeps each task's SVD took (diagnostics; valid after execute) */
 int hcore_gpu_plan_sweeps(hcore_gpu_plan plan, int *sweeps, void *stream);
