@@ -397,6 +397,9 @@ class Batch:
         return ranks[:self.n], status[:self.n]
 
     def sigma(self, i, stream=None):
+        """Task i's k singular values, descending (hcore_gpu_plan_sigma).  In
+        FP64 the values below the SVD's deflation bound
+        min(1e-13 acc, 1e-16 ||R_A R_B^T||_F) are 0."""
         k = C.c_int(0)
         lib().hcore_gpu_plan_sigma(self._plan, i, None, C.byref(k), stream or None)
         out = np.zeros(max(k.value, 1))
