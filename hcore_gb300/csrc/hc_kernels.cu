@@ -8,10 +8,15 @@
 //              F = AV^T BV, G = BU F^T, VB = [CV | G]            -> workspace
 //   2. geqrf  (hcore_dgemm.c:123, :216) Householder QR of UA and VB
 //              (blockIdx.y selects the side), LAPACK dlarfg conventions
-//   3. gesvd  (hcore_dgemm.c:296-503) T = R_A R_B^T, one-sided Jacobi SVD,
+//   3. gesvd  (hcore_dgemm.c:296-503) T = R_A R_B^T, pivoted QR (in FP64
+//              deflated below 1e-13 of the threshold), one-sided Jacobi SVD,
 //              singular values sorted, rank rule, U_r and V_r S_r
 //   4. apply  (hcore_dgemm.c:508-696) CU = Q_A [U_r; 0], CV = Q_B [V_r S_r; 0]
 //              written straight into the caller's output factors
+//
+// In FP64 plans with a + c <= 64 the QR runs blocked, its trailing updates on
+// the tensor cores (hc_qr_tc.cu), and the rebuild runs there too
+// (hc_rebuild_tc.cu); this file keeps the panels and every other case.
 //
 // The scalar type T is double (HCORE_dgemm) or float (HCORE_sgemm); every
 // step computes in T, like the reference's two copies.  With the plan flag

@@ -12,8 +12,9 @@
 //   zstack_kernel   UA = [beta CU | alpha AU], F = AV^T BV, G = BU F^T, VB = [CV | G]
 //   zgeqrf_kernel   Householder QR of UA and VB (zlarfg conventions: beta real,
 //                   tau complex, H = I - tau v v^H, Q^H applied to the trailing columns)
-//   zgesvd_kernel   T = R_A R_B^T, QR with column pivoting T P = Q R, one-sided
-//                   Jacobi on B = R^H with complex column scales, rank rule;
+//   zgesvd_kernel   T = R_A R_B^T, QR with column pivoting T P = Q R (deflated
+//                   as the real kernel's), one-sided Jacobi on B = R^H with
+//                   complex column scales, rank rule;
 //                   U_r = Q V_J, conj(W_r S_r) = conj(P (rotated B))
 //   zapply_kernel   CU = Q_A [U_r; 0], CV = Q_B [conj(W_r S_r); 0]
 //
